@@ -1,0 +1,711 @@
+// CPU FP64 oracle for the cluster-expansion Metropolis hot path.
+//
+// TEST INFRASTRUCTURE ONLY. This file is the checker: it is linked and called
+// by tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg,
+// never by the product library. It restates, independently of the product's
+// table builder, the arithmetic of the reference's hot path:
+//
+//  * cluster-expansion energy and delta correlations of the occupation basis
+//    (libcasm-clexulator, not vendored; semantics as in the generated
+//    Clexulator tests/unit/clexmonte/data/FCC_binary_vacancy/basis_sets/
+//    bset.default/FCC_binary_vacancy_Clexulator_default.cc:306-311 (site
+//    functions), :555-580 (delta point correlations), :1054-1060 (per-orbit
+//    division by the multiplicity));
+//  * the canonical and semi-grand canonical potentials
+//    (src/casm/clexmonte/monte_calculator/CanonicalCalculator.cc:137-140,
+//    SemiGrandCanonicalCalculator.cc:186-213);
+//  * the Metropolis loop occupation_metropolis_v2
+//    (include/casm/clexmonte/methods/occupation_metropolis.hh:72-123) with a
+//    std::mt19937_64 engine (canonical/canonical.hh:139) and the event
+//    proposal / acceptance / occupant-location steps of libcasm-monte, which
+//    is not vendored and is restated here (see propose_* and accept_metropolis
+//    below);
+//  * variance / covariance analyses (src/casm/clexmonte/monte_calculator/
+//    analysis_functions.cc:17-173, run/io/convariance_functions.cc:29-146).
+//
+// Clusters are enumerated here from the lattice and the per-size maximum
+// lengths, and each decorated cluster is identified by a geometric invariant
+// (sorted edge list with squared lengths and species pairs), not by the
+// product's symmetry tables. Orbit multiplicities are counted here.
+
+#include <algorithm>
+#include <array>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace {
+
+using i64 = long long;
+using u64 = unsigned long long;
+
+std::string g_err;
+
+struct Vec3 {
+  i64 x, y, z;
+};
+
+inline i64 sq(const Vec3 &a, const Vec3 &b) {
+  i64 dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+  return dx * dx + dy * dy + dz * dz;
+}
+
+bool lex_less(const Vec3 &a, const Vec3 &b) {
+  if (a.x != b.x) return a.x < b.x;
+  if (a.y != b.y) return a.y < b.y;
+  return a.z < b.z;
+}
+
+// Decorated-cluster invariant: (size, sorted edges (d2, min occ, max occ),
+// sorted occupants) flattened into a vector key.
+std::vector<i64> invariant(const std::vector<Vec3> &p, const std::vector<int> &occ) {
+  int n = (int)p.size();
+  std::vector<std::array<i64, 3>> e;
+  for (int i = 0; i < n; ++i)
+    for (int j = i + 1; j < n; ++j)
+      e.push_back({sq(p[i], p[j]), (i64)std::min(occ[i], occ[j]),
+                   (i64)std::max(occ[i], occ[j])});
+  std::sort(e.begin(), e.end());
+  std::vector<int> o(occ.begin(), occ.end());
+  std::sort(o.begin(), o.end());
+  std::vector<i64> key;
+  key.push_back(n);
+  for (auto &x : e) key.insert(key.end(), x.begin(), x.end());
+  for (int v : o) key.push_back(v);
+  return key;
+}
+
+struct AnchorType {  // cluster shape anchored at basis site b, uc (0,0,0)
+  int size;
+  int orbit;               // oracle orbit id (undecorated invariant)
+  int b[4];                // sublattice of each site (site 0 = anchor)
+  i64 du[4][3];            // unit cell offset of each site
+  std::vector<int> lut;    // n_occ^size decoration code -> function (-1: none)
+};
+
+struct System {
+  int n_basis = 1, n_occ = 2;
+  i64 lat[3][3];
+  std::vector<Vec3> basis;
+  double grid = 1.0;
+  int L[3] = {1, 1, 1};
+  int n_uc = 1, n_sites = 1;
+  int n_funcs = 1;
+  std::vector<double> eci, coeff, mult, weight;  // weight = eci*coeff/mult
+  std::vector<int> func_orbit;
+  std::vector<std::vector<AnchorType>> types;  // per basis site
+  // supercell clusters
+  std::vector<int> cl_type_b, cl_type_i;  // (anchor b, type index)
+  std::vector<int> cl_sites;              // 4 per cluster
+  std::vector<int> inc_off, inc_cl, inc_pos;  // incidence CSR over sites
+  std::vector<double> RT;  // (n_occ-1) x n_occ, param composition per mol change
+  double n_orbits = 0;
+};
+
+Vec3 cart(const System &s, int b, i64 u0, i64 u1, i64 u2) {
+  Vec3 v;
+  v.x = u0 * s.lat[0][0] + u1 * s.lat[1][0] + u2 * s.lat[2][0] + s.basis[b].x;
+  v.y = u0 * s.lat[0][1] + u1 * s.lat[1][1] + u2 * s.lat[2][1] + s.basis[b].y;
+  v.z = u0 * s.lat[0][2] + u1 * s.lat[1][2] + u2 * s.lat[2][2] + s.basis[b].z;
+  return v;
+}
+
+inline int site_index(const System &s, int b, i64 i, i64 j, i64 k) {
+  auto m = [](i64 a, int n) { return (int)(((a % n) + n) % n); };
+  return b * s.n_uc + m(i, s.L[0]) + s.L[0] * (m(j, s.L[1]) + s.L[1] * m(k, s.L[2]));
+}
+
+void build(System &s, const double *max_length /*[5], index = size*/,
+           const int *func_size, const i64 *func_pts /*n_funcs*4*3*/,
+           const int *func_occ /*n_funcs*4*/) {
+  // 1. function invariants -> function index; undecorated orbit invariants
+  std::map<std::vector<i64>, int> fmap, omap;
+  s.func_orbit.assign(s.n_funcs, -1);
+  for (int f = 1; f < s.n_funcs; ++f) {
+    int n = func_size[f];
+    std::vector<Vec3> p(n);
+    std::vector<int> o(n), z(n, 0);
+    for (int i = 0; i < n; ++i) {
+      p[i] = {func_pts[(f * 4 + i) * 3 + 0], func_pts[(f * 4 + i) * 3 + 1],
+              func_pts[(f * 4 + i) * 3 + 2]};
+      o[i] = func_occ[f * 4 + i];
+    }
+    auto key = invariant(p, o);
+    if (fmap.count(key)) throw std::runtime_error("two functions share an invariant");
+    fmap[key] = f;
+    auto okey = invariant(p, z);
+    if (!omap.count(okey)) {
+      int id = (int)omap.size();
+      omap[okey] = id;
+    }
+    s.func_orbit[f] = omap[okey];
+  }
+  int n_orbit = (int)omap.size();
+  // 2. anchored cluster shapes per basis site, by enumeration
+  double rmax = 0;
+  for (int n = 2; n <= 4; ++n) rmax = std::max(rmax, max_length[n]);
+  const double tol = 1e-5;
+  s.types.assign(s.n_basis, {});
+  std::vector<double> orbit_count(n_orbit, 0.0);
+  // inverse of lattice for site lookup not needed: enumerate (b,u) directly
+  int R = (int)std::ceil(rmax / s.grid) + 2;
+  for (int b = 0; b < s.n_basis; ++b) {
+    Vec3 c0 = cart(s, b, 0, 0, 0);
+    struct Nb {
+      Vec3 c;
+      int b;
+      i64 u[3];
+    };
+    std::vector<Nb> nb;
+    for (i64 u0 = -R; u0 <= R; ++u0)
+      for (i64 u1 = -R; u1 <= R; ++u1)
+        for (i64 u2 = -R; u2 <= R; ++u2)
+          for (int bb = 0; bb < s.n_basis; ++bb) {
+            Vec3 c = cart(s, bb, u0, u1, u2);
+            i64 d2 = sq(c, c0);
+            if (d2 > 0 && d2 * s.grid * s.grid <= rmax * rmax + tol) nb.push_back({c, bb, {u0, u1, u2}});
+          }
+    auto add_type = [&](std::vector<int> idx) {
+      int n = (int)idx.size() + 1;
+      std::vector<Vec3> p(n);
+      p[0] = c0;
+      for (int i = 1; i < n; ++i) p[i] = nb[idx[i - 1]].c;
+      double lim = max_length[n];
+      for (int i = 0; i < n; ++i)
+        for (int j = i + 1; j < n; ++j)
+          if (sq(p[i], p[j]) * s.grid * s.grid > lim * lim + tol) return;
+      for (int i = 1; i < n; ++i)
+        if (lex_less(p[i], p[0])) return;  // anchor must be the smallest point
+      std::vector<int> z(n, 0);
+      auto okey = invariant(p, z);
+      auto it = omap.find(okey);
+      if (it == omap.end()) return;
+      AnchorType t;
+      t.size = n;
+      t.orbit = it->second;
+      t.b[0] = b;
+      t.du[0][0] = t.du[0][1] = t.du[0][2] = 0;
+      for (int i = 1; i < n; ++i) {
+        t.b[i] = nb[idx[i - 1]].b;
+        for (int a = 0; a < 3; ++a) t.du[i][a] = nb[idx[i - 1]].u[a];
+      }
+      int ncode = 1;
+      for (int i = 0; i < n; ++i) ncode *= s.n_occ;
+      t.lut.assign(ncode, -1);
+      std::vector<int> occ(n);
+      for (int code = 0; code < ncode; ++code) {
+        int c = code;
+        bool all_nonref = true;
+        for (int i = 0; i < n; ++i) {
+          occ[i] = c % s.n_occ;
+          c /= s.n_occ;
+          if (occ[i] == 0) all_nonref = false;
+        }
+        if (!all_nonref) continue;
+        auto key = invariant(p, occ);
+        auto f = fmap.find(key);
+        if (f == fmap.end()) throw std::runtime_error("decorated cluster has no function");
+        t.lut[code] = f->second;
+      }
+      orbit_count[t.orbit] += 1.0;
+      s.types[b].push_back(t);
+    };
+    // point
+    {
+      std::vector<Vec3> p{c0};
+      std::vector<int> z{0};
+      auto it = omap.find(invariant(p, z));
+      if (it != omap.end()) {
+        AnchorType t;
+        t.size = 1;
+        t.orbit = it->second;
+        t.b[0] = b;
+        t.du[0][0] = t.du[0][1] = t.du[0][2] = 0;
+        t.lut.assign(s.n_occ, -1);
+        for (int o = 1; o < s.n_occ; ++o) {
+          std::vector<int> oo{o};
+          auto f = fmap.find(invariant(p, oo));
+          if (f == fmap.end()) throw std::runtime_error("point function missing");
+          t.lut[o] = f->second;
+        }
+        orbit_count[t.orbit] += 1.0;
+        s.types[b].push_back(t);
+      }
+    }
+    int m = (int)nb.size();
+    for (int i = 0; i < m; ++i) {
+      if (max_length[2] > 0) add_type({i});
+      for (int j = i + 1; j < m; ++j) {
+        if (max_length[3] > 0) add_type({i, j});
+        if (max_length[4] > 0)
+          for (int k = j + 1; k < m; ++k) add_type({i, j, k});
+      }
+    }
+  }
+  // 3. multiplicities, weights
+  s.mult.assign(s.n_funcs, 1.0);
+  s.weight.assign(s.n_funcs, 0.0);
+  for (int f = 1; f < s.n_funcs; ++f) {
+    s.mult[f] = orbit_count[s.func_orbit[f]];
+    if (s.mult[f] <= 0) throw std::runtime_error("orbit with no cluster in the crystal");
+    s.weight[f] = s.eci[f] * s.coeff[f] / s.mult[f];
+  }
+  s.weight[0] = s.eci[0];
+  // 4. supercell clusters and incidence
+  s.n_uc = s.L[0] * s.L[1] * s.L[2];
+  s.n_sites = s.n_uc * s.n_basis;
+  s.cl_sites.clear();
+  s.cl_type_b.clear();
+  s.cl_type_i.clear();
+  for (int b = 0; b < s.n_basis; ++b)
+    for (int k = 0; k < s.L[2]; ++k)
+      for (int j = 0; j < s.L[1]; ++j)
+        for (int i = 0; i < s.L[0]; ++i)
+          for (int ti = 0; ti < (int)s.types[b].size(); ++ti) {
+            const AnchorType &t = s.types[b][ti];
+            for (int q = 0; q < 4; ++q) {
+              if (q < t.size)
+                s.cl_sites.push_back(site_index(s, t.b[q], i + t.du[q][0],
+                                                j + t.du[q][1], k + t.du[q][2]));
+              else
+                s.cl_sites.push_back(-1);
+            }
+            s.cl_type_b.push_back(b);
+            s.cl_type_i.push_back(ti);
+          }
+  int ncl = (int)s.cl_type_b.size();
+  std::vector<int> cnt(s.n_sites + 1, 0);
+  for (int c = 0; c < ncl; ++c)
+    for (int q = 0; q < 4; ++q) {
+      int site = s.cl_sites[c * 4 + q];
+      if (site >= 0) cnt[site + 1]++;
+    }
+  for (int i = 0; i < s.n_sites; ++i) cnt[i + 1] += cnt[i];
+  s.inc_off = cnt;
+  s.inc_cl.assign(cnt.back(), 0);
+  s.inc_pos.assign(cnt.back(), 0);
+  std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+  for (int c = 0; c < ncl; ++c)
+    for (int q = 0; q < 4; ++q) {
+      int site = s.cl_sites[c * 4 + q];
+      if (site < 0) continue;
+      for (int q2 = 0; q2 < q; ++q2)
+        if (s.cl_sites[c * 4 + q2] == site)
+          throw std::runtime_error("supercell too small: a cluster contains a site twice");
+      s.inc_cl[fill[site]] = c;
+      s.inc_pos[fill[site]] = q;
+      fill[site]++;
+    }
+}
+
+inline int cluster_code(const System &s, int c, const signed char *occ, int site, int site_occ) {
+  const AnchorType &t = s.types[s.cl_type_b[c]][s.cl_type_i[c]];
+  int code = 0, mul = 1;
+  for (int q = 0; q < t.size; ++q) {
+    int st = s.cl_sites[c * 4 + q];
+    int o = (st == site) ? site_occ : occ[st];
+    code += o * mul;
+    mul *= s.n_occ;
+  }
+  return code;
+}
+
+// Integer count change of every function for occ[site]: occ_i -> occ_f.
+void site_delta_counts(const System &s, const signed char *occ, int site, int occ_f,
+                       i64 *dcount) {
+  int occ_i = occ[site];
+  for (int e = s.inc_off[site]; e < s.inc_off[site + 1]; ++e) {
+    int c = s.inc_cl[e];
+    const AnchorType &t = s.types[s.cl_type_b[c]][s.cl_type_i[c]];
+    int fo = t.lut[cluster_code(s, c, occ, site, occ_i)];
+    int fn = t.lut[cluster_code(s, c, occ, site, occ_f)];
+    if (fo >= 0) dcount[fo] -= 1;
+    if (fn >= 0) dcount[fn] += 1;
+  }
+}
+
+double counts_to_energy(const System &s, const i64 *count) {
+  double e = s.weight[0] * s.n_uc;
+  for (int f = 1; f < s.n_funcs; ++f) e += s.weight[f] * (double)count[f];
+  return e;
+}
+
+void all_counts(const System &s, const signed char *occ, i64 *count) {
+  for (int f = 0; f < s.n_funcs; ++f) count[f] = 0;
+  int ncl = (int)s.cl_type_b.size();
+  for (int c = 0; c < ncl; ++c) {
+    const AnchorType &t = s.types[s.cl_type_b[c]][s.cl_type_i[c]];
+    int f = t.lut[cluster_code(s, c, occ, -1, 0)];
+    if (f >= 0) count[f] += 1;
+  }
+}
+
+// ---- event delta with the reference's sequential semantics: each change is
+// applied before the next is evaluated (canonical/canonical.hh:42-45).
+double event_delta(const System &s, std::vector<signed char> &occ, int n, const i64 *sites,
+                   const int *new_occ, i64 *dcount) {
+  std::vector<i64> d(s.n_funcs, 0);
+  std::vector<signed char> saved(n);
+  for (int i = 0; i < n; ++i) {
+    saved[i] = occ[sites[i]];
+    site_delta_counts(s, occ.data(), (int)sites[i], new_occ[i], d.data());
+    occ[sites[i]] = (signed char)new_occ[i];
+  }
+  for (int i = n - 1; i >= 0; --i) occ[sites[i]] = saved[i];
+  double de = 0.0;
+  for (int f = 1; f < s.n_funcs; ++f) de += s.weight[f] * (double)d[f];
+  if (dcount)
+    for (int f = 0; f < s.n_funcs; ++f) dcount[f] = d[f];
+  return de;
+}
+
+// SGC chemical-potential term: param_chem_pot . (R^T dN), dN per component
+// (SemiGrandCanonicalCalculator.cc:201-212).
+double sgc_mu_term(const System &s, const double *mu, int n, const i64 *sites, const int *new_occ,
+                   const signed char *occ) {
+  std::vector<double> dN(s.n_occ, 0.0);
+  for (int i = 0; i < n; ++i) {
+    dN[occ[sites[i]]] += -1.0;
+    dN[new_occ[i]] += 1.0;
+  }
+  double t = 0.0;
+  for (int a = 0; a < s.n_occ - 1; ++a) {
+    double x = 0.0;
+    for (int c = 0; c < s.n_occ; ++c) x += s.RT[a * s.n_occ + c] * dN[c];
+    t += mu[a] * x;
+  }
+  return t;
+}
+
+// ---- occupant location lists (restatement of libcasm-monte OccLocation for
+// one asymmetric unit with all sites mutable): one list per species,
+// initialised in increasing site order; apply() removes a site from its old
+// list by moving the last element into its slot and appends it to the new.
+struct OccLoc {
+  std::vector<std::vector<int>> lists;
+  std::vector<int> pos;
+  void init(const signed char *occ, int n, int n_occ) {
+    lists.assign(n_occ, {});
+    pos.assign(n, 0);
+    for (int l = 0; l < n; ++l) {
+      pos[l] = (int)lists[occ[l]].size();
+      lists[occ[l]].push_back(l);
+    }
+  }
+  void move(int l, int from, int to) {
+    auto &a = lists[from];
+    int p = pos[l];
+    int last = a.back();
+    a[p] = last;
+    pos[last] = p;
+    a.pop_back();
+    pos[l] = (int)lists[to].size();
+    lists[to].push_back(l);
+  }
+};
+
+// ---- random draws exactly as libcasm-monte's RandomNumberGenerator does
+// them: std::uniform_int_distribution<long>(0, max) and
+// std::uniform_real_distribution<double>(0, max) over std::mt19937_64.
+struct Rng {
+  std::mt19937_64 eng;
+  u64 draws = 0;
+  struct Counting {
+    Rng *r;
+    using result_type = u64;
+    static constexpr u64 min() { return std::mt19937_64::min(); }
+    static constexpr u64 max() { return std::mt19937_64::max(); }
+    u64 operator()() {
+      r->draws++;
+      return r->eng();
+    }
+  };
+  long random_int(long max) {
+    Counting c{this};
+    return std::uniform_int_distribution<long>(0, max)(c);
+  }
+  double random_real(double max) {
+    Counting c{this};
+    return std::uniform_real_distribution<double>(0.0, max)(c);
+  }
+};
+
+// Metropolis acceptance (libcasm-monte metropolis_acceptance, restated):
+// accept if dE < 0, otherwise draw u in [0,1) and accept if u < exp(-beta dE).
+bool accept_metropolis(double de, double beta, Rng &rng) {
+  if (de < 0.0) return true;
+  return rng.random_real(1.0) < std::exp(-de * beta);
+}
+
+struct RunOut {
+  i64 n_accept = 0, n_reject = 0;
+  std::vector<double> energy_uc;     // formation energy per unit cell, per sample
+  std::vector<double> potential_uc;  // potential per unit cell, per sample
+  std::vector<double> comp;          // per sample, (n_occ-1) param compositions
+};
+
+}  // namespace
+
+extern "C" {
+
+const char *ora_last_error() { return g_err.c_str(); }
+
+void *ora_system_create(int n_basis, const i64 *lattice, const i64 *basis, double grid, int n_occ,
+                        const double *max_length, int n_funcs, const int *func_size,
+                        const i64 *func_pts, const int *func_occ, const double *eci,
+                        const double *coeff, const double *RT, int Lx, int Ly, int Lz) {
+  try {
+    auto s = std::make_unique<System>();
+    s->n_basis = n_basis;
+    s->n_occ = n_occ;
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) s->lat[r][c] = lattice[r * 3 + c];
+    for (int b = 0; b < n_basis; ++b) s->basis.push_back({basis[b * 3], basis[b * 3 + 1], basis[b * 3 + 2]});
+    s->grid = grid;
+    s->L[0] = Lx;
+    s->L[1] = Ly;
+    s->L[2] = Lz;
+    s->n_funcs = n_funcs;
+    s->eci.assign(eci, eci + n_funcs);
+    s->coeff.assign(coeff, coeff + n_funcs);
+    s->RT.assign(RT, RT + (n_occ - 1) * n_occ);
+    build(*s, max_length, func_size, func_pts, func_occ);
+    return s.release();
+  } catch (std::exception &e) {
+    g_err = e.what();
+    return nullptr;
+  }
+}
+
+void ora_system_destroy(void *h) { delete (System *)h; }
+
+int ora_n_sites(void *h) { return ((System *)h)->n_sites; }
+int ora_n_clusters(void *h) { return (int)((System *)h)->cl_type_b.size(); }
+void ora_multiplicities(void *h, double *out) {
+  System &s = *(System *)h;
+  for (int f = 0; f < s.n_funcs; ++f) out[f] = s.mult[f];
+}
+
+// Integer function counts over the supercell (count[0] = number of unit cells).
+void ora_counts(void *h, const signed char *occ, i64 *count) {
+  System &s = *(System *)h;
+  all_counts(s, occ, count);
+  count[0] = s.n_uc;
+}
+
+// Formation energy per supercell.
+double ora_energy(void *h, const signed char *occ) {
+  System &s = *(System *)h;
+  std::vector<i64> c(s.n_funcs);
+  all_counts(s, occ, c.data());
+  return counts_to_energy(s, c.data());
+}
+
+// Extensive correlations per unit cell: coeff_f * count_f / (mult_f n_uc).
+void ora_corr(void *h, const signed char *occ, double *corr) {
+  System &s = *(System *)h;
+  std::vector<i64> c(s.n_funcs);
+  all_counts(s, occ, c.data());
+  corr[0] = 1.0;
+  for (int f = 1; f < s.n_funcs; ++f) corr[f] = s.coeff[f] * (double)c[f] / (s.mult[f] * s.n_uc);
+}
+
+// occ_delta_per_supercell of the formation energy (canonical potential).
+double ora_delta(void *h, const signed char *occ, int n, const i64 *sites, const int *new_occ,
+                 i64 *dcount) {
+  System &s = *(System *)h;
+  std::vector<signed char> o(occ, occ + s.n_sites);
+  return event_delta(s, o, n, sites, new_occ, dcount);
+}
+
+// occ_delta_per_supercell of the semi-grand canonical potential.
+double ora_delta_sgc(void *h, const signed char *occ, int n, const i64 *sites,
+                     const int *new_occ, const double *mu, i64 *dcount) {
+  System &s = *(System *)h;
+  std::vector<signed char> o(occ, occ + s.n_sites);
+  double de = event_delta(s, o, n, sites, new_occ, dcount);
+  return de - sgc_mu_term(s, mu, n, sites, new_occ, occ);
+}
+
+// Sequential Metropolis run (occupation_metropolis_v2 restated).
+// ensemble: 0 = semi-grand canonical (flip), 1 = canonical (swap).
+// Per step records (optional, may be null): site0, site1, dE, accept.
+// Samples are taken after every pass (steps_per_pass = n_sites).
+int ora_run(void *h, signed char *occ, int ensemble, double temperature, const double *mu,
+            u64 seed, i64 n_passes, i64 record_steps, i64 *rec_site0, i64 *rec_site1,
+            double *rec_de, unsigned char *rec_accept, double *samp_energy,
+            double *samp_potential, double *samp_comp, i64 *n_accept_out,
+            u64 *draws_out) {
+  try {
+    System &s = *(System *)h;
+    const double kb = 8.617333262e-5;
+    double beta = (std::fabs(temperature) < 1e-10) ? INFINITY : 1.0 / (kb * temperature);
+    Rng rng;
+    rng.eng.seed(seed);
+    OccLoc loc;
+    loc.init(occ, s.n_sites, s.n_occ);
+    std::vector<signed char> o(occ, occ + s.n_sites);
+    // swap types: SGC (a -> b) for all a != b; canonical (a, b) for a < b
+    std::vector<std::pair<int, int>> swaps;
+    for (int a = 0; a < s.n_occ; ++a)
+      for (int b = 0; b < s.n_occ; ++b) {
+        if (a == b) continue;
+        if (ensemble == 1 && b < a) continue;
+        swaps.push_back({a, b});
+      }
+    i64 steps_per_pass = s.n_sites;
+    i64 n_acc = 0, step = 0;
+    std::vector<i64> cnt(s.n_funcs);
+    i64 sites[2];
+    int nocc[2];
+    for (i64 pass = 0; pass < n_passes; ++pass) {
+      for (i64 st = 0; st < steps_per_pass; ++st, ++step) {
+        // propose
+        long tsum = 0;
+        std::vector<long> cum(swaps.size());
+        for (size_t i = 0; i < swaps.size(); ++i) {
+          long w = (long)loc.lists[swaps[i].first].size();
+          if (ensemble == 1) w *= (long)loc.lists[swaps[i].second].size();
+          tsum += w;
+          cum[i] = tsum;
+        }
+        if (tsum == 0) throw std::runtime_error("no event can be proposed");
+        long count = rng.random_int(tsum - 1);
+        size_t it = std::upper_bound(cum.begin(), cum.end(), count) - cum.begin();
+        int a = swaps[it].first, b = swaps[it].second;
+        int n;
+        if (ensemble == 1) {
+          long ia = rng.random_int((long)loc.lists[a].size() - 1);
+          long ib = rng.random_int((long)loc.lists[b].size() - 1);
+          sites[0] = loc.lists[a][ia];
+          sites[1] = loc.lists[b][ib];
+          nocc[0] = b;
+          nocc[1] = a;
+          n = 2;
+        } else {
+          long ia = rng.random_int((long)loc.lists[a].size() - 1);
+          sites[0] = loc.lists[a][ia];
+          nocc[0] = b;
+          n = 1;
+        }
+        double de = event_delta(s, o, n, sites, nocc, nullptr);
+        if (ensemble == 0) de -= sgc_mu_term(s, mu, n, sites, nocc, o.data());
+        bool acc = accept_metropolis(de, beta, rng);
+        if (step < record_steps) {
+          if (rec_site0) rec_site0[step] = sites[0];
+          if (rec_site1) rec_site1[step] = (n == 2) ? sites[1] : -1;
+          if (rec_de) rec_de[step] = de;
+          if (rec_accept) rec_accept[step] = acc ? 1 : 0;
+        }
+        if (acc) {
+          ++n_acc;
+          for (int i = 0; i < n; ++i) {
+            loc.move((int)sites[i], o[sites[i]], nocc[i]);
+            o[sites[i]] = (signed char)nocc[i];
+          }
+        }
+      }
+      // sample: potential_energy = potential.per_unitcell() (full recompute,
+      // sampling_functions.cc:274-283), param composition
+      all_counts(s, o.data(), cnt.data());
+      double ef = counts_to_energy(s, cnt.data());
+      std::vector<double> nk(s.n_occ, 0.0);
+      for (int l = 0; l < s.n_sites; ++l) nk[o[l]] += 1.0;
+      double pot = ef;
+      for (int a = 0; a < s.n_occ - 1; ++a) {
+        double x = 0.0;  // param composition per unit cell
+        for (int c = 0; c < s.n_occ; ++c) x += s.RT[a * s.n_occ + c] * (nk[c] - (c == 0 ? s.n_sites : 0));
+        x /= s.n_uc;
+        if (samp_comp) samp_comp[pass * (s.n_occ - 1) + a] = x;
+        if (ensemble == 0) pot -= s.n_uc * mu[a] * x;
+      }
+      if (samp_energy) samp_energy[pass] = ef / s.n_uc;
+      if (samp_potential) samp_potential[pass] = pot / s.n_uc;
+    }
+    std::memcpy(occ, o.data(), s.n_sites);
+    if (n_accept_out) *n_accept_out = n_acc;
+    if (draws_out) *draws_out = rng.draws;
+    return 0;
+  } catch (std::exception &e) {
+    g_err = e.what();
+    return 1;
+  }
+}
+
+// Many independent sequential chains on host threads (CPU baseline):
+// replica r uses occ + r*n_sites, seed + r, temperature[r], mu[r*(n_occ-1)].
+// Returns wall seconds; n_steps_out = total proposals.
+double ora_run_threads(void *h, signed char *occ, int n_rep, int ensemble, const double *temps,
+                       const double *mus, u64 seed, i64 n_passes, int n_threads,
+                       i64 *n_steps_out) {
+  System &s = *(System *)h;
+  auto t0 = std::chrono::steady_clock::now();
+  std::vector<std::thread> th;
+  int nt = std::max(1, std::min(n_threads, n_rep));
+  for (int w = 0; w < nt; ++w)
+    th.emplace_back([&, w]() {
+      for (int r = w; r < n_rep; r += nt) {
+        ora_run(h, occ + (size_t)r * s.n_sites, ensemble, temps[r], mus + r * (s.n_occ - 1),
+                seed + r, n_passes, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                nullptr, nullptr, nullptr);
+      }
+    });
+  for (auto &t : th) t.join();
+  auto t1 = std::chrono::steady_clock::now();
+  if (n_steps_out) *n_steps_out = (i64)n_rep * n_passes * s.n_sites;
+  return std::chrono::duration<double>(t1 - t0).count();
+}
+
+// ---- random-stream probes used to pin the transforms the GPU restates.
+void ora_mt19937_64(u64 seed, i64 n, u64 *out) {
+  std::mt19937_64 e(seed);
+  for (i64 i = 0; i < n; ++i) out[i] = e();
+}
+void ora_std_uniform_int(u64 seed, i64 n, const long *maxv, long *out, u64 *draws) {
+  Rng r;
+  r.eng.seed(seed);
+  for (i64 i = 0; i < n; ++i) out[i] = r.random_int(maxv[i]);
+  *draws = r.draws;
+}
+void ora_std_uniform_real(u64 seed, i64 n, double *out) {
+  Rng r;
+  r.eng.seed(seed);
+  for (i64 i = 0; i < n; ++i) out[i] = r.random_real(1.0);
+}
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+// easy as 1, 2, 3", SC 2011), written from the paper's round function.
+void ora_philox4x32_10(const unsigned *ctr_in, const unsigned *key_in, unsigned *out) {
+  unsigned c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
+  unsigned k0 = key_in[0], k1 = key_in[1];
+  for (int r = 0; r < 10; ++r) {
+    u64 p0 = (u64)0xD2511F53u * c0;
+    u64 p1 = (u64)0xCD9E8D57u * c2;
+    unsigned hi0 = (unsigned)(p0 >> 32), lo0 = (unsigned)p0;
+    unsigned hi1 = (unsigned)(p1 >> 32), lo1 = (unsigned)p1;
+    unsigned n0 = hi1 ^ c1 ^ k0;
+    unsigned n1 = lo1;
+    unsigned n2 = hi0 ^ c3 ^ k1;
+    unsigned n3 = lo0;
+    c0 = n0;
+    c1 = n1;
+    c2 = n2;
+    c3 = n3;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0;
+  out[1] = c1;
+  out[2] = c2;
+  out[3] = c3;
+}
+
+}  // extern "C"

@@ -1,0 +1,244 @@
+"""ctypes wrapper around the CPU FP64 oracle (``oracle/cem_oracle.cc``).
+
+TEST INFRASTRUCTURE ONLY: imported by ``tests/``, ``__graft_entry__.smoke()``
+and the CPU-baseline leg of ``bench.py`` as the checker. The product library
+never imports this module.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libcem_oracle.so")
+
+
+def build_oracle(force: bool = False) -> str:
+    """Compile the oracle with g++ (no cmake). Returns the library path."""
+    src = os.path.join(HERE, "cem_oracle.cc")
+    os.makedirs(BUILD, exist_ok=True)
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+        cmd = [
+            "g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
+            "-o", LIB, src, "-lpthread",
+        ]
+        subprocess.run(cmd, check=True)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build_oracle()
+        L = C.CDLL(LIB)
+        P = C.c_void_p
+        i64p = np.ctypeslib.ndpointer(np.int64, flags="C")
+        f64p = np.ctypeslib.ndpointer(np.float64, flags="C")
+        i32p = np.ctypeslib.ndpointer(np.int32, flags="C")
+        i8p = np.ctypeslib.ndpointer(np.int8, flags="C")
+        u64p = np.ctypeslib.ndpointer(np.uint64, flags="C")
+        u32p = np.ctypeslib.ndpointer(np.uint32, flags="C")
+        u8p = np.ctypeslib.ndpointer(np.uint8, flags="C")
+        L.ora_last_error.restype = C.c_char_p
+        L.ora_system_create.restype = P
+        L.ora_system_create.argtypes = [
+            C.c_int, i64p, i64p, C.c_double, C.c_int, f64p, C.c_int, i32p, i64p, i32p,
+            f64p, f64p, f64p, C.c_int, C.c_int, C.c_int,
+        ]
+        L.ora_system_destroy.argtypes = [P]
+        L.ora_n_sites.argtypes = [P]
+        L.ora_n_clusters.argtypes = [P]
+        L.ora_multiplicities.argtypes = [P, f64p]
+        L.ora_counts.argtypes = [P, i8p, i64p]
+        L.ora_energy.argtypes = [P, i8p]
+        L.ora_energy.restype = C.c_double
+        L.ora_corr.argtypes = [P, i8p, f64p]
+        L.ora_delta.argtypes = [P, i8p, C.c_int, i64p, i32p, i64p]
+        L.ora_delta.restype = C.c_double
+        L.ora_delta_sgc.argtypes = [P, i8p, C.c_int, i64p, i32p, f64p, i64p]
+        L.ora_delta_sgc.restype = C.c_double
+        L.ora_run.restype = C.c_int
+        L.ora_run.argtypes = [
+            P, i8p, C.c_int, C.c_double, f64p, C.c_uint64, C.c_int64, C.c_int64,
+            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+            C.c_void_p, C.c_void_p, C.c_void_p,
+        ]
+        L.ora_run_threads.restype = C.c_double
+        L.ora_run_threads.argtypes = [
+            P, i8p, C.c_int, C.c_int, f64p, f64p, C.c_uint64, C.c_int64, C.c_int,
+            C.POINTER(C.c_int64),
+        ]
+        L.ora_mt19937_64.argtypes = [C.c_uint64, C.c_int64, u64p]
+        L.ora_std_uniform_int.argtypes = [C.c_uint64, C.c_int64, i64p, i64p, u64p]
+        L.ora_std_uniform_real.argtypes = [C.c_uint64, C.c_int64, f64p]
+        L.ora_philox4x32_10.argtypes = [u32p, u32p, u32p]
+        _ = (u8p,)
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def composition_RT(n_basis: int, n_occ: int) -> np.ndarray:
+    """R^T (param composition per change of species counts) for the standard
+    axes: origin = all sites of species 0, end member k = all of species k."""
+    Q = np.zeros((n_occ, n_occ - 1))
+    for k in range(1, n_occ):
+        Q[0, k - 1] = -n_basis
+        Q[k, k - 1] = n_basis
+    return np.ascontiguousarray(np.linalg.pinv(Q))
+
+
+class OracleSystem:
+    """A cluster expansion on one supercell, evaluated by the oracle."""
+
+    def __init__(self, ce, L):
+        self.ce = ce
+        prim = ce.prim
+        self.L = tuple(int(x) for x in L)
+        nf = ce.n_funcs
+        size = np.zeros(nf, dtype=np.int32)
+        pts = np.zeros((nf, 4, 3), dtype=np.int64)
+        occ = np.zeros((nf, 4), dtype=np.int32)
+        for f in range(1, nf):
+            o = ce.orbits[ce.func_orbit[f]]
+            size[f] = o.size
+            pts[f, : o.size] = o.prototype
+            occ[f, : o.size] = np.array(ce.func_rep[f]) + 1
+        ml = np.zeros(5)
+        for k, v in ce.max_length.items():
+            ml[k] = v
+        self.RT = composition_RT(prim.n_basis, prim.n_occ)
+        h = lib().ora_system_create(
+            prim.n_basis,
+            np.ascontiguousarray(prim.lattice.reshape(-1), dtype=np.int64),
+            np.ascontiguousarray(prim.basis.reshape(-1), dtype=np.int64),
+            float(prim.grid),
+            prim.n_occ,
+            ml,
+            nf,
+            size,
+            np.ascontiguousarray(pts.reshape(-1)),
+            np.ascontiguousarray(occ.reshape(-1)),
+            np.ascontiguousarray(ce.eci, dtype=np.float64),
+            np.ascontiguousarray(ce.func_coeff, dtype=np.float64),
+            np.ascontiguousarray(self.RT.reshape(-1)),
+            *self.L,
+        )
+        if not h:
+            raise RuntimeError(lib().ora_last_error().decode())
+        self.h = h
+        self.n_sites = lib().ora_n_sites(h)
+        self.n_uc = self.L[0] * self.L[1] * self.L[2]
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ora_system_destroy(self.h)
+            self.h = None
+
+    def multiplicities(self):
+        out = np.zeros(self.ce.n_funcs)
+        lib().ora_multiplicities(self.h, out)
+        return out
+
+    def counts(self, occ):
+        out = np.zeros(self.ce.n_funcs, dtype=np.int64)
+        lib().ora_counts(self.h, np.ascontiguousarray(occ, dtype=np.int8), out)
+        return out
+
+    def energy(self, occ) -> float:
+        return lib().ora_energy(self.h, np.ascontiguousarray(occ, dtype=np.int8))
+
+    def corr(self, occ):
+        out = np.zeros(self.ce.n_funcs)
+        lib().ora_corr(self.h, np.ascontiguousarray(occ, dtype=np.int8), out)
+        return out
+
+    def delta(self, occ, sites, new_occ, mu=None):
+        sites = np.ascontiguousarray(sites, dtype=np.int64)
+        new_occ = np.ascontiguousarray(new_occ, dtype=np.int32)
+        dc = np.zeros(self.ce.n_funcs, dtype=np.int64)
+        o = np.ascontiguousarray(occ, dtype=np.int8)
+        if mu is None:
+            de = lib().ora_delta(self.h, o, len(sites), sites, new_occ, dc)
+        else:
+            de = lib().ora_delta_sgc(
+                self.h, o, len(sites), sites, new_occ,
+                np.ascontiguousarray(mu, dtype=np.float64), dc,
+            )
+        return de, dc
+
+    def run(self, occ, ensemble, temperature, mu, seed, n_passes, record_steps=0):
+        """Sequential Metropolis chain. ``occ`` is updated in place."""
+        n = self.n_sites
+        nc = self.ce.prim.n_occ - 1
+        rs0 = np.zeros(record_steps, dtype=np.int64)
+        rs1 = np.zeros(record_steps, dtype=np.int64)
+        rde = np.zeros(record_steps, dtype=np.float64)
+        racc = np.zeros(record_steps, dtype=np.uint8)
+        se = np.zeros(n_passes)
+        sp = np.zeros(n_passes)
+        scomp = np.zeros((n_passes, nc))
+        nacc = np.zeros(1, dtype=np.int64)
+        draws = np.zeros(1, dtype=np.uint64)
+        mu = np.zeros(nc) if mu is None else np.ascontiguousarray(mu, dtype=np.float64)
+        assert occ.dtype == np.int8 and occ.flags.c_contiguous and occ.size == n
+        rc = lib().ora_run(
+            self.h, occ, int(ensemble), float(temperature), mu, int(seed), int(n_passes),
+            int(record_steps), _ptr(rs0), _ptr(rs1), _ptr(rde), _ptr(racc), _ptr(se),
+            _ptr(sp), _ptr(scomp), _ptr(nacc), _ptr(draws),
+        )
+        if rc:
+            raise RuntimeError(lib().ora_last_error().decode())
+        return dict(
+            site0=rs0, site1=rs1, dE=rde, accept=racc, energy=se, potential=sp,
+            comp=scomp, n_accept=int(nacc[0]), draws=int(draws[0]),
+        )
+
+    def run_threads(self, occ, ensemble, temps, mus, seed, n_passes, n_threads):
+        nrep = len(temps)
+        nsteps = C.c_int64(0)
+        secs = lib().ora_run_threads(
+            self.h, occ, nrep, int(ensemble), np.ascontiguousarray(temps, dtype=np.float64),
+            np.ascontiguousarray(mus, dtype=np.float64).reshape(-1), int(seed), int(n_passes),
+            int(n_threads), C.byref(nsteps),
+        )
+        return secs, nsteps.value
+
+
+def mt19937_64(seed: int, n: int) -> np.ndarray:
+    out = np.zeros(n, dtype=np.uint64)
+    lib().ora_mt19937_64(seed, n, out)
+    return out
+
+
+def std_uniform_int(seed: int, maxv) -> tuple:
+    maxv = np.ascontiguousarray(maxv, dtype=np.int64)
+    out = np.zeros(len(maxv), dtype=np.int64)
+    draws = np.zeros(1, dtype=np.uint64)
+    lib().ora_std_uniform_int(seed, len(maxv), maxv, out, draws)
+    return out, int(draws[0])
+
+
+def std_uniform_real(seed: int, n: int) -> np.ndarray:
+    out = np.zeros(n)
+    lib().ora_std_uniform_real(seed, n, out)
+    return out
+
+
+def philox4x32_10(ctr, key) -> np.ndarray:
+    out = np.zeros(4, dtype=np.uint32)
+    lib().ora_philox4x32_10(
+        np.ascontiguousarray(ctr, dtype=np.uint32), np.ascontiguousarray(key, dtype=np.uint32), out
+    )
+    return out
