@@ -1,0 +1,369 @@
+#!/usr/bin/env python3
+"""Throughput of the GPU Metropolis hot path on the canonical FCC workload
+(128 replicas of a 24x24x24 FCC A/B supercell, T in [200, 1200] K x
+x_B in {0.25, 0.5}), printed as one JSON line.
+
+A step is one Metropolis pass over every replica of the batch (each pass
+proposes about one pair swap per site). The timed region runs K passes in
+one persistent launch with occupations resident in shared memory; `value`
+is real swap proposals (pairs of different species) per second from CUDA
+events on the launching stream. `e2e` runs steps through the C ABI with
+host buffers: copy occupations in, one pass, copy occupations out.
+
+--impl reference runs the CPU restatement of the reference loop (one
+sequential std::mt19937_64 chain per host thread) on a bounded sample of the
+same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD_INDEX = 1
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+        return ws, rank, local, dist
+    return 1, 0, 0, None
+
+
+def reduce_max(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64,
+                     device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64,
+                     device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.gpu = gpu_index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.p is not None:
+            time.sleep(0.3)
+            self.p.terminate()
+            try:
+                self.p.wait(5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self) -> dict:
+        self.f.flush()
+        rows = []
+        try:
+            for line in open(self.f.name):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                    rows.append(parts)
+        except OSError:
+            pass
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(float(r[2]) for r in rows),
+                "reasons": sorted(reasons), "samples": len(rows),
+                "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())
+                if any(r[3].replace(".", "").isdigit() for r in rows) else None}
+
+
+def load_workload():
+    from casmcode_clexmonte_gb300 import workloads
+
+    return workloads.config(WORKLOAD_INDEX)
+
+
+def workload_config(w, extra=None) -> dict:
+    c = {
+        "workload": w.name,
+        "replicas": w.n_replicas,
+        "sites_per_replica": int(w.n_sites[0]),
+        "lattice": "FCC a=4.0 A, 24x24x24 primitive cells",
+        "cluster_expansion": "7 functions: empty, point, pairs to NN3, triplets to NN2",
+        "ensemble": "canonical (pair swaps)",
+        "temperatures_K": [float(w.temperature.min()), float(w.temperature.max())],
+        "x_B": sorted(set(float(x) for x in w.x_b)),
+        "mode": "parallel (colour classes of non-interacting sites)",
+        "step": "one Metropolis pass over every replica",
+        "l2": "flushed (256 MiB write) before the timed launch; occupations stay in "
+              "shared memory for the whole launch",
+    }
+    if extra:
+        c.update(extra)
+    return c
+
+
+def cpu_baseline(w, n_threads: int, target_s: float = 12.0) -> dict:
+    """Oracle (CPU restatement of the reference loop) on a bounded sample."""
+    from oracle import oracle
+
+    oracle.build_oracle()
+    o = oracle.OracleSystem(w.ce, w.L[0])
+    n = min(n_threads, w.n_replicas)
+    occ = np.concatenate([w.occupation[i] for i in range(n)]).astype(np.int8)
+    temps = w.temperature[:n].copy()
+    mus = np.zeros((n, 1))
+    secs, steps = o.run_threads(occ.copy(), 1, temps, mus, 7, 1, n)  # probe
+    rate = steps / max(secs, 1e-9)
+    passes = max(1, int(target_s * rate / (n * int(w.n_sites[0]))))
+    secs, steps = o.run_threads(occ.copy(), 1, temps, mus, 11, passes, n)
+    return {
+        "value": steps / secs, "unit": "proposals/s", "cores": n, "kind": "port",
+        "sample": f"{n} replicas x {passes} passes of the 24^3 canonical workload, one "
+                  f"sequential std::mt19937_64 chain per host thread ({secs:.1f} s)",
+        "seconds": secs,
+    }
+
+
+def run_reference(args):
+    ws, rank, local, dist = dist_init()
+    if rank != 0:
+        barrier(dist)
+        return 0
+    w = load_workload()
+    from oracle import oracle
+
+    oracle.build_oracle()
+    o = oracle.OracleSystem(w.ce, w.L[0])
+    cores = os.cpu_count() or 1
+    n = min(cores, w.n_replicas)
+    occ = np.concatenate([w.occupation[i] for i in range(n)]).astype(np.int8)
+    temps = w.temperature[:n].copy()
+    mus = np.zeros((n, 1))
+    # warm-up steps, then K timed steps; a step = one pass over the sample
+    o.run_threads(occ, 1, temps, mus, 3, args.warmup, n)
+    secs, steps = o.run_threads(occ, 1, temps, mus, 5, args.steps, n)
+    value = steps / secs
+    line = {
+        "impl": "reference", "metric": "proposals/s", "value": value, "unit": "proposals/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(w, {"sample_replicas": n, "step": "one pass over the sample"}),
+        "cpu_baseline": {"value": value, "unit": "proposals/s", "cores": n, "kind": "port",
+                         "sample": f"{n} of {w.n_replicas} replicas (one per host thread), "
+                                   f"{args.steps} passes; CPU FP64 restatement of "
+                                   "occupation_metropolis_v2 (the reference needs "
+                                   "libcasm-clexulator/libcasm-monte, absent offline)"},
+        "e2e": {"value": value, "unit": "proposals/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    barrier(dist)
+    return 0
+
+
+def run_gb300(args):
+    ws, rank, local, dist = dist_init()
+    import ctypes as C
+
+    import torch
+
+    from casmcode_clexmonte_gb300 import build as B
+
+    B.build()
+    from casmcode_clexmonte_gb300 import _lib
+    from casmcode_clexmonte_gb300 import calculator as cm
+    from casmcode_clexmonte_gb300.stats import tau_int
+
+    if not torch.cuda.is_available():
+        raise RuntimeError("no CUDA device: the GPU path has no CPU fallback")
+    torch.cuda.set_device(local)
+    w = load_workload()
+    sysd = cm.System(w.ce)
+    batch = cm.ReplicaBatch(sysd, "canonical", w.L)
+    for i in range(w.n_replicas):
+        batch.set_conditions(i, float(w.temperature[i]))
+        batch.set_seed(i, int(w.seeds[i]) + 7919 * rank)
+    packed = np.concatenate(w.occupation).astype(np.int8)
+    batch.set_occupation_all(packed)
+    lib = _lib.load()
+    smem = C.c_double()
+    _lib.check(lib.cem_smem_bandwidth(C.byref(smem)))
+    smem_gbs = smem.value
+
+    # warm-up
+    batch.run(args.warmup, 0)
+    batch.synchronize()
+    before = [batch.stats(i) for i in range(w.n_replicas)]
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    flush.fill_(1)
+    torch.cuda.synchronize()
+    barrier(dist)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        batch.run(args.steps, 0, record_samples=True)
+        batch.synchronize()
+        t1 = time.perf_counter()
+    torch.cuda.synchronize()
+    kernel_ms = batch.kernel_ms()
+    after = [batch.stats(i) for i in range(w.n_replicas)]
+    props = sum(a["n_proposed"] - b["n_proposed"] for a, b in zip(after, before))
+    accs = sum(a["n_accepted"] - b["n_accepted"] for a, b in zip(after, before))
+    t_dev = reduce_max(dist, kernel_ms / 1e3)
+    props_all = reduce_sum(dist, props)
+    value = props_all / t_dev
+    # effective independent samples of the potential energy per pass
+    n_eff = 0.0
+    taus = []
+    for i in range(w.n_replicas):
+        pot, _ = batch.samples(i, args.steps)
+        t = tau_int(pot) if pot.size > 16 else float("nan")
+        taus.append(t)
+        if np.isfinite(t):
+            n_eff += pot.size / (2.0 * t)
+    n_eff = reduce_sum(dist, n_eff)
+
+    # end-to-end through the C ABI with pinned host buffers
+    nbytes = int(packed.size)
+    hp = C.c_void_p()
+    _lib.check(lib.cem_host_alloc(nbytes, C.byref(hp)))
+    host = np.ctypeslib.as_array((C.c_int8 * nbytes).from_address(hp.value))
+    batch.get_occupation_all(host)
+    e2e_steps = max(3, min(args.steps, 200))
+    e_before = sum(batch.stats(i)["n_proposed"] for i in range(w.n_replicas))
+    barrier(dist)
+    t2 = time.perf_counter()
+    for _ in range(e2e_steps):
+        batch.set_occupation_all(host)
+        batch.run(1, 0)
+        batch.get_occupation_all(host)
+    t3 = time.perf_counter()
+    e_after = sum(batch.stats(i)["n_proposed"] for i in range(w.n_replicas))
+    e2e_time = reduce_max(dist, t3 - t2)
+    e2e_props = reduce_sum(dist, e_after - e_before)
+    _lib.check(lib.cem_host_free(hp))
+
+    p_acc = accs / max(props, 1)
+    z = 42  # distinct flower sites of an FCC site (12 + 6 + 24)
+    bytes_per_prop = 2 * (1 + z) + 2 * p_acc
+    achieved = props * bytes_per_prop / (kernel_ms / 1e3) / 1e9
+    clocks = clk.summary()
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "k_sweep_fcc24_canonical_dram.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("dram_bytes_per_launch_scaled")
+        except (OSError, ValueError):
+            traffic = None
+    line = {
+        "metric": "proposals/s", "value": value, "unit": "proposals/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": workload_config(w, {
+            "arithmetic": "int8 occupations, integer delta correlations, float-float "
+                          "(2 x f32) ECI dot, f32 acceptance, f64 running energy",
+            "parallelism": f"replicas only, {w.n_replicas} per GPU",
+        }),
+        "proposals": int(props_all), "acceptance": p_acc,
+        "effective_samples_per_s": n_eff / t_dev,
+        "tau_int_potential_median": float(np.nanmedian(taus)),
+        "host_wall_s": t1 - t0,
+        "e2e": {"value": e2e_props / e2e_time, "unit": "proposals/s",
+                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                "steps": e2e_steps},
+        "roofline": {"bound": "smem", "achieved": achieved, "peak": smem_gbs, "unit": "GB/s",
+                     "frac": achieved / smem_gbs, "traffic": traffic,
+                     "peak_source": "measured in this run by cem_smem_bandwidth "
+                                    "(16-byte shared loads, all SMs)",
+                     "bytes_per_proposal": bytes_per_prop,
+                     "kernel": "k_sweep<2>", "kernel_ms": kernel_ms},
+        "gpu_launches": 1,
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w, os.cpu_count() or 1)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    barrier(dist)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

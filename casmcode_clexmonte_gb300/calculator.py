@@ -1,0 +1,317 @@
+"""Host-side mirror of the ``libcasm.clexmonte`` calculator interface for the
+Metropolis hot path, driving the CUDA library through its C ABI.
+
+Reference interface (paths relative to the CASMcode_clexmonte tree):
+
+* ``MonteCalculator(method, system, params)`` with
+  ``method in {"canonical", "semigrand_canonical"}``
+  (``python/libcasm/clexmonte/_MonteCalculator.py:24-95``);
+* ``MonteCalculator.set_state_and_potential``, ``.potential``,
+  ``.run_fixture`` (``python/src/clexmonte_monte_calculator.cpp:2106-2145``);
+* ``MontePotential(calculator, state)`` with ``per_supercell``,
+  ``per_unitcell`` and ``occ_delta_per_supercell(linear_site_index, new_occ)``
+  (``python/src/clexmonte_monte_calculator.cpp:694-750``);
+* ``MonteCarloState(configuration, conditions)`` with conditions
+  ``temperature`` and ``param_chem_pot`` (SGC) or ``param_composition``
+  (canonical) (``python/tests/semigrand_canonical/
+  test_SemiGrandCanonicalCalculator.py:23-31``);
+* analyses ``heat_capacity``, ``param_susc`` and ``param_thermochem_susc``
+  (``src/casm/clexmonte/monte_calculator/analysis_functions.cc:17-173``).
+
+Errors are raised as exceptions with the library's message, as the
+reference's calculators throw ``std::runtime_error``
+(``CanonicalCalculator.cc:380-390``).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import CEM_CANONICAL, CEM_SEMIGRAND_CANONICAL, check, ptr
+from .system import KB, ClusterExpansion, composition_RT, system_arrays
+
+METHODS = {"semigrand_canonical": CEM_SEMIGRAND_CANONICAL, "canonical": CEM_CANONICAL}
+
+
+class System:
+    """A cluster expansion uploaded to the GPU (the role of
+    ``libcasm.clexmonte.System`` for the formation-energy clex)."""
+
+    def __init__(self, ce: ClusterExpansion):
+        self.ce = ce
+        self.lib = _lib.load()
+        self.arrays = system_arrays(ce)
+        desc, self._keep = _lib.make_desc(self.arrays)
+        h = C.c_void_p()
+        check(self.lib.cem_system_create(C.byref(desc), C.byref(h)))
+        self.handle = h
+        self.n_occ = ce.prim.n_occ
+        self.n_funcs = ce.n_funcs
+        self.RT = composition_RT(ce.prim.n_basis, ce.prim.n_occ)
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            self.lib.cem_system_destroy(h)
+            self.handle = None
+
+
+class ReplicaBatch:
+    """Replicas of one ensemble resident on the GPU (occupations in HBM)."""
+
+    def __init__(self, system: System, ensemble: str, L):
+        self.system = system
+        self.lib = system.lib
+        self.ensemble = ensemble
+        self.L = [tuple(int(x) for x in l) for l in L]
+        Ls = np.ascontiguousarray(np.array(self.L, dtype=np.int32).reshape(-1))
+        h = C.c_void_p()
+        check(self.lib.cem_replicas_create(system.handle, len(self.L), _lib.iptr(Ls),
+                                           METHODS[ensemble], C.byref(h)))
+        self.handle = h
+        self.n = len(self.L)
+        nb = system.ce.prim.n_basis
+        self.n_sites = np.array([nb * l[0] * l[1] * l[2] for l in self.L], dtype=np.int64)
+        self.offsets = np.concatenate([[0], np.cumsum(self.n_sites)])
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            self.lib.cem_replicas_destroy(h)
+            self.handle = None
+
+    def set_conditions(self, i: int, temperature: float, param_chem_pot=None):
+        mu = None
+        if param_chem_pot is not None:
+            mu = np.ascontiguousarray(param_chem_pot, dtype=np.float64)
+        check(self.lib.cem_set_conditions(self.handle, i, float(temperature),
+                                          None if mu is None else _lib.dptr(mu)))
+
+    def set_seed(self, i: int, seed: int):
+        check(self.lib.cem_set_seed(self.handle, i, int(seed) & (2**64 - 1)))
+
+    def set_occupation(self, i: int, occ):
+        occ = np.ascontiguousarray(occ, dtype=np.int8)
+        if occ.size != self.n_sites[i]:
+            raise ValueError(f"occupation has {occ.size} sites, expected {self.n_sites[i]}")
+        check(self.lib.cem_set_occupation(self.handle, i, ptr(occ)))
+
+    def get_occupation(self, i: int) -> np.ndarray:
+        out = np.zeros(self.n_sites[i], dtype=np.int8)
+        check(self.lib.cem_get_occupation(self.handle, i, ptr(out)))
+        return out
+
+    def set_occupation_all(self, packed: np.ndarray):
+        assert packed.dtype == np.int8 and packed.size == self.offsets[-1]
+        check(self.lib.cem_set_occupation_all(self.handle, ptr(packed)))
+
+    def get_occupation_all(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.zeros(self.offsets[-1], dtype=np.int8)
+        check(self.lib.cem_get_occupation_all(self.handle, ptr(out)))
+        return out
+
+    def energy(self, i: int):
+        e = C.c_double()
+        counts = np.zeros(self.system.n_funcs, dtype=np.int64)
+        check(self.lib.cem_energy(self.handle, i, C.byref(e), ptr(counts)))
+        return e.value, counts
+
+    def delta(self, i: int, sites, new_occ, potential: bool = False):
+        sites = np.ascontiguousarray(np.atleast_2d(sites), dtype=np.int64)
+        new_occ = np.ascontiguousarray(np.atleast_2d(new_occ), dtype=np.int32)
+        if sites.shape != new_occ.shape:
+            raise ValueError("sites and new_occ must have the same shape")
+        n_events, k = sites.shape
+        dE = np.zeros(n_events)
+        dc = np.zeros((n_events, self.system.n_funcs), dtype=np.int64)
+        check(self.lib.cem_delta_energy(self.handle, i, n_events, k, ptr(sites), ptr(new_occ),
+                                        int(bool(potential)), ptr(dE), ptr(dc)))
+        return dE, dc
+
+    def replay(self, i: int, mt_seed: int, n_steps: int, record: bool = True):
+        acc = np.zeros(n_steps, dtype=np.uint8) if record else None
+        de = np.zeros(n_steps) if record else None
+        sites = np.zeros((n_steps, 2), dtype=np.int64) if record else None
+        n_acc = C.c_int64()
+        draws = C.c_uint64()
+        check(self.lib.cem_replay(self.handle, i, int(mt_seed), int(n_steps), ptr(acc), ptr(de),
+                                  ptr(sites), C.byref(n_acc), C.byref(draws)))
+        return dict(accept=acc, dE=de, sites=sites, n_accept=n_acc.value, draws=draws.value)
+
+    def run(self, n_passes: int, n_equil: int = 0, record_samples: bool = False):
+        check(self.lib.cem_run(self.handle, int(n_passes), int(n_equil), int(bool(record_samples))))
+
+    def synchronize(self):
+        check(self.lib.cem_synchronize(self.handle))
+
+    def kernel_ms(self) -> float:
+        ms = C.c_double()
+        check(self.lib.cem_last_kernel_ms(self.handle, C.byref(ms)))
+        return ms.value
+
+    def reset_stats(self):
+        check(self.lib.cem_reset_stats(self.handle))
+
+    def stats(self, i: int) -> dict:
+        s = _lib.Stats()
+        check(self.lib.cem_get_stats(self.handle, i, C.byref(s)))
+        nc = self.system.n_occ - 1
+        return dict(
+            n_samples=s.n_samples, mean_potential=s.mean_potential,
+            var_potential=s.var_potential, mean_formation=s.mean_formation,
+            mean_comp=np.array(s.mean_comp[:nc]),
+            cov_comp=np.array(s.cov_comp[:]).reshape(3, 3)[:nc, :nc],
+            cov_e_comp=np.array(s.cov_e_comp[:nc]), energy=s.energy,
+            n_proposed=s.n_proposed, n_accepted=s.n_accepted, passes=s.passes,
+        )
+
+    def samples(self, i: int, capacity: int):
+        nc = self.system.n_occ - 1
+        pot = np.zeros(capacity)
+        comp = np.zeros((capacity, nc))
+        n = C.c_int64()
+        check(self.lib.cem_get_samples(self.handle, i, ptr(pot), ptr(comp), int(capacity),
+                                       C.byref(n)))
+        return pot[: n.value], comp[: n.value]
+
+
+@dataclass
+class MonteCarloState:
+    """Occupation of a diagonal supercell plus thermodynamic conditions."""
+
+    occupation: np.ndarray
+    L: tuple
+    conditions: dict = field(default_factory=dict)
+
+
+@dataclass
+class SamplingFixtureParams:
+    """Fixed-length sampling: ``n_passes`` passes, statistics over the
+    passes after the first ``n_equil`` (one sample per pass, like a
+    sampling period of one pass in the reference's fixtures)."""
+
+    n_passes: int = 1000
+    n_equil: int = 200
+    record_samples: bool = True
+
+
+def analyses(stats: dict, temperature: float, n_unitcells: int) -> dict:
+    """Heat capacity and susceptibilities per unit cell from the sampled
+    moments (analysis_functions.cc:17-173; variances and covariances are
+    population moments of the sampled tail)."""
+    beta_norm = KB * temperature
+    return dict(
+        heat_capacity=stats["var_potential"] * n_unitcells / (KB * temperature * temperature),
+        param_susc=stats["cov_comp"] * n_unitcells / beta_norm,
+        param_thermochem_susc=stats["cov_e_comp"] * n_unitcells / beta_norm,
+    )
+
+
+class MontePotential:
+    """Potential of one state: canonical (formation energy) or semi-grand
+    canonical (formation energy - n_unitcells * param_chem_pot . x)."""
+
+    def __init__(self, calculator: "MonteCalculator", state: MonteCarloState):
+        self.calculator = calculator
+        self.state = state
+        calculator._bind(state)
+
+    @property
+    def _batch(self) -> ReplicaBatch:
+        return self.calculator._batch
+
+    def _n_uc(self) -> int:
+        L = self.state.L
+        return int(L[0] * L[1] * L[2])
+
+    def per_supercell(self) -> float:
+        e, _ = self._batch.energy(0)
+        if self.calculator.method == "semigrand_canonical":
+            occ = np.asarray(self.state.occupation)
+            n_sites = occ.size
+            counts = np.bincount(occ, minlength=self.calculator.system.n_occ).astype(float)
+            dn = counts.copy()
+            dn[0] -= n_sites
+            x = self.calculator.system.RT @ dn / self._n_uc()
+            mu = np.asarray(self.state.conditions["param_chem_pot"], dtype=float)
+            e -= self._n_uc() * float(mu @ x)
+        return e
+
+    def per_unitcell(self) -> float:
+        return self.per_supercell() / self._n_uc()
+
+    def occ_delta_per_supercell(self, linear_site_index, new_occ) -> float:
+        dE, _ = self._batch.delta(
+            0, np.asarray(linear_site_index).reshape(1, -1), np.asarray(new_occ).reshape(1, -1),
+            potential=self.calculator.method == "semigrand_canonical",
+        )
+        return float(dE[0])
+
+
+class MonteCalculator:
+    """GPU Metropolis calculator for ``method`` in {"canonical",
+    "semigrand_canonical"}. ``params`` may hold ``seed`` (counter-based
+    stream of the parallel sweep)."""
+
+    def __init__(self, method: str, system: System, params: dict | None = None):
+        if method not in METHODS:
+            raise ValueError(f"Unknown method: '{method}'. Options are: {list(METHODS)}")
+        self.method = method
+        self.system = system
+        self.params = dict(params or {})
+        self._batch: ReplicaBatch | None = None
+        self._state: MonteCarloState | None = None
+        self.potential: MontePotential | None = None
+
+    def _check_conditions(self, state: MonteCarloState):
+        c = state.conditions
+        if "temperature" not in c:
+            raise ValueError("state conditions need 'temperature'")
+        if self.method == "semigrand_canonical" and "param_chem_pot" not in c:
+            raise ValueError("semi-grand canonical states need 'param_chem_pot'")
+
+    def _bind(self, state: MonteCarloState):
+        self._check_conditions(state)
+        L = tuple(int(x) for x in state.L)
+        if self._batch is None or self._batch.L[0] != L:
+            self._batch = ReplicaBatch(self.system, self.method, [L])
+        b = self._batch
+        mu = state.conditions.get("param_chem_pot") if self.method == "semigrand_canonical" else None
+        b.set_conditions(0, state.conditions["temperature"], mu)
+        b.set_seed(0, int(self.params.get("seed", 0x5EED)))
+        b.set_occupation(0, state.occupation)
+        self._state = state
+
+    def set_state_and_potential(self, state: MonteCarloState):
+        self.potential = MontePotential(self, state)
+        return self.potential
+
+    def replay(self, state: MonteCarloState, mt_seed: int, n_steps: int, record: bool = True):
+        """Sequential reference-order Metropolis steps on the GPU; updates
+        ``state.occupation``."""
+        self._bind(state)
+        out = self._batch.replay(0, mt_seed, n_steps, record)
+        state.occupation[:] = self._batch.get_occupation(0)
+        return out
+
+    def run_fixture(self, state: MonteCarloState, sampling_fixture_params: SamplingFixtureParams):
+        """Parallel Metropolis run; updates ``state.occupation`` and returns
+        the sampled statistics and analyses."""
+        p = sampling_fixture_params
+        self._bind(state)
+        b = self._batch
+        b.run(p.n_passes, p.n_equil, p.record_samples)
+        st = b.stats(0)
+        state.occupation[:] = b.get_occupation(0)
+        L = state.L
+        n_uc = int(L[0] * L[1] * L[2])
+        res = dict(st)
+        res.update(analyses(st, state.conditions["temperature"], n_uc))
+        if p.record_samples:
+            res["samples_potential"], res["samples_comp"] = b.samples(0, p.n_passes)
+        return res

@@ -1,0 +1,802 @@
+// C ABI of the GB300 Metropolis hot path: object lifetimes, validation,
+// transfers and launches. See include/cem.h for the contract.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/cem.h"
+#include "cem_common.cuh"
+#include "cem_internal.h"
+
+using namespace cem;
+
+namespace {
+
+thread_local std::string g_error;
+
+struct Err : std::runtime_error {
+  int code;
+  Err(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+#define CUDA_OK(x)                                                                    \
+  do {                                                                                \
+    cudaError_t e_ = (x);                                                             \
+    if (e_ != cudaSuccess)                                                            \
+      throw Err(CEM_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));      \
+  } while (0)
+
+template <class F>
+int guard(F &&f) {
+  try {
+    f();
+    return CEM_OK;
+  } catch (Err &e) {
+    g_error = e.what();
+    return e.code;
+  } catch (std::exception &e) {
+    g_error = e.what();
+    return CEM_ERR_INVALID;
+  }
+}
+
+void require(bool ok, const std::string &msg, int code = CEM_ERR_INVALID) {
+  if (!ok) throw Err(code, msg);
+}
+
+template <class T>
+T *dev_copy(const std::vector<T> &v) {
+  T *p = nullptr;
+  if (v.empty()) return nullptr;
+  CUDA_OK(cudaMalloc(&p, sizeof(T) * v.size()));
+  CUDA_OK(cudaMemcpy(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+  return p;
+}
+
+const double KB = 8.617333262e-5;  // eV/K
+
+// block colouring of a ring of length L with blocks of size >= p
+std::vector<int> axis_blocks(int L, int p) {
+  int q = L / p;
+  if (q == 0) return {};
+  std::vector<int> sizes(q, p);
+  int extra = L - q * p;
+  for (int r = 0; r < extra; ++r) sizes[r % q] += 1;
+  std::vector<int> col;
+  for (int s : sizes)
+    for (int t = 0; t < s; ++t) col.push_back(t);
+  return col;
+}
+
+}  // namespace
+
+struct cem_system {
+  CeTables T{};
+  int n_flower = 0, n_owned = 0;
+  std::vector<double> w;
+  std::vector<double> RT;
+  // host copies used for colouring checks
+  std::vector<int> fl_sub, fl_pb, fl_du;
+  int nb_reach = 0;
+  std::vector<void *> owned;
+  ~cem_system() {
+    for (void *p : owned) cudaFree(p);
+  }
+};
+
+struct cem_replicas {
+  const cem_system *sys = nullptr;
+  int n = 0, ensemble = 0;
+  std::vector<Replica> reps;
+  std::vector<ReplicaStats> stats_host;
+  Replica *d_reps = nullptr;
+  ReplicaStats *d_stats = nullptr;
+  int8_t *d_occ = nullptr;
+  int64_t total_sites = 0;
+  unsigned long long *d_counts = nullptr;  // scratch [n_funcs]
+  long long *d_result = nullptr;
+  double *d_samples = nullptr;
+  long long sample_capacity = 0;
+  int sample_width = 1;
+  long long n_samples_recorded = 0;
+  int max_classes = 1, sweep_smem = 0;
+  bool reps_dirty = true, stats_valid = false;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0.0;
+  ~cem_replicas() {
+    cudaFree(d_reps);
+    cudaFree(d_stats);
+    cudaFree(d_occ);
+    cudaFree(d_counts);
+    cudaFree(d_result);
+    cudaFree(d_samples);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (stream) cudaStreamDestroy(stream);
+  }
+  void upload_reps() {
+    if (!reps_dirty) return;
+    CUDA_OK(cudaMemcpyAsync(d_reps, reps.data(), sizeof(Replica) * n, cudaMemcpyHostToDevice,
+                            stream));
+    reps_dirty = false;
+  }
+};
+
+namespace {
+
+// smallest block size whose colour classes hold no two interacting sites;
+// canonical local pair moves also need 2p - reach(neighbour) > reach(flower)
+int choose_colouring(const cem_system &s, const int L[3], int ensemble) {
+  const CeTables &T = s.T;
+  const int n_uc = L[0] * L[1] * L[2];
+  for (int p = 2; p <= 8; ++p) {
+    std::vector<int> col[3];
+    bool ok = true;
+    int ncol[3];
+    for (int a = 0; a < 3; ++a) {
+      col[a] = axis_blocks(L[a], p);
+      if (col[a].empty()) ok = false;
+      else ncol[a] = *std::max_element(col[a].begin(), col[a].end()) + 1;
+      if (ok && ncol[a] > MAX_COLOURS) ok = false;
+    }
+    if (!ok) break;
+    if (ensemble == CEM_CANONICAL && 2 * p - s.nb_reach <= T.reach) continue;
+    auto cls = [&](int b, int x, int y, int z) {
+      return b * ncol[0] * ncol[1] * ncol[2] + col[0][x] + ncol[0] * (col[1][y] + ncol[1] * col[2][z]);
+    };
+    auto wr = [](int x, int Lx) { return ((x % Lx) + Lx) % Lx; };
+    for (int b = 0; b < T.n_sublat && ok; ++b)
+      for (int z = 0; z < L[2] && ok; ++z)
+        for (int y = 0; y < L[1] && ok; ++y)
+          for (int x = 0; x < L[0] && ok; ++x) {
+            const int c0 = cls(b, x, y, z);
+            const int l0 = b * n_uc + x + L[0] * (y + L[1] * z);
+            for (int c = T.fl_begin[b][0]; c < T.fl_begin[b][T.n_orbits] && ok; ++c)
+              for (int q = 0; q < 3; ++q) {
+                const int pb = s.fl_pb[c * 3 + q];
+                if (pb < 0) continue;
+                const int *du = &s.fl_du[c * 9 + q * 3];
+                const int px = wr(x + du[0], L[0]), py = wr(y + du[1], L[1]), pz = wr(z + du[2], L[2]);
+                const int l1 = pb * n_uc + px + L[0] * (py + L[1] * pz);
+                if (l1 == l0)
+                  throw Err(CEM_ERR_INVALID,
+                            "supercell too small: a cluster contains one site twice");
+                if (cls(pb, px, py, pz) == c0) ok = false;
+              }
+          }
+    if (ok) return p;
+  }
+  throw Err(CEM_ERR_UNSUPPORTED, "no valid site colouring for this supercell");
+}
+
+void check_rep(const cem_replicas *r, int i) {
+  require(r != nullptr, "null replicas handle");
+  require(i >= 0 && i < r->n, "replica index out of range");
+}
+
+void set_dmu(const cem_system &s, Replica &R) {
+  const int no = s.T.n_occ;
+  for (int a = 0; a < 16; ++a) R.dmu[a] = 0.0, R.dmu_hi[a] = 0.f, R.dmu_lo[a] = 0.f;
+  if (R.ensemble != CEM_SEMIGRAND_CANONICAL) return;
+  for (int oi = 0; oi < no; ++oi)
+    for (int of = 0; of < no; ++of) {
+      // mu . R^T dN with dN = e_of - e_oi (SemiGrandCanonicalCalculator.cc:201-212)
+      double t = 0.0;
+      for (int k = 0; k < no - 1; ++k) {
+        double x = s.RT[k * no + of] - s.RT[k * no + oi];
+        t += R.mu[k] * x;
+      }
+      R.dmu[oi * no + of] = t;
+      float hi = (float)t;
+      R.dmu_hi[oi * no + of] = hi;
+      R.dmu_lo[oi * no + of] = (float)(t - (double)hi);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *cem_last_error(void) { return g_error.c_str(); }
+
+int cem_device_info(char *name, int name_len, int *sm_count, int *cc_major, int *cc_minor) {
+  return guard([&] {
+    int dev = 0;
+    CUDA_OK(cudaGetDevice(&dev));
+    cudaDeviceProp p;
+    CUDA_OK(cudaGetDeviceProperties(&p, dev));
+    if (name && name_len > 0) {
+      std::strncpy(name, p.name, name_len - 1);
+      name[name_len - 1] = 0;
+    }
+    if (sm_count) *sm_count = p.multiProcessorCount;
+    if (cc_major) *cc_major = p.major;
+    if (cc_minor) *cc_minor = p.minor;
+  });
+}
+
+int cem_system_create(const cem_system_desc *d, cem_system **out) {
+  return guard([&] {
+    require(d && out, "null argument");
+    *out = nullptr;
+    require(d->n_sublat >= 1 && d->n_sublat <= MAX_SUBLAT, "n_sublat must be in 1..4",
+            CEM_ERR_UNSUPPORTED);
+    require(d->n_occ >= 2 && d->n_occ <= 3, "n_occ must be 2 or 3", CEM_ERR_UNSUPPORTED);
+    require(d->n_funcs >= 1 && d->n_funcs <= MAX_FUNCS, "n_funcs out of range",
+            CEM_ERR_UNSUPPORTED);
+    require(d->n_orbits >= 1 && d->n_orbits <= MAX_ORBITS, "n_orbits out of range",
+            CEM_ERR_UNSUPPORTED);
+    auto s = std::make_unique<cem_system>();
+    CeTables &T = s->T;
+    T.n_sublat = d->n_sublat;
+    T.n_occ = d->n_occ;
+    T.n_sf = d->n_occ - 1;
+    T.n_funcs = d->n_funcs;
+    T.n_orbits = d->n_orbits;
+    int fexp = 1;
+    for (int g = 0; g < d->n_orbits; ++g) {
+      T.orb_size[g] = d->orbit_size[g];
+      T.orb_func_base[g] = d->orbit_func_begin[g];
+      T.orb_n_funcs[g] = d->orbit_n_funcs[g];
+      require(T.orb_size[g] >= 1 && T.orb_size[g] <= 4, "orbit size must be 1..4",
+              CEM_ERR_UNSUPPORTED);
+      require(T.orb_func_base[g] == fexp, "orbit functions must be contiguous, in order");
+      require(T.orb_n_funcs[g] >= 1 && T.orb_n_funcs[g] <= 8,
+              "at most 8 functions per orbit", CEM_ERR_UNSUPPORTED);
+      require(d->n_occ > 2 || T.orb_n_funcs[g] == 1, "binary orbits have one function");
+      fexp += T.orb_n_funcs[g];
+    }
+    require(fexp == d->n_funcs, "functions do not match orbits");
+    const int stride = T.n_sf * T.n_sf * T.n_sf * T.n_sf;
+    const int ncl = d->n_flower + d->n_owned;
+    std::vector<int> pb(ncl * 3), du(ncl * 9), lutoff(ncl);
+    std::vector<uint8_t> lut((size_t)ncl * stride, 0);
+    auto load = [&](int base, int n, const int *sub, const int *orb, const int *psub,
+                    const int *pdu, const int16_t *plut, int begin[MAX_SUBLAT][MAX_ORBITS + 1]) {
+      int prev_b = 0, prev_g = 0;
+      for (int b = 0; b < MAX_SUBLAT; ++b)
+        for (int g = 0; g <= MAX_ORBITS; ++g) begin[b][g] = -1;
+      for (int c = 0; c < n; ++c) {
+        const int b = sub[c], g = orb[c];
+        require(b >= 0 && b < d->n_sublat && g >= 0 && g < d->n_orbits, "bad cluster entry");
+        require(b > prev_b || (b == prev_b && g >= prev_g) || c == 0,
+                "clusters must be grouped by sublattice then orbit");
+        prev_b = b;
+        prev_g = g;
+        for (int q = 0; q < 3; ++q) {
+          const int p = psub[c * 3 + q];
+          require(p >= -1 && p < d->n_sublat, "bad partner sublattice");
+          require((q < T.orb_size[g] - 1) == (p >= 0), "partner count must match orbit size");
+          pb[(base + c) * 3 + q] = p;
+          for (int a = 0; a < 3; ++a) du[(base + c) * 9 + q * 3 + a] = pdu[c * 9 + q * 3 + a];
+        }
+        lutoff[base + c] = (base + c) * stride;
+        int ncode = 1;
+        for (int q = 0; q < T.orb_size[g]; ++q) ncode *= T.n_sf;
+        for (int code = 0; code < ncode; ++code) {
+          const int f = plut[(size_t)c * stride + code];
+          require(f >= T.orb_func_base[g] && f < T.orb_func_base[g] + T.orb_n_funcs[g],
+                  "decoration table refers to a function outside the cluster's orbit");
+          lut[(size_t)(base + c) * stride + code] = (uint8_t)(f - T.orb_func_base[g]);
+        }
+      }
+      // CSR bounds per (b, g)
+      int c = 0;
+      for (int b = 0; b < d->n_sublat; ++b)
+        for (int g = 0; g < d->n_orbits; ++g) {
+          begin[b][g] = c;
+          while (c < n && sub[c] == b && orb[c] == g) ++c;
+          begin[b][g + 1] = c;
+        }
+      require(c == n, "clusters are not grouped by sublattice then orbit");
+      for (int b = d->n_sublat; b < MAX_SUBLAT; ++b)
+        for (int g = 0; g <= MAX_ORBITS; ++g) begin[b][g] = n;
+    };
+    load(0, d->n_flower, d->flower_sublat, d->flower_orbit, d->flower_partner_sublat,
+         d->flower_partner_du, d->flower_lut, T.fl_begin);
+    // the owned begin indices are relative to the owned block
+    load(d->n_flower, d->n_owned, d->owned_sublat, d->owned_orbit, d->owned_partner_sublat,
+         d->owned_partner_du, d->owned_lut, T.ow_begin);
+    T.n_fl = d->n_flower;
+    T.n_ow = d->n_owned;
+    int reach = 0;
+    for (int c = 0; c < d->n_flower; ++c)
+      for (int q = 0; q < 9; ++q) reach = std::max(reach, std::abs(du[c * 9 + q]));
+    T.reach = reach;
+    s->fl_pb.assign(pb.begin(), pb.begin() + d->n_flower * 3);
+    s->fl_du.assign(du.begin(), du.begin() + d->n_flower * 9);
+    int nbr = 0;
+    for (int b = 0; b < d->n_sublat; ++b) {
+      T.n_nb[b] = d->n_neighbour ? d->n_neighbour[b] : 0;
+      require(T.n_nb[b] >= 0 && T.n_nb[b] <= MAX_NB, "too many neighbour displacements");
+      for (int k = 0; k < T.n_nb[b]; ++k) {
+        T.nb_b[b][k] = d->neighbour_sublat[b * 16 + k];
+        for (int a = 0; a < 3; ++a) {
+          T.nb_du[b][k][a] = d->neighbour_du[(b * 16 + k) * 3 + a];
+          nbr = std::max(nbr, std::abs(T.nb_du[b][k][a]));
+        }
+      }
+    }
+    s->nb_reach = nbr;
+    s->w.assign(d->weights, d->weights + d->n_funcs);
+    std::vector<float> whi(d->n_funcs), wlo(d->n_funcs);
+    for (int f = 0; f < d->n_funcs; ++f) {
+      require(std::isfinite(s->w[f]), "non-finite weight");
+      whi[f] = (float)s->w[f];
+      wlo[f] = (float)(s->w[f] - (double)whi[f]);
+    }
+    s->RT.assign(d->param_RT, d->param_RT + (d->n_occ - 1) * d->n_occ);
+    int *dpb = dev_copy(pb), *ddu = dev_copy(du), *dlo = dev_copy(lutoff);
+    uint8_t *dlut = dev_copy(lut);
+    float *dwhi = dev_copy(whi), *dwlo = dev_copy(wlo);
+    double *dw = dev_copy(s->w);
+    s->owned = {dpb, ddu, dlo, dlut, dwhi, dwlo, dw};
+    T.cl_pb = dpb;
+    T.cl_du = ddu;
+    T.cl_lut = dlo;
+    T.lut = dlut;
+    T.w_hi = dwhi;
+    T.w_lo = dwlo;
+    T.w = dw;
+    s->n_flower = d->n_flower;
+    s->n_owned = d->n_owned;
+    *out = s.release();
+  });
+}
+
+int cem_system_destroy(cem_system *sys) {
+  return guard([&] { delete sys; });
+}
+
+int cem_replicas_create(const cem_system *sys, int n, const int *L, int ensemble,
+                        cem_replicas **out) {
+  return guard([&] {
+    require(sys && L && out, "null argument");
+    *out = nullptr;
+    require(n >= 1, "need at least one replica");
+    require(ensemble == CEM_CANONICAL || ensemble == CEM_SEMIGRAND_CANONICAL, "bad ensemble");
+    auto r = std::make_unique<cem_replicas>();
+    r->sys = sys;
+    r->n = n;
+    r->ensemble = ensemble;
+    r->reps.resize(n);
+    std::map<std::vector<int>, int> pcache;
+    int64_t off = 0;
+    int max_cls = 1;
+    for (int i = 0; i < n; ++i) {
+      Replica &R = r->reps[i];
+      std::memset(&R, 0, sizeof(R));
+      for (int a = 0; a < 3; ++a) {
+        R.L[a] = L[3 * i + a];
+        require(R.L[a] >= 1 && R.L[a] <= MAX_L, "supercell dimension out of range",
+                CEM_ERR_UNSUPPORTED);
+        require(R.L[a] >= 2 * sys->T.reach + 1,
+                "supercell too small for the cluster expansion's reach");
+      }
+      R.n_sites = R.L[0] * R.L[1] * R.L[2] * sys->T.n_sublat;
+      R.ensemble = ensemble;
+      R.occ_offset = off;
+      off += R.n_sites;
+      std::vector<int> key{R.L[0], R.L[1], R.L[2]};
+      auto it = pcache.find(key);
+      int p = (it != pcache.end()) ? it->second : (pcache[key] = choose_colouring(*sys, R.L, ensemble));
+      R.p = p;
+      int cls = sys->T.n_sublat;
+      for (int a = 0; a < 3; ++a) {
+        auto col = axis_blocks(R.L[a], p);
+        R.n_col[a] = *std::max_element(col.begin(), col.end()) + 1;
+        cls *= R.n_col[a];
+      }
+      max_cls = std::max(max_cls, cls);
+      R.temperature = 1000.0;
+      R.beta = 1.0 / (KB * R.temperature);
+      R.beta_f = (float)R.beta;
+      R.seed = 0x9E3779B97F4A7C15ull * (uint64_t)(i + 1);
+      set_dmu(*sys, R);
+    }
+    r->total_sites = off;
+    r->max_classes = max_cls;
+    int smem = 0;
+    for (int i = 0; i < n; ++i)
+      smem = std::max(smem, sweep_smem_bytes(sys->T, r->reps[i].L[0], r->reps[i].L[1],
+                                             r->reps[i].L[2], max_cls));
+    r->sweep_smem = smem;
+    r->stats_host.assign(n, ReplicaStats{});
+    CUDA_OK(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking));
+    CUDA_OK(cudaEventCreate(&r->ev0));
+    CUDA_OK(cudaEventCreate(&r->ev1));
+    CUDA_OK(cudaMalloc(&r->d_reps, sizeof(Replica) * n));
+    CUDA_OK(cudaMalloc(&r->d_stats, sizeof(ReplicaStats) * n));
+    CUDA_OK(cudaMemset(r->d_stats, 0, sizeof(ReplicaStats) * n));
+    CUDA_OK(cudaMalloc(&r->d_occ, (size_t)off + 16));
+    CUDA_OK(cudaMemset(r->d_occ, 0, (size_t)off + 16));
+    CUDA_OK(cudaMalloc(&r->d_counts, sizeof(unsigned long long) * (MAX_FUNCS + 8)));
+    CUDA_OK(cudaMalloc(&r->d_result, sizeof(long long) * 4));
+    r->sample_width = sys->T.n_occ;  // potential + (n_occ-1) compositions
+    *out = r.release();
+  });
+}
+
+int cem_replicas_destroy(cem_replicas *r) {
+  return guard([&] { delete r; });
+}
+
+int cem_n_sites(const cem_replicas *r, int i, int64_t *n) {
+  return guard([&] {
+    check_rep(r, i);
+    *n = r->reps[i].n_sites;
+  });
+}
+
+int cem_set_conditions(cem_replicas *r, int i, double temperature, const double *mu) {
+  return guard([&] {
+    check_rep(r, i);
+    require(std::isfinite(temperature) && temperature >= 0.0, "temperature must be >= 0");
+    Replica &R = r->reps[i];
+    R.temperature = temperature;
+    // Conditions.hh:17-45: beta = inf when T is zero within 1e-10
+    R.beta = (std::fabs(temperature) < 1e-10) ? INFINITY : 1.0 / (KB * temperature);
+    R.beta_f = (float)R.beta;
+    const int nc = r->sys->T.n_occ - 1;
+    for (int k = 0; k < 3; ++k) R.mu[k] = 0.0;
+    if (mu) {
+      for (int k = 0; k < nc; ++k) {
+        require(std::isfinite(mu[k]), "param_chem_pot must be finite");
+        R.mu[k] = mu[k];
+      }
+    } else {
+      require(r->ensemble == CEM_CANONICAL, "semi-grand canonical replicas need param_chem_pot");
+    }
+    set_dmu(*r->sys, R);
+    r->reps_dirty = true;
+  });
+}
+
+int cem_set_seed(cem_replicas *r, int i, uint64_t seed) {
+  return guard([&] {
+    check_rep(r, i);
+    r->reps[i].seed = seed;
+    r->reps_dirty = true;
+  });
+}
+
+int cem_set_occupation(cem_replicas *r, int i, const int8_t *occ) {
+  return guard([&] {
+    check_rep(r, i);
+    require(occ != nullptr, "null occupation");
+    const Replica &R = r->reps[i];
+    for (int l = 0; l < R.n_sites; ++l)
+      require(occ[l] >= 0 && occ[l] < r->sys->T.n_occ, "occupant index out of range");
+    CUDA_OK(cudaMemcpyAsync(r->d_occ + R.occ_offset, occ, R.n_sites, cudaMemcpyHostToDevice,
+                            r->stream));
+    CUDA_OK(cudaStreamSynchronize(r->stream));
+    r->stats_valid = false;
+  });
+}
+
+int cem_get_occupation(cem_replicas *r, int i, int8_t *occ) {
+  return guard([&] {
+    check_rep(r, i);
+    require(occ != nullptr, "null occupation");
+    const Replica &R = r->reps[i];
+    CUDA_OK(cudaMemcpyAsync(occ, r->d_occ + R.occ_offset, R.n_sites, cudaMemcpyDeviceToHost,
+                            r->stream));
+    CUDA_OK(cudaStreamSynchronize(r->stream));
+  });
+}
+
+int cem_set_occupation_all(cem_replicas *r, const int8_t *packed) {
+  return guard([&] {
+    require(r && packed, "null argument");
+    CUDA_OK(cudaMemcpyAsync(r->d_occ, packed, (size_t)r->total_sites, cudaMemcpyHostToDevice,
+                            r->stream));
+    r->stats_valid = false;
+  });
+}
+
+int cem_get_occupation_all(cem_replicas *r, int8_t *packed) {
+  return guard([&] {
+    require(r && packed, "null argument");
+    CUDA_OK(cudaMemcpyAsync(packed, r->d_occ, (size_t)r->total_sites, cudaMemcpyDeviceToHost,
+                            r->stream));
+    CUDA_OK(cudaStreamSynchronize(r->stream));
+  });
+}
+
+int cem_host_alloc(int64_t bytes, void **ptr) {
+  return guard([&] {
+    require(ptr && bytes > 0, "bad argument");
+    CUDA_OK(cudaMallocHost(ptr, (size_t)bytes));
+  });
+}
+
+int cem_host_free(void *ptr) {
+  return guard([&] { CUDA_OK(cudaFreeHost(ptr)); });
+}
+
+int cem_energy(cem_replicas *r, int i, double *energy, int64_t *counts) {
+  return guard([&] {
+    check_rep(r, i);
+    const Replica &R = r->reps[i];
+    const CeTables &T = r->sys->T;
+    CUDA_OK(launch_energy(T, r->d_occ + R.occ_offset, R.L[0], R.L[1], R.L[2], r->d_counts,
+                          r->stream));
+    std::vector<unsigned long long> c(T.n_funcs);
+    CUDA_OK(cudaMemcpyAsync(c.data(), r->d_counts, sizeof(unsigned long long) * T.n_funcs,
+                            cudaMemcpyDeviceToHost, r->stream));
+    CUDA_OK(cudaStreamSynchronize(r->stream));
+    const int n_uc = R.L[0] * R.L[1] * R.L[2];
+    double e = r->sys->w[0] * n_uc;
+    for (int f = 1; f < T.n_funcs; ++f) e += r->sys->w[f] * (double)c[f];
+    if (energy) *energy = e;
+    if (counts) {
+      counts[0] = n_uc;
+      for (int f = 1; f < T.n_funcs; ++f) counts[f] = (int64_t)c[f];
+    }
+  });
+}
+
+int cem_delta_energy(cem_replicas *r, int i, int n_events, int k, const int64_t *sites,
+                     const int32_t *new_occ, int potential, double *dE, int64_t *dcount) {
+  return guard([&] {
+    check_rep(r, i);
+    require(n_events >= 0 && k >= 1 && k <= 4, "sites_per_event must be 1..4");
+    require(sites && new_occ && dE, "null argument");
+    if (n_events == 0) return;
+    const Replica &R = r->reps[i];
+    const CeTables &T = r->sys->T;
+    for (int64_t e = 0; e < (int64_t)n_events * k; ++e) {
+      require(sites[e] >= 0 && sites[e] < R.n_sites, "site index out of range");
+      require(new_occ[e] >= 0 && new_occ[e] < T.n_occ, "occupant index out of range");
+    }
+    require(potential == 0 || r->ensemble == CEM_SEMIGRAND_CANONICAL,
+            "the semi-grand potential needs semi-grand canonical replicas");
+    long long *ds = nullptr;
+    int *dn = nullptr;
+    double *dde = nullptr, *ddmu = nullptr;
+    long long *ddc = nullptr;
+    auto cleanup = [&] {
+      cudaFree(ds);
+      cudaFree(dn);
+      cudaFree(dde);
+      cudaFree(ddmu);
+      cudaFree(ddc);
+    };
+    try {
+      const size_t ne = (size_t)n_events * k;
+      CUDA_OK(cudaMalloc(&ds, ne * 8));
+      CUDA_OK(cudaMalloc(&dn, ne * 4));
+      CUDA_OK(cudaMalloc(&dde, (size_t)n_events * 8));
+      CUDA_OK(cudaMemcpyAsync(ds, sites, ne * 8, cudaMemcpyHostToDevice, r->stream));
+      CUDA_OK(cudaMemcpyAsync(dn, new_occ, ne * 4, cudaMemcpyHostToDevice, r->stream));
+      if (potential) {
+        CUDA_OK(cudaMalloc(&ddmu, 16 * 8));
+        CUDA_OK(cudaMemcpyAsync(ddmu, R.dmu, 16 * 8, cudaMemcpyHostToDevice, r->stream));
+      }
+      if (dcount) CUDA_OK(cudaMalloc(&ddc, (size_t)n_events * T.n_funcs * 8));
+      CUDA_OK(launch_delta(T, r->d_occ + R.occ_offset, R.L[0], R.L[1], R.L[2], n_events, k, ds,
+                           dn, ddmu, dde, ddc, r->stream));
+      CUDA_OK(cudaMemcpyAsync(dE, dde, (size_t)n_events * 8, cudaMemcpyDeviceToHost, r->stream));
+      if (dcount)
+        CUDA_OK(cudaMemcpyAsync(dcount, ddc, (size_t)n_events * T.n_funcs * 8,
+                                cudaMemcpyDeviceToHost, r->stream));
+      CUDA_OK(cudaStreamSynchronize(r->stream));
+    } catch (...) {
+      cleanup();
+      throw;
+    }
+    cleanup();
+  });
+}
+
+int cem_replay(cem_replicas *r, int i, uint64_t mt_seed, int64_t n_steps, uint8_t *accept_seq,
+               double *dE_seq, int64_t *site_seq, int64_t *n_accept, uint64_t *n_draws) {
+  return guard([&] {
+    check_rep(r, i);
+    require(n_steps >= 0, "n_steps must be >= 0");
+    const Replica &R = r->reps[i];
+    const CeTables &T = r->sys->T;
+    int dev = 0, maxsm = 0;
+    CUDA_OK(cudaGetDevice(&dev));
+    CUDA_OK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    require(replay_smem_bytes(R.n_sites, T.n_occ) <= maxsm,
+            "supercell too large for the sequential replay kernel", CEM_ERR_UNSUPPORTED);
+    ReplayParams P{};
+    for (int a = 0; a < 3; ++a) P.L[a] = R.L[a];
+    P.n_sites = R.n_sites;
+    P.ensemble = R.ensemble;
+    P.beta = R.beta;
+    for (int a = 0; a < 16; ++a) P.dmu[a] = R.dmu[a];
+    P.mt_seed = mt_seed;
+    P.n_steps = n_steps;
+    P.occ = r->d_occ + R.occ_offset;
+    P.result = r->d_result;
+    unsigned char *dacc = nullptr;
+    double *dde = nullptr;
+    long long *dsite = nullptr;
+    auto cleanup = [&] {
+      cudaFree(dacc);
+      cudaFree(dde);
+      cudaFree(dsite);
+    };
+    try {
+      if (accept_seq && n_steps) CUDA_OK(cudaMalloc(&dacc, (size_t)n_steps));
+      if (dE_seq && n_steps) CUDA_OK(cudaMalloc(&dde, (size_t)n_steps * 8));
+      if (site_seq && n_steps) CUDA_OK(cudaMalloc(&dsite, (size_t)n_steps * 16));
+      P.accept_seq = dacc;
+      P.de_seq = dde;
+      P.site_seq = dsite;
+      CUDA_OK(launch_replay(T, P, r->stream));
+      long long res[3];
+      CUDA_OK(cudaMemcpyAsync(res, r->d_result, 24, cudaMemcpyDeviceToHost, r->stream));
+      if (dacc) CUDA_OK(cudaMemcpyAsync(accept_seq, dacc, (size_t)n_steps, cudaMemcpyDeviceToHost, r->stream));
+      if (dde) CUDA_OK(cudaMemcpyAsync(dE_seq, dde, (size_t)n_steps * 8, cudaMemcpyDeviceToHost, r->stream));
+      if (dsite) CUDA_OK(cudaMemcpyAsync(site_seq, dsite, (size_t)n_steps * 16, cudaMemcpyDeviceToHost, r->stream));
+      CUDA_OK(cudaStreamSynchronize(r->stream));
+      if (n_accept) *n_accept = res[0];
+      if (n_draws) *n_draws = (uint64_t)res[1];
+      if (res[2]) throw Err(CEM_ERR_DEVICE, "no event can be proposed from this occupation");
+    } catch (...) {
+      cleanup();
+      throw;
+    }
+    cleanup();
+    r->stats_valid = false;
+  });
+}
+
+// Exact energies and species counts of every replica -> running stats
+// (one batched kernel, no host round trip).
+static void init_stats(cem_replicas *r) {
+  r->upload_reps();
+  CUDA_OK(launch_init_stats(r->sys->T, r->d_reps, r->d_stats, r->d_occ, r->n, r->stream));
+  r->stats_valid = true;
+}
+
+int cem_reset_stats(cem_replicas *r) {
+  return guard([&] {
+    require(r != nullptr, "null handle");
+    init_stats(r);
+  });
+}
+
+int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_samples) {
+  return guard([&] {
+    require(r != nullptr, "null handle");
+    require(n_passes >= 0 && n_equil >= 0, "pass counts must be >= 0");
+    int dev = 0, maxsm = 0;
+    CUDA_OK(cudaGetDevice(&dev));
+    CUDA_OK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    require(r->sweep_smem <= maxsm,
+            "supercell does not fit in shared memory (" + std::to_string(r->sweep_smem) +
+                " bytes needed)",
+            CEM_ERR_UNSUPPORTED);
+    r->upload_reps();
+    if (!r->stats_valid) init_stats(r);
+    SweepParams P{};
+    P.reps = r->d_reps;
+    P.stats = r->d_stats;
+    P.occ = r->d_occ;
+    P.n_passes = n_passes;
+    P.n_equil = n_equil;
+    P.max_classes = r->max_classes;
+    const CeTables &T = r->sys->T;
+    for (size_t k = 0; k < r->sys->RT.size() && k < 16; ++k) P.RT[k] = r->sys->RT[k];
+    if (record_samples) {
+      const long long cap = std::max<long long>(1, n_passes - n_equil);
+      if (cap > r->sample_capacity) {
+        cudaFree(r->d_samples);
+        r->d_samples = nullptr;
+        CUDA_OK(cudaMalloc(&r->d_samples, sizeof(double) * cap * r->sample_width * r->n));
+        r->sample_capacity = cap;
+      }
+      P.samples = r->d_samples;
+      P.sample_capacity = r->sample_capacity;
+      P.sample_width = r->sample_width;
+      // samples are indexed by the replica's sample count: restart it
+      std::vector<ReplicaStats> s(r->n);
+      CUDA_OK(cudaMemcpyAsync(s.data(), r->d_stats, sizeof(ReplicaStats) * r->n,
+                              cudaMemcpyDeviceToHost, r->stream));
+      CUDA_OK(cudaStreamSynchronize(r->stream));
+      for (auto &x : s) {
+        x.n_samples = 0;
+        x.sum_e = x.sum_e2 = x.sum_f = 0;
+        for (int k = 0; k < 3; ++k) x.sum_x[k] = x.sum_ex[k] = 0;
+        for (int k = 0; k < 9; ++k) x.sum_xx[k] = 0;
+      }
+      CUDA_OK(cudaMemcpyAsync(r->d_stats, s.data(), sizeof(ReplicaStats) * r->n,
+                              cudaMemcpyHostToDevice, r->stream));
+      r->n_samples_recorded = std::max<long long>(0, n_passes - n_equil);
+    }
+    CUDA_OK(cudaEventRecord(r->ev0, r->stream));
+    CUDA_OK(launch_sweep(T, P, r->n, r->sweep_smem, r->stream));
+    CUDA_OK(cudaEventRecord(r->ev1, r->stream));
+  });
+}
+
+int cem_get_stats(cem_replicas *r, int i, cem_stats *out) {
+  return guard([&] {
+    check_rep(r, i);
+    require(out != nullptr, "null output");
+    ReplicaStats S;
+    CUDA_OK(cudaMemcpyAsync(&S, r->d_stats + i, sizeof(S), cudaMemcpyDeviceToHost, r->stream));
+    CUDA_OK(cudaStreamSynchronize(r->stream));
+    std::memset(out, 0, sizeof(*out));
+    const int nc = r->sys->T.n_occ - 1;
+    out->n_samples = S.n_samples;
+    const double n = S.n_samples;
+    if (n > 0) {
+      out->mean_potential = S.sum_e / n;
+      out->var_potential = S.sum_e2 / n - out->mean_potential * out->mean_potential;
+      out->mean_formation = S.sum_f / n;
+      for (int k = 0; k < nc; ++k) out->mean_comp[k] = S.sum_x[k] / n;
+      for (int k = 0; k < nc; ++k) {
+        out->cov_e_comp[k] = S.sum_ex[k] / n - out->mean_potential * out->mean_comp[k];
+        for (int k2 = 0; k2 < nc; ++k2)
+          out->cov_comp[k * 3 + k2] = S.sum_xx[k * 3 + k2] / n - out->mean_comp[k] * out->mean_comp[k2];
+      }
+    }
+    out->energy = S.energy;
+    out->n_proposed = S.n_proposed;
+    out->n_accepted = S.n_accepted;
+    out->passes = S.pass;
+  });
+}
+
+int cem_get_samples(cem_replicas *r, int i, double *potential, double *comp, int64_t capacity,
+                    int64_t *n_samples) {
+  return guard([&] {
+    check_rep(r, i);
+    require(r->d_samples != nullptr, "no samples were recorded");
+    const int64_t n = std::min<int64_t>(r->n_samples_recorded, r->sample_capacity);
+    const int64_t m = std::min<int64_t>(n, capacity);
+    std::vector<double> buf((size_t)m * r->sample_width);
+    if (m > 0)
+      CUDA_OK(cudaMemcpyAsync(buf.data(),
+                              r->d_samples + (size_t)i * r->sample_capacity * r->sample_width,
+                              sizeof(double) * buf.size(), cudaMemcpyDeviceToHost, r->stream));
+    CUDA_OK(cudaStreamSynchronize(r->stream));
+    const int nc = r->sys->T.n_occ - 1;
+    for (int64_t s = 0; s < m; ++s) {
+      if (potential) potential[s] = buf[s * r->sample_width];
+      if (comp)
+        for (int k = 0; k < nc; ++k) comp[s * nc + k] = buf[s * r->sample_width + 1 + k];
+    }
+    if (n_samples) *n_samples = m;
+  });
+}
+
+int cem_smem_bandwidth(double *gbs) {
+  return guard([&] {
+    require(gbs != nullptr, "null output");
+    CUDA_OK(smem_bandwidth(gbs, 0));
+  });
+}
+
+int cem_synchronize(cem_replicas *r) {
+  return guard([&] {
+    require(r != nullptr, "null handle");
+    CUDA_OK(cudaStreamSynchronize(r->stream));
+  });
+}
+
+int cem_last_kernel_ms(cem_replicas *r, double *ms) {
+  return guard([&] {
+    require(r && ms, "null argument");
+    CUDA_OK(cudaEventSynchronize(r->ev1));
+    float f = 0.f;
+    CUDA_OK(cudaEventElapsedTime(&f, r->ev0, r->ev1));
+    *ms = f;
+  });
+}
+
+}  // extern "C"

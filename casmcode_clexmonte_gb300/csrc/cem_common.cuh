@@ -1,0 +1,225 @@
+// Shared types and device helpers for the GB300 Metropolis hot path.
+//
+// Arithmetic contract (the oracle restates the same operation order):
+//  * delta correlations are integer cluster-count changes per function;
+//  * the ECI dot is a float-float sum: W_f = hi_f + lo_f (two floats),
+//    each term hi_f * dC_f is split exactly with an FMA, summed with TwoSum
+//    (Knuth), errors and lo_f * dC_f accumulated in a second float;
+//  * parallel-mode acceptance: u < exp(-beta * dE) with the project's own
+//    Cody-Waite exp (below), u a 24-bit uniform from Philox4x32-10;
+//  * replay-mode acceptance: the reference's FP64 rule (dE < 0 accepts,
+//    else u < exp(-dE * beta) with u from std::uniform_real_distribution
+//    over std::mt19937_64).
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+
+#ifdef __CUDACC__
+#define CEM_HD __host__ __device__ __forceinline__
+#else
+#define CEM_HD inline
+#endif
+
+namespace cem {
+
+constexpr int MAX_SUBLAT = 4;
+constexpr int MAX_ORBITS = 8;    // non-empty orbits
+constexpr int MAX_FUNCS = 64;
+constexpr int MAX_PARTNERS = 3;  // clusters of up to 4 sites
+constexpr int MAX_NB = 16;       // nearest-neighbour displacements per sublattice
+constexpr int MAX_COLOURS = 8;   // per axis
+constexpr int MAX_L = 128;       // per axis
+
+// Cluster-expansion tables in device memory (built once per system).
+struct CeTables {
+  int n_sublat, n_occ, n_sf, n_funcs, n_orbits;
+  int orb_func_base[MAX_ORBITS];
+  int orb_n_funcs[MAX_ORBITS];
+  int orb_size[MAX_ORBITS];
+  // flower clusters, grouped by centre sublattice then orbit:
+  // clusters of (b, g) are [fl_begin[b][g], fl_begin[b][g+1])
+  int fl_begin[MAX_SUBLAT][MAX_ORBITS + 1];
+  int n_fl;
+  // owned clusters (each periodic cluster counted once), same grouping
+  int ow_begin[MAX_SUBLAT][MAX_ORBITS + 1];
+  int n_ow;
+  int reach;  // max |cell offset component| over flower partners
+  // neighbour displacements per sublattice (canonical local swaps)
+  int n_nb[MAX_SUBLAT];
+  int nb_b[MAX_SUBLAT][MAX_NB];
+  int nb_du[MAX_SUBLAT][MAX_NB][3];
+  // device arrays
+  const int *cl_pb;      // [n_cl * 3] partner sublattice
+  const int *cl_du;      // [n_cl * 9] partner cell offsets
+  const int *cl_lut;     // [n_cl] offset into lut (general path)
+  const uint8_t *lut;    // local function index per decoration code
+  const float *w_hi;     // [n_funcs]
+  const float *w_lo;     // [n_funcs]
+  const double *w;       // [n_funcs]; w[0] = ECI of the empty cluster
+  // owned clusters use index n_fl + i in the cl_* arrays
+};
+
+// Per-replica description (device memory array).
+struct Replica {
+  int L[3];
+  int n_sites;
+  int ensemble;           // 0 = semi-grand canonical flips, 1 = canonical swaps
+  int64_t occ_offset;     // into the packed occupation buffer
+  double beta;            // 1/(kB T), +inf at T == 0
+  float beta_f;
+  double temperature;
+  double mu[3];           // param_chem_pot (semi-grand canonical)
+  double dmu[16];         // [o_i * n_occ + o_f]: mu . R^T (e_f - e_i)
+  float dmu_hi[16], dmu_lo[16];
+  uint64_t seed;
+  // colouring: per axis block size >= p, colour of each coordinate
+  int n_col[3];
+  int p;
+};
+
+// Per-replica running results (device memory array).
+struct ReplicaStats {
+  double energy;          // running formation energy per supercell
+  double n_samples;
+  double sum_e, sum_e2;   // potential energy per unit cell moments
+  double sum_x[3], sum_xx[9], sum_ex[3];
+  double sum_f;           // formation energy per unit cell
+  int64_t n_species[8];   // current species counts
+  int64_t n_proposed, n_accepted;
+  int64_t pass;
+  int status;             // nonzero: device-side error code
+  int pad;
+};
+
+// ------------------------------------------------------------------ Philox
+// Philox4x32-10, Salmon et al., SC'11 ("Parallel random numbers: as easy as
+// 1, 2, 3"), round function and Weyl key schedule from the paper.
+struct U4 {
+  uint32_t x, y, z, w;
+};
+
+CEM_HD U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+#ifdef __CUDA_ARCH__
+    uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+#else
+    uint64_t p0 = (uint64_t)0xD2511F53u * c.x, p1 = (uint64_t)0xCD9E8D57u * c.z;
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+#endif
+    U4 n;
+    n.x = hi1 ^ c.y ^ k0;
+    n.y = lo1;
+    n.z = hi0 ^ c.w ^ k1;
+    n.w = lo0;
+    c = n;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+
+// 24-bit uniform in [0, 1)
+CEM_HD float u24(uint32_t r) { return (float)(r >> 8) * 5.9604644775390625e-8f; }
+
+// ------------------------------------------------------- exact float ops
+#ifdef __CUDA_ARCH__
+#define FADD(a, b) __fadd_rn((a), (b))
+#define FSUB(a, b) __fsub_rn((a), (b))
+#define FMUL(a, b) __fmul_rn((a), (b))
+#define FFMA(a, b, c) __fmaf_rn((a), (b), (c))
+#else
+#define FADD(a, b) ((float)((a) + (b)))
+#define FSUB(a, b) ((float)((a) - (b)))
+#define FMUL(a, b) ((float)((a) * (b)))
+#define FFMA(a, b, c) std::fmaf((a), (b), (c))
+#endif
+
+// Float-float accumulator for sum_f W_f * dC_f.
+struct FF {
+  float s, e;
+};
+
+CEM_HD void ff_add_term(FF &acc, float hi, float lo, int dc) {
+  float c = (float)dc;
+  float p = FMUL(hi, c);
+  float pe = FFMA(hi, c, -p);  // exact error of the product
+  float t = FADD(acc.s, p);     // TwoSum(acc.s, p)
+  float z = FSUB(t, acc.s);
+  float err = FADD(FSUB(acc.s, FSUB(t, z)), FSUB(p, z));
+  acc.s = t;
+  acc.e = FADD(acc.e, FADD(err, pe));
+  acc.e = FFMA(lo, c, acc.e);
+}
+
+CEM_HD void ff_add_ff(FF &acc, float hi, float lo) {
+  float t = FADD(acc.s, hi);
+  float z = FSUB(t, acc.s);
+  float err = FADD(FSUB(acc.s, FSUB(t, z)), FSUB(hi, z));
+  acc.s = t;
+  acc.e = FADD(acc.e, FADD(err, lo));
+}
+
+// ------------------------------------------------------------------ exp
+// exp(x) for x <= 0 by Cody-Waite range reduction (Cody & Waite, "Software
+// Manual for the Elementary Functions", 1980): x = n ln2 + r, |r| <= ln2/2,
+// ln2 split in a short high part and a low part, e^r by its degree-7 Taylor
+// polynomial (truncation < 3e-9 relative), scaled by 2^n through the exponent
+// bits. Results below 2^-126 flush to 0.
+CEM_HD float cem_expf_neg(float x) {
+  if (!(x > -87.0f)) return 0.0f;  // also maps NaN to 0
+  const float log2e = 1.44269504088896341f;
+  const float ln2_hi = 0.693145751953125f;      // 0x3F317200: few mantissa bits
+  const float ln2_lo = 1.42860682030941723e-6f;  // ln2 - ln2_hi
+  float n = FMUL(x, log2e);
+#ifdef __CUDA_ARCH__
+  n = rintf(n);
+#else
+  n = std::nearbyint(n);
+#endif
+  float r = FFMA(-n, ln2_hi, x);
+  r = FFMA(-n, ln2_lo, r);
+  float p = 1.0f / 5040.0f;
+  p = FFMA(p, r, 1.0f / 720.0f);
+  p = FFMA(p, r, 1.0f / 120.0f);
+  p = FFMA(p, r, 1.0f / 24.0f);
+  p = FFMA(p, r, 1.0f / 6.0f);
+  p = FFMA(p, r, 0.5f);
+  p = FFMA(p, r, 1.0f);
+  p = FFMA(p, r, 1.0f);
+  int e = (int)n + 127;
+  if (e <= 0) return 0.0f;
+  uint32_t bits = (uint32_t)e << 23;
+  float scale;
+#ifdef __CUDA_ARCH__
+  scale = __uint_as_float(bits);
+#else
+  __builtin_memcpy(&scale, &bits, 4);
+#endif
+  return FMUL(p, scale);
+}
+
+// ------------------------------------------------------------ MT19937-64
+// Matsumoto & Nishimura 64-bit Mersenne Twister (parameters of
+// std::mt19937_64), warp-parallel twist in shared memory.
+constexpr int MT_N = 312, MT_M = 156;
+constexpr uint64_t MT_A = 0xB5026F5AA96619E9ull;
+constexpr uint64_t MT_UM = 0xFFFFFFFF80000000ull, MT_LM = 0x7FFFFFFFull;
+
+CEM_HD uint64_t mt_temper(uint64_t x) {
+  x ^= (x >> 29) & 0x5555555555555555ull;
+  x ^= (x << 17) & 0x71D67FFFEDA60000ull;
+  x ^= (x << 37) & 0xFFF7EEE000000000ull;
+  x ^= (x >> 43);
+  return x;
+}
+
+CEM_HD uint64_t mt_next_word(uint64_t cur, uint64_t nxt, uint64_t far) {
+  uint64_t y = (cur & MT_UM) | (nxt & MT_LM);
+  return far ^ (y >> 1) ^ ((y & 1ull) ? MT_A : 0ull);
+}
+
+}  // namespace cem

@@ -1,0 +1,53 @@
+// Internal launch interface between the C ABI layer and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "cem_common.cuh"
+
+namespace cem {
+
+constexpr int SWEEP_THREADS = 512;
+
+struct ReplayParams {
+  int L[3];
+  int n_sites;
+  int ensemble;
+  double beta;
+  double dmu[16];
+  unsigned long long mt_seed;
+  long long n_steps;
+  int8_t *occ;                 // device, updated in place
+  unsigned char *accept_seq;   // device, optional
+  double *de_seq;              // device, optional
+  long long *site_seq;         // device, optional (2 per step)
+  long long *result;           // device [3]: n_accept, draws, stopped
+};
+
+struct SweepParams {
+  const Replica *reps;
+  ReplicaStats *stats;
+  int8_t *occ;                 // packed occupations of all replicas
+  double *samples;             // [n_rep][capacity][width] or null
+  long long sample_capacity;
+  int sample_width;
+  long long n_passes, n_equil;
+  int max_classes;
+  double RT[16];               // (n_occ-1) x n_occ
+};
+
+cudaError_t launch_energy(const CeTables &T, const int8_t *occ, int L0, int L1, int L2,
+                          unsigned long long *counts, cudaStream_t st);
+cudaError_t launch_delta(const CeTables &T, const int8_t *occ, int L0, int L1, int L2,
+                         int n_events, int k_sites, const long long *sites, const int *new_occ,
+                         const double *dmu, double *dE, long long *dcount, cudaStream_t st);
+int replay_smem_bytes(int n_sites, int n_occ);
+cudaError_t launch_replay(const CeTables &T, const ReplayParams &P, cudaStream_t st);
+cudaError_t launch_init_stats(const CeTables &T, const Replica *reps, ReplicaStats *stats,
+                              const int8_t *occ, int n_replicas, cudaStream_t st);
+cudaError_t smem_bandwidth(double *gbs, cudaStream_t st);
+int sweep_smem_bytes(const CeTables &T, int L0, int L1, int L2, int n_classes);
+cudaError_t launch_sweep(const CeTables &T, const SweepParams &P, int n_replicas, int smem,
+                         cudaStream_t st);
+
+}  // namespace cem

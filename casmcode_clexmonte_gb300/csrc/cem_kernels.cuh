@@ -1,0 +1,1033 @@
+// Kernels of the GB300 cluster-expansion Metropolis hot path.
+//
+//  k_energy   : integer function counts of a whole occupation (per_supercell)
+//  k_delta    : batched occ_delta_per_supercell, one thread per event
+//  k_replay   : occupation_metropolis_v2 restated step by step, one warp per
+//               chain, consuming the std::mt19937_64 stream
+//  k_sweep    : parallel Metropolis, one CTA per replica, occupation resident
+//               in shared memory with a periodic halo, colour classes of
+//               non-interacting sites updated at once
+//
+// Delta correlations are integer counts: for each orbit g, the number of
+// flower clusters whose decoration changes in or out of each function class.
+// Binary systems (two occupants) count products of partner occupations;
+// systems with more occupants look the decoration up in a per-cluster table
+// and accumulate +1/-1 in 8-bit fields of a 64-bit word per orbit.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+
+#include "cem_common.cuh"
+#include "cem_internal.h"
+
+namespace cem {
+
+// ------------------------------------------------------------ accumulators
+template <int NOCC>
+struct Acc {
+  unsigned long long p[MAX_ORBITS], m[MAX_ORBITS];
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int g = 0; g < MAX_ORBITS; ++g) p[g] = m[g] = 0ull;
+  }
+};
+template <>
+struct Acc<2> {
+  int c[MAX_ORBITS];
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int g = 0; g < MAX_ORBITS; ++g) c[g] = 0;
+  }
+};
+
+// Add the delta counts of changing the centre site of sublattice b from o_i
+// to o_f. rd(c, j) returns the occupant of partner j of cluster c.
+template <int NOCC, class Reader>
+__device__ __forceinline__ void accumulate_site(const CeTables &T, int b, int o_i, int o_f,
+                                                const int *__restrict__ lutoff,
+                                                const uint8_t *__restrict__ lut, Reader rd,
+                                                Acc<NOCC> &acc) {
+#pragma unroll
+  for (int g = 0; g < MAX_ORBITS; ++g) {
+    if (g < T.n_orbits) {
+      const int c0 = T.fl_begin[b][g], c1 = T.fl_begin[b][g + 1];
+      const int size = T.orb_size[g];
+      if constexpr (NOCC == 2) {
+        int cnt = 0;
+        if (size == 1) {
+          cnt = c1 - c0;
+        } else if (size == 2) {
+          for (int c = c0; c < c1; ++c) cnt += rd(c, 0);
+        } else if (size == 3) {
+          for (int c = c0; c < c1; ++c) cnt += rd(c, 0) & rd(c, 1);
+        } else {
+          for (int c = c0; c < c1; ++c) cnt += rd(c, 0) & rd(c, 1) & rd(c, 2);
+        }
+        acc.c[g] += (o_f - o_i) * cnt;
+      } else {
+        constexpr int NSF = NOCC - 1;
+        for (int c = c0; c < c1; ++c) {
+          int code = 0, mul = NSF;
+          bool ok = true;
+          for (int j = 0; j < size - 1; ++j) {
+            int v = rd(c, j);
+            ok = ok && (v != 0);
+            code += (v - 1) * mul;
+            mul *= NSF;
+          }
+          if (ok) {
+            const int base = lutoff[c] + code;
+            if (o_f) acc.p[g] += 1ull << (8 * lut[base + o_f - 1]);
+            if (o_i) acc.m[g] += 1ull << (8 * lut[base + o_i - 1]);
+          }
+        }
+      }
+    }
+  }
+}
+
+template <int NOCC>
+__device__ __forceinline__ int acc_dc(const Acc<NOCC> &acc, int g, int fl) {
+  if constexpr (NOCC == 2) {
+    return acc.c[g];
+  } else {
+    return (int)((acc.p[g] >> (8 * fl)) & 255ull) - (int)((acc.m[g] >> (8 * fl)) & 255ull);
+  }
+}
+
+// sum_f W_f dC_f in float-float, functions in increasing order.
+template <int NOCC>
+__device__ __forceinline__ FF acc_dot(const CeTables &T, const Acc<NOCC> &acc,
+                                      const float *__restrict__ whi,
+                                      const float *__restrict__ wlo) {
+  FF r{0.f, 0.f};
+#pragma unroll
+  for (int g = 0; g < MAX_ORBITS; ++g) {
+    if (g < T.n_orbits) {
+      const int base = T.orb_func_base[g];
+      if constexpr (NOCC == 2) {
+        const int dc = acc.c[g];
+        if (dc) ff_add_term(r, whi[base], wlo[base], dc);
+      } else {
+        const int nf = T.orb_n_funcs[g];
+        for (int fl = 0; fl < nf; ++fl) {
+          const int dc = acc_dc<NOCC>(acc, g, fl);
+          if (dc) ff_add_term(r, whi[base + fl], wlo[base + fl], dc);
+        }
+      }
+    }
+  }
+  return r;
+}
+
+template <int NOCC>
+__device__ void acc_store(const CeTables &T, const Acc<NOCC> &acc, long long *out) {
+  for (int f = 0; f < T.n_funcs; ++f) out[f] = 0;
+  for (int g = 0; g < T.n_orbits; ++g) {
+    const int base = T.orb_func_base[g];
+    const int nf = T.orb_n_funcs[g];
+    for (int fl = 0; fl < nf; ++fl) out[base + fl] = acc_dc<NOCC>(acc, g, fl);
+  }
+}
+
+__device__ __forceinline__ int wrapc(int x, int L) {
+  x = (x < 0) ? x + L : x;
+  return (x >= L) ? x - L : x;
+}
+
+// ------------------------------------------------------------ full energy
+template <int NOCC>
+__global__ void k_energy(const __grid_constant__ CeTables T, const int8_t *__restrict__ occ,
+                         int L0, int L1, int L2, unsigned long long *__restrict__ counts) {
+  __shared__ int hist[MAX_FUNCS];
+  for (int f = threadIdx.x; f < MAX_FUNCS; f += blockDim.x) hist[f] = 0;
+  __syncthreads();
+  const int n_uc = L0 * L1 * L2;
+  const int n = n_uc * T.n_sublat;
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < n; l += gridDim.x * blockDim.x) {
+    const int b = l / n_uc, uc = l - b * n_uc;
+    const int i = uc % L0, j = (uc / L0) % L1, k = uc / (L0 * L1);
+    const int o0 = occ[l];
+    if (o0 == 0) continue;  // every owned cluster contains its anchor
+    for (int g = 0; g < T.n_orbits; ++g) {
+      const int size = T.orb_size[g];
+      for (int c = T.ow_begin[b][g]; c < T.ow_begin[b][g + 1]; ++c) {
+        const int cc = T.n_fl + c;
+        int code = o0 - 1, mul = NOCC - 1;
+        bool ok = true;
+        for (int q = 0; q < size - 1; ++q) {
+          const int pb = T.cl_pb[cc * 3 + q];
+          const int *du = T.cl_du + cc * 9 + q * 3;
+          const int site = pb * n_uc + wrapc(i + du[0], L0) +
+                           L0 * (wrapc(j + du[1], L1) + L1 * wrapc(k + du[2], L2));
+          const int v = occ[site];
+          ok = ok && (v != 0);
+          code += (v - 1) * mul;
+          mul *= (NOCC - 1);
+        }
+        if (ok) atomicAdd(&hist[T.orb_func_base[g] + T.lut[T.cl_lut[cc] + code]], 1);
+      }
+    }
+  }
+  __syncthreads();
+  for (int f = threadIdx.x; f < T.n_funcs; f += blockDim.x)
+    if (hist[f]) atomicAdd(&counts[f], (unsigned long long)hist[f]);
+}
+
+// Exact initial state of every replica (one CTA per replica): function
+// counts -> formation energy, species counts; clears the sampled moments.
+template <int NOCC>
+__global__ void k_init_stats(const __grid_constant__ CeTables T, const Replica *__restrict__ reps,
+                             ReplicaStats *__restrict__ stats, const int8_t *__restrict__ occ_all) {
+  __shared__ unsigned long long hist[MAX_FUNCS];
+  __shared__ unsigned long long spec[8];
+  const Replica &R = reps[blockIdx.x];
+  for (int f = threadIdx.x; f < MAX_FUNCS; f += blockDim.x) hist[f] = 0ull;
+  if (threadIdx.x < 8) spec[threadIdx.x] = 0ull;
+  __syncthreads();
+  const int L0 = R.L[0], L1 = R.L[1], L2 = R.L[2];
+  const int n_uc = L0 * L1 * L2, n = n_uc * T.n_sublat;
+  const int8_t *occ = occ_all + R.occ_offset;
+  int lspec[NOCC];
+  for (int a = 0; a < NOCC; ++a) lspec[a] = 0;
+  for (int l = threadIdx.x; l < n; l += blockDim.x) {
+    const int b = l / n_uc, uc = l - b * n_uc;
+    const int i = uc % L0, j = (uc / L0) % L1, k = uc / (L0 * L1);
+    const int o0 = occ[l];
+    lspec[o0]++;
+    if (o0 == 0) continue;
+    for (int g = 0; g < T.n_orbits; ++g) {
+      const int size = T.orb_size[g];
+      for (int c = T.ow_begin[b][g]; c < T.ow_begin[b][g + 1]; ++c) {
+        const int cc = T.n_fl + c;
+        int code = o0 - 1, mul = NOCC - 1;
+        bool ok = true;
+        for (int q = 0; q < size - 1; ++q) {
+          const int pb = T.cl_pb[cc * 3 + q];
+          const int *du = T.cl_du + cc * 9 + q * 3;
+          const int site = pb * n_uc + wrapc(i + du[0], L0) +
+                           L0 * (wrapc(j + du[1], L1) + L1 * wrapc(k + du[2], L2));
+          const int v = occ[site];
+          ok = ok && (v != 0);
+          code += (v - 1) * mul;
+          mul *= (NOCC - 1);
+        }
+        if (ok) atomicAdd(&hist[T.orb_func_base[g] + T.lut[T.cl_lut[cc] + code]], 1ull);
+      }
+    }
+  }
+  for (int a = 0; a < NOCC; ++a)
+    if (lspec[a]) atomicAdd(&spec[a], (unsigned long long)lspec[a]);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ReplicaStats &S = stats[blockIdx.x];
+    double e = T.w[0] * n_uc;
+    for (int f = 1; f < T.n_funcs; ++f) e += T.w[f] * (double)hist[f];
+    const long long pass = S.pass, np = S.n_proposed, na = S.n_accepted;
+    unsigned char *raw = reinterpret_cast<unsigned char *>(&S);
+    for (int q = 0; q < (int)sizeof(ReplicaStats); ++q) raw[q] = 0;
+    S.energy = e;
+    for (int a = 0; a < NOCC; ++a) S.n_species[a] = (int64_t)spec[a];
+    S.pass = pass;
+    S.n_proposed = np;
+    S.n_accepted = na;
+  }
+}
+
+// ------------------------------------------------------------ batched delta
+template <int NOCC>
+__global__ void k_delta(const __grid_constant__ CeTables T, const int8_t *__restrict__ occ,
+                        int L0, int L1, int L2, int n_events, int k_sites,
+                        const long long *__restrict__ sites, const int *__restrict__ new_occ,
+                        const double *__restrict__ dmu, double *__restrict__ dE,
+                        long long *__restrict__ dcount) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_events) return;
+  const int n_uc = L0 * L1 * L2;
+  Acc<NOCC> acc;
+  acc.zero();
+  double mu_term = 0.0;
+  int ov_site[4], ov_val[4];
+  for (int s = 0; s < k_sites; ++s) {
+    const int l = (int)sites[e * k_sites + s];
+    const int b = l / n_uc, uc = l - b * n_uc;
+    const int i = uc % L0, j = (uc / L0) % L1, k = uc / (L0 * L1);
+    int o_i = occ[l];
+    for (int q = 0; q < s; ++q)
+      if (ov_site[q] == l) o_i = ov_val[q];
+    const int o_f = new_occ[e * k_sites + s];
+    auto rd = [&](int c, int jj) -> int {
+      const int pb = T.cl_pb[c * 3 + jj];
+      const int *du = T.cl_du + c * 9 + jj * 3;
+      const int site = pb * n_uc + wrapc(i + du[0], L0) +
+                       L0 * (wrapc(j + du[1], L1) + L1 * wrapc(k + du[2], L2));
+      int v = occ[site];
+      for (int q = 0; q < s; ++q)
+        if (ov_site[q] == site) v = ov_val[q];
+      return v;
+    };
+    accumulate_site<NOCC>(T, b, o_i, o_f, T.cl_lut, T.lut, rd, acc);
+    if (dmu) mu_term += dmu[o_i * NOCC + o_f];
+    ov_site[s] = l;
+    ov_val[s] = o_f;
+  }
+  FF d = acc_dot<NOCC>(T, acc, T.w_hi, T.w_lo);
+  dE[e] = ((double)d.s + (double)d.e) - mu_term;
+  if (dcount) acc_store<NOCC>(T, acc, dcount + (long long)e * T.n_funcs);
+}
+
+// ------------------------------------------------------------ replay
+// std::uniform_int_distribution<long>(0, max) over a 64-bit engine, as
+// libstdc++ implements it: Lemire's nearly divisionless method (Lemire,
+// "Fast Random Integer Generation in an Interval", ACM TOMACS 2019) with a
+// 128-bit product. The oracle tests pin this against the host library.
+struct MtState {
+  unsigned long long mt[MT_N];
+  int idx;
+  unsigned long long draws;
+};
+
+__device__ inline unsigned long long mt_draw(MtState &s) {
+  if (s.idx >= MT_N) {
+    for (int i = 0; i < MT_N; ++i) {
+      s.mt[i] = mt_next_word(s.mt[i], s.mt[(i + 1) % MT_N], s.mt[(i + MT_M) % MT_N]);
+    }
+    s.idx = 0;
+  }
+  s.draws++;
+  return mt_temper(s.mt[s.idx++]);
+}
+
+__device__ inline long long std_random_int(MtState &s, long long maxv) {
+  const unsigned long long range = (unsigned long long)maxv + 1ull;  // 0 means 2^64
+  unsigned long long x = mt_draw(s);
+  if (range == 0ull) return (long long)x;
+  unsigned long long lo = x * range, hi = __umul64hi(x, range);
+  if (lo < range) {
+    const unsigned long long threshold = (0ull - range) % range;
+    while (lo < threshold) {
+      x = mt_draw(s);
+      lo = x * range;
+      hi = __umul64hi(x, range);
+    }
+  }
+  return (long long)hi;
+}
+
+// std::uniform_real_distribution<double>(0, 1) over a 64-bit engine:
+// generate_canonical<double, 53> takes one draw, x / 2^64 rounded to double,
+// with 1.0 mapped to the largest double below 1.
+__device__ inline double std_random_real(MtState &s) {
+  const unsigned long long x = mt_draw(s);
+  double r = __ull2double_rn(x) * 5.42101086242752217e-20;  // 2^-64
+  if (r >= 1.0) r = 0.99999999999999988898;                 // nextafter(1, 0)
+  return r;
+}
+
+template <int NOCC>
+__global__ void k_replay(const __grid_constant__ CeTables T, ReplayParams P) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  MtState &mt = *reinterpret_cast<MtState *>(smem);
+  int8_t *occ = reinterpret_cast<int8_t *>(smem + sizeof(MtState));
+  const int N = P.n_sites;
+  int *pos = reinterpret_cast<int *>(smem + sizeof(MtState) + ((N + 15) & ~15));
+  int *lists = pos + N;  // NOCC lists of capacity N
+  __shared__ int list_size[NOCC];
+  __shared__ long long ev_site[2];
+  __shared__ int ev_new[2], ev_n, ev_stop;
+  const int lane = threadIdx.x;
+  const int L0 = P.L[0], L1 = P.L[1], L2 = P.L[2];
+  const int n_uc = L0 * L1 * L2;
+
+  for (int l = lane; l < N; l += 32) occ[l] = P.occ[l];
+  __syncwarp();
+  if (lane == 0) {
+    mt.mt[0] = P.mt_seed;
+    for (int i = 1; i < MT_N; ++i)
+      mt.mt[i] = 6364136223846793005ull * (mt.mt[i - 1] ^ (mt.mt[i - 1] >> 62)) + (unsigned long long)i;
+    mt.idx = MT_N;
+    mt.draws = 0;
+    for (int a = 0; a < NOCC; ++a) list_size[a] = 0;
+    for (int l = 0; l < N; ++l) {
+      const int a = occ[l];
+      pos[l] = list_size[a];
+      lists[a * N + list_size[a]] = l;
+      list_size[a]++;
+    }
+    ev_stop = 0;
+  }
+  __syncwarp();
+  long long n_acc = 0;
+  const double beta = P.beta;
+  for (long long step = 0; step < P.n_steps; ++step) {
+    // ---- propose (lane 0): swap type by integer count, then candidates
+    if (lane == 0) {
+      long long cum[NOCC * NOCC];
+      int ta[NOCC * NOCC], tb[NOCC * NOCC];
+      int nt = 0;
+      long long tsum = 0;
+      for (int a = 0; a < NOCC; ++a)
+        for (int bb = 0; bb < NOCC; ++bb) {
+          if (a == bb) continue;
+          if (P.ensemble == 1 && bb < a) continue;
+          long long w = list_size[a];
+          if (P.ensemble == 1) w *= list_size[bb];
+          tsum += w;
+          cum[nt] = tsum;
+          ta[nt] = a;
+          tb[nt] = bb;
+          nt++;
+        }
+      if (tsum == 0) {
+        ev_stop = 1;
+      } else {
+        const long long cnt = std_random_int(mt, tsum - 1);
+        int it = 0;
+        while (cum[it] <= cnt) ++it;  // upper_bound
+        const int a = ta[it], bb = tb[it];
+        if (P.ensemble == 1) {
+          const long long ia = std_random_int(mt, list_size[a] - 1);
+          const long long ib = std_random_int(mt, list_size[bb] - 1);
+          ev_site[0] = lists[a * N + ia];
+          ev_site[1] = lists[bb * N + ib];
+          ev_new[0] = bb;
+          ev_new[1] = a;
+          ev_n = 2;
+        } else {
+          const long long ia = std_random_int(mt, list_size[a] - 1);
+          ev_site[0] = lists[a * N + ia];
+          ev_new[0] = bb;
+          ev_n = 1;
+        }
+      }
+    }
+    __syncwarp();
+    if (ev_stop) break;
+    // ---- delta correlations: lanes split each centre's flower clusters
+    Acc<NOCC> acc;
+    acc.zero();
+    const int n = ev_n;
+    int saved = 0;
+    for (int s = 0; s < n; ++s) {
+      const int l = (int)ev_site[s];
+      const int b = l / n_uc, uc = l - b * n_uc;
+      const int i = uc % L0, j = (uc / L0) % L1, k = uc / (L0 * L1);
+      const int o_i = occ[l], o_f = ev_new[s];
+      if (lane == 0 && s == 0) saved = o_i;
+#pragma unroll
+      for (int g = 0; g < MAX_ORBITS; ++g) {
+        if (g < T.n_orbits) {
+          const int c0 = T.fl_begin[b][g], c1 = T.fl_begin[b][g + 1];
+          const int size = T.orb_size[g];
+          int cnt = 0;
+          unsigned long long pp = 0ull, mm = 0ull;
+          for (int c = c0 + lane; c < c1; c += 32) {
+            int code = 0, mul = NOCC - 1, prod = 1;
+            bool ok = true;
+            for (int q = 0; q < size - 1; ++q) {
+              const int pb = T.cl_pb[c * 3 + q];
+              const int *du = T.cl_du + c * 9 + q * 3;
+              const int site = pb * n_uc + wrapc(i + du[0], L0) +
+                               L0 * (wrapc(j + du[1], L1) + L1 * wrapc(k + du[2], L2));
+              const int v = occ[site];
+              prod &= v;
+              ok = ok && (v != 0);
+              code += (v - 1) * mul;
+              mul *= (NOCC - 1);
+            }
+            if constexpr (NOCC == 2) {
+              cnt += prod;
+            } else {
+              if (ok) {
+                const int base = T.cl_lut[c] + code;
+                if (o_f) pp += 1ull << (8 * T.lut[base + o_f - 1]);
+                if (o_i) mm += 1ull << (8 * T.lut[base + o_i - 1]);
+              }
+            }
+          }
+          if constexpr (NOCC == 2) {
+            for (int off = 16; off; off >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
+            acc.c[g] += (o_f - o_i) * cnt;
+          } else {
+            for (int off = 16; off; off >>= 1) {
+              pp += __shfl_xor_sync(0xffffffffu, pp, off);
+              mm += __shfl_xor_sync(0xffffffffu, mm, off);
+            }
+            acc.p[g] += pp;
+            acc.m[g] += mm;
+          }
+        }
+      }
+      __syncwarp();
+      if (s + 1 < n) {  // sequential semantics: apply this change first
+        if (lane == 0) occ[l] = (int8_t)o_f;
+        __syncwarp();
+      }
+    }
+    // ---- dE, acceptance and application (lane 0)
+    if (lane == 0) {
+      if (n > 1) occ[ev_site[0]] = (int8_t)saved;
+      FF d = acc_dot<NOCC>(T, acc, T.w_hi, T.w_lo);
+      double de = (double)d.s + (double)d.e;
+      if (P.ensemble == 0) de -= P.dmu[occ[ev_site[0]] * NOCC + ev_new[0]];
+      bool accept = true;
+      if (!(de < 0.0)) accept = std_random_real(mt) < exp(-de * beta);
+      if (P.accept_seq) P.accept_seq[step] = accept ? 1 : 0;
+      if (P.de_seq) P.de_seq[step] = de;
+      if (P.site_seq) {
+        P.site_seq[2 * step] = ev_site[0];
+        P.site_seq[2 * step + 1] = (n > 1) ? ev_site[1] : -1;
+      }
+      if (accept) {
+        ++n_acc;
+        for (int s = 0; s < n; ++s) {
+          const int l = (int)ev_site[s];
+          const int from = occ[l], to = ev_new[s];
+          int *la = lists + from * N;
+          const int p = pos[l];
+          const int last = la[list_size[from] - 1];
+          la[p] = last;
+          pos[last] = p;
+          list_size[from]--;
+          pos[l] = list_size[to];
+          lists[to * N + list_size[to]] = l;
+          list_size[to]++;
+          occ[l] = (int8_t)to;
+        }
+      }
+    }
+    __syncwarp();
+  }
+  __syncwarp();
+  for (int l = lane; l < N; l += 32) P.occ[l] = occ[l];
+  if (lane == 0) {
+    P.result[0] = n_acc;
+    P.result[1] = (long long)mt.draws;
+    P.result[2] = ev_stop;
+  }
+}
+
+// ------------------------------------------------------------ parallel sweep
+// Sub-step kinds of one pass.
+enum : int { SUB_FLIP = 0, SUB_PAIR_CLASS = 1, SUB_PAIR_LOCAL = 2 };
+constexpr uint32_t TAG_SITE = 0x1u, TAG_SCHED = 0x2u;
+constexpr int N_LOCAL_SWEEPS = 4;
+
+struct SweepSmem {
+  // carved from dynamic shared memory; offsets in bytes
+  int occ, cl_off, lutoff, lut, whi, wlo, ax, sched, red, total;
+};
+
+__host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
+
+__host__ __device__ inline void sweep_layout(const CeTables &T, int L0, int L1, int L2,
+                                             int n_classes_max, SweepSmem &s) {
+  const int R = T.reach;
+  const int V = (L0 + 2 * R) * (L1 + 2 * R) * (L2 + 2 * R);
+  int o = 0;
+  s.occ = o;
+  o += align16(T.n_sublat * V);
+  s.cl_off = o;
+  o += align16(T.n_fl * 3 * 4);
+  s.lutoff = o;
+  o += align16(T.n_fl * 4);
+  s.lut = o;
+  o += align16(T.n_fl * (T.n_sf * T.n_sf * T.n_sf * T.n_sf));
+  s.whi = o;
+  o += align16(T.n_funcs * 4);
+  s.wlo = o;
+  o += align16(T.n_funcs * 4);
+  s.ax = o;  // per axis: begin[MAX_COLOURS], cnt[MAX_COLOURS], coord[MAX_L]
+  o += align16(3 * (2 * MAX_COLOURS + MAX_L) * 4);
+  s.sched = o;  // key[n], par[n], order[n] (u32 each), n = 5 * n_classes
+  o += align16(3 * (1 + N_LOCAL_SWEEPS) * n_classes_max * 4);
+  s.red = o;  // block reduction scratch: 32 warps x (2 doubles + 8 + 2 longs)
+  o += align16(32 * (2 * 8 + 10 * 8));
+  s.total = o;
+}
+
+inline int sweep_smem_bytes_impl(const CeTables &T, int L0, int L1, int L2, int n_classes) {
+  SweepSmem s;
+  sweep_layout(T, L0, L1, L2, n_classes, s);
+  return s.total;
+}
+
+struct Geo {
+  int L0, L1, L2, R, W, H, V;
+  __device__ __forceinline__ int addr(int b, int x, int y, int z) const {
+    return b * V + (x + R) + W * ((y + R) + H * (z + R));
+  }
+};
+
+// Write occupant v to core site (b,x,y,z) and all of its periodic halo images.
+__device__ __forceinline__ void put_site(int8_t *occ, const Geo &G, int b, int x, int y, int z,
+                                         int8_t v) {
+  const int xs[2] = {x, x < G.R ? x + G.L0 : (x >= G.L0 - G.R ? x - G.L0 : INT32_MIN)};
+  const int ys[2] = {y, y < G.R ? y + G.L1 : (y >= G.L1 - G.R ? y - G.L1 : INT32_MIN)};
+  const int zs[2] = {z, z < G.R ? z + G.L2 : (z >= G.L2 - G.R ? z - G.L2 : INT32_MIN)};
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int xx = xs[c & 1], yy = ys[(c >> 1) & 1], zz = zs[(c >> 2) & 1];
+    if (xx != INT32_MIN && yy != INT32_MIN && zz != INT32_MIN) occ[G.addr(b, xx, yy, zz)] = v;
+  }
+}
+
+__device__ __forceinline__ bool accept_fast(const FF &d, float beta_f, float u) {
+  const float de = FADD(d.s, d.e);
+  if (de < 0.f) return true;
+  return u < cem_expf_neg(FMUL(-beta_f, de));
+}
+
+template <int NOCC>
+__global__ void __launch_bounds__(SWEEP_THREADS, 1)
+    k_sweep(const __grid_constant__ CeTables T, const __grid_constant__ SweepParams P) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int rep = blockIdx.x;
+  const Replica &R = P.reps[rep];
+  ReplicaStats &S = P.stats[rep];
+  const int tid = threadIdx.x, nth = blockDim.x;
+  Geo G;
+  G.L0 = R.L[0];
+  G.L1 = R.L[1];
+  G.L2 = R.L[2];
+  G.R = T.reach;
+  G.W = G.L0 + 2 * G.R;
+  G.H = G.L1 + 2 * G.R;
+  G.V = G.W * G.H * (G.L2 + 2 * G.R);
+  const int n_uc = G.L0 * G.L1 * G.L2;
+  const int nsl = T.n_sublat;
+  const int ncol_all = R.n_col[0] * R.n_col[1] * R.n_col[2];
+  const int n_classes = nsl * ncol_all;
+  SweepSmem lay;
+  sweep_layout(T, G.L0, G.L1, G.L2, P.max_classes, lay);
+  int8_t *occ = reinterpret_cast<int8_t *>(smem + lay.occ);
+  int *cl_off = reinterpret_cast<int *>(smem + lay.cl_off);
+  int *lutoff = reinterpret_cast<int *>(smem + lay.lutoff);
+  uint8_t *lut = reinterpret_cast<uint8_t *>(smem + lay.lut);
+  float *whi = reinterpret_cast<float *>(smem + lay.whi);
+  float *wlo = reinterpret_cast<float *>(smem + lay.wlo);
+  int *ax = reinterpret_cast<int *>(smem + lay.ax);
+  uint32_t *sched = reinterpret_cast<uint32_t *>(smem + lay.sched);
+  unsigned char *red = smem + lay.red;
+  int *ax_begin[3], *ax_cnt[3], *ax_coord[3];
+  for (int a = 0; a < 3; ++a) {
+    ax_begin[a] = ax + a * (2 * MAX_COLOURS + MAX_L);
+    ax_cnt[a] = ax_begin[a] + MAX_COLOURS;
+    ax_coord[a] = ax_cnt[a] + MAX_COLOURS;
+  }
+  // ---- stage tables
+  for (int c = tid; c < T.n_fl; c += nth) {
+    int cb = 0;
+    for (int b = 0; b < nsl; ++b)
+      if (c >= T.fl_begin[b][0]) cb = b;
+    for (int q = 0; q < 3; ++q) {
+      const int pb = T.cl_pb[c * 3 + q];
+      const int *du = T.cl_du + c * 9 + q * 3;
+      cl_off[c * 3 + q] = (pb < 0) ? 0 : (pb - cb) * G.V + du[0] + G.W * (du[1] + G.H * du[2]);
+    }
+    lutoff[c] = T.cl_lut[c];
+  }
+  const int lut_n = T.n_fl * (T.n_sf * T.n_sf * T.n_sf * T.n_sf);
+  for (int i = tid; i < lut_n; i += nth) lut[i] = T.lut[i];
+  for (int f = tid; f < T.n_funcs; f += nth) {
+    whi[f] = T.w_hi[f];
+    wlo[f] = T.w_lo[f];
+  }
+  if (tid < 3) {  // colour lists per axis, blocks of size p (or more)
+    const int a = tid, L = R.L[a], p = R.p;
+    const int q = L / p;
+    int coord_col[MAX_L];
+    int x = 0;
+    for (int blk = 0; blk < q; ++blk) {
+      int sz = p + (L - q * p) / q + ((blk < (L - q * p) % q) ? 1 : 0);
+      for (int t = 0; t < sz; ++t) coord_col[x++] = t;
+    }
+    int k = 0;
+    for (int c = 0; c < R.n_col[a]; ++c) {
+      ax_begin[a][c] = k;
+      for (int xx = 0; xx < L; ++xx)
+        if (coord_col[xx] == c) ax_coord[a][k++] = xx;
+      ax_cnt[a][c] = k - ax_begin[a][c];
+    }
+  }
+  // ---- occupation: global -> shared core, then periodic halo
+  const int8_t *gocc = P.occ + R.occ_offset;
+  const int n_sites = n_uc * nsl;
+  for (int l = tid; l < n_sites; l += nth) {
+    const int b = l / n_uc, uc = l - b * n_uc;
+    const int x = uc % G.L0, y = (uc / G.L0) % G.L1, z = uc / (G.L0 * G.L1);
+    occ[G.addr(b, x, y, z)] = gocc[l];
+  }
+  __syncthreads();
+  {
+    const int D = G.L2 + 2 * G.R;
+    for (int h = tid; h < nsl * G.V; h += nth) {
+      const int b = h / G.V;
+      int r = h - b * G.V;
+      const int xh = r % G.W;
+      r /= G.W;
+      const int yh = r % G.H, zh = r / G.H;
+      (void)D;
+      const int x = xh - G.R, y = yh - G.R, z = zh - G.R;
+      if (x >= 0 && x < G.L0 && y >= 0 && y < G.L1 && z >= 0 && z < G.L2) continue;
+      occ[h] = occ[G.addr(b, wrapc(x, G.L0), wrapc(y, G.L1), wrapc(z, G.L2))];
+    }
+  }
+  __syncthreads();
+
+  // ---- passes
+  double energy = S.energy;
+  long long nspec[8];
+  for (int a = 0; a < 8; ++a) nspec[a] = S.n_species[a];
+  long long pass_global = S.pass;
+  const uint32_t k0 = (uint32_t)R.seed, k1 = (uint32_t)(R.seed >> 32);
+  const int n_sweeps = (R.ensemble == 1) ? 1 + N_LOCAL_SWEEPS : 1;
+  const int n_sub = n_sweeps * n_classes;
+  uint32_t *skey = sched, *spar = sched + n_sub, *sord = sched + 2 * n_sub;
+  const int lane = tid & 31, warp = tid >> 5, nwarp = nth >> 5;
+
+  for (long long ip = 0; ip < P.n_passes; ++ip, ++pass_global) {
+    const uint32_t plo = (uint32_t)pass_global, phi = (uint32_t)(pass_global >> 32) & 0xFFFFu;
+    // schedule: per sweep a random order of the classes, plus parameters
+    for (int e = tid; e < n_sub; e += nth) {
+      const int c = e % n_classes;
+      U4 r = philox4x32_10(U4{0xFFFFFFFFu - (uint32_t)e, 0u, plo, phi | (TAG_SCHED << 16)}, k0, k1);
+      skey[e] = r.x;
+      const int cb = c / ncol_all, cr = c - cb * ncol_all;
+      const int cc[3] = {cr % R.n_col[0], (cr / R.n_col[0]) % R.n_col[1],
+                         cr / (R.n_col[0] * R.n_col[1])};
+      int dims[3];
+      for (int a = 0; a < 3; ++a) dims[a] = ax_cnt[a][cc[a]];
+      const int sweep = e / n_classes;
+      uint32_t par = 0;
+      if (R.ensemble == 1 && sweep == 0) {  // pairs within the class
+        int a = r.y % 3, tries = 0;
+        while (dims[a] < 2 && tries < 3) {
+          a = (a + 1) % 3;
+          ++tries;
+        }
+        if (dims[a] >= 2) {
+          const int m = 1 + (int)(r.z % (uint32_t)(dims[a] / 2));
+          const int rot = (int)(r.w % (uint32_t)dims[a]);
+          par = (uint32_t)a | ((uint32_t)m << 2) | ((uint32_t)rot << 10);
+        } else {
+          par = 0xFFFFFFFFu;  // no pair along any axis
+        }
+      } else if (R.ensemble == 1) {  // local pairs with a neighbour
+        const int nnb = T.n_nb[cb];
+        const int dlt = (int)(r.y % (uint32_t)(nnb > 0 ? nnb : 1));
+        const uint32_t parity = r.z & 7u;
+        uint32_t rots = 0;
+        for (int a = 0; a < 3; ++a) {
+          const uint32_t ra = (r.w >> (8 * a)) & 255u;
+          rots |= (uint32_t)(ra % (uint32_t)dims[a]) << (7 * a);
+        }
+        par = parity | ((uint32_t)dlt << 3) | (rots << 7);
+      }
+      spar[e] = par;
+    }
+    __syncthreads();
+    for (int e = tid; e < n_sub; e += nth) {
+      const int sw = e / n_classes, c = e - sw * n_classes;
+      const uint32_t key = skey[e];
+      int rank = 0;
+      for (int c2 = 0; c2 < n_classes; ++c2) {
+        const uint32_t k2 = skey[sw * n_classes + c2];
+        rank += (k2 < key) || (k2 == key && c2 < c);
+      }
+      sord[sw * n_classes + rank] = (uint32_t)c;
+    }
+    __syncthreads();
+
+    double de_acc = 0.0;
+    int dspec[NOCC];
+    for (int a = 0; a < NOCC; ++a) dspec[a] = 0;
+    int n_prop = 0, n_acc = 0;
+
+    for (int sub = 0; sub < n_sub; ++sub) {
+      const int sw = sub / n_classes;
+      const int c = (int)sord[sub];
+      const uint32_t par = spar[sw * n_classes + c];
+      const int cb = c / ncol_all, cr = c - cb * ncol_all;
+      const int cc[3] = {cr % R.n_col[0], (cr / R.n_col[0]) % R.n_col[1],
+                         cr / (R.n_col[0] * R.n_col[1])};
+      const int dims[3] = {ax_cnt[0][cc[0]], ax_cnt[1][cc[1]], ax_cnt[2][cc[2]]};
+      const int *cx = ax_coord[0] + ax_begin[0][cc[0]];
+      const int *cy = ax_coord[1] + ax_begin[1][cc[1]];
+      const int *cz = ax_coord[2] + ax_begin[2][cc[2]];
+      const uint32_t ctr_sub = (uint32_t)sub;
+      if (R.ensemble == 0) {
+        // ---------------- flips of every site of the class
+        const int n = dims[0] * dims[1] * dims[2];
+        for (int q = tid; q < n; q += nth) {
+          const int ix = q % dims[0], iy = (q / dims[0]) % dims[1], iz = q / (dims[0] * dims[1]);
+          const int x = cx[ix], y = cy[iy], z = cz[iz];
+          const int ad = G.addr(cb, x, y, z);
+          const int o_i = occ[ad];
+          const int l = cb * n_uc + x + G.L0 * (y + G.L1 * z);
+          const U4 r = philox4x32_10(U4{(uint32_t)l, ctr_sub, plo, phi | (TAG_SITE << 16)}, k0, k1);
+          int o_f;
+          if constexpr (NOCC == 2) {
+            o_f = 1 - o_i;
+          } else {
+            const int alt = (int)(r.y % (uint32_t)(NOCC - 1));
+            o_f = alt < o_i ? alt : alt + 1;
+          }
+          Acc<NOCC> acc;
+          acc.zero();
+          auto rd = [&](int cl, int j) -> int { return occ[ad + cl_off[cl * 3 + j]]; };
+          accumulate_site<NOCC>(T, cb, o_i, o_f, lutoff, lut, rd, acc);
+          FF d = acc_dot<NOCC>(T, acc, whi, wlo);
+          ff_add_ff(d, -R.dmu_hi[o_i * NOCC + o_f], -R.dmu_lo[o_i * NOCC + o_f]);
+          ++n_prop;
+          if (accept_fast(d, R.beta_f, u24(r.x))) {
+            ++n_acc;
+            put_site(occ, G, cb, x, y, z, (int8_t)o_f);
+            de_acc += (double)d.s + (double)d.e + R.dmu[o_i * NOCC + o_f];
+            dspec[o_i]--;
+            dspec[o_f]++;
+          }
+        }
+      } else if (sw == 0) {
+        // ---------------- canonical swaps of pairs inside the class
+        if (par != 0xFFFFFFFFu) {
+          const int a = par & 3, m = (par >> 2) & 255, rot = par >> 10;
+          const int na = dims[a];
+          const int blocks = na / (2 * m);
+          const int half = blocks * m;  // pairs along the axis
+          const int d1 = dims[(a + 1) % 3], d2 = dims[(a + 2) % 3];
+          const int n = half * d1 * d2;
+          for (int q = tid; q < n; q += nth) {
+            const int jj = q % half, rest = q / half;
+            const int o1 = rest % d1, o2 = rest / d1;
+            const int u = 2 * m * (jj / m) + (jj % m);
+            int ia[3], ib[3];
+            ia[a] = (u + rot) % na;
+            ib[a] = (u + m + rot) % na;
+            ia[(a + 1) % 3] = ib[(a + 1) % 3] = o1;
+            ia[(a + 2) % 3] = ib[(a + 2) % 3] = o2;
+            const int xa = cx[ia[0]], ya = cy[ia[1]], za = cz[ia[2]];
+            const int xb = cx[ib[0]], yb = cy[ib[1]], zb = cz[ib[2]];
+            const int ada = G.addr(cb, xa, ya, za), adb = G.addr(cb, xb, yb, zb);
+            const int oa = occ[ada], ob = occ[adb];
+            if (oa == ob) continue;
+            const int la = cb * n_uc + xa + G.L0 * (ya + G.L1 * za);
+            const U4 r = philox4x32_10(U4{(uint32_t)la, ctr_sub, plo, phi | (TAG_SITE << 16)}, k0, k1);
+            Acc<NOCC> acc;
+            acc.zero();
+            auto rda = [&](int cl, int j) -> int { return occ[ada + cl_off[cl * 3 + j]]; };
+            auto rdb = [&](int cl, int j) -> int { return occ[adb + cl_off[cl * 3 + j]]; };
+            accumulate_site<NOCC>(T, cb, oa, ob, lutoff, lut, rda, acc);
+            accumulate_site<NOCC>(T, cb, ob, oa, lutoff, lut, rdb, acc);
+            const FF d = acc_dot<NOCC>(T, acc, whi, wlo);
+            ++n_prop;
+            if (accept_fast(d, R.beta_f, u24(r.x))) {
+              ++n_acc;
+              put_site(occ, G, cb, xa, ya, za, (int8_t)ob);
+              put_site(occ, G, cb, xb, yb, zb, (int8_t)oa);
+              de_acc += (double)d.s + (double)d.e;
+            }
+          }
+        }
+      } else {
+        // ---------------- canonical swaps with a neighbour (sequential dE)
+        const int parity = par & 7, dlt = (par >> 3) & 15;
+        const int rots[3] = {(int)((par >> 7) & 127), (int)((par >> 14) & 127),
+                             (int)((par >> 21) & 127)};
+        if (T.n_nb[cb] > 0) {
+          const int nb_b = T.nb_b[cb][dlt];
+          const int *du = T.nb_du[cb][dlt];
+          int h[3];
+          bool empty = false;
+          for (int a = 0; a < 3; ++a) {
+            h[a] = dims[a] >= 2 ? dims[a] / 2 : 1;
+            if (dims[a] < 2 && ((parity >> a) & 1)) empty = true;
+          }
+          const int n = empty ? 0 : h[0] * h[1] * h[2];
+          for (int q = tid; q < n; q += nth) {
+            const int t[3] = {q % h[0], (q / h[0]) % h[1], q / (h[0] * h[1])};
+            int ii[3];
+            for (int a = 0; a < 3; ++a)
+              ii[a] = dims[a] >= 2 ? (rots[a] + ((parity >> a) & 1) + 2 * t[a]) % dims[a] : 0;
+            const int xa = cx[ii[0]], ya = cy[ii[1]], za = cz[ii[2]];
+            const int xb = wrapc(xa + du[0], G.L0), yb = wrapc(ya + du[1], G.L1),
+                      zb = wrapc(za + du[2], G.L2);
+            const int ada = G.addr(cb, xa, ya, za), adb = G.addr(nb_b, xb, yb, zb);
+            const int oa = occ[ada], ob = occ[adb];
+            if (oa == ob) continue;
+            const int la = cb * n_uc + xa + G.L0 * (ya + G.L1 * za);
+            const U4 r = philox4x32_10(U4{(uint32_t)la, ctr_sub, plo, phi | (TAG_SITE << 16)}, k0, k1);
+            Acc<NOCC> acc;
+            acc.zero();
+            auto rda = [&](int cl, int j) -> int { return occ[ada + cl_off[cl * 3 + j]]; };
+            auto rdb = [&](int cl, int j) -> int { return occ[adb + cl_off[cl * 3 + j]]; };
+            accumulate_site<NOCC>(T, cb, oa, ob, lutoff, lut, rda, acc);
+            put_site(occ, G, cb, xa, ya, za, (int8_t)ob);  // first change applied
+            accumulate_site<NOCC>(T, nb_b, ob, oa, lutoff, lut, rdb, acc);
+            const FF d = acc_dot<NOCC>(T, acc, whi, wlo);
+            ++n_prop;
+            if (accept_fast(d, R.beta_f, u24(r.x))) {
+              ++n_acc;
+              put_site(occ, G, nb_b, xb, yb, zb, (int8_t)oa);
+              de_acc += (double)d.s + (double)d.e;
+            } else {
+              put_site(occ, G, cb, xa, ya, za, (int8_t)oa);
+            }
+          }
+        }
+      }
+      __syncthreads();
+    }
+
+    // ---- end of pass: reduce, sample
+    {
+      double v = de_acc;
+      long long vp = n_prop, va = n_acc;
+      long long vs[NOCC];
+      for (int a = 0; a < NOCC; ++a) vs[a] = dspec[a];
+      for (int off = 16; off; off >>= 1) {
+        v += __shfl_xor_sync(0xffffffffu, v, off);
+        vp += __shfl_xor_sync(0xffffffffu, vp, off);
+        va += __shfl_xor_sync(0xffffffffu, va, off);
+        for (int a = 0; a < NOCC; ++a) vs[a] += __shfl_xor_sync(0xffffffffu, vs[a], off);
+      }
+      double *rd_d = reinterpret_cast<double *>(red);
+      long long *rd_l = reinterpret_cast<long long *>(red + 32 * 8);
+      if (lane == 0) {
+        rd_d[warp] = v;
+        rd_l[warp * 10 + 0] = vp;
+        rd_l[warp * 10 + 1] = va;
+        for (int a = 0; a < NOCC; ++a) rd_l[warp * 10 + 2 + a] = vs[a];
+      }
+      __syncthreads();
+      if (tid == 0) {
+        double dsum = 0.0;
+        long long sp = 0, sa = 0;
+        for (int w = 0; w < nwarp; ++w) {
+          dsum += rd_d[w];
+          sp += rd_l[w * 10 + 0];
+          sa += rd_l[w * 10 + 1];
+          for (int a = 0; a < NOCC; ++a) nspec[a] += rd_l[w * 10 + 2 + a];
+        }
+        energy += dsum;
+        S.n_proposed += sp;
+        S.n_accepted += sa;
+        // param composition per unit cell and potential per unit cell
+        double x[3] = {0.0, 0.0, 0.0}, mux = 0.0;
+        for (int k = 0; k < NOCC - 1; ++k) {
+          double t = 0.0;
+          for (int a = 0; a < NOCC; ++a)
+            t += P.RT[k * NOCC + a] * ((double)nspec[a] - (a == 0 ? (double)n_sites : 0.0));
+          x[k] = t / n_uc;
+          mux += R.mu[k] * x[k];
+        }
+        const double ef = energy / n_uc;
+        const double ep = ef - mux;
+        if (ip >= P.n_equil) {
+          S.n_samples += 1.0;
+          S.sum_e += ep;
+          S.sum_e2 += ep * ep;
+          S.sum_f += ef;
+          for (int k = 0; k < NOCC - 1; ++k) {
+            S.sum_x[k] += x[k];
+            S.sum_ex[k] += ep * x[k];
+            for (int k2 = 0; k2 < NOCC - 1; ++k2) S.sum_xx[k * 3 + k2] += x[k] * x[k2];
+          }
+          if (P.samples) {
+            const long long si = (long long)(S.n_samples) - 1;
+            if (si < P.sample_capacity) {
+              double *out = P.samples + (long long)rep * P.sample_capacity * P.sample_width +
+                            si * P.sample_width;
+              out[0] = ep;
+              for (int k = 0; k < NOCC - 1; ++k) out[1 + k] = x[k];
+            }
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  // ---- write back
+  for (int l = tid; l < n_sites; l += nth) {
+    const int b = l / n_uc, uc = l - b * n_uc;
+    const int x = uc % G.L0, y = (uc / G.L0) % G.L1, z = uc / (G.L0 * G.L1);
+    P.occ[R.occ_offset + l] = occ[G.addr(b, x, y, z)];
+  }
+  if (tid == 0) {
+    S.energy = energy;
+    for (int a = 0; a < NOCC; ++a) S.n_species[a] = nspec[a];
+    S.pass = pass_global;
+  }
+}
+
+// ------------------------------------------------------------ launchers
+template <int NOCC>
+cudaError_t launch_energy_t(const CeTables &T, const int8_t *occ, int L0, int L1, int L2,
+                            unsigned long long *counts, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(unsigned long long) * T.n_funcs, st);
+  if (e != cudaSuccess) return e;
+  const int n = L0 * L1 * L2 * T.n_sublat;
+  int grid = (n + 255) / 256;
+  if (grid > 4096) grid = 4096;
+  k_energy<NOCC><<<grid, 256, 0, st>>>(T, occ, L0, L1, L2, counts);
+  return cudaGetLastError();
+}
+
+template <int NOCC>
+cudaError_t launch_delta_t(const CeTables &T, const int8_t *occ, int L0, int L1, int L2,
+                           int n_events, int k_sites, const long long *sites, const int *new_occ,
+                           const double *dmu, double *dE, long long *dcount, cudaStream_t st) {
+  const int grid = (n_events + 127) / 128;
+  if (grid == 0) return cudaSuccess;
+  k_delta<NOCC><<<grid, 128, 0, st>>>(T, occ, L0, L1, L2, n_events, k_sites, sites, new_occ, dmu,
+                                      dE, dcount);
+  return cudaGetLastError();
+}
+
+template <int NOCC>
+cudaError_t launch_init_stats_t(const CeTables &T, const Replica *reps, ReplicaStats *stats,
+                                const int8_t *occ, int n_replicas, cudaStream_t st) {
+  k_init_stats<NOCC><<<n_replicas, 512, 0, st>>>(T, reps, stats, occ);
+  return cudaGetLastError();
+}
+
+inline int replay_smem_bytes_impl(int n_sites, int n_occ) {
+  return (int)sizeof(MtState) + ((n_sites + 15) & ~15) + 4 * n_sites * (1 + n_occ);
+}
+
+template <int NOCC>
+cudaError_t launch_replay_t(const CeTables &T, const ReplayParams &P, cudaStream_t st) {
+  const int smem = replay_smem_bytes_impl(P.n_sites, T.n_occ);
+  cudaError_t e =
+      cudaFuncSetAttribute(k_replay<NOCC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  k_replay<NOCC><<<1, 32, smem, st>>>(T, P);
+  return cudaGetLastError();
+}
+
+template <int NOCC>
+cudaError_t launch_sweep_t(const CeTables &T, const SweepParams &P, int n_replicas, int smem,
+                           cudaStream_t st) {
+  cudaError_t e =
+      cudaFuncSetAttribute(k_sweep<NOCC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  k_sweep<NOCC><<<n_replicas, SWEEP_THREADS, smem, st>>>(T, P);
+  return cudaGetLastError();
+}
+
+#define CEM_INSTANTIATE(N)                                                                     \
+  template cudaError_t launch_energy_t<N>(const CeTables &, const int8_t *, int, int, int,     \
+                                          unsigned long long *, cudaStream_t);                 \
+  template cudaError_t launch_delta_t<N>(const CeTables &, const int8_t *, int, int, int, int, \
+                                         int, const long long *, const int *, const double *,  \
+                                         double *, long long *, cudaStream_t);                 \
+  template cudaError_t launch_replay_t<N>(const CeTables &, const ReplayParams &, cudaStream_t); \
+  template cudaError_t launch_init_stats_t<N>(const CeTables &, const Replica *, ReplicaStats *, \
+                                              const int8_t *, int, cudaStream_t);              \
+  template cudaError_t launch_sweep_t<N>(const CeTables &, const SweepParams &, int, int,       \
+                                         cudaStream_t);
+
+}  // namespace cem

@@ -1,0 +1,120 @@
+// Run-time dispatch on the number of occupants per site.
+#include "cem_kernels.cuh"
+
+namespace cem {
+
+template <int N>
+cudaError_t launch_energy_t(const CeTables &, const int8_t *, int, int, int, unsigned long long *,
+                            cudaStream_t);
+template <int N>
+cudaError_t launch_delta_t(const CeTables &, const int8_t *, int, int, int, int, int,
+                           const long long *, const int *, const double *, double *, long long *,
+                           cudaStream_t);
+template <int N>
+cudaError_t launch_replay_t(const CeTables &, const ReplayParams &, cudaStream_t);
+template <int N>
+cudaError_t launch_init_stats_t(const CeTables &, const Replica *, ReplicaStats *, const int8_t *,
+                                int, cudaStream_t);
+template <int N>
+cudaError_t launch_sweep_t(const CeTables &, const SweepParams &, int, int, cudaStream_t);
+
+
+
+cudaError_t launch_energy(const CeTables &T, const int8_t *occ, int L0, int L1, int L2,
+                          unsigned long long *counts, cudaStream_t st) {
+  if (T.n_occ == 2) return launch_energy_t<2>(T, occ, L0, L1, L2, counts, st);
+  if (T.n_occ == 3) return launch_energy_t<3>(T, occ, L0, L1, L2, counts, st);
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_delta(const CeTables &T, const int8_t *occ, int L0, int L1, int L2,
+                         int n_events, int k_sites, const long long *sites, const int *new_occ,
+                         const double *dmu, double *dE, long long *dcount, cudaStream_t st) {
+  if (T.n_occ == 2)
+    return launch_delta_t<2>(T, occ, L0, L1, L2, n_events, k_sites, sites, new_occ, dmu, dE,
+                             dcount, st);
+  if (T.n_occ == 3)
+    return launch_delta_t<3>(T, occ, L0, L1, L2, n_events, k_sites, sites, new_occ, dmu, dE,
+                             dcount, st);
+  return cudaErrorInvalidValue;
+}
+
+int replay_smem_bytes(int n_sites, int n_occ) { return replay_smem_bytes_impl(n_sites, n_occ); }
+
+cudaError_t launch_replay(const CeTables &T, const ReplayParams &P, cudaStream_t st) {
+  if (T.n_occ == 2) return launch_replay_t<2>(T, P, st);
+  if (T.n_occ == 3) return launch_replay_t<3>(T, P, st);
+  return cudaErrorInvalidValue;
+}
+
+int sweep_smem_bytes(const CeTables &T, int L0, int L1, int L2, int n_classes) {
+  return sweep_smem_bytes_impl(T, L0, L1, L2, n_classes);
+}
+
+cudaError_t launch_sweep(const CeTables &T, const SweepParams &P, int n_replicas, int smem,
+                         cudaStream_t st) {
+  if (T.n_occ == 2) return launch_sweep_t<2>(T, P, n_replicas, smem, st);
+  if (T.n_occ == 3) return launch_sweep_t<3>(T, P, n_replicas, smem, st);
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_init_stats(const CeTables &T, const Replica *reps, ReplicaStats *stats,
+                              const int8_t *occ, int n_replicas, cudaStream_t st) {
+  if (T.n_occ == 2) return launch_init_stats_t<2>(T, reps, stats, occ, n_replicas, st);
+  if (T.n_occ == 3) return launch_init_stats_t<3>(T, reps, stats, occ, n_replicas, st);
+  return cudaErrorInvalidValue;
+}
+
+// Shared-memory read bandwidth probe: every thread streams 16-byte vector
+// loads over a 64 KB shared buffer; one CTA per SM slot.
+__global__ void k_smem_probe(int iters, unsigned long long *sink) {
+  extern __shared__ __align__(16) uint4 buf[];
+  const int n = 65536 / 16;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) buf[i] = make_uint4(i, i + 1, i + 2, i + 3);
+  __syncthreads();
+  uint32_t acc = 0;
+  int idx = threadIdx.x;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll 8
+    for (int k = 0; k < 8; ++k) {
+      const uint4 v = buf[(idx + k * blockDim.x) & (n - 1)];
+      acc ^= v.x ^ v.y ^ v.z ^ v.w;
+    }
+    idx = (idx + 8 * blockDim.x) & (n - 1);
+  }
+  if (acc == 0x12345678u) sink[blockIdx.x] = acc;
+}
+
+// Shared-memory read bandwidth (GB/s) over all SMs, from CUDA events.
+cudaError_t smem_bandwidth(double *gbs, cudaStream_t st) {
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const int smem = 65536, threads = 1024, iters = 4096, blocks = sms * 2;
+  e = cudaFuncSetAttribute(k_smem_probe, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  unsigned long long *sink = nullptr;
+  e = cudaMalloc(&sink, sizeof(unsigned long long) * blocks);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  k_smem_probe<<<blocks, threads, smem, st>>>(64, sink);  // warm-up
+  cudaEventRecord(a, st);
+  k_smem_probe<<<blocks, threads, smem, st>>>(iters, sink);
+  cudaEventRecord(b, st);
+  e = cudaEventSynchronize(b);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(sink);
+  if (e != cudaSuccess) return e;
+  const double bytes = (double)blocks * threads * iters * 8.0 * 16.0;
+  *gbs = bytes / (ms * 1e-3) / 1e9;
+  return cudaGetLastError();
+}
+
+}  // namespace cem

@@ -587,3 +587,68 @@ def verify_local_pairs(ce: ClusterExpansion, sc: Supercell, col: Colouring) -> b
                                 f"local pair move interacts: class {c} delta {du}"
                             )
     return True
+
+
+def composition_RT(n_basis: int, n_occ: int) -> np.ndarray:
+    """R^T = dparam_dmol for the standard composition axes (origin: every
+    site occupant 0; end member k: every site occupant k): the change of the
+    parametric composition per change of the species counts per unit cell
+    (reference ``SemiGrandCanonicalCalculator.cc:144``)."""
+    Q = np.zeros((n_occ, n_occ - 1))
+    for k in range(1, n_occ):
+        Q[0, k - 1] = -n_basis
+        Q[k, k - 1] = n_basis
+    return np.ascontiguousarray(np.linalg.pinv(Q))
+
+
+def system_arrays(ce: ClusterExpansion) -> dict:
+    """Flat arrays of the C ABI's ``cem_system_desc`` for a cluster expansion."""
+    n_sf = ce.n_sf
+    stride = n_sf**4
+    orbits = ce.orbits
+    out = dict(
+        n_sublat=ce.prim.n_basis,
+        n_occ=ce.prim.n_occ,
+        n_funcs=ce.n_funcs,
+        n_orbits=len(orbits),
+        orbit_size=np.array([o.size for o in orbits], dtype=np.int32),
+        orbit_func_begin=np.array([o.func_begin for o in orbits], dtype=np.int32),
+        orbit_n_funcs=np.array([o.n_funcs for o in orbits], dtype=np.int32),
+        weights=np.ascontiguousarray(ce.weights(), dtype=np.float64),
+        param_RT=composition_RT(ce.prim.n_basis, ce.prim.n_occ).reshape(-1),
+    )
+    for name, table in (("flower", ce.flowers), ("owned", ce.owned)):
+        sub, orb, psub, pdu, lut = [], [], [], [], []
+        for b in range(ce.prim.n_basis):
+            for c in table[b]:
+                sub.append(b)
+                orb.append(c.orbit)
+                ps = [-1, -1, -1]
+                pd = [0] * 9
+                for j, (pb, du) in enumerate(c.partners):
+                    ps[j] = pb
+                    pd[3 * j : 3 * j + 3] = list(du)
+                psub.append(ps)
+                pdu.append(pd)
+                row = np.full(stride, -1, dtype=np.int16)
+                row[: len(c.lut)] = c.lut
+                lut.append(row)
+        out[f"n_{name}"] = len(sub)
+        out[f"{name}_sublat"] = np.array(sub, dtype=np.int32)
+        out[f"{name}_orbit"] = np.array(orb, dtype=np.int32)
+        out[f"{name}_partner_sublat"] = np.array(psub, dtype=np.int32).reshape(-1)
+        out[f"{name}_partner_du"] = np.array(pdu, dtype=np.int32).reshape(-1)
+        out[f"{name}_lut"] = np.array(lut, dtype=np.int16).reshape(-1)
+    nb_n = np.zeros(ce.prim.n_basis, dtype=np.int32)
+    nb_s = np.zeros((ce.prim.n_basis, 16), dtype=np.int32)
+    nb_d = np.zeros((ce.prim.n_basis, 16, 3), dtype=np.int32)
+    for b in range(ce.prim.n_basis):
+        nbs = ce.neighbour_partners(b)[:16]
+        nb_n[b] = len(nbs)
+        for k, (pb, du) in enumerate(nbs):
+            nb_s[b, k] = pb
+            nb_d[b, k] = du
+    out["n_neighbour"] = nb_n
+    out["neighbour_sublat"] = nb_s.reshape(-1)
+    out["neighbour_du"] = nb_d.reshape(-1)
+    return out

@@ -1,0 +1,204 @@
+/*
+ * cem.h - C ABI of the GB300 cluster-expansion Metropolis hot path.
+ *
+ * The library replaces, behind a plain C ABI (no exceptions, no C++ or torch
+ * types), the per-event potential change and the Metropolis loop of
+ * libcasm-clexmonte's canonical and semi-grand canonical calculators:
+ *
+ *   occ_delta_per_supercell  BaseMonteCalculator.hh:41-43 (BaseMontePotential),
+ *                            CanonicalCalculator.cc:137-140,
+ *                            SemiGrandCanonicalCalculator.cc:186-213
+ *   per_supercell            BaseMonteCalculator.hh:33, CanonicalCalculator.cc:127-129
+ *   run                      BaseMonteCalculator.hh:223-225,
+ *                            CanonicalCalculator.cc:413-462,
+ *                            SemiGrandCanonicalCalculator.cc:423-466
+ *   occupation_metropolis_v2 include/casm/clexmonte/methods/occupation_metropolis.hh:72-123
+ *
+ * (paths relative to the CASMcode_clexmonte source tree). Every function
+ * returns CEM_OK or an error code; cem_last_error() gives the message of the
+ * last failure on the calling thread. Objects are not thread-safe: one host
+ * thread drives one cem_replicas at a time, as the reference's calculators
+ * are single-threaded (CanonicalCalculator.cc:413-462).
+ */
+#ifndef CEM_GB300_H
+#define CEM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CEM_OK 0
+#define CEM_ERR_INVALID 1     /* bad argument or inconsistent input */
+#define CEM_ERR_CUDA 2        /* CUDA runtime error (message says which) */
+#define CEM_ERR_UNSUPPORTED 3 /* valid input outside this build's limits */
+#define CEM_ERR_DEVICE 4      /* a kernel reported an error status */
+
+#define CEM_SEMIGRAND_CANONICAL 0
+#define CEM_CANONICAL 1
+
+typedef struct cem_system cem_system;
+typedef struct cem_replicas cem_replicas;
+
+/* Cluster-expansion tables (built by the host-side system builder).
+ * Occupation basis: site function k of occupant o is [o == k+1]; occupant 0
+ * is the reference species. Function 0 is the empty cluster. Energies:
+ * E = weights[0]*n_unitcells + sum_{f>=1} weights[f]*count_f, with count_f
+ * the number of clusters whose decoration is in class f and
+ * weights[f] = eci_f * coeff_f / mult_f. */
+typedef struct cem_system_desc {
+  int n_sublat;               /* basis sites per unit cell, 1..4 */
+  int n_occ;                  /* occupants per site, 2 or 3 */
+  int n_funcs;                /* functions including the empty function */
+  int n_orbits;               /* non-empty orbits, 1..8, in function order */
+  const int *orbit_size;      /* [n_orbits] sites per cluster, 1..4 */
+  const int *orbit_func_begin;/* [n_orbits] first function index */
+  const int *orbit_n_funcs;   /* [n_orbits] number of functions */
+  const double *weights;      /* [n_funcs] */
+  /* flower: every cluster containing site (b, cell 0), grouped by b, then
+   * by orbit; partner j of cluster c is site (partner_sublat[3c+j],
+   * cell partner_du[9c+3j .. 9c+3j+2]); -1 marks an unused slot. */
+  int n_flower;
+  const int *flower_sublat;
+  const int *flower_orbit;
+  const int *flower_partner_sublat;
+  const int *flower_partner_du;
+  /* [n_flower * lut_stride] global function index of the decoration
+   * code sum_j (occ_j - 1) * (n_occ-1)^j (j = 0: centre, j >= 1: partners),
+   * -1 if none; lut_stride = (n_occ-1)^4 */
+  const int16_t *flower_lut;
+  /* owned clusters: each periodic cluster listed once, at its anchor site */
+  int n_owned;
+  const int *owned_sublat;
+  const int *owned_orbit;
+  const int *owned_partner_sublat;
+  const int *owned_partner_du;
+  const int16_t *owned_lut;
+  /* canonical local-swap displacements (nearest neighbours), per sublattice */
+  const int *n_neighbour;       /* [n_sublat], each <= 16 */
+  const int *neighbour_sublat;  /* [n_sublat*16] */
+  const int *neighbour_du;      /* [n_sublat*16*3] */
+  /* R^T = dparam_dmol ((n_occ-1) x n_occ, row-major): change of parametric
+   * composition per change of species counts
+   * (SemiGrandCanonicalCalculator.cc:144) */
+  const double *param_RT;
+} cem_system_desc;
+
+/* Run statistics of one replica (moments over the sampled passes). */
+typedef struct cem_stats {
+  double n_samples;
+  double mean_potential;   /* <potential energy per unit cell> */
+  double var_potential;    /* population variance of the same */
+  double mean_formation;   /* <formation energy per unit cell> */
+  double mean_comp[3];     /* <param composition> */
+  double cov_comp[9];      /* cov(param composition) */
+  double cov_e_comp[3];    /* cov(potential, param composition) */
+  double energy;           /* current formation energy per supercell (running) */
+  int64_t n_proposed;      /* proposals with a real occupation change */
+  int64_t n_accepted;
+  int64_t passes;
+} cem_stats;
+
+/* Last error message of the calling thread. */
+const char *cem_last_error(void);
+
+/* Device of the calling thread: name, SM count, compute capability. */
+int cem_device_info(char *name, int name_len, int *sm_count, int *cc_major, int *cc_minor);
+
+/* System tables -> device. Replaces the System / Clexulator set-up
+ * (System.cc:633-640 get_clex, StateData.cc:64-79). */
+int cem_system_create(const cem_system_desc *desc, cem_system **out);
+int cem_system_destroy(cem_system *sys);
+
+/* A batch of replicas (independent Monte Carlo states) of diagonal
+ * supercells L[3r..3r+2] of the system, one ensemble for the batch
+ * (CEM_CANONICAL or CEM_SEMIGRAND_CANONICAL). Occupations live in HBM.
+ * Replaces state construction + set_state_and_potential
+ * (CanonicalCalculator.cc:377-399). Linear site index:
+ * l = b*n_uc + i + L0*(j + L1*k) (canonical_metropolis_test.cpp:34-36). */
+int cem_replicas_create(const cem_system *sys, int n_replicas, const int *L, int ensemble,
+                        cem_replicas **out);
+int cem_replicas_destroy(cem_replicas *r);
+int cem_n_sites(const cem_replicas *r, int replica, int64_t *n_sites);
+
+/* Conditions: temperature (K) and param_chem_pot ([n_occ-1], SGC only; may be
+ * NULL for canonical). beta = 1/(kB T), infinite at T == 0
+ * (Conditions.hh:17-45). */
+int cem_set_conditions(cem_replicas *r, int replica, double temperature,
+                       const double *param_chem_pot);
+/* Seed of the replica's counter-based random stream (parallel mode). */
+int cem_set_seed(cem_replicas *r, int replica, uint64_t seed);
+
+/* Host <-> device occupations (int8 occupant indices, n_sites). */
+int cem_set_occupation(cem_replicas *r, int replica, const int8_t *occ);
+int cem_get_occupation(cem_replicas *r, int replica, int8_t *occ);
+
+/* Packed host <-> device occupations of all replicas, concatenated in
+ * replica order (sum of n_sites bytes). */
+int cem_set_occupation_all(cem_replicas *r, const int8_t *packed);
+int cem_get_occupation_all(cem_replicas *r, int8_t *packed);
+
+/* Page-locked host buffers for the transfers above. */
+int cem_host_alloc(int64_t bytes, void **ptr);
+int cem_host_free(void *ptr);
+
+/* Formation energy per supercell of the current occupation, with the integer
+ * function counts (count[0] = n_unitcells). Replaces per_supercell()
+ * (CanonicalCalculator.cc:127-129). */
+int cem_energy(cem_replicas *r, int replica, double *energy, int64_t *counts);
+
+/* Potential change of n_events events, each a series of sites_per_event
+ * occupation changes applied in order (sequential semantics,
+ * canonical/canonical.hh:42-45). potential = 0: formation energy only
+ * (CanonicalPotential); 1: semi-grand potential
+ * dE - param_chem_pot . R^T dN (SemiGrandCanonicalPotential). dcount, if not
+ * NULL, receives the integer delta correlations [n_events * n_funcs].
+ * Replaces occ_delta_per_supercell (BaseMonteCalculator.hh:41-43). */
+int cem_delta_energy(cem_replicas *r, int replica, int n_events, int sites_per_event,
+                     const int64_t *sites, const int32_t *new_occ, int potential,
+                     double *dE, int64_t *dcount);
+
+/* Sequential replay: n_steps steps of occupation_metropolis_v2
+ * (occupation_metropolis.hh:92-120) on one replica, consuming the
+ * std::mt19937_64 stream seeded with mt_seed exactly as the reference's
+ * RandomNumberGenerator does (uniform_int_distribution<long> /
+ * uniform_real_distribution<double>), with the event proposal, occupant
+ * location update and acceptance restated from libcasm-monte. Optional
+ * outputs per step: accept flag, dE, proposed sites (2 per step, -1 unused).
+ * Updates the replica's occupation on the device. */
+int cem_replay(cem_replicas *r, int replica, uint64_t mt_seed, int64_t n_steps,
+               uint8_t *accept_seq, double *dE_seq, int64_t *site_seq, int64_t *n_accept,
+               uint64_t *n_draws);
+
+/* Parallel Metropolis: n_passes passes over every replica; each pass updates
+ * colour classes of mutually non-interacting sites at once (flips for SGC,
+ * pair swaps for canonical). Passes after n_equil contribute to the
+ * statistics; record_samples != 0 keeps per-pass samples for
+ * autocorrelation analysis. Replaces run() (CanonicalCalculator.cc:413-462,
+ * SemiGrandCanonicalCalculator.cc:423-466). */
+int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_samples);
+
+/* Statistics and samples of one replica (after cem_run). */
+int cem_get_stats(cem_replicas *r, int replica, cem_stats *out);
+int cem_get_samples(cem_replicas *r, int replica, double *potential, double *comp,
+                    int64_t capacity, int64_t *n_samples);
+int cem_reset_stats(cem_replicas *r);
+
+/* Measured shared-memory read bandwidth of the device, GB/s (all SMs,
+ * 16-byte vector loads); the roofline denominator of the shared-memory
+ * resident sweep. */
+int cem_smem_bandwidth(double *gbs);
+
+/* Wait for all work of this batch. */
+int cem_synchronize(cem_replicas *r);
+
+/* Device time of the last cem_run's main kernel, in milliseconds (CUDA
+ * events on the batch's stream). */
+int cem_last_kernel_ms(cem_replicas *r, double *ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CEM_GB300_H */

@@ -108,6 +108,18 @@ struct System {
   std::vector<int> inc_off, inc_cl, inc_pos;  // incidence CSR over sites
   std::vector<double> RT;  // (n_occ-1) x n_occ, param composition per mol change
   double n_orbits = 0;
+  struct Cl {
+    const int *lut;
+    int size;
+    int sites[4];
+  };
+  std::vector<Cl> cls;  // flattened view of the supercell clusters
+  struct Inc {            // a cluster seen from one of its sites (CSR by site)
+    const int *lut;
+    int size, pos;
+    int sites[4];
+  };
+  std::vector<Inc> inc;
 };
 
 Vec3 cart(const System &s, int b, i64 u0, i64 u1, i64 u2) {
@@ -304,15 +316,29 @@ void build(System &s, const double *max_length /*[5], index = size*/,
       s.inc_pos[fill[site]] = q;
       fill[site]++;
     }
+  s.cls.resize(ncl);
+  for (int c = 0; c < ncl; ++c) {
+    const AnchorType &t = s.types[s.cl_type_b[c]][s.cl_type_i[c]];
+    s.cls[c].lut = t.lut.data();
+    s.cls[c].size = t.size;
+    for (int q = 0; q < 4; ++q) s.cls[c].sites[q] = s.cl_sites[c * 4 + q];
+  }
+  s.inc.resize(s.inc_cl.size());
+  for (size_t e = 0; e < s.inc_cl.size(); ++e) {
+    const System::Cl &k = s.cls[s.inc_cl[e]];
+    s.inc[e].lut = k.lut;
+    s.inc[e].size = k.size;
+    s.inc[e].pos = s.inc_pos[e];
+    for (int q = 0; q < 4; ++q) s.inc[e].sites[q] = k.sites[q];
+  }
 }
 
 inline int cluster_code(const System &s, int c, const signed char *occ, int site, int site_occ) {
-  const AnchorType &t = s.types[s.cl_type_b[c]][s.cl_type_i[c]];
+  const System::Cl &k = s.cls[c];
   int code = 0, mul = 1;
-  for (int q = 0; q < t.size; ++q) {
-    int st = s.cl_sites[c * 4 + q];
-    int o = (st == site) ? site_occ : occ[st];
-    code += o * mul;
+  for (int q = 0; q < k.size; ++q) {
+    const int st = k.sites[q];
+    code += ((st == site) ? site_occ : occ[st]) * mul;
     mul *= s.n_occ;
   }
   return code;
@@ -321,12 +347,20 @@ inline int cluster_code(const System &s, int c, const signed char *occ, int site
 // Integer count change of every function for occ[site]: occ_i -> occ_f.
 void site_delta_counts(const System &s, const signed char *occ, int site, int occ_f,
                        i64 *dcount) {
-  int occ_i = occ[site];
+  const int occ_i = occ[site];
+  const int no = s.n_occ;
   for (int e = s.inc_off[site]; e < s.inc_off[site + 1]; ++e) {
-    int c = s.inc_cl[e];
-    const AnchorType &t = s.types[s.cl_type_b[c]][s.cl_type_i[c]];
-    int fo = t.lut[cluster_code(s, c, occ, site, occ_i)];
-    int fn = t.lut[cluster_code(s, c, occ, site, occ_f)];
+    const System::Inc &k = s.inc[e];
+    int rest = 0, mul = 1, mul_pos = 1;
+    for (int q = 0; q < k.size; ++q) {
+      if (q == k.pos)
+        mul_pos = mul;
+      else
+        rest += occ[k.sites[q]] * mul;
+      mul *= no;
+    }
+    const int fo = k.lut[rest + occ_i * mul_pos];
+    const int fn = k.lut[rest + occ_f * mul_pos];
     if (fo >= 0) dcount[fo] -= 1;
     if (fn >= 0) dcount[fn] += 1;
   }
@@ -340,10 +374,9 @@ double counts_to_energy(const System &s, const i64 *count) {
 
 void all_counts(const System &s, const signed char *occ, i64 *count) {
   for (int f = 0; f < s.n_funcs; ++f) count[f] = 0;
-  int ncl = (int)s.cl_type_b.size();
+  const int ncl = (int)s.cls.size();
   for (int c = 0; c < ncl; ++c) {
-    const AnchorType &t = s.types[s.cl_type_b[c]][s.cl_type_i[c]];
-    int f = t.lut[cluster_code(s, c, occ, -1, 0)];
+    const int f = s.cls[c].lut[cluster_code(s, c, occ, -1, 0)];
     if (f >= 0) count[f] += 1;
   }
 }
@@ -352,8 +385,9 @@ void all_counts(const System &s, const signed char *occ, i64 *count) {
 // applied before the next is evaluated (canonical/canonical.hh:42-45).
 double event_delta(const System &s, std::vector<signed char> &occ, int n, const i64 *sites,
                    const int *new_occ, i64 *dcount) {
-  std::vector<i64> d(s.n_funcs, 0);
-  std::vector<signed char> saved(n);
+  thread_local std::vector<i64> d;
+  d.assign(s.n_funcs, 0);
+  signed char saved[4];
   for (int i = 0; i < n; ++i) {
     saved[i] = occ[sites[i]];
     site_delta_counts(s, occ.data(), (int)sites[i], new_occ[i], d.data());
@@ -566,11 +600,11 @@ int ora_run(void *h, signed char *occ, int ensemble, double temperature, const d
     std::vector<i64> cnt(s.n_funcs);
     i64 sites[2];
     int nocc[2];
+    std::vector<long> cum(swaps.size());
     for (i64 pass = 0; pass < n_passes; ++pass) {
       for (i64 st = 0; st < steps_per_pass; ++st, ++step) {
         // propose
         long tsum = 0;
-        std::vector<long> cum(swaps.size());
         for (size_t i = 0; i < swaps.size(); ++i) {
           long w = (long)loc.lists[swaps[i].first].size();
           if (ensemble == 1) w *= (long)loc.lists[swaps[i].second].size();

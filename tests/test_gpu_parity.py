@@ -1,0 +1,205 @@
+"""GPU path (through the C ABI) against the CPU FP64 oracle.
+
+Tolerances: integer delta correlations and counts, replayed site and accept
+sequences, occupations: bit-exact. Energies and dE: 1e-10 relative (the ECI
+dot runs in float-float), with an absolute floor of 1e-12 eV."""
+
+import numpy as np
+import pytest
+
+from casmcode_clexmonte_gb300 import workloads
+from casmcode_clexmonte_gb300.stats import batch_means
+from casmcode_clexmonte_gb300.system import ClusterExpansion, fcc_prim
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10
+ATOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def cm():
+    from casmcode_clexmonte_gb300 import build
+
+    build.build()
+    from casmcode_clexmonte_gb300 import calculator
+
+    return calculator
+
+
+def _close(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    assert np.all(np.abs(a - b) <= RTOL * np.abs(b) + ATOL), np.max(np.abs(a - b))
+
+
+def _systems():
+    t = ClusterExpansion(fcc_prim(4.0, ("A", "B", "Va")), {2: 4.1, 3: 4.01})
+    t.eci = np.random.default_rng(11).normal(0, 0.05, t.n_funcs)
+    return [
+        ("fcc_binary", workloads.fcc_binary_ce(1), (10, 10, 10)),
+        ("fcc_binary_odd", workloads.fcc_binary_ce(2), (7, 9, 11)),
+        ("fcc_ternary", t, (6, 6, 6)),
+        ("bcc_ternary", workloads.bcc_ternary_ce(3), (6, 5, 7)),
+    ]
+
+
+@pytest.mark.parametrize("name,ce,L", _systems())
+def test_energy_and_delta_match_oracle(name, ce, L, cm, oracle_mod):
+    sysd = cm.System(ce)
+    ens = "semigrand_canonical"
+    b = cm.ReplicaBatch(sysd, ens, [L])
+    o = oracle_mod.OracleSystem(ce, L)
+    rng = np.random.default_rng(5)
+    nocc = ce.prim.n_occ
+    mu = rng.uniform(-0.3, 0.3, nocc - 1)
+    b.set_conditions(0, 800.0, mu)
+    for trial in range(3):
+        occ = rng.integers(0, nocc, o.n_sites).astype(np.int8)
+        b.set_occupation(0, occ)
+        e, counts = b.energy(0)
+        oc = o.counts(occ)
+        np.testing.assert_array_equal(counts[1:], oc[1:])
+        _close(e, o.energy(occ))
+        # single-site changes and two-site sequential events (incl. neighbours)
+        n_ev = 400
+        s1 = rng.integers(0, o.n_sites, n_ev)
+        f1 = (occ[s1] + rng.integers(1, nocc, n_ev)) % nocc
+        dE, dc = b.delta(0, s1[:, None], f1[:, None])
+        dEp, _ = b.delta(0, s1[:, None], f1[:, None], potential=True)
+        nb = np.array([o.n_sites])
+        part_sites = []
+        for k in range(n_ev):
+            de_o, dc_o = o.delta(occ, [s1[k]], [f1[k]])
+            np.testing.assert_array_equal(dc[k], dc_o)
+            _close(dE[k], de_o)
+            dep_o, _ = o.delta(occ, [s1[k]], [f1[k]], mu=mu)
+            _close(dEp[k], dep_o)
+        # swaps: random pairs and close pairs (second site sees the first change)
+        s2 = np.where(rng.random(n_ev) < 0.5, rng.integers(0, o.n_sites, n_ev), (s1 + 1) % nb[0])
+        ev_s = np.stack([s1, s2], 1)
+        ev_f = np.stack([occ[s2], occ[s1]], 1)
+        dE2, dc2 = b.delta(0, ev_s, ev_f)
+        for k in range(n_ev):
+            de_o, dc_o = o.delta(occ, ev_s[k], ev_f[k])
+            np.testing.assert_array_equal(dc2[k], dc_o)
+            _close(dE2[k], de_o)
+
+
+@pytest.mark.parametrize("kind", ["sgc_config0", "canonical_fcc", "sgc_bcc_ternary"])
+def test_replay_matches_oracle_exactly(kind, cm, oracle_mod):
+    rng = np.random.default_rng(17)
+    if kind == "sgc_config0":
+        w = workloads.config(0)
+        ce, L, ens, T, mu = w.ce, w.L[0], "semigrand_canonical", 1000.0, np.zeros(1)
+        occ = w.occupation[0].copy()
+        n_passes = 60
+    elif kind == "canonical_fcc":
+        ce, L, ens, T, mu = workloads.fcc_binary_ce(4), (8, 8, 8), "canonical", 600.0, np.zeros(1)
+        occ = workloads.fixed_composition(rng, 512, 0.5)
+        n_passes = 60
+    else:
+        ce, L, ens, T = workloads.bcc_ternary_ce(6), (5, 5, 5), "semigrand_canonical", 900.0
+        mu = np.array([0.05, -0.1])
+        occ = rng.integers(0, 3, 250).astype(np.int8)
+        n_passes = 80
+    o = oracle_mod.OracleSystem(ce, L)
+    n = o.n_sites
+    steps = n_passes * n
+    seed = 987654321
+    occ_o = occ.copy()
+    ref = o.run(occ_o, 0 if ens == "semigrand_canonical" else 1, T, mu, seed, n_passes,
+                record_steps=steps)
+    sysd = cm.System(ce)
+    b = cm.ReplicaBatch(sysd, ens, [L])
+    b.set_conditions(0, T, mu if ens == "semigrand_canonical" else None)
+    b.set_occupation(0, occ)
+    got = b.replay(0, seed, steps)
+    np.testing.assert_array_equal(got["sites"][:, 0], ref["site0"])
+    np.testing.assert_array_equal(got["sites"][:, 1], ref["site1"])
+    np.testing.assert_array_equal(got["accept"], ref["accept"])
+    _close(got["dE"], ref["dE"])
+    assert got["n_accept"] == ref["n_accept"]
+    assert got["draws"] == ref["draws"]
+    np.testing.assert_array_equal(b.get_occupation(0), occ_o)
+
+
+@pytest.mark.parametrize("ens", ["semigrand_canonical", "canonical"])
+def test_parallel_running_energy_and_invariants(ens, cm):
+    ce = workloads.bcc_ternary_ce(8) if ens == "semigrand_canonical" else workloads.fcc_binary_ce(8)
+    L = [(6, 6, 6), (7, 7, 7), (9, 9, 9)] if ens == "semigrand_canonical" else [(8, 8, 8), (10, 10, 10), (12, 12, 12)]
+    sysd = cm.System(ce)
+    b = cm.ReplicaBatch(sysd, ens, L)
+    rng = np.random.default_rng(9)
+    occs = []
+    for i, l in enumerate(L):
+        n = int(b.n_sites[i])
+        if ens == "canonical":
+            occ = workloads.fixed_composition(rng, n, 0.3 + 0.1 * i)
+            b.set_conditions(i, 500.0 + 300 * i)
+        else:
+            occ = rng.integers(0, 3, n).astype(np.int8)
+            b.set_conditions(i, 700.0 + 200 * i, rng.uniform(-0.2, 0.2, 2))
+        b.set_seed(i, 1000 + i)
+        b.set_occupation(i, occ)
+        occs.append(occ)
+    b.run(40, 10)
+    for i in range(len(L)):
+        st = b.stats(i)
+        e, _ = b.energy(i)
+        assert abs(st["energy"] - e) <= 1e-9 * max(1.0, abs(e))
+        assert st["n_samples"] == 30
+        assert st["n_accepted"] > 0
+        new = b.get_occupation(i)
+        assert new.min() >= 0 and new.max() < ce.prim.n_occ
+        if ens == "canonical":
+            assert np.bincount(new, minlength=2).tolist() == np.bincount(occs[i], minlength=2).tolist()
+
+
+def test_parallel_deterministic_for_fixed_seed(cm):
+    ce = workloads.fcc_binary_ce(1)
+    sysd = cm.System(ce)
+    outs = []
+    for _ in range(2):
+        b = cm.ReplicaBatch(sysd, "canonical", [(12, 12, 12)])
+        b.set_conditions(0, 700.0)
+        b.set_seed(0, 77)
+        b.set_occupation(0, workloads.fixed_composition(np.random.default_rng(1), 1728, 0.5))
+        b.run(20, 0)
+        outs.append(b.get_occupation(0))
+    np.testing.assert_array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("ens", ["semigrand_canonical", "canonical"])
+def test_parallel_equilibrium_matches_oracle(ens, cm, oracle_mod):
+    """<potential energy> and <x> of the parallel GPU sampler against the
+    sequential oracle chain, within 4 combined standard errors."""
+    ce = workloads.fcc_binary_ce(0)
+    L = (8, 8, 8)
+    n = 512
+    T = 900.0
+    mu = np.array([0.05])
+    rng = np.random.default_rng(21)
+    occ0 = workloads.fixed_composition(rng, n, 0.4)
+    o = oracle_mod.OracleSystem(ce, L)
+    occ_o = occ0.copy()
+    ref = o.run(occ_o, 0 if ens == "semigrand_canonical" else 1, T, mu, 5, 6000)
+    e_o, se_o = batch_means(ref["potential"][1000:])
+    sysd = cm.System(ce)
+    nrep = 16
+    b = cm.ReplicaBatch(sysd, ens, [L] * nrep)
+    for i in range(nrep):
+        b.set_conditions(i, T, mu if ens == "semigrand_canonical" else None)
+        b.set_seed(i, 100 + i)
+        b.set_occupation(i, occ0)
+    b.run(3000, 500, record_samples=True)
+    means = []
+    for i in range(nrep):
+        pot, _ = b.samples(i, 2500)
+        means.append(pot.mean())
+    means = np.array(means)
+    e_g, se_g = means.mean(), means.std(ddof=1) / np.sqrt(nrep)
+    assert abs(e_g - e_o) < 4.0 * np.hypot(se_g, se_o), (e_g, se_g, e_o, se_o)
+    if ens == "semigrand_canonical":
+        x_o, sx_o = batch_means(ref["comp"][1000:, 0])
+        xs = np.array([b.stats(i)["mean_comp"][0] for i in range(nrep)])
+        assert abs(xs.mean() - x_o) < 4.0 * np.hypot(xs.std(ddof=1) / np.sqrt(nrep), sx_o)
