@@ -54,6 +54,7 @@ EXPORTS = [
     "cem_get_occupation_all", "cem_host_alloc", "cem_host_free", "cem_energy",
     "cem_delta_energy", "cem_replay", "cem_run", "cem_get_stats", "cem_get_samples",
     "cem_reset_stats", "cem_synchronize", "cem_last_kernel_ms", "cem_smem_bandwidth",
+    "cem_set_option", "cem_get_option",
 ]
 
 _lib = None
@@ -97,6 +98,8 @@ def load(path: str = LIB):
     L.cem_synchronize.argtypes = [P]
     L.cem_last_kernel_ms.argtypes = [P, _dp]
     L.cem_smem_bandwidth.argtypes = [_dp]
+    L.cem_set_option.argtypes = [P, C.c_char_p, C.c_int64]
+    L.cem_get_option.argtypes = [P, C.c_char_p, C.POINTER(C.c_int64)]
     _lib = L
     return L
 

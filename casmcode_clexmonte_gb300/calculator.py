@@ -146,6 +146,14 @@ class ReplicaBatch:
     def run(self, n_passes: int, n_equil: int = 0, record_samples: bool = False):
         check(self.lib.cem_run(self.handle, int(n_passes), int(n_equil), int(bool(record_samples))))
 
+    def set_option(self, key: str, value: int):
+        check(self.lib.cem_set_option(self.handle, key.encode(), int(value)))
+
+    def get_option(self, key: str) -> int:
+        v = C.c_int64()
+        check(self.lib.cem_get_option(self.handle, key.encode(), C.byref(v)))
+        return v.value
+
     def synchronize(self):
         check(self.lib.cem_synchronize(self.handle))
 

@@ -62,6 +62,7 @@ T *dev_copy(const std::vector<T> &v) {
 }
 
 const double KB = 8.617333262e-5;  // eV/K
+constexpr int MAX_SWEEPS_API = 8;
 
 // block colouring of a ring of length L with blocks of size >= p
 std::vector<int> axis_blocks(int L, int p) {
@@ -86,6 +87,7 @@ struct cem_system {
   // host copies used for colouring checks
   std::vector<int> fl_sub, fl_pb, fl_du;
   int nb_reach = 0;
+  bool fcc_generated = false;  // flower matches the generated binary FCC evaluator
   std::vector<void *> owned;
   ~cem_system() {
     for (void *p : owned) cudaFree(p);
@@ -107,7 +109,8 @@ struct cem_replicas {
   long long sample_capacity = 0;
   int sample_width = 1;
   long long n_samples_recorded = 0;
-  int max_classes = 1, sweep_smem = 0;
+  int max_classes = 1, sweep_smem = 0, pitch = 0, generic_smem = 0;
+  int n_pair_sweeps = 2, n_local_sweeps = 1;
   bool reps_dirty = true, stats_valid = false;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -314,6 +317,7 @@ int cem_system_create(const cem_system_desc *d, cem_system **out) {
     T.reach = reach;
     s->fl_pb.assign(pb.begin(), pb.begin() + d->n_flower * 3);
     s->fl_du.assign(du.begin(), du.begin() + d->n_flower * 9);
+    s->fcc_generated = matches_generated_fcc(T, s->fl_pb.data(), s->fl_du.data());
     int nbr = 0;
     for (int b = 0; b < d->n_sublat; ++b) {
       T.n_nb[b] = d->n_neighbour ? d->n_neighbour[b] : 0;
@@ -405,11 +409,24 @@ int cem_replicas_create(const cem_system *sys, int n, const int *L, int ensemble
     }
     r->total_sites = off;
     r->max_classes = max_cls;
-    int smem = 0;
+    int dev = 0, maxsm = 0;
+    CUDA_OK(cudaGetDevice(&dev));
+    CUDA_OK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    int need = 0;
     for (int i = 0; i < n; ++i)
-      smem = std::max(smem, sweep_smem_bytes(sys->T, r->reps[i].L[0], r->reps[i].L[1],
-                                             r->reps[i].L[2], max_cls));
-    r->sweep_smem = smem;
+      need = std::max({need, r->reps[i].L[0] + 2 * sys->T.reach, r->reps[i].L[1] + 2 * sys->T.reach});
+    int pitch = 0;
+    if (sys->fcc_generated) pitch = need <= 32 ? 32 : need <= 48 ? 48 : need <= 64 ? 64 : 0;
+    int smem = 0, gsmem = 0;
+    for (int i = 0; i < n; ++i) {
+      const int *Li = r->reps[i].L;
+      gsmem = std::max(gsmem, sweep_smem_bytes(sys->T, Li[0], Li[1], Li[2], max_cls, 0));
+      if (pitch) smem = std::max(smem, sweep_smem_bytes(sys->T, Li[0], Li[1], Li[2], max_cls, pitch));
+    }
+    if (pitch && smem > maxsm) pitch = 0;  // generated layout does not fit: run-time tables
+    r->pitch = pitch;
+    r->generic_smem = gsmem;
+    r->sweep_smem = pitch ? smem : gsmem;
     r->stats_host.assign(n, ReplicaStats{});
     CUDA_OK(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking));
     CUDA_OK(cudaEventCreate(&r->ev0));
@@ -658,7 +675,10 @@ int cem_replay(cem_replicas *r, int i, uint64_t mt_seed, int64_t n_steps, uint8_
 // (one batched kernel, no host round trip).
 static void init_stats(cem_replicas *r) {
   r->upload_reps();
-  CUDA_OK(launch_init_stats(r->sys->T, r->d_reps, r->d_stats, r->d_occ, r->n, r->stream));
+  int max_sites = 0;
+  for (const Replica &R : r->reps) max_sites = std::max(max_sites, R.n_sites);
+  CUDA_OK(launch_init_stats(r->sys->T, r->d_reps, r->d_stats, r->d_occ, r->n, max_sites,
+                            r->stream));
   r->stats_valid = true;
 }
 
@@ -689,6 +709,8 @@ int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_sampl
     P.n_passes = n_passes;
     P.n_equil = n_equil;
     P.max_classes = r->max_classes;
+    P.n_pair_sweeps = r->n_pair_sweeps;
+    P.n_local_sweeps = r->n_local_sweeps;
     const CeTables &T = r->sys->T;
     for (size_t k = 0; k < r->sys->RT.size() && k < 16; ++k) P.RT[k] = r->sys->RT[k];
     if (record_samples) {
@@ -718,7 +740,7 @@ int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_sampl
       r->n_samples_recorded = std::max<long long>(0, n_passes - n_equil);
     }
     CUDA_OK(cudaEventRecord(r->ev0, r->stream));
-    CUDA_OK(launch_sweep(T, P, r->n, r->sweep_smem, r->stream));
+    CUDA_OK(launch_sweep(T, P, r->n, r->sweep_smem, r->pitch, r->stream));
     CUDA_OK(cudaEventRecord(r->ev1, r->stream));
   });
 }
@@ -779,6 +801,43 @@ int cem_smem_bandwidth(double *gbs) {
   return guard([&] {
     require(gbs != nullptr, "null output");
     CUDA_OK(smem_bandwidth(gbs, 0));
+  });
+}
+
+int cem_set_option(cem_replicas *r, const char *key, int64_t value) {
+  return guard([&] {
+    require(r && key, "null argument");
+    const std::string k(key);
+    if (k == "pair_sweeps") {
+      require(value >= 0 && value + r->n_local_sweeps <= MAX_SWEEPS_API, "too many sweeps");
+      r->n_pair_sweeps = (int)value;
+    } else if (k == "local_sweeps") {
+      require(value >= 1 && value + r->n_pair_sweeps <= MAX_SWEEPS_API,
+              "local_sweeps must be >= 1 (swaps between colour classes keep the chain ergodic)");
+      r->n_local_sweeps = (int)value;
+    } else if (k == "generic_evaluator") {
+      if (value) {
+        r->pitch = 0;
+        r->sweep_smem = r->generic_smem;
+      } else {
+        throw Err(CEM_ERR_INVALID, "generic_evaluator can only be switched on");
+      }
+    } else {
+      throw Err(CEM_ERR_INVALID, "unknown option '" + k + "'");
+    }
+  });
+}
+
+int cem_get_option(cem_replicas *r, const char *key, int64_t *value) {
+  return guard([&] {
+    require(r && key && value, "null argument");
+    const std::string k(key);
+    if (k == "pair_sweeps") *value = r->n_pair_sweeps;
+    else if (k == "local_sweeps") *value = r->n_local_sweeps;
+    else if (k == "pitch") *value = r->pitch;
+    else if (k == "smem_bytes") *value = r->sweep_smem;
+    else if (k == "colour_classes") *value = r->max_classes;
+    else throw Err(CEM_ERR_INVALID, "unknown option '" + k + "'");
   });
 }
 

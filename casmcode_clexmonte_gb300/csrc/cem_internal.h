@@ -33,6 +33,7 @@ struct SweepParams {
   int sample_width;
   long long n_passes, n_equil;
   int max_classes;
+  int n_pair_sweeps, n_local_sweeps;  // canonical pass composition
   double RT[16];               // (n_occ-1) x n_occ
 };
 
@@ -44,10 +45,13 @@ cudaError_t launch_delta(const CeTables &T, const int8_t *occ, int L0, int L1, i
 int replay_smem_bytes(int n_sites, int n_occ);
 cudaError_t launch_replay(const CeTables &T, const ReplayParams &P, cudaStream_t st);
 cudaError_t launch_init_stats(const CeTables &T, const Replica *reps, ReplicaStats *stats,
-                              const int8_t *occ, int n_replicas, cudaStream_t st);
+                              const int8_t *occ, int n_replicas, int max_sites, cudaStream_t st);
 cudaError_t smem_bandwidth(double *gbs, cudaStream_t st);
-int sweep_smem_bytes(const CeTables &T, int L0, int L1, int L2, int n_classes);
+int sweep_smem_bytes(const CeTables &T, int L0, int L1, int L2, int n_classes, int pitch);
+// pitch 0: run-time tables; 32/48/64: generated binary FCC evaluator
 cudaError_t launch_sweep(const CeTables &T, const SweepParams &P, int n_replicas, int smem,
-                         cudaStream_t st);
+                         int pitch, cudaStream_t st);
+// true if the system is the binary FCC topology of the generated evaluator
+bool matches_generated_fcc(const CeTables &T, const int *pb, const int *du);
 
 }  // namespace cem

@@ -22,6 +22,7 @@
 
 #include "cem_common.cuh"
 #include "cem_internal.h"
+#include "gen_fcc_binary.cuh"
 
 namespace cem {
 
@@ -179,18 +180,26 @@ __global__ void k_energy(const __grid_constant__ CeTables T, const int8_t *__res
 
 // Exact initial state of every replica (one CTA per replica): function
 // counts -> formation energy, species counts; clears the sampled moments.
+// The replica's occupation is staged in shared memory when it fits
+// (smem_cap bytes), else read from global memory.
 template <int NOCC>
 __global__ void k_init_stats(const __grid_constant__ CeTables T, const Replica *__restrict__ reps,
-                             ReplicaStats *__restrict__ stats, const int8_t *__restrict__ occ_all) {
+                             ReplicaStats *__restrict__ stats, const int8_t *__restrict__ occ_all,
+                             int smem_cap) {
+  extern __shared__ __align__(16) int8_t socc[];
   __shared__ unsigned long long hist[MAX_FUNCS];
   __shared__ unsigned long long spec[8];
   const Replica &R = reps[blockIdx.x];
   for (int f = threadIdx.x; f < MAX_FUNCS; f += blockDim.x) hist[f] = 0ull;
   if (threadIdx.x < 8) spec[threadIdx.x] = 0ull;
-  __syncthreads();
   const int L0 = R.L[0], L1 = R.L[1], L2 = R.L[2];
   const int n_uc = L0 * L1 * L2, n = n_uc * T.n_sublat;
-  const int8_t *occ = occ_all + R.occ_offset;
+  const int8_t *gocc = occ_all + R.occ_offset;
+  const bool staged = n <= smem_cap;
+  if (staged)
+    for (int l = threadIdx.x; l < n; l += blockDim.x) socc[l] = gocc[l];
+  __syncthreads();
+  const int8_t *occ = staged ? socc : gocc;
   int lspec[NOCC];
   for (int a = 0; a < NOCC; ++a) lspec[a] = 0;
   for (int l = threadIdx.x; l < n; l += blockDim.x) {
@@ -511,47 +520,55 @@ __global__ void k_replay(const __grid_constant__ CeTables T, ReplayParams P) {
 }
 
 // ------------------------------------------------------------ parallel sweep
-// Sub-step kinds of one pass.
-enum : int { SUB_FLIP = 0, SUB_PAIR_CLASS = 1, SUB_PAIR_LOCAL = 2 };
+// A pass = n_pair_sweeps sweeps of pair swaps inside each colour class plus
+// n_local_sweeps sweeps of swaps with a nearest neighbour (canonical), or one
+// sweep of flips over every class (semi-grand canonical). Each sweep visits
+// the classes in a random order drawn per pass.
 constexpr uint32_t TAG_SITE = 0x1u, TAG_SCHED = 0x2u;
-constexpr int N_LOCAL_SWEEPS = 4;
+constexpr int MAX_SWEEPS = 8;
 
 struct SweepSmem {
   // carved from dynamic shared memory; offsets in bytes
-  int occ, cl_off, lutoff, lut, whi, wlo, ax, sched, red, total;
+  int occ, cl_off, lutoff, lut, whi, wlo, dmu, ax, sched, red, total;
 };
 
 __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 
+// pitch > 0: fixed x/y pitch of the generated evaluator; 0: L + 2 reach
 __host__ __device__ inline void sweep_layout(const CeTables &T, int L0, int L1, int L2,
-                                             int n_classes_max, SweepSmem &s) {
+                                             int n_classes_max, int pitch, SweepSmem &s) {
   const int R = T.reach;
-  const int V = (L0 + 2 * R) * (L1 + 2 * R) * (L2 + 2 * R);
+  const int W = pitch ? pitch : L0 + 2 * R, H = pitch ? pitch : L1 + 2 * R;
+  const int V = W * H * (L2 + 2 * R);
+  const bool tables = (pitch == 0);
   int o = 0;
   s.occ = o;
   o += align16(T.n_sublat * V);
   s.cl_off = o;
-  o += align16(T.n_fl * 3 * 4);
+  o += tables ? align16(T.n_fl * 3 * 4) : 0;
   s.lutoff = o;
-  o += align16(T.n_fl * 4);
+  o += tables ? align16(T.n_fl * 4) : 0;
   s.lut = o;
-  o += align16(T.n_fl * (T.n_sf * T.n_sf * T.n_sf * T.n_sf));
+  o += tables ? align16(T.n_fl * (T.n_sf * T.n_sf * T.n_sf * T.n_sf)) : 0;
   s.whi = o;
   o += align16(T.n_funcs * 4);
   s.wlo = o;
   o += align16(T.n_funcs * 4);
+  s.dmu = o;  // hi[16], lo[16] floats
+  o += 128;
   s.ax = o;  // per axis: begin[MAX_COLOURS], cnt[MAX_COLOURS], coord[MAX_L]
   o += align16(3 * (2 * MAX_COLOURS + MAX_L) * 4);
-  s.sched = o;  // key[n], par[n], order[n] (u32 each), n = 5 * n_classes
-  o += align16(3 * (1 + N_LOCAL_SWEEPS) * n_classes_max * 4);
-  s.red = o;  // block reduction scratch: 32 warps x (2 doubles + 8 + 2 longs)
-  o += align16(32 * (2 * 8 + 10 * 8));
+  s.sched = o;  // key[n], par[n], order[n] (u32 each), n = MAX_SWEEPS * n_classes
+  o += align16(3 * MAX_SWEEPS * n_classes_max * 4);
+  s.red = o;  // block reduction scratch: 32 warps x 16 slots of 8 bytes
+  o += 32 * 16 * 8;
   s.total = o;
 }
 
-inline int sweep_smem_bytes_impl(const CeTables &T, int L0, int L1, int L2, int n_classes) {
+inline int sweep_smem_bytes_impl(const CeTables &T, int L0, int L1, int L2, int n_classes,
+                                 int pitch) {
   SweepSmem s;
-  sweep_layout(T, L0, L1, L2, n_classes, s);
+  sweep_layout(T, L0, L1, L2, n_classes, pitch, s);
   return s.total;
 }
 
@@ -581,7 +598,48 @@ __device__ __forceinline__ bool accept_fast(const FF &d, float beta_f, float u) 
   return u < cem_expf_neg(FMUL(-beta_f, de));
 }
 
+// Site evaluation policy: PITCH > 0 uses the generated binary FCC evaluator
+// (compile-time neighbour offsets); PITCH == 0 walks the run-time tables.
+template <int NOCC, int PITCH>
+struct SiteEval {
+  const CeTables *T;
+  const int *cl_off;
+  const int *lutoff;
+  const uint8_t *lut;
+  __device__ __forceinline__ void add(int b, int o_i, int o_f, const int8_t *occ, int ad,
+                                      Acc<NOCC> &acc) const {
+    if constexpr (PITCH > 0) {
+      int n[gen_fcc::N_ORBITS];
+      gen_fcc::counts<PITCH>(occ + ad, n);
+      const int d = o_f - o_i;
+#pragma unroll
+      for (int g = 0; g < gen_fcc::N_ORBITS; ++g) acc.c[g] += d * n[g];
+    } else {
+      auto rd = [&](int cl, int j) -> int { return occ[ad + cl_off[cl * 3 + j]]; };
+      accumulate_site<NOCC>(*T, b, o_i, o_f, lutoff, lut, rd, acc);
+    }
+  }
+};
+
+// running energy bookkeeping: exact integer delta correlations per orbit for
+// binary systems, FP64 sums of dE otherwise
 template <int NOCC>
+struct EnergyAcc {
+  double de = 0.0;
+  __device__ __forceinline__ void add(const Acc<NOCC> &, const FF &d, double extra) {
+    de += (double)d.s + (double)d.e + extra;
+  }
+};
+template <>
+struct EnergyAcc<2> {
+  int dc[MAX_ORBITS] = {0, 0, 0, 0, 0, 0, 0, 0};
+  __device__ __forceinline__ void add(const Acc<2> &a, const FF &, double) {
+#pragma unroll
+    for (int g = 0; g < MAX_ORBITS; ++g) dc[g] += a.c[g];
+  }
+};
+
+template <int NOCC, int PITCH>
 __global__ void __launch_bounds__(SWEEP_THREADS, 1)
     k_sweep(const __grid_constant__ CeTables T, const __grid_constant__ SweepParams P) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -594,21 +652,26 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
   G.L1 = R.L[1];
   G.L2 = R.L[2];
   G.R = T.reach;
-  G.W = G.L0 + 2 * G.R;
-  G.H = G.L1 + 2 * G.R;
+  G.W = PITCH ? PITCH : G.L0 + 2 * G.R;
+  G.H = PITCH ? PITCH : G.L1 + 2 * G.R;
   G.V = G.W * G.H * (G.L2 + 2 * G.R);
   const int n_uc = G.L0 * G.L1 * G.L2;
   const int nsl = T.n_sublat;
-  const int ncol_all = R.n_col[0] * R.n_col[1] * R.n_col[2];
+  const int ncol0 = R.n_col[0], ncol1 = R.n_col[1];
+  const int ncol_all = ncol0 * ncol1 * R.n_col[2];
   const int n_classes = nsl * ncol_all;
+  const int ensemble = R.ensemble;
+  const float beta_f = R.beta_f;
   SweepSmem lay;
-  sweep_layout(T, G.L0, G.L1, G.L2, P.max_classes, lay);
+  sweep_layout(T, G.L0, G.L1, G.L2, P.max_classes, PITCH, lay);
   int8_t *occ = reinterpret_cast<int8_t *>(smem + lay.occ);
   int *cl_off = reinterpret_cast<int *>(smem + lay.cl_off);
   int *lutoff = reinterpret_cast<int *>(smem + lay.lutoff);
   uint8_t *lut = reinterpret_cast<uint8_t *>(smem + lay.lut);
   float *whi = reinterpret_cast<float *>(smem + lay.whi);
   float *wlo = reinterpret_cast<float *>(smem + lay.wlo);
+  float *dmu_hi = reinterpret_cast<float *>(smem + lay.dmu);
+  float *dmu_lo = dmu_hi + 16;
   int *ax = reinterpret_cast<int *>(smem + lay.ax);
   uint32_t *sched = reinterpret_cast<uint32_t *>(smem + lay.sched);
   unsigned char *red = smem + lay.red;
@@ -619,37 +682,41 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
     ax_coord[a] = ax_cnt[a] + MAX_COLOURS;
   }
   // ---- stage tables
-  for (int c = tid; c < T.n_fl; c += nth) {
-    int cb = 0;
-    for (int b = 0; b < nsl; ++b)
-      if (c >= T.fl_begin[b][0]) cb = b;
-    for (int q = 0; q < 3; ++q) {
-      const int pb = T.cl_pb[c * 3 + q];
-      const int *du = T.cl_du + c * 9 + q * 3;
-      cl_off[c * 3 + q] = (pb < 0) ? 0 : (pb - cb) * G.V + du[0] + G.W * (du[1] + G.H * du[2]);
+  if constexpr (PITCH == 0) {
+    for (int c = tid; c < T.n_fl; c += nth) {
+      int cb = 0;
+      for (int b = 0; b < nsl; ++b)
+        if (c >= T.fl_begin[b][0]) cb = b;
+      for (int q = 0; q < 3; ++q) {
+        const int pb = T.cl_pb[c * 3 + q];
+        const int *du = T.cl_du + c * 9 + q * 3;
+        cl_off[c * 3 + q] = (pb < 0) ? 0 : (pb - cb) * G.V + du[0] + G.W * (du[1] + G.H * du[2]);
+      }
+      lutoff[c] = T.cl_lut[c];
     }
-    lutoff[c] = T.cl_lut[c];
+    const int lut_n = T.n_fl * (T.n_sf * T.n_sf * T.n_sf * T.n_sf);
+    for (int i = tid; i < lut_n; i += nth) lut[i] = T.lut[i];
   }
-  const int lut_n = T.n_fl * (T.n_sf * T.n_sf * T.n_sf * T.n_sf);
-  for (int i = tid; i < lut_n; i += nth) lut[i] = T.lut[i];
   for (int f = tid; f < T.n_funcs; f += nth) {
     whi[f] = T.w_hi[f];
     wlo[f] = T.w_lo[f];
   }
+  if (tid < 16) {
+    dmu_hi[tid] = R.dmu_hi[tid];
+    dmu_lo[tid] = R.dmu_lo[tid];
+  }
   if (tid < 3) {  // colour lists per axis, blocks of size p (or more)
     const int a = tid, L = R.L[a], p = R.p;
     const int q = L / p;
-    int coord_col[MAX_L];
-    int x = 0;
-    for (int blk = 0; blk < q; ++blk) {
-      int sz = p + (L - q * p) / q + ((blk < (L - q * p) % q) ? 1 : 0);
-      for (int t = 0; t < sz; ++t) coord_col[x++] = t;
-    }
     int k = 0;
     for (int c = 0; c < R.n_col[a]; ++c) {
       ax_begin[a][c] = k;
-      for (int xx = 0; xx < L; ++xx)
-        if (coord_col[xx] == c) ax_coord[a][k++] = xx;
+      int x = 0;
+      for (int blk = 0; blk < q; ++blk) {
+        const int sz = p + (L - q * p) / q + ((blk < (L - q * p) % q) ? 1 : 0);
+        if (c < sz) ax_coord[a][k++] = x + c;
+        x += sz;
+      }
       ax_cnt[a][c] = k - ax_begin[a][c];
     }
   }
@@ -662,29 +729,27 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
     occ[G.addr(b, x, y, z)] = gocc[l];
   }
   __syncthreads();
-  {
-    const int D = G.L2 + 2 * G.R;
-    for (int h = tid; h < nsl * G.V; h += nth) {
-      const int b = h / G.V;
-      int r = h - b * G.V;
-      const int xh = r % G.W;
-      r /= G.W;
-      const int yh = r % G.H, zh = r / G.H;
-      (void)D;
-      const int x = xh - G.R, y = yh - G.R, z = zh - G.R;
-      if (x >= 0 && x < G.L0 && y >= 0 && y < G.L1 && z >= 0 && z < G.L2) continue;
-      occ[h] = occ[G.addr(b, wrapc(x, G.L0), wrapc(y, G.L1), wrapc(z, G.L2))];
-    }
+  for (int h = tid; h < nsl * G.V; h += nth) {
+    const int b = h / G.V;
+    int r = h - b * G.V;
+    const int xh = r % G.W;
+    r /= G.W;
+    const int yh = r % G.H, zh = r / G.H;
+    const int x = xh - G.R, y = yh - G.R, z = zh - G.R;
+    if (x >= 0 && x < G.L0 && y >= 0 && y < G.L1 && z >= 0 && z < G.L2) continue;
+    if (x >= G.L0 + G.R || y >= G.L1 + G.R) continue;  // pitch padding
+    occ[h] = occ[G.addr(b, wrapc(x, G.L0), wrapc(y, G.L1), wrapc(z, G.L2))];
   }
   __syncthreads();
 
-  // ---- passes
+  const SiteEval<NOCC, PITCH> ev{&T, cl_off, lutoff, lut};
   double energy = S.energy;
   long long nspec[8];
   for (int a = 0; a < 8; ++a) nspec[a] = S.n_species[a];
   long long pass_global = S.pass;
   const uint32_t k0 = (uint32_t)R.seed, k1 = (uint32_t)(R.seed >> 32);
-  const int n_sweeps = (R.ensemble == 1) ? 1 + N_LOCAL_SWEEPS : 1;
+  const int n_pair_sw = P.n_pair_sweeps, n_local_sw = P.n_local_sweeps;
+  const int n_sweeps = (ensemble == 1) ? n_pair_sw + n_local_sw : 1;
   const int n_sub = n_sweeps * n_classes;
   uint32_t *skey = sched, *spar = sched + n_sub, *sord = sched + 2 * n_sub;
   const int lane = tid & 31, warp = tid >> 5, nwarp = nth >> 5;
@@ -694,16 +759,16 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
     // schedule: per sweep a random order of the classes, plus parameters
     for (int e = tid; e < n_sub; e += nth) {
       const int c = e % n_classes;
-      U4 r = philox4x32_10(U4{0xFFFFFFFFu - (uint32_t)e, 0u, plo, phi | (TAG_SCHED << 16)}, k0, k1);
+      const U4 r =
+          philox4x32_10(U4{0xFFFFFFFFu - (uint32_t)e, 0u, plo, phi | (TAG_SCHED << 16)}, k0, k1);
       skey[e] = r.x;
       const int cb = c / ncol_all, cr = c - cb * ncol_all;
-      const int cc[3] = {cr % R.n_col[0], (cr / R.n_col[0]) % R.n_col[1],
-                         cr / (R.n_col[0] * R.n_col[1])};
+      const int cc[3] = {cr % ncol0, (cr / ncol0) % ncol1, cr / (ncol0 * ncol1)};
       int dims[3];
       for (int a = 0; a < 3; ++a) dims[a] = ax_cnt[a][cc[a]];
       const int sweep = e / n_classes;
       uint32_t par = 0;
-      if (R.ensemble == 1 && sweep == 0) {  // pairs within the class
+      if (ensemble == 1 && sweep < n_pair_sw) {  // pairs within the class
         int a = r.y % 3, tries = 0;
         while (dims[a] < 2 && tries < 3) {
           a = (a + 1) % 3;
@@ -716,7 +781,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
         } else {
           par = 0xFFFFFFFFu;  // no pair along any axis
         }
-      } else if (R.ensemble == 1) {  // local pairs with a neighbour
+      } else if (ensemble == 1) {  // local pairs with a neighbour
         const int nnb = T.n_nb[cb];
         const int dlt = (int)(r.y % (uint32_t)(nnb > 0 ? nnb : 1));
         const uint32_t parity = r.z & 7u;
@@ -742,7 +807,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
     }
     __syncthreads();
 
-    double de_acc = 0.0;
+    EnergyAcc<NOCC> eacc;
     int dspec[NOCC];
     for (int a = 0; a < NOCC; ++a) dspec[a] = 0;
     int n_prop = 0, n_acc = 0;
@@ -752,14 +817,13 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
       const int c = (int)sord[sub];
       const uint32_t par = spar[sw * n_classes + c];
       const int cb = c / ncol_all, cr = c - cb * ncol_all;
-      const int cc[3] = {cr % R.n_col[0], (cr / R.n_col[0]) % R.n_col[1],
-                         cr / (R.n_col[0] * R.n_col[1])};
+      const int cc[3] = {cr % ncol0, (cr / ncol0) % ncol1, cr / (ncol0 * ncol1)};
       const int dims[3] = {ax_cnt[0][cc[0]], ax_cnt[1][cc[1]], ax_cnt[2][cc[2]]};
       const int *cx = ax_coord[0] + ax_begin[0][cc[0]];
       const int *cy = ax_coord[1] + ax_begin[1][cc[1]];
       const int *cz = ax_coord[2] + ax_begin[2][cc[2]];
       const uint32_t ctr_sub = (uint32_t)sub;
-      if (R.ensemble == 0) {
+      if (ensemble == 0) {
         // ---------------- flips of every site of the class
         const int n = dims[0] * dims[1] * dims[2];
         for (int q = tid; q < n; q += nth) {
@@ -778,37 +842,34 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
           }
           Acc<NOCC> acc;
           acc.zero();
-          auto rd = [&](int cl, int j) -> int { return occ[ad + cl_off[cl * 3 + j]]; };
-          accumulate_site<NOCC>(T, cb, o_i, o_f, lutoff, lut, rd, acc);
+          ev.add(cb, o_i, o_f, occ, ad, acc);
           FF d = acc_dot<NOCC>(T, acc, whi, wlo);
-          ff_add_ff(d, -R.dmu_hi[o_i * NOCC + o_f], -R.dmu_lo[o_i * NOCC + o_f]);
+          ff_add_ff(d, -dmu_hi[o_i * NOCC + o_f], -dmu_lo[o_i * NOCC + o_f]);
           ++n_prop;
-          if (accept_fast(d, R.beta_f, u24(r.x))) {
+          if (accept_fast(d, beta_f, u24(r.x))) {
             ++n_acc;
             put_site(occ, G, cb, x, y, z, (int8_t)o_f);
-            de_acc += (double)d.s + (double)d.e + R.dmu[o_i * NOCC + o_f];
+            eacc.add(acc, d, R.dmu[o_i * NOCC + o_f]);
             dspec[o_i]--;
             dspec[o_f]++;
           }
         }
-      } else if (sw == 0) {
+      } else if (sw < n_pair_sw) {
         // ---------------- canonical swaps of pairs inside the class
         if (par != 0xFFFFFFFFu) {
           const int a = par & 3, m = (par >> 2) & 255, rot = par >> 10;
           const int na = dims[a];
-          const int blocks = na / (2 * m);
-          const int half = blocks * m;  // pairs along the axis
-          const int d1 = dims[(a + 1) % 3], d2 = dims[(a + 2) % 3];
-          const int n = half * d1 * d2;
+          const int half = (na / (2 * m)) * m;  // pairs along the axis
+          int e3[3] = {dims[0], dims[1], dims[2]};
+          e3[a] = half;
+          const int n = e3[0] * e3[1] * e3[2];
           for (int q = tid; q < n; q += nth) {
-            const int jj = q % half, rest = q / half;
-            const int o1 = rest % d1, o2 = rest / d1;
+            int ia[3] = {q % e3[0], (q / e3[0]) % e3[1], q / (e3[0] * e3[1])};
+            int ib[3] = {ia[0], ia[1], ia[2]};
+            const int jj = ia[a];
             const int u = 2 * m * (jj / m) + (jj % m);
-            int ia[3], ib[3];
             ia[a] = (u + rot) % na;
             ib[a] = (u + m + rot) % na;
-            ia[(a + 1) % 3] = ib[(a + 1) % 3] = o1;
-            ia[(a + 2) % 3] = ib[(a + 2) % 3] = o2;
             const int xa = cx[ia[0]], ya = cy[ia[1]], za = cz[ia[2]];
             const int xb = cx[ib[0]], yb = cy[ib[1]], zb = cz[ib[2]];
             const int ada = G.addr(cb, xa, ya, za), adb = G.addr(cb, xb, yb, zb);
@@ -818,17 +879,15 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
             const U4 r = philox4x32_10(U4{(uint32_t)la, ctr_sub, plo, phi | (TAG_SITE << 16)}, k0, k1);
             Acc<NOCC> acc;
             acc.zero();
-            auto rda = [&](int cl, int j) -> int { return occ[ada + cl_off[cl * 3 + j]]; };
-            auto rdb = [&](int cl, int j) -> int { return occ[adb + cl_off[cl * 3 + j]]; };
-            accumulate_site<NOCC>(T, cb, oa, ob, lutoff, lut, rda, acc);
-            accumulate_site<NOCC>(T, cb, ob, oa, lutoff, lut, rdb, acc);
+            ev.add(cb, oa, ob, occ, ada, acc);
+            ev.add(cb, ob, oa, occ, adb, acc);
             const FF d = acc_dot<NOCC>(T, acc, whi, wlo);
             ++n_prop;
-            if (accept_fast(d, R.beta_f, u24(r.x))) {
+            if (accept_fast(d, beta_f, u24(r.x))) {
               ++n_acc;
               put_site(occ, G, cb, xa, ya, za, (int8_t)ob);
               put_site(occ, G, cb, xb, yb, zb, (int8_t)oa);
-              de_acc += (double)d.s + (double)d.e;
+              eacc.add(acc, d, 0.0);
             }
           }
         }
@@ -862,17 +921,15 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
             const U4 r = philox4x32_10(U4{(uint32_t)la, ctr_sub, plo, phi | (TAG_SITE << 16)}, k0, k1);
             Acc<NOCC> acc;
             acc.zero();
-            auto rda = [&](int cl, int j) -> int { return occ[ada + cl_off[cl * 3 + j]]; };
-            auto rdb = [&](int cl, int j) -> int { return occ[adb + cl_off[cl * 3 + j]]; };
-            accumulate_site<NOCC>(T, cb, oa, ob, lutoff, lut, rda, acc);
+            ev.add(cb, oa, ob, occ, ada, acc);
             put_site(occ, G, cb, xa, ya, za, (int8_t)ob);  // first change applied
-            accumulate_site<NOCC>(T, nb_b, ob, oa, lutoff, lut, rdb, acc);
+            ev.add(nb_b, ob, oa, occ, adb, acc);
             const FF d = acc_dot<NOCC>(T, acc, whi, wlo);
             ++n_prop;
-            if (accept_fast(d, R.beta_f, u24(r.x))) {
+            if (accept_fast(d, beta_f, u24(r.x))) {
               ++n_acc;
               put_site(occ, G, nb_b, xb, yb, zb, (int8_t)oa);
-              de_acc += (double)d.s + (double)d.e;
+              eacc.add(acc, d, 0.0);
             } else {
               put_site(occ, G, cb, xa, ya, za, (int8_t)oa);
             }
@@ -884,37 +941,49 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
 
     // ---- end of pass: reduce, sample
     {
-      double v = de_acc;
-      long long vp = n_prop, va = n_acc;
-      long long vs[NOCC];
-      for (int a = 0; a < NOCC; ++a) vs[a] = dspec[a];
-      for (int off = 16; off; off >>= 1) {
-        v += __shfl_xor_sync(0xffffffffu, v, off);
-        vp += __shfl_xor_sync(0xffffffffu, vp, off);
-        va += __shfl_xor_sync(0xffffffffu, va, off);
-        for (int a = 0; a < NOCC; ++a) vs[a] += __shfl_xor_sync(0xffffffffu, vs[a], off);
+      // slots: 0 proposals, 1 accepts, 2..2+NOCC species, 8..15 energy terms
+      long long vals[16];
+      for (int k = 0; k < 16; ++k) vals[k] = 0;
+      vals[0] = n_prop;
+      vals[1] = n_acc;
+      for (int a = 0; a < NOCC; ++a) vals[2 + a] = dspec[a];
+      double dsum = 0.0;
+      if constexpr (NOCC == 2) {
+        for (int g = 0; g < MAX_ORBITS; ++g) vals[8 + g] = eacc.dc[g];
+      } else {
+        dsum = eacc.de;
       }
-      double *rd_d = reinterpret_cast<double *>(red);
-      long long *rd_l = reinterpret_cast<long long *>(red + 32 * 8);
+#pragma unroll
+      for (int k = 0; k < 16; ++k)
+        for (int off = 16; off; off >>= 1) vals[k] += __shfl_xor_sync(0xffffffffu, vals[k], off);
+      for (int off = 16; off; off >>= 1) dsum += __shfl_xor_sync(0xffffffffu, dsum, off);
+      long long *rd_l = reinterpret_cast<long long *>(red);
       if (lane == 0) {
-        rd_d[warp] = v;
-        rd_l[warp * 10 + 0] = vp;
-        rd_l[warp * 10 + 1] = va;
-        for (int a = 0; a < NOCC; ++a) rd_l[warp * 10 + 2 + a] = vs[a];
+        for (int k = 0; k < 15; ++k) rd_l[warp * 16 + k] = vals[k];
+        reinterpret_cast<double *>(rd_l)[warp * 16 + 15] = dsum;
+        if constexpr (NOCC == 2) rd_l[warp * 16 + 15] = vals[15];
       }
       __syncthreads();
       if (tid == 0) {
-        double dsum = 0.0;
-        long long sp = 0, sa = 0;
+        long long tot[16];
+        double dtot = 0.0;
+        for (int k = 0; k < 16; ++k) tot[k] = 0;
         for (int w = 0; w < nwarp; ++w) {
-          dsum += rd_d[w];
-          sp += rd_l[w * 10 + 0];
-          sa += rd_l[w * 10 + 1];
-          for (int a = 0; a < NOCC; ++a) nspec[a] += rd_l[w * 10 + 2 + a];
+          for (int k = 0; k < 15; ++k) tot[k] += rd_l[w * 16 + k];
+          if constexpr (NOCC == 2) {
+            tot[15] += rd_l[w * 16 + 15];
+          } else {
+            dtot += reinterpret_cast<double *>(rd_l)[w * 16 + 15];
+          }
         }
-        energy += dsum;
-        S.n_proposed += sp;
-        S.n_accepted += sa;
+        if constexpr (NOCC == 2) {
+          for (int g = 0; g < T.n_orbits; ++g)
+            dtot += T.w[T.orb_func_base[g]] * (double)tot[8 + g];
+        }
+        energy += dtot;
+        S.n_proposed += tot[0];
+        S.n_accepted += tot[1];
+        for (int a = 0; a < NOCC; ++a) nspec[a] += tot[2 + a];
         // param composition per unit cell and potential per unit cell
         double x[3] = {0.0, 0.0, 0.0}, mux = 0.0;
         for (int k = 0; k < NOCC - 1; ++k) {
@@ -989,8 +1058,12 @@ cudaError_t launch_delta_t(const CeTables &T, const int8_t *occ, int L0, int L1,
 
 template <int NOCC>
 cudaError_t launch_init_stats_t(const CeTables &T, const Replica *reps, ReplicaStats *stats,
-                                const int8_t *occ, int n_replicas, cudaStream_t st) {
-  k_init_stats<NOCC><<<n_replicas, 512, 0, st>>>(T, reps, stats, occ);
+                                const int8_t *occ, int n_replicas, int max_sites, cudaStream_t st) {
+  const int cap = max_sites <= 160 * 1024 ? ((max_sites + 15) & ~15) : 0;
+  cudaError_t e =
+      cudaFuncSetAttribute(k_init_stats<NOCC>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  if (e != cudaSuccess) return e;
+  k_init_stats<NOCC><<<n_replicas, 512, cap, st>>>(T, reps, stats, occ, cap);
   return cudaGetLastError();
 }
 
@@ -1008,13 +1081,13 @@ cudaError_t launch_replay_t(const CeTables &T, const ReplayParams &P, cudaStream
   return cudaGetLastError();
 }
 
-template <int NOCC>
+template <int NOCC, int PITCH>
 cudaError_t launch_sweep_t(const CeTables &T, const SweepParams &P, int n_replicas, int smem,
                            cudaStream_t st) {
-  cudaError_t e =
-      cudaFuncSetAttribute(k_sweep<NOCC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaError_t e = cudaFuncSetAttribute(k_sweep<NOCC, PITCH>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  k_sweep<NOCC><<<n_replicas, SWEEP_THREADS, smem, st>>>(T, P);
+  k_sweep<NOCC, PITCH><<<n_replicas, SWEEP_THREADS, smem, st>>>(T, P);
   return cudaGetLastError();
 }
 
@@ -1026,8 +1099,8 @@ cudaError_t launch_sweep_t(const CeTables &T, const SweepParams &P, int n_replic
                                          double *, long long *, cudaStream_t);                 \
   template cudaError_t launch_replay_t<N>(const CeTables &, const ReplayParams &, cudaStream_t); \
   template cudaError_t launch_init_stats_t<N>(const CeTables &, const Replica *, ReplicaStats *, \
-                                              const int8_t *, int, cudaStream_t);              \
-  template cudaError_t launch_sweep_t<N>(const CeTables &, const SweepParams &, int, int,       \
-                                         cudaStream_t);
+                                              const int8_t *, int, int, cudaStream_t);         \
+  template cudaError_t launch_sweep_t<N, 0>(const CeTables &, const SweepParams &, int, int,    \
+                                            cudaStream_t);
 
 }  // namespace cem

@@ -14,8 +14,8 @@ template <int N>
 cudaError_t launch_replay_t(const CeTables &, const ReplayParams &, cudaStream_t);
 template <int N>
 cudaError_t launch_init_stats_t(const CeTables &, const Replica *, ReplicaStats *, const int8_t *,
-                                int, cudaStream_t);
-template <int N>
+                                int, int, cudaStream_t);
+template <int N, int PITCH>
 cudaError_t launch_sweep_t(const CeTables &, const SweepParams &, int, int, cudaStream_t);
 
 
@@ -47,21 +47,45 @@ cudaError_t launch_replay(const CeTables &T, const ReplayParams &P, cudaStream_t
   return cudaErrorInvalidValue;
 }
 
-int sweep_smem_bytes(const CeTables &T, int L0, int L1, int L2, int n_classes) {
-  return sweep_smem_bytes_impl(T, L0, L1, L2, n_classes);
+int sweep_smem_bytes(const CeTables &T, int L0, int L1, int L2, int n_classes, int pitch) {
+  return sweep_smem_bytes_impl(T, L0, L1, L2, n_classes, pitch);
 }
 
 cudaError_t launch_sweep(const CeTables &T, const SweepParams &P, int n_replicas, int smem,
-                         cudaStream_t st) {
-  if (T.n_occ == 2) return launch_sweep_t<2>(T, P, n_replicas, smem, st);
-  if (T.n_occ == 3) return launch_sweep_t<3>(T, P, n_replicas, smem, st);
+                         int pitch, cudaStream_t st) {
+  if (pitch == 32) return launch_sweep_t<2, 32>(T, P, n_replicas, smem, st);
+  if (pitch == 48) return launch_sweep_t<2, 48>(T, P, n_replicas, smem, st);
+  if (pitch == 64) return launch_sweep_t<2, 64>(T, P, n_replicas, smem, st);
+  if (pitch != 0) return cudaErrorInvalidValue;
+  if (T.n_occ == 2) return launch_sweep_t<2, 0>(T, P, n_replicas, smem, st);
+  if (T.n_occ == 3) return launch_sweep_t<3, 0>(T, P, n_replicas, smem, st);
   return cudaErrorInvalidValue;
 }
 
+bool matches_generated_fcc(const CeTables &T, const int *pb, const int *du) {
+  if (T.n_sublat != 1 || T.n_occ != 2 || T.n_orbits != gen_fcc::N_ORBITS) return false;
+  if (T.reach != 2) return false;
+  for (int g = 0; g < T.n_orbits; ++g) {
+    if (T.orb_size[g] != gen_fcc::ORBIT_SIZE[g]) return false;
+    if (T.fl_begin[0][g + 1] - T.fl_begin[0][g] != gen_fcc::ORBIT_CLUSTERS[g]) return false;
+  }
+  if (T.n_fl != gen_fcc::N_CL) return false;
+  for (int c = 0; c < T.n_fl; ++c)
+    for (int q = 0; q < 3; ++q) {
+      const int k = gen_fcc::CL_P[c][q];
+      if ((k < 0) != (pb[c * 3 + q] < 0)) return false;
+      if (k < 0) continue;
+      if (pb[c * 3 + q] != 0) return false;
+      for (int a = 0; a < 3; ++a)
+        if (du[c * 9 + q * 3 + a] != gen_fcc::NB[k][a]) return false;
+    }
+  return true;
+}
+
 cudaError_t launch_init_stats(const CeTables &T, const Replica *reps, ReplicaStats *stats,
-                              const int8_t *occ, int n_replicas, cudaStream_t st) {
-  if (T.n_occ == 2) return launch_init_stats_t<2>(T, reps, stats, occ, n_replicas, st);
-  if (T.n_occ == 3) return launch_init_stats_t<3>(T, reps, stats, occ, n_replicas, st);
+                              const int8_t *occ, int n_replicas, int max_sites, cudaStream_t st) {
+  if (T.n_occ == 2) return launch_init_stats_t<2>(T, reps, stats, occ, n_replicas, max_sites, st);
+  if (T.n_occ == 3) return launch_init_stats_t<3>(T, reps, stats, occ, n_replicas, max_sites, st);
   return cudaErrorInvalidValue;
 }
 

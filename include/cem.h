@@ -179,6 +179,17 @@ int cem_replay(cem_replicas *r, int replica, uint64_t mt_seed, int64_t n_steps,
  * SemiGrandCanonicalCalculator.cc:423-466). */
 int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_samples);
 
+/* Run options of a batch (canonical pass composition and evaluator):
+ *   "pair_sweeps"  (default 2): sweeps of swaps between sites of one colour
+ *                  class per pass;
+ *   "local_sweeps" (default 1, >= 1): sweeps of swaps with a nearest
+ *                  neighbour per pass (these move atoms between classes);
+ *   "generic_evaluator" (1): use the run-time cluster tables even where the
+ *                  generated binary FCC evaluator applies.
+ * cem_get_option also reads "pitch", "smem_bytes" and "colour_classes". */
+int cem_set_option(cem_replicas *r, const char *key, int64_t value);
+int cem_get_option(cem_replicas *r, const char *key, int64_t *value);
+
 /* Statistics and samples of one replica (after cem_run). */
 int cem_get_stats(cem_replicas *r, int replica, cem_stats *out);
 int cem_get_samples(cem_replicas *r, int replica, double *potential, double *comp,

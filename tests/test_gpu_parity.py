@@ -203,3 +203,33 @@ def test_parallel_equilibrium_matches_oracle(ens, cm, oracle_mod):
         x_o, sx_o = batch_means(ref["comp"][1000:, 0])
         xs = np.array([b.stats(i)["mean_comp"][0] for i in range(nrep)])
         assert abs(xs.mean() - x_o) < 4.0 * np.hypot(xs.std(ddof=1) / np.sqrt(nrep), sx_o)
+
+
+@pytest.mark.parametrize("ens,L", [("canonical", (24, 24, 24)), ("semigrand_canonical", (10, 10, 10)),
+                                   ("canonical", (30, 30, 30))])
+def test_generated_evaluator_matches_runtime_tables(ens, L, cm):
+    """The generated binary FCC evaluator and the run-time table walk make
+    the same decisions: identical occupations and statistics."""
+    ce = workloads.fcc_binary_ce(2)
+    sysd = cm.System(ce)
+    rng = np.random.default_rng(4)
+    n = L[0] * L[1] * L[2]
+    occ0 = workloads.fixed_composition(rng, n, 0.35)
+    out = []
+    for generic in (False, True):
+        b = cm.ReplicaBatch(sysd, ens, [L, L])
+        if generic:
+            b.set_option("generic_evaluator", 1)
+            assert b.get_option("pitch") == 0
+        else:
+            assert b.get_option("pitch") == (32 if L[0] <= 28 else 48)
+        for i in range(2):
+            b.set_conditions(i, 500.0 + 400 * i, np.array([0.02]) if ens != "canonical" else None)
+            b.set_seed(i, 31 + i)
+            b.set_occupation(i, occ0)
+        b.run(25, 5)
+        out.append([(b.get_occupation(i), b.stats(i)) for i in range(2)])
+    for (oa, sa), (ob, sb) in zip(*out):
+        np.testing.assert_array_equal(oa, ob)
+        assert sa["n_accepted"] == sb["n_accepted"] and sa["n_proposed"] == sb["n_proposed"]
+        assert abs(sa["energy"] - sb["energy"]) <= 1e-9 * abs(sb["energy"]) + 1e-9

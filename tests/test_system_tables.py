@@ -117,3 +117,10 @@ def test_system_arrays_shapes():
     assert a["n_flower"] == 222 and a["flower_lut"].size == 222 * 16
     assert a["flower_partner_du"].size == 222 * 9
     assert np.all(a["n_neighbour"] == 8)
+
+
+def test_generated_fcc_header_is_current():
+    from casmcode_clexmonte_gb300 import codegen
+
+    with open(codegen.OUT) as f:
+        assert f.read() == codegen.fcc_binary_header()
