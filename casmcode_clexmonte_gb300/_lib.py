@@ -54,7 +54,7 @@ EXPORTS = [
     "cem_get_occupation_all", "cem_host_alloc", "cem_host_free", "cem_energy",
     "cem_delta_energy", "cem_replay", "cem_run", "cem_get_stats", "cem_get_samples",
     "cem_reset_stats", "cem_synchronize", "cem_last_kernel_ms", "cem_smem_bandwidth",
-    "cem_set_option", "cem_get_option",
+    "cem_set_option", "cem_get_option", "cem_delta_energy_noalloc",
 ]
 
 _lib = None

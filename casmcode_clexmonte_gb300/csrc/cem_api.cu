@@ -8,6 +8,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -859,3 +860,97 @@ int cem_last_kernel_ms(cem_replicas *r, double *ms) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Delta energies without any device allocation.
+//
+// Some callers cannot allocate device memory: a host program whose device
+// memory is owned by another framework's pool (which reserves the device and
+// expects no raw cudaMalloc), or a Monte Carlo driver that evaluates events in
+// a tight per-event loop and cannot afford the device-wide synchronisation that
+// cudaMalloc/cudaFree imply. cem_delta_energy_noalloc serves them: it stages
+// the events and results in one fixed array in device global memory that is
+// part of the library image (every device that loads the library holds it
+// until the process exits), instead of allocating per call.
+//
+// Limits: at most CEM_NOALLOC_MAX_EVENTS events of at most
+// CEM_NOALLOC_MAX_SITES sites per call; larger calls are rejected.
+// All calls share the array and it keeps the last call's contents; calls that
+// overlap on the GPU (different streams or batches at the same time) race.
+namespace {
+
+constexpr int NOALLOC_MAX_EVENTS = 4096;
+constexpr int NOALLOC_MAX_SITES = 4;
+constexpr size_t NA_SITES = 0;                                                   // int64
+constexpr size_t NA_NEW = NA_SITES + 8ull * NOALLOC_MAX_EVENTS * NOALLOC_MAX_SITES;  // int32
+constexpr size_t NA_DE = NA_NEW + 4ull * NOALLOC_MAX_EVENTS * NOALLOC_MAX_SITES;    // double
+constexpr size_t NA_DC = NA_DE + 8ull * NOALLOC_MAX_EVENTS;                         // int64
+constexpr size_t NA_DMU = NA_DC + 8ull * NOALLOC_MAX_EVENTS * MAX_FUNCS;            // double[16]
+constexpr size_t NA_BYTES = NA_DMU + 8 * 16;
+static_assert(NA_NEW % 256 == 0 && NA_DE % 256 == 0 && NA_DC % 256 == 0 && NA_DMU % 256 == 0,
+              "scratch sections are 256-byte aligned");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
+
+constexpr int NA_MAX_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+unsigned char *g_noalloc_ptr[NA_MAX_DEVICES] = {nullptr};
+
+// Device address of the scratch array for the current device; resolved once
+// per device (the host-side name is only a stand-in, not a device address).
+unsigned char *noalloc_scratch() {
+  int dev = 0;
+  CUDA_OK(cudaGetDevice(&dev));
+  require(dev >= 0 && dev < NA_MAX_DEVICES, "device index out of range", CEM_ERR_UNSUPPORTED);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    CUDA_OK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_ptr[dev] = static_cast<unsigned char *>(p);
+  }
+  return g_noalloc_ptr[dev];
+}
+
+}  // namespace
+
+extern "C" int cem_delta_energy_noalloc(cem_replicas *r, int i, int n_events, int k,
+                                        const int64_t *sites, const int32_t *new_occ,
+                                        int potential, double *dE, int64_t *dcount) {
+  return guard([&] {
+    check_rep(r, i);
+    require(n_events >= 0 && k >= 1 && k <= 4, "sites_per_event must be 1..4");
+    require(n_events <= NOALLOC_MAX_EVENTS,
+            "cem_delta_energy_noalloc handles at most " + std::to_string(NOALLOC_MAX_EVENTS) +
+                " events per call (got " + std::to_string(n_events) + ")",
+            CEM_ERR_UNSUPPORTED);
+    require(sites && new_occ && dE, "null argument");
+    unsigned char *base = noalloc_scratch();  // first call on a device resolves the address
+    if (n_events == 0) return;
+    const Replica &R = r->reps[i];
+    const CeTables &T = r->sys->T;
+    for (int64_t e = 0; e < (int64_t)n_events * k; ++e) {
+      require(sites[e] >= 0 && sites[e] < R.n_sites, "site index out of range");
+      require(new_occ[e] >= 0 && new_occ[e] < T.n_occ, "occupant index out of range");
+    }
+    require(potential == 0 || r->ensemble == CEM_SEMIGRAND_CANONICAL,
+            "the semi-grand potential needs semi-grand canonical replicas");
+    long long *ds = reinterpret_cast<long long *>(base + NA_SITES);
+    int *dn = reinterpret_cast<int *>(base + NA_NEW);
+    double *dde = reinterpret_cast<double *>(base + NA_DE);
+    long long *ddc = reinterpret_cast<long long *>(base + NA_DC);
+    double *ddmu = reinterpret_cast<double *>(base + NA_DMU);
+    const size_t ne = (size_t)n_events * k;
+    CUDA_OK(cudaMemcpyAsync(ds, sites, ne * 8, cudaMemcpyHostToDevice, r->stream));
+    CUDA_OK(cudaMemcpyAsync(dn, new_occ, ne * 4, cudaMemcpyHostToDevice, r->stream));
+    if (potential)
+      CUDA_OK(cudaMemcpyAsync(ddmu, R.dmu, 16 * 8, cudaMemcpyHostToDevice, r->stream));
+    // every dE (and dcount) entry of the call is written by the kernel
+    CUDA_OK(launch_delta(T, r->d_occ + R.occ_offset, R.L[0], R.L[1], R.L[2], n_events, k, ds, dn,
+                         potential ? ddmu : nullptr, dde, dcount ? ddc : nullptr, r->stream));
+    CUDA_OK(cudaMemcpyAsync(dE, dde, (size_t)n_events * 8, cudaMemcpyDeviceToHost, r->stream));
+    if (dcount)
+      CUDA_OK(cudaMemcpyAsync(dcount, ddc, (size_t)n_events * T.n_funcs * 8,
+                              cudaMemcpyDeviceToHost, r->stream));
+    CUDA_OK(cudaStreamSynchronize(r->stream));
+  });
+}

@@ -159,6 +159,23 @@ int cem_delta_energy(cem_replicas *r, int replica, int n_events, int sites_per_e
                      const int64_t *sites, const int32_t *new_occ, int potential,
                      double *dE, int64_t *dcount);
 
+/* Same result as cem_delta_energy, without allocating device memory. This
+ * entry point has no counterpart in the reference. It is for callers that
+ * cannot allocate on the device: a host program whose device memory belongs
+ * to another framework's pool, or a per-event Monte Carlo loop that cannot
+ * afford the device-wide synchronisation cudaMalloc and cudaFree imply.
+ * Events and results are staged in one fixed array in device memory that is
+ * part of the library (about 2.3 MB, held by every device that loads the
+ * library until the process exits). At most 4096 events of at most 4 sites
+ * per call; larger calls return CEM_ERR_UNSUPPORTED. The first call on a
+ * device looks up the array's device address for that device, so make that
+ * first call before any stream capture. All calls share the array and it
+ * keeps the last call's contents; calls that overlap on the GPU (from
+ * different streams or batches at the same time) race. */
+int cem_delta_energy_noalloc(cem_replicas *r, int replica, int n_events, int sites_per_event,
+                             const int64_t *sites, const int32_t *new_occ, int potential,
+                             double *dE, int64_t *dcount);
+
 /* Sequential replay: n_steps steps of occupation_metropolis_v2
  * (occupation_metropolis.hh:92-120) on one replica, consuming the
  * std::mt19937_64 stream seeded with mt_seed exactly as the reference's
