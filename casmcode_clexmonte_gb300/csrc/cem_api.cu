@@ -417,7 +417,19 @@ int cem_replicas_create(const cem_system *sys, int n, const int *L, int ensemble
     for (int i = 0; i < n; ++i)
       need = std::max({need, r->reps[i].L[0] + 2 * sys->T.reach, r->reps[i].L[1] + 2 * sys->T.reach});
     int pitch = 0;
-    if (sys->fcc_generated) pitch = need <= 32 ? 32 : need <= 48 ? 48 : need <= 64 ? 64 : 0;
+    if (sys->fcc_generated) {
+      // exact fit L + 2 reach when every replica has it, else the smallest that holds all
+      bool same = true;
+      for (int i = 0; i < n; ++i)
+        same = same && r->reps[i].L[0] + 2 * sys->T.reach == need &&
+               r->reps[i].L[1] + 2 * sys->T.reach == need;
+      for (int cand : SWEEP_PITCHES) {
+        if (cand < need) continue;
+        if (same && cand != need && cand != 64) continue;
+        pitch = cand;
+        break;
+      }
+    }
     int smem = 0, gsmem = 0;
     for (int i = 0; i < n; ++i) {
       const int *Li = r->reps[i].L;
@@ -702,8 +714,12 @@ int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_sampl
                 " bytes needed)",
             CEM_ERR_UNSUPPORTED);
     r->upload_reps();
-    if (!r->stats_valid) init_stats(r);
+    // binary systems compute the exact initial stats inside the sweep kernel
+    const bool fused_init = !r->stats_valid && r->sys->T.n_occ == 2;
+    if (!r->stats_valid && !fused_init) init_stats(r);
     SweepParams P{};
+    P.init = fused_init ? 1 : 0;
+    r->stats_valid = true;
     P.reps = r->d_reps;
     P.stats = r->d_stats;
     P.occ = r->d_occ;

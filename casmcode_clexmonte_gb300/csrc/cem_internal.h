@@ -8,6 +8,9 @@
 namespace cem {
 
 constexpr int SWEEP_THREADS = 512;
+// pitches of the generated evaluator: L + 4 for L = 10, 24, 32, 48 (a warp's
+// class rows fall on distinct shared-memory banks), and 64 for the rest
+constexpr int SWEEP_PITCHES[5] = {14, 28, 36, 52, 64};
 
 struct ReplayParams {
   int L[3];
@@ -34,6 +37,7 @@ struct SweepParams {
   long long n_passes, n_equil;
   int max_classes;
   int n_pair_sweeps, n_local_sweeps;  // canonical pass composition
+  int init;                    // binary systems: compute the exact initial stats in-kernel
   double RT[16];               // (n_occ-1) x n_occ
 };
 
@@ -48,7 +52,8 @@ cudaError_t launch_init_stats(const CeTables &T, const Replica *reps, ReplicaSta
                               const int8_t *occ, int n_replicas, int max_sites, cudaStream_t st);
 cudaError_t smem_bandwidth(double *gbs, cudaStream_t st);
 int sweep_smem_bytes(const CeTables &T, int L0, int L1, int L2, int n_classes, int pitch);
-// pitch 0: run-time tables; 32/48/64: generated binary FCC evaluator
+// pitch 0: run-time tables; otherwise the generated binary FCC evaluator with
+// that x/y pitch (one of SWEEP_PITCHES)
 cudaError_t launch_sweep(const CeTables &T, const SweepParams &P, int n_replicas, int smem,
                          int pitch, cudaStream_t st);
 // true if the system is the binary FCC topology of the generated evaluator

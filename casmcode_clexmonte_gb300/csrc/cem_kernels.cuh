@@ -743,6 +743,57 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
   __syncthreads();
 
   const SiteEval<NOCC, PITCH> ev{&T, cl_off, lutoff, lut};
+  const int lane = tid & 31, warp = tid >> 5, nwarp = nth >> 5;
+  if constexpr (NOCC == 2) {
+    if (P.init) {
+      // exact initial state: every cluster of orbit g with all sites occupant 1
+      // is seen from each of its size_g sites, so count_g = sum over sites with
+      // occupant 1 of its flower count / size_g
+      long long cnt[MAX_ORBITS];
+      for (int g = 0; g < MAX_ORBITS; ++g) cnt[g] = 0;
+      long long n1 = 0;
+      for (int l = tid; l < n_sites; l += nth) {
+        const int b = l / n_uc, uc = l - b * n_uc;
+        const int x = uc % G.L0, y = (uc / G.L0) % G.L1, z = uc / (G.L0 * G.L1);
+        const int ad = G.addr(b, x, y, z);
+        const int o = occ[ad];
+        if (o == 0) continue;
+        ++n1;
+        Acc<2> acc;
+        acc.zero();
+        ev.add(b, 0, 1, occ, ad, acc);
+        for (int g = 0; g < MAX_ORBITS; ++g) cnt[g] += acc.c[g];
+      }
+      long long *rd_l = reinterpret_cast<long long *>(red);
+      for (int off = 16; off; off >>= 1) {
+        n1 += __shfl_xor_sync(0xffffffffu, n1, off);
+        for (int g = 0; g < MAX_ORBITS; ++g) cnt[g] += __shfl_xor_sync(0xffffffffu, cnt[g], off);
+      }
+      if (lane == 0) {
+        for (int g = 0; g < MAX_ORBITS; ++g) rd_l[warp * 16 + g] = cnt[g];
+        rd_l[warp * 16 + 8] = n1;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        long long tot[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (int w = 0; w < nwarp; ++w)
+          for (int k = 0; k < 9; ++k) tot[k] += rd_l[w * 16 + k];
+        double e = T.w[0] * n_uc;
+        for (int g = 0; g < T.n_orbits; ++g)
+          e += T.w[T.orb_func_base[g]] * (double)(tot[g] / T.orb_size[g]);
+        const long long pass = S.pass, np = S.n_proposed, na = S.n_accepted;
+        unsigned char *raw = reinterpret_cast<unsigned char *>(&S);
+        for (int q = 0; q < (int)sizeof(ReplicaStats); ++q) raw[q] = 0;
+        S.energy = e;
+        S.n_species[0] = n_sites - tot[8];
+        S.n_species[1] = tot[8];
+        S.pass = pass;
+        S.n_proposed = np;
+        S.n_accepted = na;
+      }
+      __syncthreads();
+    }
+  }
   double energy = S.energy;
   long long nspec[8];
   for (int a = 0; a < 8; ++a) nspec[a] = S.n_species[a];
@@ -752,7 +803,6 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
   const int n_sweeps = (ensemble == 1) ? n_pair_sw + n_local_sw : 1;
   const int n_sub = n_sweeps * n_classes;
   uint32_t *skey = sched, *spar = sched + n_sub, *sord = sched + 2 * n_sub;
-  const int lane = tid & 31, warp = tid >> 5, nwarp = nth >> 5;
 
   for (long long ip = 0; ip < P.n_passes; ++ip, ++pass_global) {
     const uint32_t plo = (uint32_t)pass_global, phi = (uint32_t)(pass_global >> 32) & 0xFFFFu;

@@ -1,11 +1,9 @@
-// Sweep kernels with the generated binary FCC site evaluator, one per
-// shared-memory pitch (32, 48, 64 bytes per row and rows per plane).
+// Sweep kernels with the generated binary FCC site evaluator for the
+// shared-memory pitches 28 and 52 (24^3 and 48^3 supercells).
 #include "cem_kernels.cuh"
 namespace cem {
-template cudaError_t launch_sweep_t<2, 32>(const CeTables &, const SweepParams &, int, int,
+template cudaError_t launch_sweep_t<2, 28>(const CeTables &, const SweepParams &, int, int,
                                            cudaStream_t);
-template cudaError_t launch_sweep_t<2, 48>(const CeTables &, const SweepParams &, int, int,
-                                           cudaStream_t);
-template cudaError_t launch_sweep_t<2, 64>(const CeTables &, const SweepParams &, int, int,
+template cudaError_t launch_sweep_t<2, 52>(const CeTables &, const SweepParams &, int, int,
                                            cudaStream_t);
 }  // namespace cem

@@ -53,8 +53,10 @@ int sweep_smem_bytes(const CeTables &T, int L0, int L1, int L2, int n_classes, i
 
 cudaError_t launch_sweep(const CeTables &T, const SweepParams &P, int n_replicas, int smem,
                          int pitch, cudaStream_t st) {
-  if (pitch == 32) return launch_sweep_t<2, 32>(T, P, n_replicas, smem, st);
-  if (pitch == 48) return launch_sweep_t<2, 48>(T, P, n_replicas, smem, st);
+  if (pitch == 14) return launch_sweep_t<2, 14>(T, P, n_replicas, smem, st);
+  if (pitch == 28) return launch_sweep_t<2, 28>(T, P, n_replicas, smem, st);
+  if (pitch == 36) return launch_sweep_t<2, 36>(T, P, n_replicas, smem, st);
+  if (pitch == 52) return launch_sweep_t<2, 52>(T, P, n_replicas, smem, st);
   if (pitch == 64) return launch_sweep_t<2, 64>(T, P, n_replicas, smem, st);
   if (pitch != 0) return cudaErrorInvalidValue;
   if (T.n_occ == 2) return launch_sweep_t<2, 0>(T, P, n_replicas, smem, st);

@@ -222,7 +222,7 @@ def test_generated_evaluator_matches_runtime_tables(ens, L, cm):
             b.set_option("generic_evaluator", 1)
             assert b.get_option("pitch") == 0
         else:
-            assert b.get_option("pitch") == (32 if L[0] <= 28 else 48)
+            assert b.get_option("pitch") == {24: 28, 10: 14, 30: 64}[L[0]]
         for i in range(2):
             b.set_conditions(i, 500.0 + 400 * i, np.array([0.02]) if ens != "canonical" else None)
             b.set_seed(i, 31 + i)
