@@ -55,6 +55,9 @@ EXPORTS = [
     "cem_delta_energy", "cem_replay", "cem_run", "cem_get_stats", "cem_get_samples",
     "cem_reset_stats", "cem_synchronize", "cem_last_kernel_ms", "cem_smem_bandwidth",
     "cem_set_option", "cem_get_option", "cem_delta_energy_noalloc",
+    "cem_mlp_info", "cem_mlp_create", "cem_mlp_destroy", "cem_mlp_get_params",
+    "cem_mlp_set_params", "cem_mlp_forward", "cem_mlp_gradient", "cem_mlp_train",
+    "cem_learned_features", "cem_learned_run", "cem_learned_samples",
 ]
 
 _lib = None
@@ -99,6 +102,17 @@ def load(path: str = LIB):
     L.cem_last_kernel_ms.argtypes = [P, _dp]
     L.cem_smem_bandwidth.argtypes = [_dp]
     L.cem_set_option.argtypes = [P, C.c_char_p, C.c_int64]
+    L.cem_mlp_info.argtypes = [_ip, _ip, _ip]
+    L.cem_mlp_create.argtypes = [C.c_uint64, C.POINTER(P)]
+    L.cem_mlp_destroy.argtypes = [P]
+    L.cem_mlp_get_params.argtypes = [P, vp]
+    L.cem_mlp_set_params.argtypes = [P, vp]
+    L.cem_mlp_forward.argtypes = [P, C.c_int64, vp, vp]
+    L.cem_mlp_gradient.argtypes = [P, C.c_int64, vp, vp, vp, C.POINTER(C.c_double)]
+    L.cem_mlp_train.argtypes = [P, C.c_int64, vp, vp, C.c_int, C.c_int, C.c_float, C.c_uint64, vp]
+    L.cem_learned_features.argtypes = [P, C.c_int, vp, vp]
+    L.cem_learned_run.argtypes = [P, P, C.c_int64, C.c_int64, C.c_int]
+    L.cem_learned_samples.argtypes = [P, C.c_int, vp, vp, C.c_int64, C.POINTER(C.c_int64)]
     L.cem_get_option.argtypes = [P, C.c_char_p, C.POINTER(C.c_int64)]
     _lib = L
     return L

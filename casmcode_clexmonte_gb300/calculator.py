@@ -157,6 +157,27 @@ class ReplicaBatch:
     def synchronize(self):
         check(self.lib.cem_synchronize(self.handle))
 
+    # ---- learned proposal
+    def learned_features(self, i: int):
+        n = int(self.n_sites[i])
+        X = np.zeros((n, LearnedProposal.N_IN), dtype=np.int8)
+        t = np.zeros(n, dtype=np.float32)
+        check(self.lib.cem_learned_features(self.handle, i, ptr(X), ptr(t)))
+        return X, t
+
+    def learned_run(self, proposal, n_passes: int, n_equil: int = 0, record_samples: bool = False):
+        h = None if proposal is None else proposal.handle
+        check(self.lib.cem_learned_run(self.handle, h, int(n_passes), int(n_equil),
+                                       int(bool(record_samples))))
+
+    def learned_samples(self, i: int, capacity: int):
+        e = np.zeros(capacity)
+        op = np.zeros(capacity)
+        n = C.c_int64()
+        check(self.lib.cem_learned_samples(self.handle, i, ptr(e), ptr(op), int(capacity),
+                                           C.byref(n)))
+        return e[: n.value], op[: n.value]
+
     def kernel_ms(self) -> float:
         ms = C.c_double()
         check(self.lib.cem_last_kernel_ms(self.handle, C.byref(ms)))
@@ -186,6 +207,60 @@ class ReplicaBatch:
         check(self.lib.cem_get_samples(self.handle, i, ptr(pot), ptr(comp), int(capacity),
                                        C.byref(n)))
         return pot[: n.value], comp[: n.value]
+
+
+class LearnedProposal:
+    """The proposal network (43 -> 64 -> 64 -> 1, bf16 parameters) on the GPU."""
+
+    N_IN = 43
+    N_HIDDEN = 64
+
+    def __init__(self, seed: int = 0):
+        self.lib = _lib.load()
+        ni, nh, npar = C.c_int(), C.c_int(), C.c_int()
+        check(self.lib.cem_mlp_info(C.byref(ni), C.byref(nh), C.byref(npar)))
+        self.n_params = npar.value
+        h = C.c_void_p()
+        check(self.lib.cem_mlp_create(int(seed), C.byref(h)))
+        self.handle = h
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            self.lib.cem_mlp_destroy(h)
+            self.handle = None
+
+    def get_params(self) -> np.ndarray:
+        p = np.zeros(self.n_params, dtype=np.float32)
+        check(self.lib.cem_mlp_get_params(self.handle, ptr(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.n_params
+        check(self.lib.cem_mlp_set_params(self.handle, ptr(p)))
+
+    def forward(self, X) -> np.ndarray:
+        X = np.ascontiguousarray(X, dtype=np.int8)
+        z = np.zeros(len(X), dtype=np.float32)
+        check(self.lib.cem_mlp_forward(self.handle, len(X), ptr(X), ptr(z)))
+        return z
+
+    def gradient(self, X, t):
+        X = np.ascontiguousarray(X, dtype=np.int8)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        g = np.zeros(self.n_params, dtype=np.float32)
+        loss = C.c_double()
+        check(self.lib.cem_mlp_gradient(self.handle, len(X), ptr(X), ptr(t), ptr(g), C.byref(loss)))
+        return g, loss.value
+
+    def train(self, X, t, epochs=5, batch=4096, lr=1e-3, seed=0):
+        X = np.ascontiguousarray(X, dtype=np.int8)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        losses = np.zeros(epochs)
+        check(self.lib.cem_mlp_train(self.handle, len(X), ptr(X), ptr(t), int(epochs), int(batch),
+                                     float(lr), int(seed), ptr(losses)))
+        return losses
 
 
 @dataclass

@@ -73,6 +73,12 @@ def render(ce, name="gen_fcc") -> str:
     L.append("constexpr int CL_ORBIT[N_CL] = {" + ", ".join(str(g) for g, _ in flat) + "};")
     L.append("constexpr int CL_P[N_CL][3] = {" + ", ".join(
         "{%s}" % ", ".join(str(x) for x in (list(c) + [-1] * (3 - len(c)))) for _, c in flat) + "};")
+    L.append("// copies in constant memory for run-time indexing on the device")
+    L.append("static __constant__ int NB_D[N_NB][3] = {")
+    L.append("    " + ", ".join("{%d, %d, %d}" % tuple(d) for d in nbs) + "};")
+    L.append("static __constant__ int CL_ORBIT_D[N_CL] = {" + ", ".join(str(g) for g, _ in flat) + "};")
+    L.append("static __constant__ int CL_P_D[N_CL][3] = {" + ", ".join(
+        "{%s}" % ", ".join(str(x) for x in (list(c) + [-1] * (3 - len(c)))) for _, c in flat) + "};")
     L.append("")
     L.append("// counts[g] = number of clusters of orbit g whose partners are all 1")
     L.append("template <int P>")

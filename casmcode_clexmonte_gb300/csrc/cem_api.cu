@@ -9,6 +9,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <random>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -16,6 +17,7 @@
 #include "../../include/cem.h"
 #include "cem_common.cuh"
 #include "cem_internal.h"
+#include "cem_learned.cuh"
 
 using namespace cem;
 
@@ -116,7 +118,15 @@ struct cem_replicas {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;
+  // learned-proposal state
+  long long *d_lw = nullptr;             // per-site integer weights
+  unsigned long long *d_trees = nullptr; // two sum trees per replica
+  double *d_lsamples = nullptr;          // [rep][cap][3]
+  long long lsample_capacity = 0, lsamples_recorded = 0;
   ~cem_replicas() {
+    cudaFree(d_lw);
+    cudaFree(d_trees);
+    cudaFree(d_lsamples);
     cudaFree(d_reps);
     cudaFree(d_stats);
     cudaFree(d_occ);
@@ -970,3 +980,304 @@ extern "C" int cem_delta_energy_noalloc(cem_replicas *r, int i, int n_events, in
     CUDA_OK(cudaStreamSynchronize(r->stream));
   });
 }
+
+// ---------------------------------------------------------------------------
+// Learned proposal: network objects and the sampler.
+struct cem_mlp {
+  float *d_master = nullptr, *d_grad = nullptr, *d_m = nullptr, *d_v = nullptr;
+  __nv_bfloat16 *d_params = nullptr;
+  double *d_loss = nullptr;
+  int step = 0;
+  cudaStream_t stream = nullptr;
+  ~cem_mlp() {
+    cudaFree(d_master);
+    cudaFree(d_grad);
+    cudaFree(d_m);
+    cudaFree(d_v);
+    cudaFree(d_params);
+    cudaFree(d_loss);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+extern "C" {
+
+int cem_mlp_info(int *n_inputs, int *n_hidden, int *n_params) {
+  return guard([&] {
+    if (n_inputs) *n_inputs = MLP_IN;
+    if (n_hidden) *n_hidden = MLP_H;
+    if (n_params) *n_params = MLP_NPARAM;
+  });
+}
+
+int cem_mlp_create(uint64_t seed, cem_mlp **out) {
+  return guard([&] {
+    require(out != nullptr, "null output");
+    *out = nullptr;
+    auto m = std::make_unique<cem_mlp>();
+    CUDA_OK(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+    CUDA_OK(cudaMalloc(&m->d_master, MLP_NPARAM * 4));
+    CUDA_OK(cudaMalloc(&m->d_grad, MLP_NPARAM * 4));
+    CUDA_OK(cudaMalloc(&m->d_m, MLP_NPARAM * 4));
+    CUDA_OK(cudaMalloc(&m->d_v, MLP_NPARAM * 4));
+    CUDA_OK(cudaMalloc(&m->d_params, MLP_NPARAM * 2));
+    CUDA_OK(cudaMalloc(&m->d_loss, 8));
+    CUDA_OK(cudaMemset(m->d_grad, 0, MLP_NPARAM * 4));
+    CUDA_OK(cudaMemset(m->d_m, 0, MLP_NPARAM * 4));
+    CUDA_OK(cudaMemset(m->d_v, 0, MLP_NPARAM * 4));
+    // He-style initialisation from a seeded stream (host side, once)
+    std::vector<float> h(MLP_NPARAM, 0.f);
+    uint64_t x = seed * 0x9E3779B97F4A7C15ull + 1ull;
+    auto gauss = [&]() {
+      double s = 0.0;  // sum of 12 uniforms - 6: approximately N(0, 1)
+      for (int k = 0; k < 12; ++k) {
+        x ^= x << 13;
+        x ^= x >> 7;
+        x ^= x << 17;
+        s += (double)(x >> 11) * (1.0 / 9007199254740992.0);
+      }
+      return (float)(s - 6.0);
+    };
+    for (int i = 0; i < MLP_IN * MLP_H; ++i) h[MLP_W1 + i] = gauss() * std::sqrt(2.f / MLP_IN);
+    for (int i = 0; i < MLP_H * MLP_H; ++i) h[MLP_W2 + i] = gauss() * std::sqrt(2.f / MLP_H);
+    for (int i = 0; i < MLP_H; ++i) h[MLP_W3 + i] = gauss() * std::sqrt(1.f / MLP_H);
+    CUDA_OK(cudaMemcpy(m->d_master, h.data(), MLP_NPARAM * 4, cudaMemcpyHostToDevice));
+    CUDA_OK(mlp_pack(m->d_master, m->d_params, m->stream));
+    CUDA_OK(cudaStreamSynchronize(m->stream));
+    *out = m.release();
+  });
+}
+
+int cem_mlp_destroy(cem_mlp *m) {
+  return guard([&] { delete m; });
+}
+
+int cem_mlp_get_params(cem_mlp *m, float *master) {
+  return guard([&] {
+    require(m && master, "null argument");
+    CUDA_OK(cudaMemcpy(master, m->d_master, MLP_NPARAM * 4, cudaMemcpyDeviceToHost));
+  });
+}
+
+int cem_mlp_set_params(cem_mlp *m, const float *master) {
+  return guard([&] {
+    require(m && master, "null argument");
+    for (int i = 0; i < MLP_NPARAM; ++i) require(std::isfinite(master[i]), "non-finite parameter");
+    CUDA_OK(cudaMemcpy(m->d_master, master, MLP_NPARAM * 4, cudaMemcpyHostToDevice));
+    CUDA_OK(mlp_pack(m->d_master, m->d_params, m->stream));
+    CUDA_OK(cudaStreamSynchronize(m->stream));
+  });
+}
+
+int cem_mlp_forward(cem_mlp *m, int64_t n, const int8_t *features, float *logits) {
+  return guard([&] {
+    require(m && features && logits && n >= 0, "bad argument");
+    if (n == 0) return;
+    int8_t *dx = nullptr;
+    float *dz = nullptr;
+    try {
+      CUDA_OK(cudaMalloc(&dx, (size_t)n * MLP_IN));
+      CUDA_OK(cudaMalloc(&dz, (size_t)n * 4));
+      CUDA_OK(cudaMemcpyAsync(dx, features, (size_t)n * MLP_IN, cudaMemcpyHostToDevice, m->stream));
+      CUDA_OK(mlp_forward(m->d_params, dx, n, dz, m->stream));
+      CUDA_OK(cudaMemcpyAsync(logits, dz, (size_t)n * 4, cudaMemcpyDeviceToHost, m->stream));
+      CUDA_OK(cudaStreamSynchronize(m->stream));
+    } catch (...) {
+      cudaFree(dx);
+      cudaFree(dz);
+      throw;
+    }
+    cudaFree(dx);
+    cudaFree(dz);
+  });
+}
+
+int cem_mlp_gradient(cem_mlp *m, int64_t n, const int8_t *features, const float *targets,
+                     float *grad, double *loss) {
+  return guard([&] {
+    require(m && features && targets && grad && n > 0, "bad argument");
+    int8_t *dx = nullptr;
+    float *dt = nullptr;
+    try {
+      CUDA_OK(cudaMalloc(&dx, (size_t)n * MLP_IN));
+      CUDA_OK(cudaMalloc(&dt, (size_t)n * 4));
+      CUDA_OK(cudaMemcpyAsync(dx, features, (size_t)n * MLP_IN, cudaMemcpyHostToDevice, m->stream));
+      CUDA_OK(cudaMemcpyAsync(dt, targets, (size_t)n * 4, cudaMemcpyHostToDevice, m->stream));
+      CUDA_OK(cudaMemsetAsync(m->d_grad, 0, MLP_NPARAM * 4, m->stream));
+      CUDA_OK(cudaMemsetAsync(m->d_loss, 0, 8, m->stream));
+      CUDA_OK(mlp_grad(m->d_params, dx, dt, nullptr, 0, n, m->d_grad, m->d_loss, m->stream));
+      CUDA_OK(cudaMemcpyAsync(grad, m->d_grad, MLP_NPARAM * 4, cudaMemcpyDeviceToHost, m->stream));
+      double l = 0.0;
+      CUDA_OK(cudaMemcpyAsync(&l, m->d_loss, 8, cudaMemcpyDeviceToHost, m->stream));
+      CUDA_OK(cudaMemsetAsync(m->d_grad, 0, MLP_NPARAM * 4, m->stream));
+      CUDA_OK(cudaStreamSynchronize(m->stream));
+      if (loss) *loss = l / (double)n;
+    } catch (...) {
+      cudaFree(dx);
+      cudaFree(dt);
+      throw;
+    }
+    cudaFree(dx);
+    cudaFree(dt);
+  });
+}
+
+int cem_mlp_train(cem_mlp *m, int64_t n, const int8_t *features, const float *targets,
+                  int epochs, int batch, float lr, uint64_t seed, double *loss_per_epoch) {
+  return guard([&] {
+    require(m && features && targets && n > 0 && epochs >= 1 && batch >= 1 && lr > 0.f,
+            "bad argument");
+    require(n < (1ll << 31), "too many training samples");
+    int8_t *dx = nullptr;
+    float *dt = nullptr;
+    int *dord = nullptr;
+    auto cleanup = [&] {
+      cudaFree(dx);
+      cudaFree(dt);
+      cudaFree(dord);
+    };
+    try {
+      CUDA_OK(cudaMalloc(&dx, (size_t)n * MLP_IN));
+      CUDA_OK(cudaMalloc(&dt, (size_t)n * 4));
+      CUDA_OK(cudaMalloc(&dord, (size_t)n * 4));
+      CUDA_OK(cudaMemcpyAsync(dx, features, (size_t)n * MLP_IN, cudaMemcpyHostToDevice, m->stream));
+      CUDA_OK(cudaMemcpyAsync(dt, targets, (size_t)n * 4, cudaMemcpyHostToDevice, m->stream));
+      std::vector<int> order((size_t)n);
+      for (int64_t i = 0; i < n; ++i) order[i] = (int)i;
+      std::mt19937_64 eng(seed);
+      for (int ep = 0; ep < epochs; ++ep) {
+        std::shuffle(order.begin(), order.end(), eng);
+        CUDA_OK(cudaMemcpyAsync(dord, order.data(), (size_t)n * 4, cudaMemcpyHostToDevice,
+                                m->stream));
+        CUDA_OK(cudaMemsetAsync(m->d_loss, 0, 8, m->stream));
+        for (int64_t b0 = 0; b0 < n; b0 += batch) {
+          const int64_t nb = std::min<int64_t>(batch, n - b0);
+          CUDA_OK(mlp_grad(m->d_params, dx, dt, dord, b0, nb, m->d_grad, m->d_loss, m->stream));
+          CUDA_OK(mlp_adam(m->d_master, m->d_params, m->d_grad, m->d_m, m->d_v, lr, ++m->step,
+                           m->stream));
+        }
+        double l = 0.0;
+        CUDA_OK(cudaMemcpyAsync(&l, m->d_loss, 8, cudaMemcpyDeviceToHost, m->stream));
+        CUDA_OK(cudaStreamSynchronize(m->stream));
+        if (loss_per_epoch) loss_per_epoch[ep] = l / (double)n;
+      }
+    } catch (...) {
+      cleanup();
+      throw;
+    }
+    cleanup();
+  });
+}
+
+static void require_learned(const cem_replicas *r) {
+  require(r->sys->fcc_generated && r->ensemble == CEM_CANONICAL,
+          "the learned proposal supports canonical binary FCC systems of the generated topology",
+          CEM_ERR_UNSUPPORTED);
+  for (const Replica &R : r->reps)
+    require(R.L[0] == R.L[1] && R.L[1] == R.L[2] && R.L[0] == r->reps[0].L[0] &&
+                (R.L[0] + 4 == 14 || R.L[0] + 4 == 28 || R.L[0] + 4 == 36 || R.L[0] + 4 == 52),
+            "the learned proposal needs equal cubic supercells of 10, 24, 32 or 48 cells",
+            CEM_ERR_UNSUPPORTED);
+}
+
+int cem_learned_features(cem_replicas *r, int i, int8_t *features, float *targets) {
+  return guard([&] {
+    check_rep(r, i);
+    require(features && targets, "null argument");
+    require_learned(r);
+    const Replica &R = r->reps[i];
+    const int n = R.n_sites;
+    int8_t *dx = nullptr;
+    float *dt = nullptr;
+    double *dw = nullptr;
+    int *dof = nullptr;
+    auto cleanup = [&] {
+      cudaFree(dx);
+      cudaFree(dt);
+      cudaFree(dw);
+      cudaFree(dof);
+    };
+    try {
+      CUDA_OK(cudaMalloc(&dx, (size_t)n * MLP_IN));
+      CUDA_OK(cudaMalloc(&dt, (size_t)n * 4));
+      CUDA_OK(cudaMalloc(&dw, 8 * r->sys->w.size()));
+      CUDA_OK(cudaMalloc(&dof, 4 * MAX_ORBITS));
+      CUDA_OK(cudaMemcpyAsync(dw, r->sys->w.data(), 8 * r->sys->w.size(), cudaMemcpyHostToDevice,
+                              r->stream));
+      CUDA_OK(cudaMemcpyAsync(dof, r->sys->T.orb_func_base, 4 * MAX_ORBITS, cudaMemcpyHostToDevice,
+                              r->stream));
+      CUDA_OK(learned_features(r->d_occ + R.occ_offset, R.L[0], dw, dof, R.beta, dx, dt, r->stream));
+      CUDA_OK(cudaMemcpyAsync(features, dx, (size_t)n * MLP_IN, cudaMemcpyDeviceToHost, r->stream));
+      CUDA_OK(cudaMemcpyAsync(targets, dt, (size_t)n * 4, cudaMemcpyDeviceToHost, r->stream));
+      CUDA_OK(cudaStreamSynchronize(r->stream));
+    } catch (...) {
+      cleanup();
+      throw;
+    }
+    cleanup();
+  });
+}
+
+int cem_learned_run(cem_replicas *r, const cem_mlp *m, int64_t n_passes, int64_t n_equil,
+                    int record_samples) {
+  return guard([&] {
+    require(r != nullptr, "null handle");
+    require(n_passes >= 0 && n_equil >= 0, "pass counts must be >= 0");
+    require_learned(r);
+    const int L = r->reps[0].L[0], n = r->reps[0].n_sites;
+    const int pitch = L + 4;
+    int dev = 0, maxsm = 0;
+    CUDA_OK(cudaGetDevice(&dev));
+    CUDA_OK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    require(learned_smem_bytes(L, pitch) <= maxsm, "supercell does not fit in shared memory",
+            CEM_ERR_UNSUPPORTED);
+    r->upload_reps();
+    const long long tsize = learned_tree_size(n);
+    if (!r->d_lw) {
+      CUDA_OK(cudaMalloc(&r->d_lw, sizeof(long long) * (size_t)n * r->n));
+      CUDA_OK(cudaMalloc(&r->d_trees, sizeof(unsigned long long) * (size_t)tsize * 2 * r->n));
+    }
+    double *samples = nullptr;
+    long long cap = 0;
+    if (record_samples) {
+      cap = std::max<long long>(1, n_passes - n_equil);
+      if (cap > r->lsample_capacity) {
+        cudaFree(r->d_lsamples);
+        r->d_lsamples = nullptr;
+        CUDA_OK(cudaMalloc(&r->d_lsamples, sizeof(double) * 3 * cap * r->n));
+        r->lsample_capacity = cap;
+      }
+      samples = r->d_lsamples;
+      cap = r->lsample_capacity;
+      r->lsamples_recorded = std::max<long long>(0, n_passes - n_equil);
+    }
+    CUDA_OK(cudaEventRecord(r->ev0, r->stream));
+    CUDA_OK(learned_run(r->sys->T, r->d_reps, r->d_stats, r->d_occ, m ? m->d_params : nullptr,
+                        m ? 1 : 0, r->d_lw, n, r->d_trees, tsize, n, r->n, L, n_passes, n_equil,
+                        samples, cap, pitch, r->stream));
+    CUDA_OK(cudaEventRecord(r->ev1, r->stream));
+    r->stats_valid = false;  // the sweep recomputes its own state next time
+  });
+}
+
+int cem_learned_samples(cem_replicas *r, int i, double *energy, double *order, int64_t capacity,
+                        int64_t *n_samples) {
+  return guard([&] {
+    check_rep(r, i);
+    require(r->d_lsamples != nullptr, "no learned-proposal samples were recorded");
+    const int64_t nrec = std::min<int64_t>(r->lsamples_recorded, r->lsample_capacity);
+    const int64_t mm = std::min<int64_t>(nrec, capacity);
+    std::vector<double> buf((size_t)mm * 3);
+    if (mm > 0)
+      CUDA_OK(cudaMemcpyAsync(buf.data(), r->d_lsamples + (size_t)i * r->lsample_capacity * 3,
+                              sizeof(double) * buf.size(), cudaMemcpyDeviceToHost, r->stream));
+    CUDA_OK(cudaStreamSynchronize(r->stream));
+    for (int64_t s = 0; s < mm; ++s) {
+      if (energy) energy[s] = buf[s * 3];
+      if (order) order[s] = buf[s * 3 + 2];
+    }
+    if (n_samples) *n_samples = mm;
+  });
+}
+
+}  // extern "C"

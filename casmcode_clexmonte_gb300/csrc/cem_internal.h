@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <cuda_bf16.h>
+
 #include "cem_common.cuh"
 
 namespace cem {
@@ -58,5 +60,25 @@ cudaError_t launch_sweep(const CeTables &T, const SweepParams &P, int n_replicas
                          int pitch, cudaStream_t st);
 // true if the system is the binary FCC topology of the generated evaluator
 bool matches_generated_fcc(const CeTables &T, const int *pb, const int *du);
+
+// learned proposal (cem_learned.cu)
+struct TreeGeo;
+cudaError_t mlp_forward(const __nv_bfloat16 *params, const int8_t *X, long long n, float *z,
+                        cudaStream_t st);
+cudaError_t mlp_grad(const __nv_bfloat16 *params, const int8_t *X, const float *t,
+                     const int *order, long long b0, long long n, float *grad, double *loss,
+                     cudaStream_t st);
+cudaError_t mlp_adam(float *master, __nv_bfloat16 *params, float *grad, float *m, float *v,
+                     float lr, int step, cudaStream_t st);
+cudaError_t mlp_pack(const float *master, __nv_bfloat16 *params, cudaStream_t st);
+cudaError_t learned_features(const int8_t *occ, int L, const double *w, const int *orb_func,
+                             double beta, int8_t *X, float *t, cudaStream_t st);
+int learned_tree_size(int n_sites);
+int learned_smem_bytes(int L, int pitch);
+cudaError_t learned_run(const CeTables &T, const Replica *reps, ReplicaStats *stats,
+                        int8_t *occ, const __nv_bfloat16 *params, int use_mlp, long long *weights,
+                        long long w_stride, unsigned long long *trees, long long tree_stride,
+                        int n_sites, int n_replicas, int L, long long n_passes, long long n_equil,
+                        double *samples, long long capacity, int pitch, cudaStream_t st);
 
 }  // namespace cem

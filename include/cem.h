@@ -207,6 +207,45 @@ int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_sampl
 int cem_set_option(cem_replicas *r, const char *key, int64_t value);
 int cem_get_option(cem_replicas *r, const char *key, int64_t *value);
 
+/* ---- Learned proposal (canonical swaps, binary FCC of the generated topology).
+ * A network scores each site's environment (its 42 neighbours in the first three
+ * shells, then its own occupant: 43 inputs) -> 64 -> 64 -> 1 logit z, with bf16
+ * parameters and fp32 accumulation. Site weight w = max(1, round(4096 exp(z)))
+ * with z clamped to [-12, 8]. A swap draws one A site and one B site with
+ * probability proportional to w from per-species int64 sum trees; acceptance
+ * min(1, exp(-beta dE) q_rev / q_fwd) with the exact proposal probabilities,
+ * so the canonical distribution is sampled whatever the network predicts.
+ * Parameter vector (fp32 masters): W1[43][64] (input-major), b1[64],
+ * W2[64][64] (input-major), b2[64], w3[64], b3. No counterpart in the
+ * reference (its canonical proposal is uniform, CanonicalCalculator.cc:78-83). */
+typedef struct cem_mlp cem_mlp;
+int cem_mlp_info(int *n_inputs, int *n_hidden, int *n_params);
+int cem_mlp_create(uint64_t seed, cem_mlp **out);
+int cem_mlp_destroy(cem_mlp *m);
+int cem_mlp_get_params(cem_mlp *m, float *master);
+int cem_mlp_set_params(cem_mlp *m, const float *master);
+/* logits of n environments (n x 43 int8 occupants) */
+int cem_mlp_forward(cem_mlp *m, int64_t n, const int8_t *features, float *logits);
+/* gradient of the mean-squared error 1/(2n) sum (z - t)^2 at the current
+ * (bf16) parameters, and the loss */
+int cem_mlp_gradient(cem_mlp *m, int64_t n, const int8_t *features, const float *targets,
+                     float *grad, double *loss);
+/* Adam (Kingma & Ba 2015) on the same loss, minibatches in a seeded order */
+int cem_mlp_train(cem_mlp *m, int64_t n, const int8_t *features, const float *targets,
+                  int epochs, int batch, float lr, uint64_t seed, double *loss_per_epoch);
+/* Environments of every site of a replica and the training target
+ * t = clamp(-beta dE_flip / 2, -12, 8) (half the log Metropolis weight of
+ * flipping the site), from the device occupation. */
+int cem_learned_features(cem_replicas *r, int replica, int8_t *features, float *targets);
+/* n_passes x n_sites proposals per replica with the learned proposal
+ * (m == NULL: every weight 1, i.e. the uniform global swap proposal).
+ * Samples per pass: energy per unit cell and the L1_2 order parameter
+ * sqrt(sum_k (x_k - x)^2) over the four simple-cubic sublattices. */
+int cem_learned_run(cem_replicas *r, const cem_mlp *m, int64_t n_passes, int64_t n_equil,
+                    int record_samples);
+int cem_learned_samples(cem_replicas *r, int replica, double *energy, double *order,
+                        int64_t capacity, int64_t *n_samples);
+
 /* Statistics and samples of one replica (after cem_run). */
 int cem_get_stats(cem_replicas *r, int replica, cem_stats *out);
 int cem_get_samples(cem_replicas *r, int replica, double *potential, double *comp,
