@@ -350,6 +350,165 @@ def run_gb300(args):
     return 0
 
 
+def _plain_batch(cm, w, rank=0):
+    sysd = cm.System(w.ce)
+    batch = cm.ReplicaBatch(sysd, w.ensemble, w.L)
+    for i in range(w.n_replicas):
+        mu = w.param_chem_pot[i] if w.ensemble == "semigrand_canonical" else None
+        batch.set_conditions(i, float(w.temperature[i]), mu)
+        batch.set_seed(i, int(w.seeds[i]) + 7919 * rank)
+    batch.set_occupation_all(np.concatenate(w.occupation).astype(np.int8))
+    return sysd, batch
+
+
+def run_other_workload(args):
+    """Throughput line of configurations 0, 2 and 4 (plain parallel sampler)."""
+    import torch
+
+    from casmcode_clexmonte_gb300 import build as B
+
+    B.build()
+    from casmcode_clexmonte_gb300 import calculator as cm
+    from casmcode_clexmonte_gb300 import workloads
+
+    w = workloads.config(args.workload)
+    notes = {}
+    if args.workload == 4:
+        # the 96^3 replicas need the HBM-streamed sweep; this line covers the
+        # 512 shared-memory-resident 32^3 replicas
+        keep = [i for i, l in enumerate(w.L) if l[0] == 32]
+        w.L = [w.L[i] for i in keep]
+        w.temperature = w.temperature[keep]
+        w.param_chem_pot = w.param_chem_pot[keep]
+        w.x_b = w.x_b[keep]
+        w.occupation = [w.occupation[i] for i in keep]
+        w.seeds = w.seeds[keep]
+        notes["subset"] = "512 x 32^3 replicas (the 96^3 replicas are not included)"
+    sysd, batch = _plain_batch(cm, w)
+    batch.run(args.warmup, 0)
+    batch.synchronize()
+    before = sum(batch.stats(i)["n_proposed"] for i in range(w.n_replicas))
+    torch.cuda.synchronize()
+    batch.run(args.steps, 0)
+    batch.synchronize()
+    ms = batch.kernel_ms()
+    after = sum(batch.stats(i)["n_proposed"] for i in range(w.n_replicas))
+    line = {
+        "metric": "proposals/s", "value": (after - before) / (ms / 1e3), "unit": "proposals/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": w.name, "replicas": w.n_replicas,
+                   "sites": [int(x) for x in sorted(set(w.n_sites))][:4],
+                   "ensemble": w.ensemble, "pitch": batch.get_option("pitch"),
+                   "smem_bytes": batch.get_option("smem_bytes"),
+                   "colour_classes": batch.get_option("colour_classes"), **notes},
+        "gpu_launches": 1,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_learned_comparison(args):
+    """Configuration 3: T_c from a temperature scan of the plain sampler, then
+    plain vs learned-proposal effective independent samples per second of the
+    energy and the L1_2 order parameter at T = 0.9 T_c (48^3, x_B = 0.25)."""
+    from casmcode_clexmonte_gb300 import build as B
+
+    B.build()
+    from casmcode_clexmonte_gb300 import calculator as cm
+    from casmcode_clexmonte_gb300 import workloads
+    from casmcode_clexmonte_gb300.stats import tau_int
+
+    w = workloads.config(3)
+    ce = w.ce
+    sysd = cm.System(ce)
+    # 1. temperature scan (24^3, plain sampler): heat capacity peak
+    temps = np.linspace(20.0, 320.0, 31)
+    scan = cm.ReplicaBatch(sysd, "canonical", [(24, 24, 24)] * len(temps))
+    rng = np.random.default_rng(3)
+    for i, t in enumerate(temps):
+        scan.set_conditions(i, float(t))
+        scan.set_seed(i, 300 + i)
+        scan.set_occupation(i, workloads.fixed_composition(rng, 24 ** 3, 0.25))
+    scan.run(6000, 3000)
+    cv = np.array([scan.stats(i)["var_potential"] * 24 ** 3 / (8.617333262e-5 * t * t)
+                   for i, t in enumerate(temps)])
+    inner = slice(1, len(temps) - 1)  # a maximum at the scan's edge is no transition
+    tc = float(temps[inner][int(np.argmax(cv[inner]))])
+    T = 0.9 * tc
+    # 2. plain sampler, 32 x 48^3
+    n_rep = w.n_replicas
+    plain = cm.ReplicaBatch(sysd, "canonical", w.L)
+    for i in range(n_rep):
+        plain.set_conditions(i, T)
+        plain.set_seed(i, 1000 + i)
+        plain.set_occupation(i, w.occupation[i])
+    plain.run(args.warmup * 50, 0)
+    plain.run(args.steps, 0, record_samples=True)
+    plain.synchronize()
+    t_plain = plain.kernel_ms() / 1e3
+    prop_plain = sum(plain.stats(i)["n_proposed"] for i in range(n_rep))
+    neff_e = neff_op = 0.0
+    taus_p = []
+    for i in range(n_rep):
+        e, _ = plain.samples(i, args.steps)
+        op = plain.order_samples(i, args.steps)
+        te, to = tau_int(e), tau_int(op)
+        taus_p.append((te, to))
+        neff_e += e.size / (2 * te)
+        neff_op += op.size / (2 * to)
+    mean_e_plain = float(np.mean([plain.stats(i)["mean_potential"] for i in range(n_rep)]))
+    # 3. train the proposal network on plain-sampler snapshots (1e6 environments)
+    X, t = [], []
+    for i in range(n_rep):
+        x_i, t_i = plain.learned_features(i)
+        X.append(x_i)
+        t.append(t_i)
+    X = np.concatenate(X)[:1_000_000]
+    t = np.concatenate(t)[:1_000_000]
+    net = cm.LearnedProposal(seed=11)
+    t0 = time.perf_counter()
+    losses = net.train(X, t, epochs=4, batch=4096, lr=2e-3, seed=5)
+    train_s = time.perf_counter() - t0
+    # 4. learned-proposal sampler from the equilibrated plain states
+    lp = args.learned_passes
+    plain.learned_run(net, lp, lp // 5, record_samples=True)
+    plain.synchronize()
+    t_learned = plain.kernel_ms() / 1e3
+    neff_e_l = neff_op_l = 0.0
+    taus_l = []
+    acc_l = []
+    for i in range(n_rep):
+        e, op = plain.learned_samples(i, lp)
+        te, to = tau_int(e), tau_int(op)
+        taus_l.append((te, to))
+        neff_e_l += e.size / (2 * te)
+        neff_op_l += op.size / (2 * to)
+    mean_e_learned = float(np.mean([plain.learned_samples(i, lp)[0].mean() for i in range(n_rep)]))
+    line = {
+        "metric": "effective samples/s (learned vs plain GPU Metropolis, same <E>)",
+        "workload": w.name, "T_c_scan_K": tc, "temperature_K": T,
+        "heat_capacity_scan": {"T_K": [float(x) for x in temps], "C_per_uc": [float(x) for x in cv]},
+        "plain": {"passes": args.steps, "seconds": t_plain, "proposals_per_s": prop_plain / t_plain,
+                  "tau_int_E_median": float(np.median([a for a, _ in taus_p])),
+                  "tau_int_order_median": float(np.median([b for _, b in taus_p])),
+                  "eff_samples_per_s_E": neff_e / t_plain,
+                  "eff_samples_per_s_order": neff_op / t_plain, "mean_E": mean_e_plain},
+        "learned": {"passes": lp, "seconds": t_learned,
+                    "proposals_per_s": n_rep * lp * int(w.n_sites[0]) / t_learned,
+                    "tau_int_E_median": float(np.median([a for a, _ in taus_l])),
+                    "tau_int_order_median": float(np.median([b for _, b in taus_l])),
+                    "eff_samples_per_s_E": neff_e_l / t_learned,
+                    "eff_samples_per_s_order": neff_op_l / t_learned, "mean_E": mean_e_learned,
+                    "train_seconds": train_s, "train_loss": [float(x) for x in losses]},
+        "ratio_learned_over_plain_E": (neff_e_l / t_learned) / (neff_e / t_plain),
+        "ratio_learned_over_plain_order": (neff_op_l / t_learned) / (neff_op / t_plain),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -357,11 +516,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", type=int, default=WORKLOAD_INDEX, choices=[0, 1, 2, 3, 4])
+    ap.add_argument("--learned-passes", type=int, default=40)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == 3:
+        return run_learned_comparison(args)
+    if args.workload != WORKLOAD_INDEX:
+        return run_other_workload(args)
     return run_gb300(args)
 
 

@@ -57,7 +57,7 @@ EXPORTS = [
     "cem_set_option", "cem_get_option", "cem_delta_energy_noalloc",
     "cem_mlp_info", "cem_mlp_create", "cem_mlp_destroy", "cem_mlp_get_params",
     "cem_mlp_set_params", "cem_mlp_forward", "cem_mlp_gradient", "cem_mlp_train",
-    "cem_learned_features", "cem_learned_run", "cem_learned_samples",
+    "cem_learned_features", "cem_learned_run", "cem_learned_samples", "cem_get_order_samples",
 ]
 
 _lib = None
@@ -103,6 +103,7 @@ def load(path: str = LIB):
     L.cem_smem_bandwidth.argtypes = [_dp]
     L.cem_set_option.argtypes = [P, C.c_char_p, C.c_int64]
     L.cem_mlp_info.argtypes = [_ip, _ip, _ip]
+    L.cem_get_order_samples.argtypes = [P, C.c_int, vp, C.c_int64, C.POINTER(C.c_int64)]
     L.cem_mlp_create.argtypes = [C.c_uint64, C.POINTER(P)]
     L.cem_mlp_destroy.argtypes = [P]
     L.cem_mlp_get_params.argtypes = [P, vp]

@@ -157,6 +157,12 @@ class ReplicaBatch:
     def synchronize(self):
         check(self.lib.cem_synchronize(self.handle))
 
+    def order_samples(self, i: int, capacity: int) -> np.ndarray:
+        op = np.zeros(capacity)
+        n = C.c_int64()
+        check(self.lib.cem_get_order_samples(self.handle, i, ptr(op), int(capacity), C.byref(n)))
+        return op[: n.value]
+
     # ---- learned proposal
     def learned_features(self, i: int):
         n = int(self.n_sites[i])

@@ -461,7 +461,7 @@ int cem_replicas_create(const cem_system *sys, int n, const int *L, int ensemble
     CUDA_OK(cudaMemset(r->d_occ, 0, (size_t)off + 16));
     CUDA_OK(cudaMalloc(&r->d_counts, sizeof(unsigned long long) * (MAX_FUNCS + 8)));
     CUDA_OK(cudaMalloc(&r->d_result, sizeof(long long) * 4));
-    r->sample_width = sys->T.n_occ;  // potential + (n_occ-1) compositions
+    r->sample_width = sys->T.n_occ + 1;  // potential, (n_occ-1) compositions, order parameter
     *out = r.release();
   });
 }
@@ -865,6 +865,24 @@ int cem_get_option(cem_replicas *r, const char *key, int64_t *value) {
     else if (k == "smem_bytes") *value = r->sweep_smem;
     else if (k == "colour_classes") *value = r->max_classes;
     else throw Err(CEM_ERR_INVALID, "unknown option '" + k + "'");
+  });
+}
+
+int cem_get_order_samples(cem_replicas *r, int i, double *order, int64_t capacity,
+                          int64_t *n_samples) {
+  return guard([&] {
+    check_rep(r, i);
+    require(r->d_samples != nullptr, "no samples were recorded");
+    const int64_t n = std::min<int64_t>(r->n_samples_recorded, r->sample_capacity);
+    const int64_t m = std::min<int64_t>(n, capacity);
+    std::vector<double> buf((size_t)m * r->sample_width);
+    if (m > 0)
+      CUDA_OK(cudaMemcpyAsync(buf.data(),
+                              r->d_samples + (size_t)i * r->sample_capacity * r->sample_width,
+                              sizeof(double) * buf.size(), cudaMemcpyDeviceToHost, r->stream));
+    CUDA_OK(cudaStreamSynchronize(r->stream));
+    for (int64_t s = 0; s < m; ++s) order[s] = buf[s * r->sample_width + r->sys->T.n_occ];
+    if (n_samples) *n_samples = m;
   });
 }
 

@@ -86,6 +86,7 @@ struct ReplicaStats {
   double sum_x[3], sum_xx[9], sum_ex[3];
   double sum_f;           // formation energy per unit cell
   int64_t n_species[8];   // current species counts
+  int64_t n_sub[4];       // binary FCC: occupant-1 counts on the 4 simple-cubic sublattices
   int64_t n_proposed, n_accepted;
   int64_t pass;
   int status;             // nonzero: device-side error code

@@ -598,6 +598,12 @@ __device__ __forceinline__ bool accept_fast(const FF &d, float beta_f, float u) 
   return u < cem_expf_neg(FMUL(-beta_f, de));
 }
 
+// One of the four simple-cubic sublattices of FCC (L1_2 order parameter), for
+// a site in primitive-cell coordinates.
+__device__ __forceinline__ int sc_sublattice(int x, int y, int z) {
+  return ((y + z) & 1) | (((x + z) & 1) << 1);
+}
+
 // Site evaluation policy: PITCH > 0 uses the generated binary FCC evaluator
 // (compile-time neighbour offsets); PITCH == 0 walks the run-time tables.
 template <int NOCC, int PITCH>
@@ -751,7 +757,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
       // occupant 1 of its flower count / size_g
       long long cnt[MAX_ORBITS];
       for (int g = 0; g < MAX_ORBITS; ++g) cnt[g] = 0;
-      long long n1 = 0;
+      long long n1 = 0, sub[4] = {0, 0, 0, 0};
       for (int l = tid; l < n_sites; l += nth) {
         const int b = l / n_uc, uc = l - b * n_uc;
         const int x = uc % G.L0, y = (uc / G.L0) % G.L1, z = uc / (G.L0 * G.L1);
@@ -759,6 +765,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
         const int o = occ[ad];
         if (o == 0) continue;
         ++n1;
+        sub[sc_sublattice(x, y, z)]++;
         Acc<2> acc;
         acc.zero();
         ev.add(b, 0, 1, occ, ad, acc);
@@ -768,16 +775,18 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
       for (int off = 16; off; off >>= 1) {
         n1 += __shfl_xor_sync(0xffffffffu, n1, off);
         for (int g = 0; g < MAX_ORBITS; ++g) cnt[g] += __shfl_xor_sync(0xffffffffu, cnt[g], off);
+        for (int k = 0; k < 4; ++k) sub[k] += __shfl_xor_sync(0xffffffffu, sub[k], off);
       }
       if (lane == 0) {
         for (int g = 0; g < MAX_ORBITS; ++g) rd_l[warp * 16 + g] = cnt[g];
         rd_l[warp * 16 + 8] = n1;
+        for (int k = 0; k < 4; ++k) rd_l[warp * 16 + 9 + k] = sub[k];
       }
       __syncthreads();
       if (tid == 0) {
-        long long tot[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        long long tot[13] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         for (int w = 0; w < nwarp; ++w)
-          for (int k = 0; k < 9; ++k) tot[k] += rd_l[w * 16 + k];
+          for (int k = 0; k < 13; ++k) tot[k] += rd_l[w * 16 + k];
         double e = T.w[0] * n_uc;
         for (int g = 0; g < T.n_orbits; ++g)
           e += T.w[T.orb_func_base[g]] * (double)(tot[g] / T.orb_size[g]);
@@ -787,6 +796,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
         S.energy = e;
         S.n_species[0] = n_sites - tot[8];
         S.n_species[1] = tot[8];
+        for (int k = 0; k < 4; ++k) S.n_sub[k] = tot[9 + k];
         S.pass = pass;
         S.n_proposed = np;
         S.n_accepted = na;
@@ -795,8 +805,9 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
     }
   }
   double energy = S.energy;
-  long long nspec[8];
+  long long nspec[8], nsub[4];
   for (int a = 0; a < 8; ++a) nspec[a] = S.n_species[a];
+  for (int k = 0; k < 4; ++k) nsub[k] = S.n_sub[k];
   long long pass_global = S.pass;
   const uint32_t k0 = (uint32_t)R.seed, k1 = (uint32_t)(R.seed >> 32);
   const int n_pair_sw = P.n_pair_sweeps, n_local_sw = P.n_local_sweeps;
@@ -860,6 +871,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
     EnergyAcc<NOCC> eacc;
     int dspec[NOCC];
     for (int a = 0; a < NOCC; ++a) dspec[a] = 0;
+    int dsub[4] = {0, 0, 0, 0};  // binary FCC only (PITCH > 0)
     int n_prop = 0, n_acc = 0;
 
     for (int sub = 0; sub < n_sub; ++sub) {
@@ -902,6 +914,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
             eacc.add(acc, d, R.dmu[o_i * NOCC + o_f]);
             dspec[o_i]--;
             dspec[o_f]++;
+            if constexpr (PITCH > 0) dsub[sc_sublattice(x, y, z)] += o_f - o_i;
           }
         }
       } else if (sw < n_pair_sw) {
@@ -980,6 +993,10 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
               ++n_acc;
               put_site(occ, G, nb_b, xb, yb, zb, (int8_t)oa);
               eacc.add(acc, d, 0.0);
+              if constexpr (PITCH > 0) {
+                dsub[sc_sublattice(xa, ya, za)] += ob - oa;
+                dsub[sc_sublattice(xb, yb, zb)] += oa - ob;
+              }
             } else {
               put_site(occ, G, cb, xa, ya, za, (int8_t)oa);
             }
@@ -997,6 +1014,8 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
       vals[0] = n_prop;
       vals[1] = n_acc;
       for (int a = 0; a < NOCC; ++a) vals[2 + a] = dspec[a];
+      if constexpr (PITCH > 0)
+        for (int k = 0; k < 4; ++k) vals[4 + k] = dsub[k];
       double dsum = 0.0;
       if constexpr (NOCC == 2) {
         for (int g = 0; g < MAX_ORBITS; ++g) vals[8 + g] = eacc.dc[g];
@@ -1034,6 +1053,16 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
         S.n_proposed += tot[0];
         S.n_accepted += tot[1];
         for (int a = 0; a < NOCC; ++a) nspec[a] += tot[2 + a];
+        double op = 0.0;
+        if constexpr (PITCH > 0) {
+          for (int k = 0; k < 4; ++k) nsub[k] += tot[4 + k];
+          const double xb = (double)nspec[1] / n_sites;
+          for (int k = 0; k < 4; ++k) {
+            const double c = (double)nsub[k] / (0.25 * n_sites) - xb;
+            op += c * c;
+          }
+          op = sqrt(op);
+        }
         // param composition per unit cell and potential per unit cell
         double x[3] = {0.0, 0.0, 0.0}, mux = 0.0;
         for (int k = 0; k < NOCC - 1; ++k) {
@@ -1062,6 +1091,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
                             si * P.sample_width;
               out[0] = ep;
               for (int k = 0; k < NOCC - 1; ++k) out[1 + k] = x[k];
+              out[NOCC] = op;
             }
           }
         }
@@ -1078,6 +1108,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
   if (tid == 0) {
     S.energy = energy;
     for (int a = 0; a < NOCC; ++a) S.n_species[a] = nspec[a];
+    for (int k = 0; k < 4; ++k) S.n_sub[k] = nsub[k];
     S.pass = pass_global;
   }
 }

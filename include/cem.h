@@ -251,6 +251,11 @@ int cem_get_stats(cem_replicas *r, int replica, cem_stats *out);
 int cem_get_samples(cem_replicas *r, int replica, double *potential, double *comp,
                     int64_t capacity, int64_t *n_samples);
 int cem_reset_stats(cem_replicas *r);
+/* Per-pass L1_2 order parameter sqrt(sum_k (x_k - x)^2) over the four
+ * simple-cubic sublattices (binary FCC with the generated evaluator; 0
+ * otherwise), from the last cem_run with record_samples. */
+int cem_get_order_samples(cem_replicas *r, int replica, double *order, int64_t capacity,
+                          int64_t *n_samples);
 
 /* Measured shared-memory read bandwidth of the device, GB/s (all SMs,
  * 16-byte vector loads); the roofline denominator of the shared-memory

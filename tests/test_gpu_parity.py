@@ -233,3 +233,25 @@ def test_generated_evaluator_matches_runtime_tables(ens, L, cm):
         np.testing.assert_array_equal(oa, ob)
         assert sa["n_accepted"] == sb["n_accepted"] and sa["n_proposed"] == sb["n_proposed"]
         assert abs(sa["energy"] - sb["energy"]) <= 1e-9 * abs(sb["energy"]) + 1e-9
+
+
+def test_order_parameter_samples_match_final_state(cm):
+    """The per-pass L1_2 order parameter of the plain sweep equals the one
+    recomputed from the final occupation."""
+    ce = workloads.fcc_binary_ce(3, nn1=0.08)
+    sysd = cm.System(ce)
+    L = (24, 24, 24)
+    b = cm.ReplicaBatch(sysd, "canonical", [L])
+    rng = np.random.default_rng(8)
+    b.set_conditions(0, 250.0)
+    b.set_seed(0, 3)
+    b.set_occupation(0, workloads.fixed_composition(rng, 24 ** 3, 0.25))
+    b.run(30, 0, record_samples=True)
+    op = b.order_samples(0, 30)
+    assert op.size == 30
+    occ = b.get_occupation(0).reshape(24, 24, 24)  # [z][y][x]
+    z, y, x = np.meshgrid(np.arange(24), np.arange(24), np.arange(24), indexing="ij")
+    lab = ((y + z) & 1) | (((x + z) & 1) << 1)
+    xb = occ.mean()
+    c = np.array([occ[lab == k].mean() for k in range(4)])
+    assert abs(op[-1] - np.sqrt(((c - xb) ** 2).sum())) < 1e-12
