@@ -373,37 +373,56 @@ def run_other_workload(args):
 
     w = workloads.config(args.workload)
     notes = {}
+    groups = [w]
     if args.workload == 4:
-        # the 96^3 replicas need the HBM-streamed sweep; this line covers the
-        # 512 shared-memory-resident 32^3 replicas
-        keep = [i for i, l in enumerate(w.L) if l[0] == 32]
-        w.L = [w.L[i] for i in keep]
-        w.temperature = w.temperature[keep]
-        w.param_chem_pot = w.param_chem_pot[keep]
-        w.x_b = w.x_b[keep]
-        w.occupation = [w.occupation[i] for i in keep]
-        w.seeds = w.seeds[keep]
-        notes["subset"] = "512 x 32^3 replicas (the 96^3 replicas are not included)"
-    sysd, batch = _plain_batch(cm, w)
-    batch.run(args.warmup, 0)
-    batch.synchronize()
-    before = sum(batch.stats(i)["n_proposed"] for i in range(w.n_replicas))
+        # two batches on their own streams, run concurrently: 512 x 32^3 in
+        # shared memory and 4 x 96^3 HBM-streamed (one kernel per sub-step)
+        def subset(keep):
+            import copy
+
+            v = copy.copy(w)
+            v.L = [w.L[i] for i in keep]
+            v.temperature = w.temperature[keep]
+            v.param_chem_pot = w.param_chem_pot[keep]
+            v.x_b = w.x_b[keep]
+            v.occupation = [w.occupation[i] for i in keep]
+            v.seeds = w.seeds[keep]
+            return v
+
+        groups = [subset([i for i, l in enumerate(w.L) if l[0] == 32]),
+                  subset([i for i, l in enumerate(w.L) if l[0] == 96])]
+    batches = [_plain_batch(cm, g)[1] for g in groups]
+    for b in batches:
+        b.run(args.warmup, 0)
+    for b in batches:
+        b.synchronize()
+    before = [sum(b.stats(i)["n_proposed"] for i in range(b.n)) for b in batches]
     torch.cuda.synchronize()
-    batch.run(args.steps, 0)
-    batch.synchronize()
-    ms = batch.kernel_ms()
-    after = sum(batch.stats(i)["n_proposed"] for i in range(w.n_replicas))
+    t0 = time.perf_counter()
+    for b in batches:
+        b.run(args.steps, 0)
+    for b in batches:
+        b.synchronize()
+    wall = time.perf_counter() - t0
+    ms = [b.kernel_ms() for b in batches]
+    after = [sum(b.stats(i)["n_proposed"] for i in range(b.n)) for b in batches]
+    props = [a - bb for a, bb in zip(after, before)]
+    parts = []
+    for g, b, p_, m in zip(groups, batches, props, ms):
+        parts.append({"replicas": b.n, "sites": int(g.n_sites[0]), "streamed": b.get_option("streamed"),
+                      "pitch": b.get_option("pitch"), "device_ms": m,
+                      "proposals_per_s": p_ / (m / 1e3)})
+    value = sum(props) / (max(ms) / 1e3) if len(batches) > 1 else props[0] / (ms[0] / 1e3)
     line = {
-        "metric": "proposals/s", "value": (after - before) / (ms / 1e3), "unit": "proposals/s",
+        "metric": "proposals/s", "value": value, "unit": "proposals/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": max(ms) / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": w.name, "replicas": w.n_replicas,
                    "sites": [int(x) for x in sorted(set(w.n_sites))][:4],
-                   "ensemble": w.ensemble, "pitch": batch.get_option("pitch"),
-                   "smem_bytes": batch.get_option("smem_bytes"),
-                   "colour_classes": batch.get_option("colour_classes"), **notes},
-        "gpu_launches": 1,
+                   "ensemble": w.ensemble, "batches": parts, "wall_s_all_batches": wall,
+                   "colour_classes": batches[0].get_option("colour_classes"), **notes},
+        "gpu_launches": "1 per shared-memory batch; 25 per pass for a streamed batch (CUDA graph)",
     }
     print(json.dumps(line), flush=True)
     return 0

@@ -118,12 +118,21 @@ struct cem_replicas {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;
+  // HBM-streamed batches (supercells too large for shared memory)
+  bool streamed = false;
+  int stream_pitch = 0;
+  StreamState sstate;
+  long long stream_pass = 0;
   // learned-proposal state
   long long *d_lw = nullptr;             // per-site integer weights
   unsigned long long *d_trees = nullptr; // two sum trees per replica
   double *d_lsamples = nullptr;          // [rep][cap][3]
   long long lsample_capacity = 0, lsamples_recorded = 0;
   ~cem_replicas() {
+    cudaFree(sstate.halo);
+    cudaFree(sstate.acc);
+    cudaFree(sstate.run);
+    if (sstate.exec) cudaGraphExecDestroy(sstate.exec);
     cudaFree(d_lw);
     cudaFree(d_trees);
     cudaFree(d_lsamples);
@@ -146,6 +155,16 @@ struct cem_replicas {
 };
 
 namespace {
+
+// HBM-streamed mode: binary FCC of the generated topology, equal even cubic
+// supercells whose pitch L + 4 has a compiled kernel
+int stream_pitch_for(const cem_system &s, const std::vector<Replica> &reps) {
+  if (!s.fcc_generated) return 0;
+  const int L = reps[0].L[0];
+  for (const Replica &R : reps)
+    if (R.L[0] != L || R.L[1] != L || R.L[2] != L || (L & 1) || R.p != 2) return 0;
+  return (L + 4 == 100 || L + 4 == 28) ? L + 4 : 0;
+}
 
 // smallest block size whose colour classes hold no two interacting sites;
 // canonical local pair moves also need 2p - reach(neighbour) > reach(flower)
@@ -450,6 +469,10 @@ int cem_replicas_create(const cem_system *sys, int n, const int *L, int ensemble
     r->pitch = pitch;
     r->generic_smem = gsmem;
     r->sweep_smem = pitch ? smem : gsmem;
+    if (r->sweep_smem > maxsm && stream_pitch_for(*sys, r->reps)) {
+      r->streamed = true;
+      r->stream_pitch = stream_pitch_for(*sys, r->reps);
+    }
     r->stats_host.assign(n, ReplicaStats{});
     CUDA_OK(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking));
     CUDA_OK(cudaEventCreate(&r->ev0));
@@ -719,11 +742,63 @@ int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_sampl
     int dev = 0, maxsm = 0;
     CUDA_OK(cudaGetDevice(&dev));
     CUDA_OK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    require(r->sweep_smem <= maxsm,
+    require(r->streamed || r->sweep_smem <= maxsm,
             "supercell does not fit in shared memory (" + std::to_string(r->sweep_smem) +
-                " bytes needed)",
+                " bytes needed) and has no HBM-streamed kernel",
             CEM_ERR_UNSUPPORTED);
     r->upload_reps();
+    if (r->streamed) {
+      const int L = r->reps[0].L[0];
+      const long long hb = stream_halo_bytes(L, r->stream_pitch);
+      if (!r->sstate.halo) {
+        CUDA_OK(cudaMalloc(&r->sstate.halo, (size_t)hb * r->n));
+        CUDA_OK(cudaMalloc(&r->sstate.acc, sizeof(long long) * 16 * r->n));
+        CUDA_OK(cudaMalloc(&r->sstate.run, sizeof(StreamRun)));
+      }
+      const bool fresh = !r->stats_valid;
+      if (fresh) init_stats(r);
+      r->stats_valid = true;
+      double *samples = nullptr;
+      long long cap = 0;
+      if (record_samples) {
+        cap = std::max<long long>(1, n_passes - n_equil);
+        if (cap > r->sample_capacity) {
+          cudaFree(r->d_samples);
+          r->d_samples = nullptr;
+          CUDA_OK(cudaMalloc(&r->d_samples, sizeof(double) * cap * r->sample_width * r->n));
+          r->sample_capacity = cap;
+        }
+        samples = r->d_samples;
+        cap = r->sample_capacity;
+        r->n_samples_recorded = std::max<long long>(0, n_passes - n_equil);
+      }
+      if (fresh || record_samples) {
+        // samples are indexed by the sample count: restart the moments
+        std::vector<ReplicaStats> st(r->n);
+        CUDA_OK(cudaMemcpyAsync(st.data(), r->d_stats, sizeof(ReplicaStats) * r->n,
+                                cudaMemcpyDeviceToHost, r->stream));
+        CUDA_OK(cudaStreamSynchronize(r->stream));
+        for (auto &x : st) {
+          x.n_samples = 0;
+          x.sum_e = x.sum_e2 = x.sum_f = 0;
+          for (int k = 0; k < 3; ++k) x.sum_x[k] = x.sum_ex[k] = 0;
+          for (int k = 0; k < 9; ++k) x.sum_xx[k] = 0;
+        }
+        r->stream_pass = st[0].pass;
+        CUDA_OK(cudaMemcpyAsync(r->d_stats, st.data(), sizeof(ReplicaStats) * r->n,
+                                cudaMemcpyHostToDevice, r->stream));
+      }
+      double RT[16] = {0};
+      for (size_t k = 0; k < r->sys->RT.size() && k < 16; ++k) RT[k] = r->sys->RT[k];
+      CUDA_OK(stream_run(r->sys->T, r->sstate, r->d_reps, r->d_stats, r->d_occ, r->n, L,
+                         r->stream_pitch, r->max_classes,
+                         r->ensemble == CEM_CANONICAL ? r->n_pair_sweeps : 0,
+                         r->ensemble == CEM_CANONICAL ? r->n_local_sweeps : 1, RT, n_passes, n_equil,
+                         r->stream_pass, samples, cap, r->sample_width, fresh ? 1 : 0, r->stream,
+                         r->ev0, r->ev1));
+      r->stream_pass += n_passes;
+      return;
+    }
     // binary systems compute the exact initial stats inside the sweep kernel
     const bool fused_init = !r->stats_valid && r->sys->T.n_occ == 2;
     if (!r->stats_valid && !fused_init) init_stats(r);
@@ -842,6 +917,12 @@ int cem_set_option(cem_replicas *r, const char *key, int64_t value) {
       require(value >= 1 && value + r->n_pair_sweeps <= MAX_SWEEPS_API,
               "local_sweeps must be >= 1 (swaps between colour classes keep the chain ergodic)");
       r->n_local_sweeps = (int)value;
+    } else if (k == "streamed") {
+      require(value == 1, "streamed can only be switched on");
+      const int sp = stream_pitch_for(*r->sys, r->reps);
+      require(sp != 0, "this batch has no HBM-streamed kernel", CEM_ERR_UNSUPPORTED);
+      r->streamed = true;
+      r->stream_pitch = sp;
     } else if (k == "generic_evaluator") {
       if (value) {
         r->pitch = 0;
@@ -864,6 +945,7 @@ int cem_get_option(cem_replicas *r, const char *key, int64_t *value) {
     else if (k == "pitch") *value = r->pitch;
     else if (k == "smem_bytes") *value = r->sweep_smem;
     else if (k == "colour_classes") *value = r->max_classes;
+    else if (k == "streamed") *value = r->streamed ? 1 : 0;
     else throw Err(CEM_ERR_INVALID, "unknown option '" + k + "'");
   });
 }

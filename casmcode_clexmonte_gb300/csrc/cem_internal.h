@@ -61,6 +61,29 @@ cudaError_t launch_sweep(const CeTables &T, const SweepParams &P, int n_replicas
 // true if the system is the binary FCC topology of the generated evaluator
 bool matches_generated_fcc(const CeTables &T, const int *pb, const int *du);
 
+// HBM-streamed sweep (cem_stream.cu)
+struct StreamRun {       // device-resident run parameters, written per run
+  long long n_equil;
+  long long start_pass;  // pass counter at the start of the run
+  double *samples;
+  long long sample_capacity;
+  int sample_width;
+  int pad;
+};
+struct StreamState {
+  int8_t *halo = nullptr;        // [n_rep][halo bytes]
+  long long *acc = nullptr;      // [n_rep][16]
+  StreamRun *run = nullptr;      // device
+  cudaGraphExec_t exec = nullptr;
+  int key = -1;
+};
+long long stream_halo_bytes(int L2, int pitch);
+cudaError_t stream_run(const CeTables &T, StreamState &st, const Replica *reps, ReplicaStats *stats,
+                       int8_t *occ_all, int n_rep, int L2, int pitch, int n_classes, int n_pair_sw,
+                       int n_local_sw, const double *RT, long long n_passes, long long n_equil,
+                       long long start_pass, double *samples, long long capacity, int width,
+                       int count_sub, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1);
+
 // learned proposal (cem_learned.cu)
 struct TreeGeo;
 cudaError_t mlp_forward(const __nv_bfloat16 *params, const int8_t *X, long long n, float *z,

@@ -598,10 +598,64 @@ __device__ __forceinline__ bool accept_fast(const FF &d, float beta_f, float u) 
   return u < cem_expf_neg(FMUL(-beta_f, de));
 }
 
+// Per-pass sample values of a replica: param composition per unit cell x,
+// potential energy per unit cell ep = E_f / n_uc - mu . x, formation energy per
+// unit cell ef. Explicitly rounded double operations, so every kernel that
+// samples gets the same bits.
+template <int NOCC>
+__device__ __forceinline__ void sample_values(const double *RT, const double *mu,
+                                              const long long *nspec, int n_sites, int n_uc,
+                                              double energy, double x[3], double &ef, double &ep) {
+  double mux = 0.0;
+  for (int k = 0; k < NOCC - 1; ++k) {
+    double t = 0.0;
+    for (int a = 0; a < NOCC; ++a) {
+      const double cnt = (double)nspec[a] - (a == 0 ? (double)n_sites : 0.0);
+      t = __dadd_rn(t, __dmul_rn(RT[k * NOCC + a], cnt));
+    }
+    x[k] = __ddiv_rn(t, (double)n_uc);
+    mux = __dadd_rn(mux, __dmul_rn(mu[k], x[k]));
+  }
+  ef = __ddiv_rn(energy, (double)n_uc);
+  ep = __dsub_rn(ef, mux);
+}
+
 // One of the four simple-cubic sublattices of FCC (L1_2 order parameter), for
 // a site in primitive-cell coordinates.
 __device__ __forceinline__ int sc_sublattice(int x, int y, int z) {
   return ((y + z) & 1) | (((x + z) & 1) << 1);
+}
+
+// Parameters of one sub-step, from its Philox draw r: pairs inside the
+// class (axis, shift m, rotation) or swaps with a neighbour (parity pattern,
+// neighbour index, rotations); 0xFFFFFFFF = no pair along any axis.
+__device__ __forceinline__ uint32_t sched_param(const U4 &r, int ensemble, int sweep,
+                                                int n_pair_sw, const int dims[3], int nnb) {
+  uint32_t par = 0;
+  if (ensemble == 1 && sweep < n_pair_sw) {
+    int a = r.y % 3, tries = 0;
+    while (dims[a] < 2 && tries < 3) {
+      a = (a + 1) % 3;
+      ++tries;
+    }
+    if (dims[a] >= 2) {
+      const int m = 1 + (int)(r.z % (uint32_t)(dims[a] / 2));
+      const int rot = (int)(r.w % (uint32_t)dims[a]);
+      par = (uint32_t)a | ((uint32_t)m << 2) | ((uint32_t)rot << 10);
+    } else {
+      par = 0xFFFFFFFFu;
+    }
+  } else if (ensemble == 1) {
+    const int dlt = (int)(r.y % (uint32_t)(nnb > 0 ? nnb : 1));
+    const uint32_t parity = r.z & 7u;
+    uint32_t rots = 0;
+    for (int a = 0; a < 3; ++a) {
+      const uint32_t ra = (r.w >> (8 * a)) & 255u;
+      rots |= (uint32_t)(ra % (uint32_t)dims[a]) << (7 * a);
+    }
+    par = parity | ((uint32_t)dlt << 3) | (rots << 7);
+  }
+  return par;
 }
 
 // Site evaluation policy: PITCH > 0 uses the generated binary FCC evaluator
@@ -828,31 +882,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
       int dims[3];
       for (int a = 0; a < 3; ++a) dims[a] = ax_cnt[a][cc[a]];
       const int sweep = e / n_classes;
-      uint32_t par = 0;
-      if (ensemble == 1 && sweep < n_pair_sw) {  // pairs within the class
-        int a = r.y % 3, tries = 0;
-        while (dims[a] < 2 && tries < 3) {
-          a = (a + 1) % 3;
-          ++tries;
-        }
-        if (dims[a] >= 2) {
-          const int m = 1 + (int)(r.z % (uint32_t)(dims[a] / 2));
-          const int rot = (int)(r.w % (uint32_t)dims[a]);
-          par = (uint32_t)a | ((uint32_t)m << 2) | ((uint32_t)rot << 10);
-        } else {
-          par = 0xFFFFFFFFu;  // no pair along any axis
-        }
-      } else if (ensemble == 1) {  // local pairs with a neighbour
-        const int nnb = T.n_nb[cb];
-        const int dlt = (int)(r.y % (uint32_t)(nnb > 0 ? nnb : 1));
-        const uint32_t parity = r.z & 7u;
-        uint32_t rots = 0;
-        for (int a = 0; a < 3; ++a) {
-          const uint32_t ra = (r.w >> (8 * a)) & 255u;
-          rots |= (uint32_t)(ra % (uint32_t)dims[a]) << (7 * a);
-        }
-        par = parity | ((uint32_t)dlt << 3) | (rots << 7);
-      }
+      const uint32_t par = sched_param(r, ensemble, sweep, n_pair_sw, dims, T.n_nb[cb]);
       spar[e] = par;
     }
     __syncthreads();
@@ -1064,16 +1094,8 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1)
           op = sqrt(op);
         }
         // param composition per unit cell and potential per unit cell
-        double x[3] = {0.0, 0.0, 0.0}, mux = 0.0;
-        for (int k = 0; k < NOCC - 1; ++k) {
-          double t = 0.0;
-          for (int a = 0; a < NOCC; ++a)
-            t += P.RT[k * NOCC + a] * ((double)nspec[a] - (a == 0 ? (double)n_sites : 0.0));
-          x[k] = t / n_uc;
-          mux += R.mu[k] * x[k];
-        }
-        const double ef = energy / n_uc;
-        const double ep = ef - mux;
+        double x[3] = {0.0, 0.0, 0.0}, ef, ep;
+        sample_values<NOCC>(P.RT, R.mu, nspec, n_sites, n_uc, energy, x, ef, ep);
         if (ip >= P.n_equil) {
           S.n_samples += 1.0;
           S.sum_e += ep;

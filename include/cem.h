@@ -202,8 +202,13 @@ int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_sampl
  *   "local_sweeps" (default 1, >= 1): sweeps of swaps with a nearest
  *                  neighbour per pass (these move atoms between classes);
  *   "generic_evaluator" (1): use the run-time cluster tables even where the
- *                  generated binary FCC evaluator applies.
- * cem_get_option also reads "pitch", "smem_bytes" and "colour_classes". */
+ *                  generated binary FCC evaluator applies;
+ *   "streamed" (1): keep the occupations in HBM and run one kernel per colour
+ *                  sub-step over many CTAs per replica (a captured CUDA graph
+ *                  per pass); chosen automatically when a supercell does not
+ *                  fit in shared memory (binary FCC, equal even supercells).
+ * cem_get_option also reads "pitch", "smem_bytes", "colour_classes" and
+ * "streamed". */
 int cem_set_option(cem_replicas *r, const char *key, int64_t value);
 int cem_get_option(cem_replicas *r, const char *key, int64_t *value);
 

@@ -255,3 +255,38 @@ def test_order_parameter_samples_match_final_state(cm):
     xb = occ.mean()
     c = np.array([occ[lab == k].mean() for k in range(4)])
     assert abs(op[-1] - np.sqrt(((c - xb) ** 2).sum())) < 1e-12
+
+
+@pytest.mark.parametrize("ens", ["canonical", "semigrand_canonical"])
+def test_streamed_sweep_matches_shared_memory_sweep(ens, cm):
+    """The HBM-streamed path (one kernel per colour sub-step, CUDA graph per
+    pass) runs the same chain as the shared-memory sweep: identical
+    occupations, counts, energies and samples."""
+    ce = workloads.fcc_binary_ce(5, nn1=0.08)
+    sysd = cm.System(ce)
+    L = (24, 24, 24)
+    rng = np.random.default_rng(2)
+    occs = [workloads.fixed_composition(rng, 24 ** 3, x) for x in (0.25, 0.5)]
+    out = []
+    for streamed in (False, True):
+        b = cm.ReplicaBatch(sysd, ens, [L, L])
+        if streamed:
+            b.set_option("streamed", 1)
+        assert b.get_option("streamed") == int(streamed)
+        for i in range(2):
+            b.set_conditions(i, 300.0 + 400 * i, np.array([0.01]) if ens != "canonical" else None)
+            b.set_seed(i, 17 + i)
+            b.set_occupation(i, occs[i])
+        b.run(12, 2, record_samples=True)
+        b.run(8, 0, record_samples=True)
+        res = []
+        for i in range(2):
+            pot, comp = b.samples(i, 8)
+            res.append((b.get_occupation(i), b.stats(i), pot, b.order_samples(i, 8)))
+        out.append(res)
+    for (oa, sa, pa, qa), (ob, sb, pb, qb) in zip(*out):
+        np.testing.assert_array_equal(oa, ob)
+        assert sa["n_accepted"] == sb["n_accepted"] and sa["n_proposed"] == sb["n_proposed"]
+        assert sa["energy"] == sb["energy"]
+        np.testing.assert_array_equal(pa, pb)
+        np.testing.assert_array_equal(qa, qb)
