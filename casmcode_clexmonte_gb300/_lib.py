@@ -58,6 +58,7 @@ EXPORTS = [
     "cem_mlp_info", "cem_mlp_create", "cem_mlp_destroy", "cem_mlp_get_params",
     "cem_mlp_set_params", "cem_mlp_forward", "cem_mlp_gradient", "cem_mlp_train",
     "cem_learned_features", "cem_learned_run", "cem_learned_samples", "cem_get_order_samples",
+    "cem_state_bytes", "cem_get_state", "cem_set_state",
 ]
 
 _lib = None
@@ -103,6 +104,9 @@ def load(path: str = LIB):
     L.cem_smem_bandwidth.argtypes = [_dp]
     L.cem_set_option.argtypes = [P, C.c_char_p, C.c_int64]
     L.cem_mlp_info.argtypes = [_ip, _ip, _ip]
+    L.cem_state_bytes.argtypes = [P, C.POINTER(C.c_int64)]
+    L.cem_get_state.argtypes = [P, C.c_int, vp, vp]
+    L.cem_set_state.argtypes = [P, C.c_int, vp, vp]
     L.cem_get_order_samples.argtypes = [P, C.c_int, vp, C.c_int64, C.POINTER(C.c_int64)]
     L.cem_mlp_create.argtypes = [C.c_uint64, C.POINTER(P)]
     L.cem_mlp_destroy.argtypes = [P]

@@ -157,6 +157,20 @@ class ReplicaBatch:
     def synchronize(self):
         check(self.lib.cem_synchronize(self.handle))
 
+    def get_state(self, i: int):
+        """(occupation, state bytes) checkpoint of replica i."""
+        nb = C.c_int64()
+        check(self.lib.cem_state_bytes(self.handle, C.byref(nb)))
+        occ = np.zeros(self.n_sites[i], dtype=np.int8)
+        st = np.zeros(nb.value, dtype=np.uint8)
+        check(self.lib.cem_get_state(self.handle, i, ptr(occ), ptr(st)))
+        return occ, st
+
+    def set_state(self, i: int, occ, state):
+        occ = np.ascontiguousarray(occ, dtype=np.int8)
+        state = np.ascontiguousarray(state, dtype=np.uint8)
+        check(self.lib.cem_set_state(self.handle, i, ptr(occ), ptr(state)))
+
     def order_samples(self, i: int, capacity: int) -> np.ndarray:
         op = np.zeros(capacity)
         n = C.c_int64()

@@ -114,6 +114,7 @@ struct cem_replicas {
   long long n_samples_recorded = 0;
   int max_classes = 1, sweep_smem = 0, pitch = 0, generic_smem = 0;
   int n_pair_sweeps = 2, n_local_sweeps = 1;
+  int threads = SWEEP_THREADS;
   bool reps_dirty = true, stats_valid = false;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -772,21 +773,26 @@ int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_sampl
         cap = r->sample_capacity;
         r->n_samples_recorded = std::max<long long>(0, n_passes - n_equil);
       }
-      if (fresh || record_samples) {
+      {
+        // pass counter at the start of this run (restored states keep theirs);
         // samples are indexed by the sample count: restart the moments
         std::vector<ReplicaStats> st(r->n);
         CUDA_OK(cudaMemcpyAsync(st.data(), r->d_stats, sizeof(ReplicaStats) * r->n,
                                 cudaMemcpyDeviceToHost, r->stream));
         CUDA_OK(cudaStreamSynchronize(r->stream));
-        for (auto &x : st) {
-          x.n_samples = 0;
-          x.sum_e = x.sum_e2 = x.sum_f = 0;
-          for (int k = 0; k < 3; ++k) x.sum_x[k] = x.sum_ex[k] = 0;
-          for (int k = 0; k < 9; ++k) x.sum_xx[k] = 0;
-        }
         r->stream_pass = st[0].pass;
-        CUDA_OK(cudaMemcpyAsync(r->d_stats, st.data(), sizeof(ReplicaStats) * r->n,
-                                cudaMemcpyHostToDevice, r->stream));
+        for (const auto &x : st)
+          require(x.pass == r->stream_pass, "streamed replicas must share one pass counter");
+        if (fresh || record_samples) {
+          for (auto &x : st) {
+            x.n_samples = 0;
+            x.sum_e = x.sum_e2 = x.sum_f = 0;
+            for (int k = 0; k < 3; ++k) x.sum_x[k] = x.sum_ex[k] = 0;
+            for (int k = 0; k < 9; ++k) x.sum_xx[k] = 0;
+          }
+          CUDA_OK(cudaMemcpyAsync(r->d_stats, st.data(), sizeof(ReplicaStats) * r->n,
+                                  cudaMemcpyHostToDevice, r->stream));
+        }
       }
       double RT[16] = {0};
       for (size_t k = 0; k < r->sys->RT.size() && k < 16; ++k) RT[k] = r->sys->RT[k];
@@ -842,7 +848,7 @@ int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_sampl
       r->n_samples_recorded = std::max<long long>(0, n_passes - n_equil);
     }
     CUDA_OK(cudaEventRecord(r->ev0, r->stream));
-    CUDA_OK(launch_sweep(T, P, r->n, r->sweep_smem, r->pitch, r->stream));
+    CUDA_OK(launch_sweep(T, P, r->n, r->sweep_smem, r->pitch, r->threads, r->stream));
     CUDA_OK(cudaEventRecord(r->ev1, r->stream));
   });
 }
@@ -946,7 +952,56 @@ int cem_get_option(cem_replicas *r, const char *key, int64_t *value) {
     else if (k == "smem_bytes") *value = r->sweep_smem;
     else if (k == "colour_classes") *value = r->max_classes;
     else if (k == "streamed") *value = r->streamed ? 1 : 0;
+    else if (k == "threads") *value = r->threads;
     else throw Err(CEM_ERR_INVALID, "unknown option '" + k + "'");
+  });
+}
+
+int cem_state_bytes(const cem_replicas *r, int64_t *bytes) {
+  return guard([&] {
+    require(r && bytes, "null argument");
+    *bytes = (int64_t)sizeof(ReplicaStats);
+  });
+}
+
+int cem_get_state(cem_replicas *r, int i, int8_t *occ, void *state) {
+  return guard([&] {
+    check_rep(r, i);
+    require(occ && state, "null argument");
+    const Replica &R = r->reps[i];
+    if (!r->stats_valid) {
+      r->upload_reps();
+      init_stats(r);
+    }
+    CUDA_OK(cudaMemcpyAsync(occ, r->d_occ + R.occ_offset, R.n_sites, cudaMemcpyDeviceToHost,
+                            r->stream));
+    CUDA_OK(cudaMemcpyAsync(state, r->d_stats + i, sizeof(ReplicaStats), cudaMemcpyDeviceToHost,
+                            r->stream));
+    CUDA_OK(cudaStreamSynchronize(r->stream));
+  });
+}
+
+int cem_set_state(cem_replicas *r, int i, const int8_t *occ, const void *state) {
+  return guard([&] {
+    check_rep(r, i);
+    require(occ && state, "null argument");
+    const Replica &R = r->reps[i];
+    for (int l = 0; l < R.n_sites; ++l)
+      require(occ[l] >= 0 && occ[l] < r->sys->T.n_occ, "occupant index out of range");
+    ReplicaStats S;
+    std::memcpy(&S, state, sizeof(S));
+    long long tot = 0;
+    for (int a = 0; a < r->sys->T.n_occ; ++a) tot += S.n_species[a];
+    require(tot == R.n_sites && std::isfinite(S.energy), "state does not belong to this replica");
+    if (!r->stats_valid) {
+      r->upload_reps();
+      init_stats(r);
+    }
+    CUDA_OK(cudaMemcpyAsync(r->d_occ + R.occ_offset, occ, R.n_sites, cudaMemcpyHostToDevice,
+                            r->stream));
+    CUDA_OK(cudaMemcpyAsync(r->d_stats + i, &S, sizeof(S), cudaMemcpyHostToDevice, r->stream));
+    CUDA_OK(cudaStreamSynchronize(r->stream));
+    r->stats_valid = true;
   });
 }
 

@@ -57,7 +57,7 @@ int sweep_smem_bytes(const CeTables &T, int L0, int L1, int L2, int n_classes, i
 // pitch 0: run-time tables; otherwise the generated binary FCC evaluator with
 // that x/y pitch (one of SWEEP_PITCHES)
 cudaError_t launch_sweep(const CeTables &T, const SweepParams &P, int n_replicas, int smem,
-                         int pitch, cudaStream_t st);
+                         int pitch, int threads, cudaStream_t st);
 // true if the system is the binary FCC topology of the generated evaluator
 bool matches_generated_fcc(const CeTables &T, const int *pb, const int *du);
 

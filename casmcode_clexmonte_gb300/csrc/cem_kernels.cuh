@@ -699,8 +699,8 @@ struct EnergyAcc<2> {
   }
 };
 
-template <int NOCC, int PITCH>
-__global__ void __launch_bounds__(SWEEP_THREADS, 1)
+template <int NOCC, int PITCH, int THREADS = SWEEP_THREADS>
+__global__ void __launch_bounds__(THREADS, 1)
     k_sweep(const __grid_constant__ CeTables T, const __grid_constant__ SweepParams P) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int rep = blockIdx.x;
@@ -1184,13 +1184,13 @@ cudaError_t launch_replay_t(const CeTables &T, const ReplayParams &P, cudaStream
   return cudaGetLastError();
 }
 
-template <int NOCC, int PITCH>
+template <int NOCC, int PITCH, int THREADS = SWEEP_THREADS>
 cudaError_t launch_sweep_t(const CeTables &T, const SweepParams &P, int n_replicas, int smem,
                            cudaStream_t st) {
-  cudaError_t e = cudaFuncSetAttribute(k_sweep<NOCC, PITCH>,
+  cudaError_t e = cudaFuncSetAttribute(k_sweep<NOCC, PITCH, THREADS>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  k_sweep<NOCC, PITCH><<<n_replicas, SWEEP_THREADS, smem, st>>>(T, P);
+  k_sweep<NOCC, PITCH, THREADS><<<n_replicas, THREADS, smem, st>>>(T, P);
   return cudaGetLastError();
 }
 
@@ -1203,7 +1203,7 @@ cudaError_t launch_sweep_t(const CeTables &T, const SweepParams &P, int n_replic
   template cudaError_t launch_replay_t<N>(const CeTables &, const ReplayParams &, cudaStream_t); \
   template cudaError_t launch_init_stats_t<N>(const CeTables &, const Replica *, ReplicaStats *, \
                                               const int8_t *, int, int, cudaStream_t);         \
-  template cudaError_t launch_sweep_t<N, 0>(const CeTables &, const SweepParams &, int, int,    \
-                                            cudaStream_t);
+  template cudaError_t launch_sweep_t<N, 0, SWEEP_THREADS>(const CeTables &, const SweepParams &, \
+                                                           int, int, cudaStream_t);
 
 }  // namespace cem

@@ -15,7 +15,7 @@ cudaError_t launch_replay_t(const CeTables &, const ReplayParams &, cudaStream_t
 template <int N>
 cudaError_t launch_init_stats_t(const CeTables &, const Replica *, ReplicaStats *, const int8_t *,
                                 int, int, cudaStream_t);
-template <int N, int PITCH>
+template <int N, int PITCH, int THREADS>
 cudaError_t launch_sweep_t(const CeTables &, const SweepParams &, int, int, cudaStream_t);
 
 
@@ -52,15 +52,16 @@ int sweep_smem_bytes(const CeTables &T, int L0, int L1, int L2, int n_classes, i
 }
 
 cudaError_t launch_sweep(const CeTables &T, const SweepParams &P, int n_replicas, int smem,
-                         int pitch, cudaStream_t st) {
-  if (pitch == 14) return launch_sweep_t<2, 14>(T, P, n_replicas, smem, st);
-  if (pitch == 28) return launch_sweep_t<2, 28>(T, P, n_replicas, smem, st);
-  if (pitch == 36) return launch_sweep_t<2, 36>(T, P, n_replicas, smem, st);
-  if (pitch == 52) return launch_sweep_t<2, 52>(T, P, n_replicas, smem, st);
-  if (pitch == 64) return launch_sweep_t<2, 64>(T, P, n_replicas, smem, st);
+                         int pitch, int threads, cudaStream_t st) {
+  if (threads != SWEEP_THREADS) return cudaErrorInvalidValue;
+  if (pitch == 14) return launch_sweep_t<2, 14, SWEEP_THREADS>(T, P, n_replicas, smem, st);
+  if (pitch == 28) return launch_sweep_t<2, 28, SWEEP_THREADS>(T, P, n_replicas, smem, st);
+  if (pitch == 36) return launch_sweep_t<2, 36, SWEEP_THREADS>(T, P, n_replicas, smem, st);
+  if (pitch == 52) return launch_sweep_t<2, 52, SWEEP_THREADS>(T, P, n_replicas, smem, st);
+  if (pitch == 64) return launch_sweep_t<2, 64, SWEEP_THREADS>(T, P, n_replicas, smem, st);
   if (pitch != 0) return cudaErrorInvalidValue;
-  if (T.n_occ == 2) return launch_sweep_t<2, 0>(T, P, n_replicas, smem, st);
-  if (T.n_occ == 3) return launch_sweep_t<3, 0>(T, P, n_replicas, smem, st);
+  if (T.n_occ == 2) return launch_sweep_t<2, 0, SWEEP_THREADS>(T, P, n_replicas, smem, st);
+  if (T.n_occ == 3) return launch_sweep_t<3, 0, SWEEP_THREADS>(T, P, n_replicas, smem, st);
   return cudaErrorInvalidValue;
 }
 

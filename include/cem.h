@@ -267,6 +267,17 @@ int cem_get_order_samples(cem_replicas *r, int replica, double *order, int64_t c
  * resident sweep. */
 int cem_smem_bandwidth(double *gbs);
 
+/* Checkpoint / restart of one replica: occupation plus an opaque state
+ * block (running energy, species and sublattice counts, moments, pass
+ * counter; cem_state_bytes bytes). The random streams are counter based
+ * (seed, pass, sub-step, site), so restoring the occupation and the state
+ * into a batch with the same seed continues the chain bit for bit. The
+ * reference restarts whole runs from completed_runs.json and saved final
+ * states (canonical_fullrun_test.cpp:337-344); this restarts inside a run. */
+int cem_state_bytes(const cem_replicas *r, int64_t *bytes);
+int cem_get_state(cem_replicas *r, int replica, int8_t *occ, void *state);
+int cem_set_state(cem_replicas *r, int replica, const int8_t *occ, const void *state);
+
 /* Wait for all work of this batch. */
 int cem_synchronize(cem_replicas *r);
 
