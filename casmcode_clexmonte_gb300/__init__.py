@@ -16,13 +16,19 @@ from .system import (  # noqa: F401
     system_arrays,
     verify_local_pairs,
 )
+from .casm_io import (  # noqa: F401
+    SummaryWriter,
+    read_cluster_expansion,
+    read_prim,
+    write_eci_json,
+)
 
 
 def __getattr__(name):
     # the CUDA-backed classes load the shared library on first use
     if name in (
         "System", "ReplicaBatch", "MonteCarloState", "MontePotential", "MonteCalculator",
-        "SamplingFixtureParams", "analyses",
+        "SamplingFixtureParams", "analyses", "enforce_composition", "mol_composition",
     ):
         from . import calculator
 

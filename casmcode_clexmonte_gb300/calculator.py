@@ -143,6 +143,22 @@ class ReplicaBatch:
                                   ptr(sites), C.byref(n_acc), C.byref(draws)))
         return dict(accept=acc, dE=de, sites=sites, n_accept=n_acc.value, draws=draws.value)
 
+    def enforce_composition(self, target_mol, mt_seed: int) -> np.ndarray:
+        """Greedy flips toward ``target_mol`` (species per unit cell; one row
+        per replica, or one row for all); replica i draws from
+        std::mt19937_64(mt_seed + i). Returns the flips per replica."""
+        t = np.asarray(target_mol, dtype=np.float64)
+        n = len(self.L)
+        if t.ndim == 1:
+            t = np.tile(t, (n, 1))
+        if t.shape != (n, self.system.n_occ):
+            raise ValueError(f"target_mol must have {self.system.n_occ} components per replica")
+        t = np.ascontiguousarray(t)
+        flips = np.zeros(n, dtype=np.int64)
+        check(self.lib.cem_enforce_composition(self.handle, t.ctypes.data_as(_lib._dp),
+                                               int(mt_seed), flips.ctypes.data_as(C.POINTER(C.c_int64))))
+        return flips
+
     def run(self, n_passes: int, n_equil: int = 0, record_samples: bool = False):
         check(self.lib.cem_run(self.handle, int(n_passes), int(n_equil), int(bool(record_samples))))
 
@@ -227,6 +243,35 @@ class ReplicaBatch:
         check(self.lib.cem_get_samples(self.handle, i, ptr(pot), ptr(comp), int(capacity),
                                        C.byref(n)))
         return pot[: n.value], comp[: n.value]
+
+
+def mol_composition(system: "System", param_composition) -> np.ndarray:
+    """Species per unit cell for a parametric composition on the standard
+    axes (origin: every site occupant 0; end member k: every site occupant k)."""
+    nb = system.ce.prim.n_basis
+    x = np.atleast_1d(np.asarray(param_composition, dtype=np.float64))
+    if x.size != system.n_occ - 1:
+        raise ValueError(f"param_composition must have {system.n_occ - 1} components")
+    return np.concatenate([[nb * (1.0 - x.sum())], nb * x])
+
+
+def enforce_composition(state: "MonteCarloState", target_mol_composition, system: "System",
+                        seed: int = 0) -> int:
+    """Apply semi-grand canonical flips to ``state.occupation`` until no flip
+    brings its composition closer to ``target_mol_composition`` (species per
+    unit cell), on the GPU; the draws follow std::mt19937_64(seed) as the
+    reference's ``enforce_composition`` (python/src/clexmonte_functions.cpp:
+    71-140) does with its engine. Returns the number of flips."""
+    t = np.asarray(target_mol_composition, dtype=np.float64)
+    if t.shape != (system.n_occ,):
+        raise ValueError(
+            f"Error in enforce_composition: mismatch target_mol_composition={t.tolist()}, "
+            f"expected {system.n_occ} components")
+    b = ReplicaBatch(system, "canonical", [tuple(int(x) for x in state.L)])
+    b.set_occupation(0, state.occupation)
+    n = int(b.enforce_composition(t, seed)[0])
+    state.occupation[:] = b.get_occupation(0)
+    return n
 
 
 class LearnedProposal:

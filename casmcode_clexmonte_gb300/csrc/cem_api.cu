@@ -736,6 +736,51 @@ int cem_reset_stats(cem_replicas *r) {
   });
 }
 
+int cem_enforce_composition(cem_replicas *r, const double *target_mol, uint64_t mt_seed,
+                            int64_t *n_flips) {
+  return guard([&] {
+    require(r != nullptr, "null replica batch");
+    require(target_mol != nullptr, "null target composition");
+    const int nocc = r->sys->T.n_occ;
+    for (int i = 0; i < r->n * nocc; ++i)
+      require(std::isfinite(target_mol[i]), "target composition must be finite");
+    int *scratch = nullptr;
+    double *d_target = nullptr;
+    long long *d_out = nullptr;
+    auto cleanup = [&] {
+      cudaFree(scratch);
+      cudaFree(d_target);
+      cudaFree(d_out);
+    };
+    std::vector<long long> res(3 * (size_t)r->n);
+    try {
+      CUDA_OK(cudaMalloc(&scratch, (size_t)r->total_sites * (nocc + 1) * sizeof(int)));
+      CUDA_OK(cudaMalloc(&d_target, sizeof(double) * r->n * nocc));
+      CUDA_OK(cudaMalloc(&d_out, sizeof(long long) * 3 * r->n));
+      r->upload_reps();
+      CUDA_OK(cudaMemcpyAsync(d_target, target_mol, sizeof(double) * r->n * nocc,
+                              cudaMemcpyHostToDevice, r->stream));
+      long long max_sites = 0;
+      for (const Replica &R : r->reps) max_sites = std::max<long long>(max_sites, R.n_sites);
+      CUDA_OK(launch_enforce(nocc, r->d_reps, r->n, r->d_occ, d_target, mt_seed,
+                             r->sys->T.n_sublat, scratch, d_out, 4 * max_sites + 16, r->stream));
+      CUDA_OK(cudaMemcpyAsync(res.data(), d_out, sizeof(long long) * 3 * r->n,
+                              cudaMemcpyDeviceToHost, r->stream));
+      CUDA_OK(cudaStreamSynchronize(r->stream));
+    } catch (...) {
+      cleanup();
+      throw;
+    }
+    cleanup();
+    r->stats_valid = false;
+    for (int i = 0; i < r->n; ++i) {
+      if (res[3 * i + 2] == 3) throw Err(CEM_ERR_INVALID, "occupation holds an occupant index outside [0, n_occ)");
+      if (res[3 * i + 2] != 0) throw Err(CEM_ERR_DEVICE, "composition enforcement did not terminate");
+      if (n_flips) n_flips[i] = res[3 * i];
+    }
+  });
+}
+
 int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_samples) {
   return guard([&] {
     require(r != nullptr, "null handle");

@@ -50,6 +50,11 @@ cudaError_t launch_delta(const CeTables &T, const int8_t *occ, int L0, int L1, i
                          const double *dmu, double *dE, long long *dcount, cudaStream_t st);
 int replay_smem_bytes(int n_sites, int n_occ);
 cudaError_t launch_replay(const CeTables &T, const ReplayParams &P, cudaStream_t st);
+// Greedy composition enforcement, one warp per replica; scratch holds
+// (n_occ + 1) ints per site; out[3 r + {0,1,2}] = flips, draws, status.
+cudaError_t launch_enforce(int n_occ, const Replica *reps, int n_reps, int8_t *occ,
+                           const double *target, unsigned long long seed, int n_sublat,
+                           int *scratch, long long *out, long long max_flips, cudaStream_t st);
 cudaError_t launch_init_stats(const CeTables &T, const Replica *reps, ReplicaStats *stats,
                               const int8_t *occ, int n_replicas, int max_sites, cudaStream_t st);
 cudaError_t smem_bandwidth(double *gbs, cudaStream_t st);

@@ -188,6 +188,19 @@ int cem_replay(cem_replicas *r, int replica, uint64_t mt_seed, int64_t n_steps,
                uint8_t *accept_seq, double *dE_seq, int64_t *site_seq, int64_t *n_accept,
                uint64_t *n_draws);
 
+/* Composition enforcement: greedy semi-grand canonical flips that move each
+ * replica toward target_mol (n_occ values per replica, replica-major:
+ * species count per unit cell, e.g. {1 - x, x} for a one-site binary cell)
+ * until no flip type brings it closer; replica i draws from
+ * std::mt19937_64(mt_seed + i) exactly as the reference's
+ * RandomNumberGenerator does. Replaces clexmonte::enforce_composition
+ * (include/casm/clexmonte/state/enforce_composition.hh:172-210; python
+ * binding python/src/clexmonte_functions.cpp:71-140). n_flips (optional,
+ * n_replicas values) receives the flips applied per replica. Invalidates the
+ * running statistics of every replica. */
+int cem_enforce_composition(cem_replicas *r, const double *target_mol, uint64_t mt_seed,
+                            int64_t *n_flips);
+
 /* Parallel Metropolis: n_passes passes over every replica; each pass updates
  * colour classes of mutually non-interacting sites at once (flips for SGC,
  * pair swaps for canonical). Passes after n_equil contribute to the

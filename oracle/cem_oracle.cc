@@ -674,6 +674,92 @@ int ora_run(void *h, signed char *occ, int ensemble, double temperature, const d
   }
 }
 
+// Greedy composition enforcement (clexmonte::enforce_composition restated,
+// include/casm/clexmonte/state/enforce_composition.hh:56-126 and 172-210):
+// flip types a -> b (a != b) in a-major order; the distance is the Euclidean
+// norm of (mol composition per unit cell - target); a type is a candidate if
+// it improves the distance by more than tol = 1e-3 / volume; ties within tol
+// are broken by random_real(sum of their site counts); the flipped site is
+// the random_int-th entry of the species' occupant list. Returns the number
+// of flips (or -1 on error) and the engine draws consumed.
+i64 ora_enforce_composition(void *h, signed char *occ, const double *target, u64 seed,
+                            u64 *draws_out) {
+  try {
+    System &s = *(System *)h;
+    const int n = s.n_sites, no = s.n_occ;
+    Rng rng;
+    rng.eng.seed(seed);
+    OccLoc loc;
+    loc.init(occ, n, no);
+    const double volume = (double)(n / s.n_basis);
+    const double dn = 1. / volume;
+    const double tol = dn * 1e-3;
+    std::vector<double> cur(no);
+    for (int c = 0; c < no; ++c) cur[c] = (double)loc.lists[c].size() / volume;
+    auto dist = [&](const std::vector<double> &m) {
+      double q = 0.0;
+      for (int c = 0; c < no; ++c) {
+        double d = m[c] - target[c];
+        q += d * d;
+      }
+      return std::sqrt(q);
+    };
+    struct Choice {
+      int a, b;
+      long count;
+      std::vector<double> mol;
+    };
+    i64 flips = 0;
+    while (true) {
+      const double orig = dist(cur);
+      double best = orig;
+      std::vector<Choice> ch;
+      for (int a = 0; a < no; ++a)
+        for (int b = 0; b < no; ++b) {
+          if (a == b || loc.lists[a].empty()) continue;
+          std::vector<double> t = cur;
+          t[a] -= dn;
+          t[b] += dn;
+          double d = dist(t);
+          if (d > orig - tol) {
+            continue;
+          } else if (d < best - tol) {
+            ch.clear();
+            ch.push_back({a, b, (long)loc.lists[a].size(), t});
+            best = d;
+          } else if (d < best + tol) {
+            ch.push_back({a, b, (long)loc.lists[a].size(), t});
+          }
+        }
+      if (ch.empty()) break;
+      double sum = 0.0;
+      for (auto &c : ch) sum += c.count;
+      double u = rng.random_real(sum);
+      sum = 0.0;
+      const Choice *pick = nullptr;
+      for (auto &c : ch) {
+        sum += c.count;
+        if (u < sum) {
+          pick = &c;
+          break;
+        }
+      }
+      if (!pick) throw std::runtime_error("failed enforcing composition");
+      cur = pick->mol;
+      long ia = rng.random_int((long)loc.lists[pick->a].size() - 1);
+      int l = loc.lists[pick->a][ia];
+      loc.move(l, pick->a, pick->b);
+      occ[l] = (signed char)pick->b;
+      ++flips;
+    }
+    if (draws_out) *draws_out = rng.draws;
+    return flips;
+  } catch (std::exception &e) {
+    g_err = e.what();
+    return -1;
+  }
+}
+
 // Many independent sequential chains on host threads (CPU baseline):
 // replica r uses occ + r*n_sites, seed + r, temperature[r], mu[r*(n_occ-1)].
 // Returns wall seconds; n_steps_out = total proposals.

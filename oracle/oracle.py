@@ -76,6 +76,8 @@ def lib():
             P, i8p, C.c_int, C.c_int, f64p, f64p, C.c_uint64, C.c_int64, C.c_int,
             C.POINTER(C.c_int64),
         ]
+        L.ora_enforce_composition.restype = C.c_int64
+        L.ora_enforce_composition.argtypes = [P, i8p, f64p, C.c_uint64, u64p]
         L.ora_mt19937_64.argtypes = [C.c_uint64, C.c_int64, u64p]
         L.ora_std_uniform_int.argtypes = [C.c_uint64, C.c_int64, i64p, i64p, u64p]
         L.ora_std_uniform_real.argtypes = [C.c_uint64, C.c_int64, f64p]
@@ -204,6 +206,17 @@ class OracleSystem:
             site0=rs0, site1=rs1, dE=rde, accept=racc, energy=se, potential=sp,
             comp=scomp, n_accept=int(nacc[0]), draws=int(draws[0]),
         )
+
+    def enforce_composition(self, occ, target_mol, seed):
+        """Greedy composition enforcement; ``occ`` is updated in place.
+        Returns (flips, engine draws)."""
+        assert occ.dtype == np.int8 and occ.flags.c_contiguous and occ.size == self.n_sites
+        draws = np.zeros(1, dtype=np.uint64)
+        n = lib().ora_enforce_composition(
+            self.h, occ, np.ascontiguousarray(target_mol, dtype=np.float64), int(seed), draws)
+        if n < 0:
+            raise RuntimeError(lib().ora_last_error().decode())
+        return int(n), int(draws[0])
 
     def run_threads(self, occ, ensemble, temps, mus, seed, n_passes, n_threads):
         nrep = len(temps)
