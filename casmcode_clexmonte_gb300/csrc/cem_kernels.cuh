@@ -529,7 +529,7 @@ constexpr int MAX_SWEEPS = 8;
 
 struct SweepSmem {
   // carved from dynamic shared memory; offsets in bytes
-  int occ, cl_off, lutoff, lut, whi, wlo, dmu, ax, sched, red, total;
+  int occ, cl_off, lutoff, lut, whi, wlo, dmu, ax, sched, red, clist, wkept, total;
 };
 
 __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
@@ -562,6 +562,10 @@ __host__ __device__ inline void sweep_layout(const CeTables &T, int L0, int L1, 
   o += align16(3 * MAX_SWEEPS * n_classes_max * 4);
   s.red = o;  // block reduction scratch: 32 warps x 16 slots of 8 bytes
   o += 32 * 16 * 8;
+  s.clist = o;  // kept canonical candidates (u16): a class holds <= n_uc / 8 sites
+  o += align16(2 * ((L0 * L1 * L2) / 8 + 32));
+  s.wkept = o;  // kept candidates per warp
+  o += 32 * 4;
   s.total = o;
 }
 
@@ -597,6 +601,36 @@ __device__ __forceinline__ bool accept_fast(const FF &d, float beta_f, float u) 
   if (de < 0.f) return true;
   return u < cem_expf_neg(FMUL(-beta_f, de));
 }
+
+// floor(n / d) for a block-uniform divisor 1 <= d < 2^16 and numerators
+// 0 <= n < 2^16: umulhi(n, m) with m = floor((2^32 - 1) / d) + 1 (= ceil(2^32 / d),
+// or 2^32 / d for powers of two); exact because the rounding error of m is
+// below d and n * d < 2^32 (Granlund and Montgomery, "Division by invariant
+// integers using multiplication", PLDI 1994).
+struct FastDiv {
+  int d;
+  uint32_t m;
+  __device__ __forceinline__ explicit FastDiv(int dd)
+      : d(dd), m(dd > 1 ? 0xFFFFFFFFu / (uint32_t)dd + 1u : 0u) {}
+  __device__ __forceinline__ int div(int n) const {
+    return d > 1 ? (int)__umulhi((uint32_t)n, m) : n;
+  }
+};
+
+// Small counters indexed by a run-time value, kept in registers (unrolled
+// selects rather than a local-memory array).
+template <int N>
+struct RegCounts {
+  int v[N];
+  __device__ __forceinline__ RegCounts() {
+#pragma unroll
+    for (int k = 0; k < N; ++k) v[k] = 0;
+  }
+  __device__ __forceinline__ void add(int i, int d) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) v[k] += (k == i) ? d : 0;
+  }
+};
 
 // Per-pass sample values of a replica: param composition per unit cell x,
 // potential energy per unit cell ep = E_f / n_uc - mu . x, formation energy per
@@ -735,6 +769,8 @@ __global__ void __launch_bounds__(THREADS, 1)
   int *ax = reinterpret_cast<int *>(smem + lay.ax);
   uint32_t *sched = reinterpret_cast<uint32_t *>(smem + lay.sched);
   unsigned char *red = smem + lay.red;
+  uint16_t *clist = reinterpret_cast<uint16_t *>(smem + lay.clist);
+  int *wkept = reinterpret_cast<int *>(smem + lay.wkept);
   int *ax_begin[3], *ax_cnt[3], *ax_coord[3];
   for (int a = 0; a < 3; ++a) {
     ax_begin[a] = ax + a * (2 * MAX_COLOURS + MAX_L);
@@ -899,9 +935,8 @@ __global__ void __launch_bounds__(THREADS, 1)
     __syncthreads();
 
     EnergyAcc<NOCC> eacc;
-    int dspec[NOCC];
-    for (int a = 0; a < NOCC; ++a) dspec[a] = 0;
-    int dsub[4] = {0, 0, 0, 0};  // binary FCC only (PITCH > 0)
+    RegCounts<NOCC> dspec;
+    RegCounts<4> dsub;  // binary FCC only (PITCH > 0)
     int n_prop = 0, n_acc = 0;
 
     for (int sub = 0; sub < n_sub; ++sub) {
@@ -909,17 +944,19 @@ __global__ void __launch_bounds__(THREADS, 1)
       const int c = (int)sord[sub];
       const uint32_t par = spar[sw * n_classes + c];
       const int cb = c / ncol_all, cr = c - cb * ncol_all;
-      const int cc[3] = {cr % ncol0, (cr / ncol0) % ncol1, cr / (ncol0 * ncol1)};
-      const int dims[3] = {ax_cnt[0][cc[0]], ax_cnt[1][cc[1]], ax_cnt[2][cc[2]]};
-      const int *cx = ax_coord[0] + ax_begin[0][cc[0]];
-      const int *cy = ax_coord[1] + ax_begin[1][cc[1]];
-      const int *cz = ax_coord[2] + ax_begin[2][cc[2]];
+      const int c0 = cr % ncol0, c1 = (cr / ncol0) % ncol1, c2 = cr / (ncol0 * ncol1);
+      const int d0 = ax_cnt[0][c0], d1 = ax_cnt[1][c1], d2 = ax_cnt[2][c2];
+      const int *cx = ax_coord[0] + ax_begin[0][c0];
+      const int *cy = ax_coord[1] + ax_begin[1][c1];
+      const int *cz = ax_coord[2] + ax_begin[2][c2];
       const uint32_t ctr_sub = (uint32_t)sub;
       if (ensemble == 0) {
         // ---------------- flips of every site of the class
-        const int n = dims[0] * dims[1] * dims[2];
+        const int n = d0 * d1 * d2;
+        const FastDiv f0(d0), f1(d1);
         for (int q = tid; q < n; q += nth) {
-          const int ix = q % dims[0], iy = (q / dims[0]) % dims[1], iz = q / (dims[0] * dims[1]);
+          const int t = f0.div(q), iz = f1.div(t);
+          const int ix = q - t * d0, iy = t - iz * d1;
           const int x = cx[ix], y = cy[iy], z = cz[iz];
           const int ad = G.addr(cb, x, y, z);
           const int o_i = occ[ad];
@@ -942,94 +979,136 @@ __global__ void __launch_bounds__(THREADS, 1)
             ++n_acc;
             put_site(occ, G, cb, x, y, z, (int8_t)o_f);
             eacc.add(acc, d, R.dmu[o_i * NOCC + o_f]);
-            dspec[o_i]--;
-            dspec[o_f]++;
-            if constexpr (PITCH > 0) dsub[sc_sublattice(x, y, z)] += o_f - o_i;
-          }
-        }
-      } else if (sw < n_pair_sw) {
-        // ---------------- canonical swaps of pairs inside the class
-        if (par != 0xFFFFFFFFu) {
-          const int a = par & 3, m = (par >> 2) & 255, rot = par >> 10;
-          const int na = dims[a];
-          const int half = (na / (2 * m)) * m;  // pairs along the axis
-          int e3[3] = {dims[0], dims[1], dims[2]};
-          e3[a] = half;
-          const int n = e3[0] * e3[1] * e3[2];
-          for (int q = tid; q < n; q += nth) {
-            int ia[3] = {q % e3[0], (q / e3[0]) % e3[1], q / (e3[0] * e3[1])};
-            int ib[3] = {ia[0], ia[1], ia[2]};
-            const int jj = ia[a];
-            const int u = 2 * m * (jj / m) + (jj % m);
-            ia[a] = (u + rot) % na;
-            ib[a] = (u + m + rot) % na;
-            const int xa = cx[ia[0]], ya = cy[ia[1]], za = cz[ia[2]];
-            const int xb = cx[ib[0]], yb = cy[ib[1]], zb = cz[ib[2]];
-            const int ada = G.addr(cb, xa, ya, za), adb = G.addr(cb, xb, yb, zb);
-            const int oa = occ[ada], ob = occ[adb];
-            if (oa == ob) continue;
-            const int la = cb * n_uc + xa + G.L0 * (ya + G.L1 * za);
-            const U4 r = philox4x32_10(U4{(uint32_t)la, ctr_sub, plo, phi | (TAG_SITE << 16)}, k0, k1);
-            Acc<NOCC> acc;
-            acc.zero();
-            ev.add(cb, oa, ob, occ, ada, acc);
-            ev.add(cb, ob, oa, occ, adb, acc);
-            const FF d = acc_dot<NOCC>(T, acc, whi, wlo);
-            ++n_prop;
-            if (accept_fast(d, beta_f, u24(r.x))) {
-              ++n_acc;
-              put_site(occ, G, cb, xa, ya, za, (int8_t)ob);
-              put_site(occ, G, cb, xb, yb, zb, (int8_t)oa);
-              eacc.add(acc, d, 0.0);
-            }
+            dspec.add(o_i, -1);
+            dspec.add(o_f, 1);
+            if constexpr (PITCH > 0) dsub.add(sc_sublattice(x, y, z), o_f - o_i);
           }
         }
       } else {
-        // ---------------- canonical swaps with a neighbour (sequential dE)
-        const int parity = par & 7, dlt = (par >> 3) & 15;
-        const int rots[3] = {(int)((par >> 7) & 127), (int)((par >> 14) & 127),
-                             (int)((par >> 21) & 127)};
-        if (T.n_nb[cb] > 0) {
-          const int nb_b = T.nb_b[cb][dlt];
-          const int *du = T.nb_du[cb][dlt];
-          int h[3];
-          bool empty = false;
-          for (int a = 0; a < 3; ++a) {
-            h[a] = dims[a] >= 2 ? dims[a] / 2 : 1;
-            if (dims[a] < 2 && ((parity >> a) & 1)) empty = true;
+        // ---------------- canonical swaps: pairs inside the class (pair
+        // sweeps) or a site with a neighbour (local sweeps, sequential dE).
+        // Phase A: each warp scans a contiguous chunk of candidate pairs and
+        // keeps, in order, those whose occupants differ (the only proposals);
+        // phase B spreads the kept pairs evenly over the block. The kept
+        // order and the pair -> thread map depend only on the occupations,
+        // so runs stay deterministic.
+        const bool local = sw >= n_pair_sw;
+        int n = 0;
+        // pair sweeps: pairs along axis pa at class distance pm, rotated by
+        // prot; candidate grid e0 x e1 x e2 (the pair axis halved)
+        int pa = 0, pm = 1, prot = 0, pna = 1, e0 = 1, e1 = 1;
+        // local sweeps: every other class coordinate (parity bits) along
+        // each axis, rotated, paired with neighbour (nb_b, du)
+        int parity = 0, nb_b = cb, h0 = 1, h1 = 1, h2 = 1, r0 = 0, r1 = 0, r2 = 0;
+        int du0 = 0, du1 = 0, du2 = 0;
+        if (!local) {
+          if (par != 0xFFFFFFFFu) {
+            pa = par & 3;
+            pm = (par >> 2) & 255;
+            prot = par >> 10;
+            pna = pa == 0 ? d0 : (pa == 1 ? d1 : d2);
+            const int half = (pna / (2 * pm)) * pm;
+            e0 = pa == 0 ? half : d0;
+            e1 = pa == 1 ? half : d1;
+            const int e2 = pa == 2 ? half : d2;
+            n = e0 * e1 * e2;
           }
-          const int n = empty ? 0 : h[0] * h[1] * h[2];
-          for (int q = tid; q < n; q += nth) {
-            const int t[3] = {q % h[0], (q / h[0]) % h[1], q / (h[0] * h[1])};
-            int ii[3];
-            for (int a = 0; a < 3; ++a)
-              ii[a] = dims[a] >= 2 ? (rots[a] + ((parity >> a) & 1) + 2 * t[a]) % dims[a] : 0;
-            const int xa = cx[ii[0]], ya = cy[ii[1]], za = cz[ii[2]];
-            const int xb = wrapc(xa + du[0], G.L0), yb = wrapc(ya + du[1], G.L1),
-                      zb = wrapc(za + du[2], G.L2);
-            const int ada = G.addr(cb, xa, ya, za), adb = G.addr(nb_b, xb, yb, zb);
-            const int oa = occ[ada], ob = occ[adb];
-            if (oa == ob) continue;
-            const int la = cb * n_uc + xa + G.L0 * (ya + G.L1 * za);
-            const U4 r = philox4x32_10(U4{(uint32_t)la, ctr_sub, plo, phi | (TAG_SITE << 16)}, k0, k1);
-            Acc<NOCC> acc;
-            acc.zero();
-            ev.add(cb, oa, ob, occ, ada, acc);
-            put_site(occ, G, cb, xa, ya, za, (int8_t)ob);  // first change applied
-            ev.add(nb_b, ob, oa, occ, adb, acc);
-            const FF d = acc_dot<NOCC>(T, acc, whi, wlo);
-            ++n_prop;
-            if (accept_fast(d, beta_f, u24(r.x))) {
-              ++n_acc;
-              put_site(occ, G, nb_b, xb, yb, zb, (int8_t)oa);
-              eacc.add(acc, d, 0.0);
-              if constexpr (PITCH > 0) {
-                dsub[sc_sublattice(xa, ya, za)] += ob - oa;
-                dsub[sc_sublattice(xb, yb, zb)] += oa - ob;
-              }
-            } else {
-              put_site(occ, G, cb, xa, ya, za, (int8_t)oa);
+        } else if (T.n_nb[cb] > 0) {
+          parity = par & 7;
+          const int dlt = (par >> 3) & 15;
+          r0 = (int)((par >> 7) & 127);
+          r1 = (int)((par >> 14) & 127);
+          r2 = (int)((par >> 21) & 127);
+          nb_b = T.nb_b[cb][dlt];
+          du0 = T.nb_du[cb][dlt][0];
+          du1 = T.nb_du[cb][dlt][1];
+          du2 = T.nb_du[cb][dlt][2];
+          h0 = d0 >= 2 ? d0 / 2 : 1;
+          h1 = d1 >= 2 ? d1 / 2 : 1;
+          h2 = d2 >= 2 ? d2 / 2 : 1;
+          const bool empty = (d0 < 2 && (parity & 1)) || (d1 < 2 && (parity & 2)) ||
+                             (d2 < 2 && (parity & 4));
+          n = empty ? 0 : h0 * h1 * h2;
+        }
+        const int bb = local ? nb_b : cb;
+        const FastDiv fe0(local ? h0 : e0), fe1(local ? h1 : e1), fpm(pm);
+        auto wrap_lt2 = [](int v, int L) { return v >= L ? v - L : v; };  // v < 2L
+        auto sites_of = [&](int q, int &xa, int &ya, int &za, int &xb, int &yb, int &zb) {
+          const int t = fe0.div(q), i2 = fe1.div(t);
+          const int i0 = q - t * fe0.d, i1 = t - i2 * (int)fe1.d;
+          if (!local) {
+            const int jj = pa == 0 ? i0 : (pa == 1 ? i1 : i2);
+            const int jq = fpm.div(jj);
+            const int u = 2 * pm * jq + (jj - jq * pm);
+            const int ja = wrap_lt2(u + prot, pna), jb = wrap_lt2(u + pm + prot, pna);
+            xa = cx[pa == 0 ? ja : i0];
+            xb = cx[pa == 0 ? jb : i0];
+            ya = cy[pa == 1 ? ja : i1];
+            yb = cy[pa == 1 ? jb : i1];
+            za = cz[pa == 2 ? ja : i2];
+            zb = cz[pa == 2 ? jb : i2];
+          } else {
+            xa = cx[d0 >= 2 ? wrap_lt2(r0 + (parity & 1) + 2 * i0, d0) : 0];
+            ya = cy[d1 >= 2 ? wrap_lt2(r1 + ((parity >> 1) & 1) + 2 * i1, d1) : 0];
+            za = cz[d2 >= 2 ? wrap_lt2(r2 + ((parity >> 2) & 1) + 2 * i2, d2) : 0];
+            xb = wrapc(xa + du0, G.L0);
+            yb = wrapc(ya + du1, G.L1);
+            zb = wrapc(za + du2, G.L2);
+          }
+        };
+        // phase A: ordered per-warp compaction of the proposals
+        const int chunk = (n + nwarp - 1) / nwarp;
+        const int q_begin = warp * chunk;
+        const int q_end = min(n, q_begin + chunk);
+        int kept = 0;
+        for (int q0 = q_begin; q0 < q_end; q0 += 32) {
+          const int q = q0 + lane;
+          bool act = false;
+          if (q < q_end) {
+            int xa, ya, za, xb, yb, zb;
+            sites_of(q, xa, ya, za, xb, yb, zb);
+            act = occ[G.addr(cb, xa, ya, za)] != occ[G.addr(bb, xb, yb, zb)];
+          }
+          const unsigned m = __ballot_sync(0xffffffffu, act);
+          if (act) clist[q_begin + kept + __popc(m & ((1u << lane) - 1u))] = (uint16_t)q;
+          kept += __popc(m);
+        }
+        if (lane == 0) wkept[warp] = kept;
+        __syncthreads();
+        // phase B: proposal i of the block goes to thread i mod block size
+        int total = 0;
+        for (int w = 0; w < nwarp; ++w) total += wkept[w];
+        for (int i = tid; i < total; i += nth) {
+          int w = 0, base = 0;
+          while (base + wkept[w] <= i) {
+            base += wkept[w];
+            ++w;
+          }
+          const int q = clist[w * chunk + (i - base)];
+          int xa, ya, za, xb, yb, zb;
+          sites_of(q, xa, ya, za, xb, yb, zb);
+          const int ada = G.addr(cb, xa, ya, za), adb = G.addr(bb, xb, yb, zb);
+          const int oa = occ[ada], ob = occ[adb];
+          const int la = cb * n_uc + xa + G.L0 * (ya + G.L1 * za);
+          const U4 r = philox4x32_10(U4{(uint32_t)la, ctr_sub, plo, phi | (TAG_SITE << 16)}, k0, k1);
+          Acc<NOCC> acc;
+          acc.zero();
+          ev.add(cb, oa, ob, occ, ada, acc);
+          if (local) put_site(occ, G, cb, xa, ya, za, (int8_t)ob);  // first change applied
+          ev.add(bb, ob, oa, occ, adb, acc);
+          const FF d = acc_dot<NOCC>(T, acc, whi, wlo);
+          ++n_prop;
+          if (accept_fast(d, beta_f, u24(r.x))) {
+            ++n_acc;
+            if (!local) put_site(occ, G, cb, xa, ya, za, (int8_t)ob);
+            put_site(occ, G, bb, xb, yb, zb, (int8_t)oa);
+            eacc.add(acc, d, 0.0);
+            if constexpr (PITCH > 0) {
+              dsub.add(sc_sublattice(xa, ya, za), ob - oa);
+              dsub.add(sc_sublattice(xb, yb, zb), oa - ob);
             }
+          } else if (local) {
+            put_site(occ, G, cb, xa, ya, za, (int8_t)oa);
           }
         }
       }
@@ -1043,9 +1122,11 @@ __global__ void __launch_bounds__(THREADS, 1)
       for (int k = 0; k < 16; ++k) vals[k] = 0;
       vals[0] = n_prop;
       vals[1] = n_acc;
-      for (int a = 0; a < NOCC; ++a) vals[2 + a] = dspec[a];
+#pragma unroll
+      for (int a = 0; a < NOCC; ++a) vals[2 + a] = dspec.v[a];
       if constexpr (PITCH > 0)
-        for (int k = 0; k < 4; ++k) vals[4 + k] = dsub[k];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) vals[4 + k] = dsub.v[k];
       double dsum = 0.0;
       if constexpr (NOCC == 2) {
         for (int g = 0; g < MAX_ORBITS; ++g) vals[8 + g] = eacc.dc[g];

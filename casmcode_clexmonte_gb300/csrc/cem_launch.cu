@@ -3,22 +3,34 @@
 
 namespace cem {
 
-template <int N>
-cudaError_t launch_energy_t(const CeTables &, const int8_t *, int, int, int, unsigned long long *,
-                            cudaStream_t);
-template <int N>
-cudaError_t launch_delta_t(const CeTables &, const int8_t *, int, int, int, int, int,
-                           const long long *, const int *, const double *, double *, long long *,
-                           cudaStream_t);
-template <int N>
-cudaError_t launch_replay_t(const CeTables &, const ReplayParams &, cudaStream_t);
-template <int N>
-cudaError_t launch_init_stats_t(const CeTables &, const Replica *, ReplicaStats *, const int8_t *,
-                                int, int, cudaStream_t);
-template <int N, int PITCH, int THREADS>
-cudaError_t launch_sweep_t(const CeTables &, const SweepParams &, int, int, cudaStream_t);
-
-
+// The launchers are instantiated in the kernel translation units (cem_k2.cu,
+// cem_k3.cu, cem_kfcc.cu, cem_kfcc_b.cu); extern declarations keep this file
+// from compiling a second copy of every kernel.
+#define CEM_EXTERN(N)                                                                          \
+  extern template cudaError_t launch_energy_t<N>(const CeTables &, const int8_t *, int, int,   \
+                                                 int, unsigned long long *, cudaStream_t);     \
+  extern template cudaError_t launch_delta_t<N>(const CeTables &, const int8_t *, int, int,    \
+                                                int, int, int, const long long *, const int *, \
+                                                const double *, double *, long long *,         \
+                                                cudaStream_t);                                 \
+  extern template cudaError_t launch_replay_t<N>(const CeTables &, const ReplayParams &,       \
+                                                 cudaStream_t);                                \
+  extern template cudaError_t launch_init_stats_t<N>(const CeTables &, const Replica *,        \
+                                                     ReplicaStats *, const int8_t *, int, int, \
+                                                     cudaStream_t);                            \
+  extern template cudaError_t launch_sweep_t<N, 0, SWEEP_THREADS>(                             \
+      const CeTables &, const SweepParams &, int, int, cudaStream_t);
+CEM_EXTERN(2)
+CEM_EXTERN(3)
+#define CEM_EXTERN_PITCH(P)                                                        \
+  extern template cudaError_t launch_sweep_t<2, P, SWEEP_THREADS>(const CeTables &, \
+                                                                 const SweepParams &, int, int, \
+                                                                 cudaStream_t);
+CEM_EXTERN_PITCH(14)
+CEM_EXTERN_PITCH(28)
+CEM_EXTERN_PITCH(36)
+CEM_EXTERN_PITCH(52)
+CEM_EXTERN_PITCH(64)
 
 cudaError_t launch_energy(const CeTables &T, const int8_t *occ, int L0, int L1, int L2,
                           unsigned long long *counts, cudaStream_t st) {
