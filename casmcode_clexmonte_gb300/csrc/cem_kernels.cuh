@@ -110,8 +110,7 @@ __device__ __forceinline__ FF acc_dot(const CeTables &T, const Acc<NOCC> &acc,
     if (g < T.n_orbits) {
       const int base = T.orb_func_base[g];
       if constexpr (NOCC == 2) {
-        const int dc = acc.c[g];
-        if (dc) ff_add_term(r, whi[base], wlo[base], dc);
+        ff_add_term(r, whi[base], wlo[base], acc.c[g]);  // a zero term adds exact zeros
       } else {
         const int nf = T.orb_n_funcs[g];
         for (int fl = 0; fl < nf; ++fl) {
@@ -529,7 +528,7 @@ constexpr int MAX_SWEEPS = 8;
 
 struct SweepSmem {
   // carved from dynamic shared memory; offsets in bytes
-  int occ, cl_off, lutoff, lut, whi, wlo, dmu, ax, sched, red, clist, wkept, total;
+  int occ, cl_off, lutoff, lut, whi, wlo, dmu, ax, sched, red, clist, wkept, stats, desc, total;
 };
 
 __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
@@ -566,6 +565,10 @@ __host__ __device__ inline void sweep_layout(const CeTables &T, int L0, int L1, 
   o += align16(2 * ((L0 * L1 * L2) / 8 + 32));
   s.wkept = o;  // kept candidates per warp
   o += 32 * 4;
+  s.stats = o;  // the replica's running statistics, resident for the launch
+  o += align16((int)sizeof(ReplicaStats));
+  s.desc = o;  // decoded sub-steps of the current pass
+  o += MAX_SWEEPS * n_classes_max * 80;
   s.total = o;
 }
 
@@ -586,6 +589,10 @@ struct Geo {
 // Write occupant v to core site (b,x,y,z) and all of its periodic halo images.
 __device__ __forceinline__ void put_site(int8_t *occ, const Geo &G, int b, int x, int y, int z,
                                          int8_t v) {
+  if (x >= G.R && x < G.L0 - G.R && y >= G.R && y < G.L1 - G.R && z >= G.R && z < G.L2 - G.R) {
+    occ[G.addr(b, x, y, z)] = v;  // no periodic image
+    return;
+  }
   const int xs[2] = {x, x < G.R ? x + G.L0 : (x >= G.L0 - G.R ? x - G.L0 : INT32_MIN)};
   const int ys[2] = {y, y < G.R ? y + G.L1 : (y >= G.L1 - G.R ? y - G.L1 : INT32_MIN)};
   const int zs[2] = {z, z < G.R ? z + G.L2 : (z >= G.L2 - G.R ? z - G.L2 : INT32_MIN)};
@@ -610,12 +617,27 @@ __device__ __forceinline__ bool accept_fast(const FF &d, float beta_f, float u) 
 struct FastDiv {
   int d;
   uint32_t m;
-  __device__ __forceinline__ explicit FastDiv(int dd)
-      : d(dd), m(dd > 1 ? 0xFFFFFFFFu / (uint32_t)dd + 1u : 0u) {}
+  __host__ __device__ __forceinline__ static uint32_t magic(int dd) {
+    return dd > 1 ? 0xFFFFFFFFu / (uint32_t)dd + 1u : 0u;
+  }
+  __device__ __forceinline__ explicit FastDiv(int dd) : d(dd), m(magic(dd)) {}
+  __device__ __forceinline__ FastDiv(int dd, uint32_t mm) : d(dd), m(mm) {}
   __device__ __forceinline__ int div(int n) const {
     return d > 1 ? (int)__umulhi((uint32_t)n, m) : n;
   }
 };
+
+// One sub-step of a pass, decoded once per pass by the thread that ranks its
+// class (so the serial sub-step loop only loads it).
+struct SubDesc {
+  int cb, mode, n, chunk;  // mode: 0 flips, 1 pairs inside the class, 2 neighbour swaps
+  int d0, d1, d2, bb;      // class extent per axis; sublattice of the partner site
+  int cxo, cyo, czo, g0;   // class coordinate lists; candidate grid extent along x
+  int g1, m0, m1, mpm;     // candidate grid extent along y; FastDiv magics (g0, g1, pm)
+  int par, du0, du1, du2;  // packed sub-step parameters; neighbour displacement
+};
+static_assert(sizeof(SubDesc) == 80, "SubDesc is five 16-byte words");
+static_assert(sizeof(ReplicaStats) % 8 == 0, "ReplicaStats is copied as 8-byte words");
 
 // Small counters indexed by a run-time value, kept in registers (unrolled
 // selects rather than a local-memory array).
@@ -739,8 +761,9 @@ __global__ void __launch_bounds__(THREADS, 1)
   extern __shared__ __align__(16) unsigned char smem[];
   const int rep = blockIdx.x;
   const Replica &R = P.reps[rep];
-  ReplicaStats &S = P.stats[rep];
-  const int tid = threadIdx.x, nth = blockDim.x;
+  ReplicaStats &Sg = P.stats[rep];
+  constexpr int NW = THREADS / 32;
+  const int tid = threadIdx.x, nth = THREADS;
   Geo G;
   G.L0 = R.L[0];
   G.L1 = R.L[1];
@@ -771,6 +794,13 @@ __global__ void __launch_bounds__(THREADS, 1)
   unsigned char *red = smem + lay.red;
   uint16_t *clist = reinterpret_cast<uint16_t *>(smem + lay.clist);
   int *wkept = reinterpret_cast<int *>(smem + lay.wkept);
+  ReplicaStats &S = *reinterpret_cast<ReplicaStats *>(smem + lay.stats);
+  SubDesc *sdesc = reinterpret_cast<SubDesc *>(smem + lay.desc);
+  {  // running statistics: global -> shared for the launch
+    const long long *src = reinterpret_cast<const long long *>(&Sg);
+    long long *dst = reinterpret_cast<long long *>(&S);
+    for (int q = tid; q < (int)(sizeof(ReplicaStats) / 8); q += nth) dst[q] = src[q];
+  }
   int *ax_begin[3], *ax_cnt[3], *ax_coord[3];
   for (int a = 0; a < 3; ++a) {
     ax_begin[a] = ax + a * (2 * MAX_COLOURS + MAX_L);
@@ -839,7 +869,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   __syncthreads();
 
   const SiteEval<NOCC, PITCH> ev{&T, cl_off, lutoff, lut};
-  const int lane = tid & 31, warp = tid >> 5, nwarp = nth >> 5;
+  const int lane = tid & 31, warp = tid >> 5, nwarp = NW;
   if constexpr (NOCC == 2) {
     if (P.init) {
       // exact initial state: every cluster of orbit g with all sites occupant 1
@@ -903,7 +933,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   const int n_pair_sw = P.n_pair_sweeps, n_local_sw = P.n_local_sweeps;
   const int n_sweeps = (ensemble == 1) ? n_pair_sw + n_local_sw : 1;
   const int n_sub = n_sweeps * n_classes;
-  uint32_t *skey = sched, *spar = sched + n_sub, *sord = sched + 2 * n_sub;
+  uint32_t *skey = sched, *spar = sched + n_sub;
 
   for (long long ip = 0; ip < P.n_passes; ++ip, ++pass_global) {
     const uint32_t plo = (uint32_t)pass_global, phi = (uint32_t)(pass_global >> 32) & 0xFFFFu;
@@ -922,6 +952,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       spar[e] = par;
     }
     __syncthreads();
+    // rank each class inside its sweep and decode its sub-step into that slot
     for (int e = tid; e < n_sub; e += nth) {
       const int sw = e / n_classes, c = e - sw * n_classes;
       const uint32_t key = skey[e];
@@ -930,7 +961,66 @@ __global__ void __launch_bounds__(THREADS, 1)
         const uint32_t k2 = skey[sw * n_classes + c2];
         rank += (k2 < key) || (k2 == key && c2 < c);
       }
-      sord[sw * n_classes + rank] = (uint32_t)c;
+      const uint32_t par = spar[e];
+      SubDesc D;
+      const int cb = c / ncol_all, cr = c - cb * ncol_all;
+      const int c0 = cr % ncol0, c1 = (cr / ncol0) % ncol1, c2 = cr / (ncol0 * ncol1);
+      D.cb = cb;
+      D.d0 = ax_cnt[0][c0];
+      D.d1 = ax_cnt[1][c1];
+      D.d2 = ax_cnt[2][c2];
+      D.cxo = ax_begin[0][c0];
+      D.cyo = ax_begin[1][c1];
+      D.czo = ax_begin[2][c2];
+      D.bb = cb;
+      D.par = (int)par;
+      D.du0 = D.du1 = D.du2 = 0;
+      int g0 = 1, g1 = 1, n = 0, pm = 1;
+      if (ensemble == 0) {
+        D.mode = 0;
+        g0 = D.d0;
+        g1 = D.d1;
+        n = D.d0 * D.d1 * D.d2;
+      } else if (sw < n_pair_sw) {
+        // pairs along axis pa at class distance pm: candidate grid with the
+        // pair axis halved
+        D.mode = 1;
+        if (par != 0xFFFFFFFFu) {
+          const int pa = par & 3;
+          pm = (par >> 2) & 255;
+          const int pna = pa == 0 ? D.d0 : (pa == 1 ? D.d1 : D.d2);
+          const int half = (pna / (2 * pm)) * pm;
+          g0 = pa == 0 ? half : D.d0;
+          g1 = pa == 1 ? half : D.d1;
+          n = g0 * g1 * (pa == 2 ? half : D.d2);
+        }
+      } else {
+        // every other class coordinate (parity bits) along each axis, paired
+        // with neighbour dlt
+        D.mode = 2;
+        if (T.n_nb[cb] > 0) {
+          const int parity = par & 7, dlt = (par >> 3) & 15;
+          D.bb = T.nb_b[cb][dlt];
+          D.du0 = T.nb_du[cb][dlt][0];
+          D.du1 = T.nb_du[cb][dlt][1];
+          D.du2 = T.nb_du[cb][dlt][2];
+          const int h0 = D.d0 >= 2 ? D.d0 / 2 : 1, h1 = D.d1 >= 2 ? D.d1 / 2 : 1,
+                    h2 = D.d2 >= 2 ? D.d2 / 2 : 1;
+          const bool empty = (D.d0 < 2 && (parity & 1)) || (D.d1 < 2 && (parity & 2)) ||
+                             (D.d2 < 2 && (parity & 4));
+          g0 = h0;
+          g1 = h1;
+          n = empty ? 0 : h0 * h1 * h2;
+        }
+      }
+      D.n = n;
+      D.chunk = (n + NW - 1) / NW;
+      D.g0 = g0;
+      D.g1 = g1;
+      D.m0 = (int)FastDiv::magic(g0);
+      D.m1 = (int)FastDiv::magic(g1);
+      D.mpm = (int)FastDiv::magic(pm);
+      sdesc[sw * n_classes + rank] = D;
     }
     __syncthreads();
 
@@ -940,22 +1030,17 @@ __global__ void __launch_bounds__(THREADS, 1)
     int n_prop = 0, n_acc = 0;
 
     for (int sub = 0; sub < n_sub; ++sub) {
-      const int sw = sub / n_classes;
-      const int c = (int)sord[sub];
-      const uint32_t par = spar[sw * n_classes + c];
-      const int cb = c / ncol_all, cr = c - cb * ncol_all;
-      const int c0 = cr % ncol0, c1 = (cr / ncol0) % ncol1, c2 = cr / (ncol0 * ncol1);
-      const int d0 = ax_cnt[0][c0], d1 = ax_cnt[1][c1], d2 = ax_cnt[2][c2];
-      const int *cx = ax_coord[0] + ax_begin[0][c0];
-      const int *cy = ax_coord[1] + ax_begin[1][c1];
-      const int *cz = ax_coord[2] + ax_begin[2][c2];
+      const SubDesc D = sdesc[sub];
+      const int cb = D.cb, d0 = D.d0, d1 = D.d1, d2 = D.d2;
+      const int *cx = ax_coord[0] + D.cxo;
+      const int *cy = ax_coord[1] + D.cyo;
+      const int *cz = ax_coord[2] + D.czo;
       const uint32_t ctr_sub = (uint32_t)sub;
-      if (ensemble == 0) {
+      const FastDiv fe0(D.g0, (uint32_t)D.m0), fe1(D.g1, (uint32_t)D.m1);
+      if (D.mode == 0) {
         // ---------------- flips of every site of the class
-        const int n = d0 * d1 * d2;
-        const FastDiv f0(d0), f1(d1);
-        for (int q = tid; q < n; q += nth) {
-          const int t = f0.div(q), iz = f1.div(t);
+        for (int q = tid; q < D.n; q += nth) {
+          const int t = fe0.div(q), iz = fe1.div(t);
           const int ix = q - t * d0, iy = t - iz * d1;
           const int x = cx[ix], y = cy[iy], z = cz[iz];
           const int ad = G.addr(cb, x, y, z);
@@ -985,57 +1070,26 @@ __global__ void __launch_bounds__(THREADS, 1)
           }
         }
       } else {
-        // ---------------- canonical swaps: pairs inside the class (pair
-        // sweeps) or a site with a neighbour (local sweeps, sequential dE).
+        // ---------------- canonical swaps: pairs inside the class (mode 1)
+        // or a site with a neighbour (mode 2, sequential dE).
         // Phase A: each warp scans a contiguous chunk of candidate pairs and
         // keeps, in order, those whose occupants differ (the only proposals);
         // phase B spreads the kept pairs evenly over the block. The kept
         // order and the pair -> thread map depend only on the occupations,
         // so runs stay deterministic.
-        const bool local = sw >= n_pair_sw;
-        int n = 0;
-        // pair sweeps: pairs along axis pa at class distance pm, rotated by
-        // prot; candidate grid e0 x e1 x e2 (the pair axis halved)
-        int pa = 0, pm = 1, prot = 0, pna = 1, e0 = 1, e1 = 1;
-        // local sweeps: every other class coordinate (parity bits) along
-        // each axis, rotated, paired with neighbour (nb_b, du)
-        int parity = 0, nb_b = cb, h0 = 1, h1 = 1, h2 = 1, r0 = 0, r1 = 0, r2 = 0;
-        int du0 = 0, du1 = 0, du2 = 0;
-        if (!local) {
-          if (par != 0xFFFFFFFFu) {
-            pa = par & 3;
-            pm = (par >> 2) & 255;
-            prot = par >> 10;
-            pna = pa == 0 ? d0 : (pa == 1 ? d1 : d2);
-            const int half = (pna / (2 * pm)) * pm;
-            e0 = pa == 0 ? half : d0;
-            e1 = pa == 1 ? half : d1;
-            const int e2 = pa == 2 ? half : d2;
-            n = e0 * e1 * e2;
-          }
-        } else if (T.n_nb[cb] > 0) {
-          parity = par & 7;
-          const int dlt = (par >> 3) & 15;
-          r0 = (int)((par >> 7) & 127);
-          r1 = (int)((par >> 14) & 127);
-          r2 = (int)((par >> 21) & 127);
-          nb_b = T.nb_b[cb][dlt];
-          du0 = T.nb_du[cb][dlt][0];
-          du1 = T.nb_du[cb][dlt][1];
-          du2 = T.nb_du[cb][dlt][2];
-          h0 = d0 >= 2 ? d0 / 2 : 1;
-          h1 = d1 >= 2 ? d1 / 2 : 1;
-          h2 = d2 >= 2 ? d2 / 2 : 1;
-          const bool empty = (d0 < 2 && (parity & 1)) || (d1 < 2 && (parity & 2)) ||
-                             (d2 < 2 && (parity & 4));
-          n = empty ? 0 : h0 * h1 * h2;
-        }
-        const int bb = local ? nb_b : cb;
-        const FastDiv fe0(local ? h0 : e0), fe1(local ? h1 : e1), fpm(pm);
+        const bool local = D.mode == 2;
+        const uint32_t par = (uint32_t)D.par;
+        const int bb = D.bb, chunk = D.chunk, n = D.n;
+        const int pa = par & 3, pm = (par >> 2) & 255, prot = (int)(par >> 10);
+        const int pna = pa == 0 ? d0 : (pa == 1 ? d1 : d2);
+        const int parity = par & 7;
+        const int r0 = (int)((par >> 7) & 127), r1 = (int)((par >> 14) & 127),
+                  r2 = (int)((par >> 21) & 127);
+        const FastDiv fpm(pm, (uint32_t)D.mpm);
         auto wrap_lt2 = [](int v, int L) { return v >= L ? v - L : v; };  // v < 2L
         auto sites_of = [&](int q, int &xa, int &ya, int &za, int &xb, int &yb, int &zb) {
           const int t = fe0.div(q), i2 = fe1.div(t);
-          const int i0 = q - t * fe0.d, i1 = t - i2 * (int)fe1.d;
+          const int i0 = q - t * fe0.d, i1 = t - i2 * fe1.d;
           if (!local) {
             const int jj = pa == 0 ? i0 : (pa == 1 ? i1 : i2);
             const int jq = fpm.div(jj);
@@ -1051,13 +1105,12 @@ __global__ void __launch_bounds__(THREADS, 1)
             xa = cx[d0 >= 2 ? wrap_lt2(r0 + (parity & 1) + 2 * i0, d0) : 0];
             ya = cy[d1 >= 2 ? wrap_lt2(r1 + ((parity >> 1) & 1) + 2 * i1, d1) : 0];
             za = cz[d2 >= 2 ? wrap_lt2(r2 + ((parity >> 2) & 1) + 2 * i2, d2) : 0];
-            xb = wrapc(xa + du0, G.L0);
-            yb = wrapc(ya + du1, G.L1);
-            zb = wrapc(za + du2, G.L2);
+            xb = wrapc(xa + D.du0, G.L0);
+            yb = wrapc(ya + D.du1, G.L1);
+            zb = wrapc(za + D.du2, G.L2);
           }
         };
         // phase A: ordered per-warp compaction of the proposals
-        const int chunk = (n + nwarp - 1) / nwarp;
         const int q_begin = warp * chunk;
         const int q_end = min(n, q_begin + chunk);
         int kept = 0;
@@ -1077,14 +1130,20 @@ __global__ void __launch_bounds__(THREADS, 1)
         __syncthreads();
         // phase B: proposal i of the block goes to thread i mod block size
         int total = 0;
-        for (int w = 0; w < nwarp; ++w) total += wkept[w];
+#pragma unroll
+        for (int w = 0; w < NW; ++w) total += wkept[w];
         for (int i = tid; i < total; i += nth) {
-          int w = 0, base = 0;
-          while (base + wkept[w] <= i) {
-            base += wkept[w];
-            ++w;
+          int wsel = 0, bsel = 0, run = 0;
+#pragma unroll
+          for (int w = 0; w < NW; ++w) {  // last warp whose kept range starts at or before i
+            const int k = wkept[w];
+            if (i >= run) {
+              wsel = w;
+              bsel = run;
+            }
+            run += k;
           }
-          const int q = clist[w * chunk + (i - base)];
+          const int q = clist[wsel * chunk + (i - bsel)];
           int xa, ya, za, xb, yb, zb;
           sites_of(q, xa, ya, za, xb, yb, zb);
           const int ada = G.addr(cb, xa, ya, za), adb = G.addr(bb, xb, yb, zb);
@@ -1115,20 +1174,24 @@ __global__ void __launch_bounds__(THREADS, 1)
       __syncthreads();
     }
 
-    // ---- end of pass: reduce, sample
+    // ---- end of pass: reduce (32-bit per-pass counters), sample
     {
-      // slots: 0 proposals, 1 accepts, 2..2+NOCC species, 8..15 energy terms
-      long long vals[16];
+      // slots: 0 proposals, 1 accepts, 2..2+NOCC species, 4..7 sublattice
+      // counts (binary FCC), 8..15 energy terms (binary); double slot: dE sum
+      int vals[16];
+#pragma unroll
       for (int k = 0; k < 16; ++k) vals[k] = 0;
       vals[0] = n_prop;
       vals[1] = n_acc;
 #pragma unroll
       for (int a = 0; a < NOCC; ++a) vals[2 + a] = dspec.v[a];
-      if constexpr (PITCH > 0)
+      if constexpr (PITCH > 0) {
 #pragma unroll
         for (int k = 0; k < 4; ++k) vals[4 + k] = dsub.v[k];
+      }
       double dsum = 0.0;
       if constexpr (NOCC == 2) {
+#pragma unroll
         for (int g = 0; g < MAX_ORBITS; ++g) vals[8 + g] = eacc.dc[g];
       } else {
         dsum = eacc.de;
@@ -1136,70 +1199,75 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
       for (int k = 0; k < 16; ++k)
         for (int off = 16; off; off >>= 1) vals[k] += __shfl_xor_sync(0xffffffffu, vals[k], off);
-      for (int off = 16; off; off >>= 1) dsum += __shfl_xor_sync(0xffffffffu, dsum, off);
-      long long *rd_l = reinterpret_cast<long long *>(red);
+      if constexpr (NOCC != 2)
+        for (int off = 16; off; off >>= 1) dsum += __shfl_xor_sync(0xffffffffu, dsum, off);
+      int *rd_i = reinterpret_cast<int *>(red);                   // [NW][16]
+      double *rd_d = reinterpret_cast<double *>(red + NW * 64);  // [NW]
       if (lane == 0) {
-        for (int k = 0; k < 15; ++k) rd_l[warp * 16 + k] = vals[k];
-        reinterpret_cast<double *>(rd_l)[warp * 16 + 15] = dsum;
-        if constexpr (NOCC == 2) rd_l[warp * 16 + 15] = vals[15];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) rd_i[warp * 16 + k] = vals[k];
+        rd_d[warp] = dsum;
       }
       __syncthreads();
-      if (tid == 0) {
+      if (warp == 0) {
+        // lane k < 16 sums slot k over the warps; lane 16 sums the dE slot in
+        // warp order
+        long long v = 0;
+        double dv = 0.0;
+        if (lane < 16)
+          for (int w = 0; w < NW; ++w) v += rd_i[w * 16 + lane];
+        if (lane == 16)
+          for (int w = 0; w < NW; ++w) dv += rd_d[w];
         long long tot[16];
-        double dtot = 0.0;
-        for (int k = 0; k < 16; ++k) tot[k] = 0;
-        for (int w = 0; w < nwarp; ++w) {
-          for (int k = 0; k < 15; ++k) tot[k] += rd_l[w * 16 + k];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) tot[k] = __shfl_sync(0xffffffffu, v, k);
+        double dtot = __shfl_sync(0xffffffffu, dv, 16);
+        if (lane == 0) {
           if constexpr (NOCC == 2) {
-            tot[15] += rd_l[w * 16 + 15];
-          } else {
-            dtot += reinterpret_cast<double *>(rd_l)[w * 16 + 15];
+            dtot = 0.0;
+            for (int g = 0; g < T.n_orbits; ++g)
+              dtot += T.w[T.orb_func_base[g]] * (double)tot[8 + g];
           }
-        }
-        if constexpr (NOCC == 2) {
-          for (int g = 0; g < T.n_orbits; ++g)
-            dtot += T.w[T.orb_func_base[g]] * (double)tot[8 + g];
-        }
-        energy += dtot;
-        S.n_proposed += tot[0];
-        S.n_accepted += tot[1];
-        for (int a = 0; a < NOCC; ++a) nspec[a] += tot[2 + a];
-        double op = 0.0;
-        if constexpr (PITCH > 0) {
-          for (int k = 0; k < 4; ++k) nsub[k] += tot[4 + k];
-          const double xb = (double)nspec[1] / n_sites;
-          for (int k = 0; k < 4; ++k) {
-            const double c = (double)nsub[k] / (0.25 * n_sites) - xb;
-            op += c * c;
+          energy += dtot;
+          S.n_proposed += tot[0];
+          S.n_accepted += tot[1];
+          for (int a = 0; a < NOCC; ++a) nspec[a] += tot[2 + a];
+          double op = 0.0;
+          if constexpr (PITCH > 0) {
+            for (int k = 0; k < 4; ++k) nsub[k] += tot[4 + k];
+            const double xb = (double)nspec[1] / n_sites;
+            for (int k = 0; k < 4; ++k) {
+              const double c = (double)nsub[k] / (0.25 * n_sites) - xb;
+              op += c * c;
+            }
+            op = sqrt(op);
           }
-          op = sqrt(op);
-        }
-        // param composition per unit cell and potential per unit cell
-        double x[3] = {0.0, 0.0, 0.0}, ef, ep;
-        sample_values<NOCC>(P.RT, R.mu, nspec, n_sites, n_uc, energy, x, ef, ep);
-        if (ip >= P.n_equil) {
-          S.n_samples += 1.0;
-          S.sum_e += ep;
-          S.sum_e2 += ep * ep;
-          S.sum_f += ef;
-          for (int k = 0; k < NOCC - 1; ++k) {
-            S.sum_x[k] += x[k];
-            S.sum_ex[k] += ep * x[k];
-            for (int k2 = 0; k2 < NOCC - 1; ++k2) S.sum_xx[k * 3 + k2] += x[k] * x[k2];
-          }
-          if (P.samples) {
-            const long long si = (long long)(S.n_samples) - 1;
-            if (si < P.sample_capacity) {
-              double *out = P.samples + (long long)rep * P.sample_capacity * P.sample_width +
-                            si * P.sample_width;
-              out[0] = ep;
-              for (int k = 0; k < NOCC - 1; ++k) out[1 + k] = x[k];
-              out[NOCC] = op;
+          // param composition per unit cell and potential per unit cell
+          double x[3] = {0.0, 0.0, 0.0}, ef, ep;
+          sample_values<NOCC>(P.RT, R.mu, nspec, n_sites, n_uc, energy, x, ef, ep);
+          if (ip >= P.n_equil) {
+            S.n_samples += 1.0;
+            S.sum_e += ep;
+            S.sum_e2 += ep * ep;
+            S.sum_f += ef;
+            for (int k = 0; k < NOCC - 1; ++k) {
+              S.sum_x[k] += x[k];
+              S.sum_ex[k] += ep * x[k];
+              for (int k2 = 0; k2 < NOCC - 1; ++k2) S.sum_xx[k * 3 + k2] += x[k] * x[k2];
+            }
+            if (P.samples) {
+              const long long si = (long long)(S.n_samples) - 1;
+              if (si < P.sample_capacity) {
+                double *out = P.samples + (long long)rep * P.sample_capacity * P.sample_width +
+                              si * P.sample_width;
+                out[0] = ep;
+                for (int k = 0; k < NOCC - 1; ++k) out[1 + k] = x[k];
+                out[NOCC] = op;
+              }
             }
           }
         }
       }
-      __syncthreads();
     }
   }
   // ---- write back
@@ -1213,6 +1281,12 @@ __global__ void __launch_bounds__(THREADS, 1)
     for (int a = 0; a < NOCC; ++a) S.n_species[a] = nspec[a];
     for (int k = 0; k < 4; ++k) S.n_sub[k] = nsub[k];
     S.pass = pass_global;
+  }
+  __syncthreads();
+  {
+    const long long *src = reinterpret_cast<const long long *>(&S);
+    long long *dst = reinterpret_cast<long long *>(&Sg);
+    for (int q = tid; q < (int)(sizeof(ReplicaStats) / 8); q += nth) dst[q] = src[q];
   }
 }
 
