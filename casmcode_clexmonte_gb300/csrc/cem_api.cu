@@ -370,6 +370,44 @@ int cem_system_create(const cem_system_desc *d, cem_system **out) {
       wlo[f] = (float)(s->w[f] - (double)whi[f]);
     }
     s->RT.assign(d->param_RT, d->param_RT + (d->n_occ - 1) * d->n_occ);
+    // binary sweep weights: integer multiples of a power-of-two quantum plus
+    // an f32 remainder, so the sweep's energy change is an exact int32 sum
+    // plus one f32 FMA chain
+    for (int g = 0; g < MAX_ORBITS; ++g) {
+      T.wq[g] = 0;
+      T.wr[g] = 0.f;
+    }
+    T.wq_scale = 1.f;
+    if (d->n_occ == 2) {
+      double wmax = 0.0;
+      long long dcmax[MAX_ORBITS] = {0};
+      for (int g = 0; g < T.n_orbits; ++g) {
+        wmax = std::max(wmax, std::fabs(s->w[T.orb_func_base[g]]));
+        for (int b = 0; b < T.n_sublat; ++b)
+          dcmax[g] = std::max<long long>(dcmax[g], 2 * (T.fl_begin[b][g + 1] - T.fl_begin[b][g]));
+      }
+      if (wmax > 0.0) {
+        for (int bits = 13; bits >= 0; --bits) {
+          const double q = std::ldexp(1.0, std::ilogb(wmax) - bits);
+          long long bound = 0;
+          long long A[MAX_ORBITS] = {0};
+          for (int g = 0; g < T.n_orbits; ++g) {
+            A[g] = std::llround(s->w[T.orb_func_base[g]] / q);
+            bound += std::llabs(A[g]) * dcmax[g];
+          }
+          if (bound < (1ll << 24) || bits == 0) {
+            require(bound < (1ll << 24), "cluster expansion too large for the binary sweep weights",
+                    CEM_ERR_UNSUPPORTED);
+            T.wq_scale = (float)q;
+            for (int g = 0; g < T.n_orbits; ++g) {
+              T.wq[g] = (int)A[g];
+              T.wr[g] = (float)(s->w[T.orb_func_base[g]] - (double)A[g] * q);
+            }
+            break;
+          }
+        }
+      }
+    }
     int *dpb = dev_copy(pb), *ddu = dev_copy(du), *dlo = dev_copy(lutoff);
     uint8_t *dlut = dev_copy(lut);
     float *dwhi = dev_copy(whi), *dwlo = dev_copy(wlo);

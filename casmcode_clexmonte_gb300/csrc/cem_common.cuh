@@ -57,6 +57,12 @@ struct CeTables {
   const float *w_hi;     // [n_funcs]
   const float *w_lo;     // [n_funcs]
   const double *w;       // [n_funcs]; w[0] = ECI of the empty cluster
+  // binary systems (one function per orbit): w[orbit function] = wq * wq_scale
+  // + wr, wq integer, wq_scale a power of two chosen so that sum_g wq * dC
+  // stays below 2^24 in magnitude; zero for padding orbits and other systems
+  int wq[MAX_ORBITS];
+  float wr[MAX_ORBITS];
+  float wq_scale;
   // owned clusters use index n_fl + i in the cl_* arrays
 };
 

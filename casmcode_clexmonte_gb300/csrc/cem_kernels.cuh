@@ -533,6 +533,10 @@ struct SweepSmem {
 
 __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 
+__host__ __device__ inline int clist_capacity(int L0, int L1, int L2) {
+  return (L0 * L1 * L2) / 8 + 32;
+}
+
 // pitch > 0: fixed x/y pitch of the generated evaluator; 0: L + 2 reach
 __host__ __device__ inline void sweep_layout(const CeTables &T, int L0, int L1, int L2,
                                              int n_classes_max, int pitch, SweepSmem &s) {
@@ -561,10 +565,10 @@ __host__ __device__ inline void sweep_layout(const CeTables &T, int L0, int L1, 
   o += align16(3 * MAX_SWEEPS * n_classes_max * 4);
   s.red = o;  // block reduction scratch: 32 warps x 16 slots of 8 bytes
   o += 32 * 16 * 8;
-  s.clist = o;  // kept canonical candidates (u16): a class holds <= n_uc / 8 sites
-  o += align16(2 * ((L0 * L1 * L2) / 8 + 32));
-  s.wkept = o;  // kept candidates per warp
-  o += 32 * 4;
+  s.clist = o;  // kept canonical candidates (u16), two buffers: a class holds <= n_uc / 8 sites
+  o += 2 * align16(2 * clist_capacity(L0, L1, L2));
+  s.wkept = o;  // kept candidates per warp, two buffers
+  o += 2 * 32 * 4;
   s.stats = o;  // the replica's running statistics, resident for the launch
   o += align16((int)sizeof(ReplicaStats));
   s.desc = o;  // decoded sub-steps of the current pass
@@ -603,8 +607,32 @@ __device__ __forceinline__ void put_site(int8_t *occ, const Geo &G, int b, int x
   }
 }
 
-__device__ __forceinline__ bool accept_fast(const FF &d, float beta_f, float u) {
-  const float de = FADD(d.s, d.e);
+// Energy change of a sweep proposal (f32, minus the chemical potential term
+// mu_hi + mu_lo). Binary systems: exact int32 sum of wq * dC scaled by the
+// power-of-two quantum, plus the f32 remainder terms (one FMA chain); other
+// systems: float-float dot, also returned in d for the FP64 bookkeeping.
+template <int NOCC>
+__device__ __forceinline__ float sweep_de(const CeTables &T, const Acc<NOCC> &acc,
+                                          const float *whi, const float *wlo, float mu_hi,
+                                          float mu_lo, FF &d) {
+  if constexpr (NOCC == 2) {
+    int n = 0;
+    float r = 0.f;
+#pragma unroll
+    for (int g = 0; g < MAX_ORBITS; ++g) {
+      n += T.wq[g] * acc.c[g];
+      r = FFMA(T.wr[g], (float)acc.c[g], r);
+    }
+    d = FF{0.f, 0.f};
+    return FADD(FADD(FFMA((float)n, T.wq_scale, r), -mu_hi), -mu_lo);
+  } else {
+    d = acc_dot<NOCC>(T, acc, whi, wlo);
+    ff_add_ff(d, -mu_hi, -mu_lo);
+    return FADD(d.s, d.e);
+  }
+}
+
+__device__ __forceinline__ bool accept_de(float de, float beta_f, float u) {
   if (de < 0.f) return true;
   return u < cem_expf_neg(FMUL(-beta_f, de));
 }
@@ -755,6 +783,76 @@ struct EnergyAcc<2> {
   }
 };
 
+// Candidate pairs of a canonical sub-step: pairs inside the class along axis
+// pa at class distance pm, rotated by prot (mode 1), or every other class
+// coordinate (parity bits, rotations r0..r2) paired with the neighbour
+// (bb, du) (mode 2). Candidate q indexes a g0 x g1 x g2 grid.
+struct PairGeom {
+  const int *cx, *cy, *cz;
+  int cb, bb, d0, d1, d2, pa, pm, prot, pna, parity, r0, r1, r2, du0, du1, du2;
+  bool local;
+  FastDiv fe0, fe1, fpm;
+  __device__ __forceinline__ PairGeom(const SubDesc &D, int *const *ax_coord)
+      : cx(ax_coord[0] + D.cxo), cy(ax_coord[1] + D.cyo), cz(ax_coord[2] + D.czo), cb(D.cb),
+        bb(D.bb), d0(D.d0), d1(D.d1), d2(D.d2), pa(D.par & 3), pm(((uint32_t)D.par >> 2) & 255),
+        prot((int)((uint32_t)D.par >> 10)), pna(0), parity(D.par & 7),
+        r0((int)(((uint32_t)D.par >> 7) & 127)), r1((int)(((uint32_t)D.par >> 14) & 127)),
+        r2((int)(((uint32_t)D.par >> 21) & 127)), du0(D.du0), du1(D.du1), du2(D.du2),
+        local(D.mode == 2), fe0(D.g0, (uint32_t)D.m0), fe1(D.g1, (uint32_t)D.m1),
+        fpm(pm, (uint32_t)D.mpm) {
+    pna = pa == 0 ? d0 : (pa == 1 ? d1 : d2);
+  }
+  __device__ __forceinline__ void sites(int q, const Geo &G, int &xa, int &ya, int &za, int &xb,
+                                        int &yb, int &zb) const {
+    auto wrap_lt2 = [](int v, int L) { return v >= L ? v - L : v; };  // v < 2L
+    const int t = fe0.div(q), i2 = fe1.div(t);
+    const int i0 = q - t * fe0.d, i1 = t - i2 * fe1.d;
+    if (!local) {
+      const int jj = pa == 0 ? i0 : (pa == 1 ? i1 : i2);
+      const int jq = fpm.div(jj);
+      const int u = 2 * pm * jq + (jj - jq * pm);
+      const int ja = wrap_lt2(u + prot, pna), jb = wrap_lt2(u + pm + prot, pna);
+      xa = cx[pa == 0 ? ja : i0];
+      xb = cx[pa == 0 ? jb : i0];
+      ya = cy[pa == 1 ? ja : i1];
+      yb = cy[pa == 1 ? jb : i1];
+      za = cz[pa == 2 ? ja : i2];
+      zb = cz[pa == 2 ? jb : i2];
+    } else {
+      xa = cx[d0 >= 2 ? wrap_lt2(r0 + (parity & 1) + 2 * i0, d0) : 0];
+      ya = cy[d1 >= 2 ? wrap_lt2(r1 + ((parity >> 1) & 1) + 2 * i1, d1) : 0];
+      za = cz[d2 >= 2 ? wrap_lt2(r2 + ((parity >> 2) & 1) + 2 * i2, d2) : 0];
+      xb = wrapc(xa + du0, G.L0);
+      yb = wrapc(ya + du1, G.L1);
+      zb = wrapc(za + du2, G.L2);
+    }
+  }
+};
+
+// Phase A of a canonical sub-step: warp w scans candidates [w chunk,
+// (w + 1) chunk) and keeps, in order, those whose two occupants differ (the
+// only proposals) in cl[w chunk ...]; wk[w] = number kept.
+__device__ __forceinline__ void compact_pairs(const PairGeom &pg, const Geo &G, const int8_t *occ,
+                                              int n, int chunk, int warp, int lane, uint16_t *cl,
+                                              int *wk) {
+  const int q_begin = warp * chunk;
+  const int q_end = min(n, q_begin + chunk);
+  int kept = 0;
+  for (int q0 = q_begin; q0 < q_end; q0 += 32) {
+    const int q = q0 + lane;
+    bool act = false;
+    if (q < q_end) {
+      int xa, ya, za, xb, yb, zb;
+      pg.sites(q, G, xa, ya, za, xb, yb, zb);
+      act = occ[G.addr(pg.cb, xa, ya, za)] != occ[G.addr(pg.bb, xb, yb, zb)];
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, act);
+    if (act) cl[q_begin + kept + __popc(m & ((1u << lane) - 1u))] = (uint16_t)q;
+    kept += __popc(m);
+  }
+  if (lane == 0) wk[warp] = kept;
+}
+
 template <int NOCC, int PITCH, int THREADS = SWEEP_THREADS>
 __global__ void __launch_bounds__(THREADS, 1)
     k_sweep(const __grid_constant__ CeTables T, const __grid_constant__ SweepParams P) {
@@ -794,6 +892,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   unsigned char *red = smem + lay.red;
   uint16_t *clist = reinterpret_cast<uint16_t *>(smem + lay.clist);
   int *wkept = reinterpret_cast<int *>(smem + lay.wkept);
+  const int clist_cap = align16(2 * clist_capacity(G.L0, G.L1, G.L2)) / 2;
   ReplicaStats &S = *reinterpret_cast<ReplicaStats *>(smem + lay.stats);
   SubDesc *sdesc = reinterpret_cast<SubDesc *>(smem + lay.desc);
   {  // running statistics: global -> shared for the launch
@@ -1028,10 +1127,11 @@ __global__ void __launch_bounds__(THREADS, 1)
     RegCounts<NOCC> dspec;
     RegCounts<4> dsub;  // binary FCC only (PITCH > 0)
     int n_prop = 0, n_acc = 0;
+    int a_buf = -1;  // clist buffer already holding this sub-step's phase A
 
     for (int sub = 0; sub < n_sub; ++sub) {
       const SubDesc D = sdesc[sub];
-      const int cb = D.cb, d0 = D.d0, d1 = D.d1, d2 = D.d2;
+      const int cb = D.cb, d0 = D.d0, d1 = D.d1;
       const int *cx = ax_coord[0] + D.cxo;
       const int *cy = ax_coord[1] + D.cyo;
       const int *cz = ax_coord[2] + D.czo;
@@ -1057,10 +1157,11 @@ __global__ void __launch_bounds__(THREADS, 1)
           Acc<NOCC> acc;
           acc.zero();
           ev.add(cb, o_i, o_f, occ, ad, acc);
-          FF d = acc_dot<NOCC>(T, acc, whi, wlo);
-          ff_add_ff(d, -dmu_hi[o_i * NOCC + o_f], -dmu_lo[o_i * NOCC + o_f]);
+          FF d;
+          const float de = sweep_de<NOCC>(T, acc, whi, wlo, dmu_hi[o_i * NOCC + o_f],
+                                          dmu_lo[o_i * NOCC + o_f], d);
           ++n_prop;
-          if (accept_fast(d, beta_f, u24(r.x))) {
+          if (accept_de(de, beta_f, u24(r.x))) {
             ++n_acc;
             put_site(occ, G, cb, x, y, z, (int8_t)o_f);
             eacc.add(acc, d, R.dmu[o_i * NOCC + o_f]);
@@ -1072,80 +1173,40 @@ __global__ void __launch_bounds__(THREADS, 1)
       } else {
         // ---------------- canonical swaps: pairs inside the class (mode 1)
         // or a site with a neighbour (mode 2, sequential dE).
-        // Phase A: each warp scans a contiguous chunk of candidate pairs and
-        // keeps, in order, those whose occupants differ (the only proposals);
-        // phase B spreads the kept pairs evenly over the block. The kept
-        // order and the pair -> thread map depend only on the occupations,
-        // so runs stay deterministic.
-        const bool local = D.mode == 2;
-        const uint32_t par = (uint32_t)D.par;
-        const int bb = D.bb, chunk = D.chunk, n = D.n;
-        const int pa = par & 3, pm = (par >> 2) & 255, prot = (int)(par >> 10);
-        const int pna = pa == 0 ? d0 : (pa == 1 ? d1 : d2);
-        const int parity = par & 7;
-        const int r0 = (int)((par >> 7) & 127), r1 = (int)((par >> 14) & 127),
-                  r2 = (int)((par >> 21) & 127);
-        const FastDiv fpm(pm, (uint32_t)D.mpm);
-        auto wrap_lt2 = [](int v, int L) { return v >= L ? v - L : v; };  // v < 2L
-        auto sites_of = [&](int q, int &xa, int &ya, int &za, int &xb, int &yb, int &zb) {
-          const int t = fe0.div(q), i2 = fe1.div(t);
-          const int i0 = q - t * fe0.d, i1 = t - i2 * fe1.d;
-          if (!local) {
-            const int jj = pa == 0 ? i0 : (pa == 1 ? i1 : i2);
-            const int jq = fpm.div(jj);
-            const int u = 2 * pm * jq + (jj - jq * pm);
-            const int ja = wrap_lt2(u + prot, pna), jb = wrap_lt2(u + pm + prot, pna);
-            xa = cx[pa == 0 ? ja : i0];
-            xb = cx[pa == 0 ? jb : i0];
-            ya = cy[pa == 1 ? ja : i1];
-            yb = cy[pa == 1 ? jb : i1];
-            za = cz[pa == 2 ? ja : i2];
-            zb = cz[pa == 2 ? jb : i2];
-          } else {
-            xa = cx[d0 >= 2 ? wrap_lt2(r0 + (parity & 1) + 2 * i0, d0) : 0];
-            ya = cy[d1 >= 2 ? wrap_lt2(r1 + ((parity >> 1) & 1) + 2 * i1, d1) : 0];
-            za = cz[d2 >= 2 ? wrap_lt2(r2 + ((parity >> 2) & 1) + 2 * i2, d2) : 0];
-            xb = wrapc(xa + D.du0, G.L0);
-            yb = wrapc(ya + D.du1, G.L1);
-            zb = wrapc(za + D.du2, G.L2);
-          }
-        };
-        // phase A: ordered per-warp compaction of the proposals
-        const int q_begin = warp * chunk;
-        const int q_end = min(n, q_begin + chunk);
-        int kept = 0;
-        for (int q0 = q_begin; q0 < q_end; q0 += 32) {
-          const int q = q0 + lane;
-          bool act = false;
-          if (q < q_end) {
-            int xa, ya, za, xb, yb, zb;
-            sites_of(q, xa, ya, za, xb, yb, zb);
-            act = occ[G.addr(cb, xa, ya, za)] != occ[G.addr(bb, xb, yb, zb)];
-          }
-          const unsigned m = __ballot_sync(0xffffffffu, act);
-          if (act) clist[q_begin + kept + __popc(m & ((1u << lane) - 1u))] = (uint16_t)q;
-          kept += __popc(m);
+        // Phase A compacts the candidate pairs whose occupants differ (the
+        // only proposals); phase B spreads them evenly over the block. The
+        // kept order and the pair -> thread map depend only on the
+        // occupations, so runs stay deterministic. Phase A of a pair sub-step
+        // that follows a pair sub-step on another class runs at the end of
+        // the previous phase B: it reads only its own class's sites, which
+        // that phase B does not write.
+        const PairGeom pg(D, ax_coord);
+        const int buf = sub & 1, chunk = D.chunk;
+        uint16_t *cl = clist + buf * clist_cap;
+        int *wk = wkept + buf * 32;
+        if (a_buf != buf) {
+          compact_pairs(pg, G, occ, D.n, chunk, warp, lane, cl, wk);
+          __syncthreads();
         }
-        if (lane == 0) wkept[warp] = kept;
-        __syncthreads();
-        // phase B: proposal i of the block goes to thread i mod block size
+        const bool local = pg.local;
+        const int bb = pg.bb;
         int total = 0;
 #pragma unroll
-        for (int w = 0; w < NW; ++w) total += wkept[w];
+        for (int w = 0; w < NW; ++w) total += wk[w];
         for (int i = tid; i < total; i += nth) {
           int wsel = 0, bsel = 0, run = 0;
 #pragma unroll
           for (int w = 0; w < NW; ++w) {  // last warp whose kept range starts at or before i
-            const int k = wkept[w];
+            const int k = wk[w];
             if (i >= run) {
               wsel = w;
               bsel = run;
             }
             run += k;
           }
-          const int q = clist[wsel * chunk + (i - bsel)];
+          const int q = cl[wsel * chunk + (i - bsel)];
           int xa, ya, za, xb, yb, zb;
-          sites_of(q, xa, ya, za, xb, yb, zb);
+          pg.sites(q, G, xa, ya, za, xb, yb, zb);
           const int ada = G.addr(cb, xa, ya, za), adb = G.addr(bb, xb, yb, zb);
           const int oa = occ[ada], ob = occ[adb];
           const int la = cb * n_uc + xa + G.L0 * (ya + G.L1 * za);
@@ -1155,9 +1216,10 @@ __global__ void __launch_bounds__(THREADS, 1)
           ev.add(cb, oa, ob, occ, ada, acc);
           if (local) put_site(occ, G, cb, xa, ya, za, (int8_t)ob);  // first change applied
           ev.add(bb, ob, oa, occ, adb, acc);
-          const FF d = acc_dot<NOCC>(T, acc, whi, wlo);
+          FF d;
+          const float de = sweep_de<NOCC>(T, acc, whi, wlo, 0.f, 0.f, d);
           ++n_prop;
-          if (accept_fast(d, beta_f, u24(r.x))) {
+          if (accept_de(de, beta_f, u24(r.x))) {
             ++n_acc;
             if (!local) put_site(occ, G, cb, xa, ya, za, (int8_t)ob);
             put_site(occ, G, bb, xb, yb, zb, (int8_t)oa);
@@ -1168,6 +1230,17 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
           } else if (local) {
             put_site(occ, G, cb, xa, ya, za, (int8_t)oa);
+          }
+        }
+        a_buf = -1;
+        if (D.mode == 1 && sub + 1 < n_sub) {
+          const SubDesc Dn = sdesc[sub + 1];
+          if (Dn.mode == 1 &&
+              (Dn.cb != D.cb || Dn.cxo != D.cxo || Dn.cyo != D.cyo || Dn.czo != D.czo)) {
+            const PairGeom pn(Dn, ax_coord);
+            compact_pairs(pn, G, occ, Dn.n, Dn.chunk, warp, lane, clist + (buf ^ 1) * clist_cap,
+                          wkept + (buf ^ 1) * 32);
+            a_buf = buf ^ 1;
           }
         }
       }

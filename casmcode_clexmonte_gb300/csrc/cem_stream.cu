@@ -117,10 +117,10 @@ __global__ void __launch_bounds__(256) k_stream_sub(const __grid_constant__ CeTa
       Acc<2> acc;
       acc.zero();
       ev.add(0, o_i, o_f, occ, ad, acc);
-      FF d = acc_dot<2>(T, acc, whi, wlo);
-      ff_add_ff(d, -R.dmu_hi[o_i * 2 + o_f], -R.dmu_lo[o_i * 2 + o_f]);
+      FF d;
+      const float de = sweep_de<2>(T, acc, whi, wlo, R.dmu_hi[o_i * 2 + o_f], R.dmu_lo[o_i * 2 + o_f], d);
       ++n_prop;
-      if (accept_fast(d, beta_f, u24(r.x))) {
+      if (accept_de(de, beta_f, u24(r.x))) {
         ++n_acc;
         put_site(occ, G, 0, x, y, z, (int8_t)o_f);
         eacc.add(acc, d, 0.0);
@@ -154,9 +154,10 @@ __global__ void __launch_bounds__(256) k_stream_sub(const __grid_constant__ CeTa
         acc.zero();
         ev.add(0, oa, ob, occ, ada, acc);
         ev.add(0, ob, oa, occ, adb, acc);
-        const FF d = acc_dot<2>(T, acc, whi, wlo);
+        FF d;
+        const float de = sweep_de<2>(T, acc, whi, wlo, 0.f, 0.f, d);
         ++n_prop;
-        if (accept_fast(d, beta_f, u24(r.x))) {
+        if (accept_de(de, beta_f, u24(r.x))) {
           ++n_acc;
           put_site(occ, G, 0, xa, ya, za, (int8_t)ob);
           put_site(occ, G, 0, xb, yb, zb, (int8_t)oa);
@@ -188,9 +189,10 @@ __global__ void __launch_bounds__(256) k_stream_sub(const __grid_constant__ CeTa
         ev.add(0, oa, ob, occ, ada, acc);
         put_site(occ, G, 0, xa, ya, za, (int8_t)ob);
         ev.add(0, ob, oa, occ, adb, acc);
-        const FF d = acc_dot<2>(T, acc, whi, wlo);
+        FF d;
+        const float de = sweep_de<2>(T, acc, whi, wlo, 0.f, 0.f, d);
         ++n_prop;
-        if (accept_fast(d, beta_f, u24(r.x))) {
+        if (accept_de(de, beta_f, u24(r.x))) {
           ++n_acc;
           put_site(occ, G, 0, xb, yb, zb, (int8_t)oa);
           eacc.add(acc, d, 0.0);
