@@ -528,7 +528,8 @@ constexpr int MAX_SWEEPS = 8;
 
 struct SweepSmem {
   // carved from dynamic shared memory; offsets in bytes
-  int occ, cl_off, lutoff, lut, whi, wlo, dmu, ax, sched, red, clist, wkept, stats, desc, total;
+  int occ, cl_off, lutoff, lut, whi, wlo, dmu, ax, sched, red, clist, wkept, stats, desc, initq,
+      total;
 };
 
 __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
@@ -573,6 +574,8 @@ __host__ __device__ inline void sweep_layout(const CeTables &T, int L0, int L1, 
   o += align16((int)sizeof(ReplicaStats));
   s.desc = o;  // decoded sub-steps of the current pass
   o += MAX_SWEEPS * n_classes_max * 80;
+  s.initq = o;  // per-warp queues of occupied sites (initial energy)
+  o += 32 * 64 * 4;
   s.total = o;
 }
 
@@ -583,6 +586,24 @@ inline int sweep_smem_bytes_impl(const CeTables &T, int L0, int L1, int L2, int 
   return s.total;
 }
 
+// floor(n / d) for a block-uniform divisor d >= 1 and numerators n >= 0 with
+// n * d < 2^32: umulhi(n, m) with m = floor((2^32 - 1) / d) + 1 (= ceil(2^32 / d),
+// or 2^32 / d for powers of two); exact because the rounding error of m is
+// below d (Granlund and Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994).
+struct FastDiv {
+  int d;
+  uint32_t m;
+  __host__ __device__ __forceinline__ static uint32_t magic(int dd) {
+    return dd > 1 ? 0xFFFFFFFFu / (uint32_t)dd + 1u : 0u;
+  }
+  __device__ __forceinline__ explicit FastDiv(int dd) : d(dd), m(magic(dd)) {}
+  __device__ __forceinline__ FastDiv(int dd, uint32_t mm) : d(dd), m(mm) {}
+  __device__ __forceinline__ int div(int n) const {
+    return d > 1 ? (int)__umulhi((uint32_t)n, m) : n;
+  }
+};
+
 struct Geo {
   int L0, L1, L2, R, W, H, V;
   __device__ __forceinline__ int addr(int b, int x, int y, int z) const {
@@ -590,21 +611,41 @@ struct Geo {
   }
 };
 
+// Linear site index l = b n_uc + x + L0 (y + L1 z) -> (b, x, y, z) without
+// hardware division (n_uc L0 < 2^32 for every supercell that fits in shared
+// memory; at most 4 sublattices).
+struct SiteIndex {
+  int n_uc, L0, L1;
+  FastDiv f0, f1;
+  __device__ __forceinline__ SiteIndex(int n, int l0, int l1)
+      : n_uc(n), L0(l0), L1(l1), f0(l0), f1(l1) {}
+  __device__ __forceinline__ void operator()(int l, int &b, int &x, int &y, int &z) const {
+    b = (l >= n_uc) + (l >= 2 * n_uc) + (l >= 3 * n_uc);
+    const int uc = l - b * n_uc;
+    const int t = f0.div(uc);
+    x = uc - t * L0;
+    z = f1.div(t);
+    y = t - z * L1;
+  }
+};
+
 // Write occupant v to core site (b,x,y,z) and all of its periodic halo images.
 __device__ __forceinline__ void put_site(int8_t *occ, const Geo &G, int b, int x, int y, int z,
                                          int8_t v) {
-  if (x >= G.R && x < G.L0 - G.R && y >= G.R && y < G.L1 - G.R && z >= G.R && z < G.L2 - G.R) {
-    occ[G.addr(b, x, y, z)] = v;  // no periodic image
-    return;
-  }
-  const int xs[2] = {x, x < G.R ? x + G.L0 : (x >= G.L0 - G.R ? x - G.L0 : INT32_MIN)};
-  const int ys[2] = {y, y < G.R ? y + G.L1 : (y >= G.L1 - G.R ? y - G.L1 : INT32_MIN)};
-  const int zs[2] = {z, z < G.R ? z + G.L2 : (z >= G.L2 - G.R ? z - G.L2 : INT32_MIN)};
-#pragma unroll
-  for (int c = 0; c < 8; ++c) {
-    const int xx = xs[c & 1], yy = ys[(c >> 1) & 1], zz = zs[(c >> 2) & 1];
-    if (xx != INT32_MIN && yy != INT32_MIN && zz != INT32_MIN) occ[G.addr(b, xx, yy, zz)] = v;
-  }
+  const int base = G.addr(b, x, y, z);
+  occ[base] = v;
+  // periodic images: along each axis at most one, L cells away
+  const int ox = x < G.R ? G.L0 : (x >= G.L0 - G.R ? -G.L0 : 0);
+  const int oy = (y < G.R ? G.L1 : (y >= G.L1 - G.R ? -G.L1 : 0)) * G.W;
+  const int oz = (z < G.R ? G.L2 : (z >= G.L2 - G.R ? -G.L2 : 0)) * (G.W * G.H);
+  if ((ox | oy | oz) == 0) return;
+  if (ox) occ[base + ox] = v;
+  if (oy) occ[base + oy] = v;
+  if (oz) occ[base + oz] = v;
+  if (ox && oy) occ[base + ox + oy] = v;
+  if (ox && oz) occ[base + ox + oz] = v;
+  if (oy && oz) occ[base + oy + oz] = v;
+  if (ox && oy && oz) occ[base + ox + oy + oz] = v;
 }
 
 // Energy change of a sweep proposal (f32, minus the chemical potential term
@@ -636,24 +677,6 @@ __device__ __forceinline__ bool accept_de(float de, float beta_f, float u) {
   if (de < 0.f) return true;
   return u < cem_expf_neg(FMUL(-beta_f, de));
 }
-
-// floor(n / d) for a block-uniform divisor 1 <= d < 2^16 and numerators
-// 0 <= n < 2^16: umulhi(n, m) with m = floor((2^32 - 1) / d) + 1 (= ceil(2^32 / d),
-// or 2^32 / d for powers of two); exact because the rounding error of m is
-// below d and n * d < 2^32 (Granlund and Montgomery, "Division by invariant
-// integers using multiplication", PLDI 1994).
-struct FastDiv {
-  int d;
-  uint32_t m;
-  __host__ __device__ __forceinline__ static uint32_t magic(int dd) {
-    return dd > 1 ? 0xFFFFFFFFu / (uint32_t)dd + 1u : 0u;
-  }
-  __device__ __forceinline__ explicit FastDiv(int dd) : d(dd), m(magic(dd)) {}
-  __device__ __forceinline__ FastDiv(int dd, uint32_t mm) : d(dd), m(mm) {}
-  __device__ __forceinline__ int div(int n) const {
-    return d > 1 ? (int)__umulhi((uint32_t)n, m) : n;
-  }
-};
 
 // One sub-step of a pass, decoded once per pass by the thread that ranks its
 // class (so the serial sub-step loop only loads it).
@@ -948,22 +971,25 @@ __global__ void __launch_bounds__(THREADS, 1)
   // ---- occupation: global -> shared core, then periodic halo
   const int8_t *gocc = P.occ + R.occ_offset;
   const int n_sites = n_uc * nsl;
+  const SiteIndex site_of(n_uc, G.L0, G.L1);
   for (int l = tid; l < n_sites; l += nth) {
-    const int b = l / n_uc, uc = l - b * n_uc;
-    const int x = uc % G.L0, y = (uc / G.L0) % G.L1, z = uc / (G.L0 * G.L1);
+    int b, x, y, z;
+    site_of(l, b, x, y, z);
     occ[G.addr(b, x, y, z)] = gocc[l];
   }
   __syncthreads();
-  for (int h = tid; h < nsl * G.V; h += nth) {
-    const int b = h / G.V;
-    int r = h - b * G.V;
-    const int xh = r % G.W;
-    r /= G.W;
-    const int yh = r % G.H, zh = r / G.H;
-    const int x = xh - G.R, y = yh - G.R, z = zh - G.R;
-    if (x >= 0 && x < G.L0 && y >= 0 && y < G.L1 && z >= 0 && z < G.L2) continue;
-    if (x >= G.L0 + G.R || y >= G.L1 + G.R) continue;  // pitch padding
-    occ[h] = occ[G.addr(b, wrapc(x, G.L0), wrapc(y, G.L1), wrapc(z, G.L2))];
+  {
+    const FastDiv fw(G.W), fh(G.H);
+    for (int h = tid; h < nsl * G.V; h += nth) {
+      const int b = (h >= G.V) + (h >= 2 * G.V) + (h >= 3 * G.V);
+      const int r = h - b * G.V;
+      const int t = fw.div(r), zh = fh.div(t);
+      const int xh = r - t * G.W, yh = t - zh * G.H;
+      const int x = xh - G.R, y = yh - G.R, z = zh - G.R;
+      if (x >= 0 && x < G.L0 && y >= 0 && y < G.L1 && z >= 0 && z < G.L2) continue;
+      if (x >= G.L0 + G.R || y >= G.L1 + G.R) continue;  // pitch padding
+      occ[h] = occ[G.addr(b, wrapc(x, G.L0), wrapc(y, G.L1), wrapc(z, G.L2))];
+    }
   }
   __syncthreads();
 
@@ -974,22 +1000,41 @@ __global__ void __launch_bounds__(THREADS, 1)
       // exact initial state: every cluster of orbit g with all sites occupant 1
       // is seen from each of its size_g sites, so count_g = sum over sites with
       // occupant 1 of its flower count / size_g
+      // Occupied sites are queued per warp and evaluated 32 at a time, so
+      // no lane idles on an empty site.
       long long cnt[MAX_ORBITS];
       for (int g = 0; g < MAX_ORBITS; ++g) cnt[g] = 0;
       long long n1 = 0, sub[4] = {0, 0, 0, 0};
-      for (int l = tid; l < n_sites; l += nth) {
-        const int b = l / n_uc, uc = l - b * n_uc;
-        const int x = uc % G.L0, y = (uc / G.L0) % G.L1, z = uc / (G.L0 * G.L1);
-        const int ad = G.addr(b, x, y, z);
-        const int o = occ[ad];
-        if (o == 0) continue;
-        ++n1;
-        sub[sc_sublattice(x, y, z)]++;
+      int *q = reinterpret_cast<int *>(smem + lay.initq) + warp * 64;
+      int qn = 0;
+      auto eval_site = [&](int l) {
+        int b, x, y, z;
+        site_of(l, b, x, y, z);
         Acc<2> acc;
         acc.zero();
-        ev.add(b, 0, 1, occ, ad, acc);
+        ev.add(b, 0, 1, occ, G.addr(b, x, y, z), acc);
         for (int g = 0; g < MAX_ORBITS; ++g) cnt[g] += acc.c[g];
+        ++n1;
+        sub[sc_sublattice(x, y, z)]++;
+      };
+      const int per_warp = (n_sites + NW - 1) / NW;
+      const int l_begin = warp * per_warp, l_end = min(n_sites, l_begin + per_warp);
+      for (int l0 = l_begin; l0 < l_end; l0 += 32) {
+        const int l = l0 + lane;
+        const bool one = l < l_end && gocc[l] != 0;
+        const unsigned m = __ballot_sync(0xffffffffu, one);
+        if (one) q[qn + __popc(m & ((1u << lane) - 1u))] = l;
+        qn += __popc(m);
+        __syncwarp();
+        if (qn >= 32) {
+          eval_site(q[lane]);
+          __syncwarp();
+          if (lane < qn - 32) q[lane] = q[32 + lane];
+          qn -= 32;
+          __syncwarp();
+        }
       }
+      if (lane < qn) eval_site(q[lane]);
       long long *rd_l = reinterpret_cast<long long *>(red);
       for (int off = 16; off; off >>= 1) {
         n1 += __shfl_xor_sync(0xffffffffu, n1, off);
@@ -1345,8 +1390,8 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
   // ---- write back
   for (int l = tid; l < n_sites; l += nth) {
-    const int b = l / n_uc, uc = l - b * n_uc;
-    const int x = uc % G.L0, y = (uc / G.L0) % G.L1, z = uc / (G.L0 * G.L1);
+    int b, x, y, z;
+    site_of(l, b, x, y, z);
     P.occ[R.occ_offset + l] = occ[G.addr(b, x, y, z)];
   }
   if (tid == 0) {
