@@ -575,7 +575,7 @@ __host__ __device__ inline void sweep_layout(const CeTables &T, int L0, int L1, 
   s.desc = o;  // decoded sub-steps of the current pass
   o += MAX_SWEEPS * n_classes_max * 80;
   s.initq = o;  // per-warp queues of occupied sites (initial energy)
-  o += 32 * 64 * 4;
+  o += 32 * 96 * 4;
   s.total = o;
 }
 
@@ -953,45 +953,59 @@ __global__ void __launch_bounds__(THREADS, 1)
     dmu_hi[tid] = R.dmu_hi[tid];
     dmu_lo[tid] = R.dmu_lo[tid];
   }
-  if (tid < 3) {  // colour lists per axis, blocks of size p (or more)
-    const int a = tid, L = R.L[a], p = R.p;
-    const int q = L / p;
-    int k = 0;
-    for (int c = 0; c < R.n_col[a]; ++c) {
-      ax_begin[a][c] = k;
-      int x = 0;
-      for (int blk = 0; blk < q; ++blk) {
-        const int sz = p + (L - q * p) / q + ((blk < (L - q * p) % q) ? 1 : 0);
-        if (c < sz) ax_coord[a][k++] = x + c;
-        x += sz;
+  // colour lists per axis: L = q blocks, the first r = (L - q p) mod q of
+  // size big = small + 1, the others of size small = p + (L - q p) / q;
+  // colour = offset inside the block, list order = block order
+  for (int i = tid; i < 3 * MAX_L; i += nth) {
+    const int a = i / MAX_L, x = i - a * MAX_L;
+    const int L = R.L[a], p = R.p, q = L / p, e = L - q * p, r = e % q;
+    const int small = p + e / q, big = small + 1;
+    if (x < R.n_col[a]) {
+      ax_cnt[a][x] = x < small ? q : r;
+      ax_begin[a][x] = x * q;
+    }
+    if (x < L) {
+      int blk, off;
+      if (x < r * big) {
+        blk = x / big;
+        off = x - blk * big;
+      } else {
+        const int y = x - r * big;
+        blk = r + y / small;
+        off = y - (blk - r) * small;
       }
-      ax_cnt[a][c] = k - ax_begin[a][c];
+      ax_coord[a][off * q + blk] = x;
     }
   }
-  // ---- occupation: global -> shared core, then periodic halo
+  // ---- occupation: global -> shared core and its periodic halo images
   const int8_t *gocc = P.occ + R.occ_offset;
   const int n_sites = n_uc * nsl;
   const SiteIndex site_of(n_uc, G.L0, G.L1);
-  for (int l = tid; l < n_sites; l += nth) {
-    int b, x, y, z;
-    site_of(l, b, x, y, z);
-    occ[G.addr(b, x, y, z)] = gocc[l];
-  }
-  __syncthreads();
-  {
-    const FastDiv fw(G.W), fh(G.H);
-    for (int h = tid; h < nsl * G.V; h += nth) {
-      const int b = (h >= G.V) + (h >= 2 * G.V) + (h >= 3 * G.V);
-      const int r = h - b * G.V;
-      const int t = fw.div(r), zh = fh.div(t);
-      const int xh = r - t * G.W, yh = t - zh * G.H;
-      const int x = xh - G.R, y = yh - G.R, z = zh - G.R;
-      if (x >= 0 && x < G.L0 && y >= 0 && y < G.L1 && z >= 0 && z < G.L2) continue;
-      if (x >= G.L0 + G.R || y >= G.L1 + G.R) continue;  // pitch padding
-      occ[h] = occ[G.addr(b, wrapc(x, G.L0), wrapc(y, G.L1), wrapc(z, G.L2))];
+  // 16-byte loads when the replica's occupations are 16-byte aligned (the
+  // loads of a thread are issued together, then scattered into the halo'd
+  // layout); byte loads otherwise
+  const bool vec16 = ((R.occ_offset | n_sites) & 15) == 0;
+  if (vec16) {
+    const uint4 *g16 = reinterpret_cast<const uint4 *>(gocc);
+    for (int v = tid; v < n_sites / 16; v += nth) {
+      const uint4 w = g16[v];
+      const uint32_t words[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        int b, x, y, z;
+        site_of(16 * v + k, b, x, y, z);
+        put_site(occ, G, b, x, y, z, (int8_t)((words[k >> 2] >> (8 * (k & 3))) & 0xFF));
+      }
+    }
+  } else {
+    for (int l = tid; l < n_sites; l += nth) {
+      int b, x, y, z;
+      site_of(l, b, x, y, z);
+      put_site(occ, G, b, x, y, z, gocc[l]);
     }
   }
-  __syncthreads();
+  __syncthreads();  // core and periodic halo images (every halo cell is the
+                    // image of one core site: L >= 2 reach + 1 on every axis)
 
   const SiteEval<NOCC, PITCH> ev{&T, cl_off, lutoff, lut};
   const int lane = tid & 31, warp = tid >> 5, nwarp = NW;
@@ -1000,12 +1014,12 @@ __global__ void __launch_bounds__(THREADS, 1)
       // exact initial state: every cluster of orbit g with all sites occupant 1
       // is seen from each of its size_g sites, so count_g = sum over sites with
       // occupant 1 of its flower count / size_g
-      // Occupied sites are queued per warp and evaluated 32 at a time, so
-      // no lane idles on an empty site.
+      // Occupied sites are queued per warp and evaluated 64 at a time (two
+      // independent sites per lane), so no lane idles on an empty site.
       long long cnt[MAX_ORBITS];
       for (int g = 0; g < MAX_ORBITS; ++g) cnt[g] = 0;
       long long n1 = 0, sub[4] = {0, 0, 0, 0};
-      int *q = reinterpret_cast<int *>(smem + lay.initq) + warp * 64;
+      int *q = reinterpret_cast<int *>(smem + lay.initq) + warp * 96;
       int qn = 0;
       auto eval_site = [&](int l) {
         int b, x, y, z;
@@ -1021,20 +1035,27 @@ __global__ void __launch_bounds__(THREADS, 1)
       const int l_begin = warp * per_warp, l_end = min(n_sites, l_begin + per_warp);
       for (int l0 = l_begin; l0 < l_end; l0 += 32) {
         const int l = l0 + lane;
-        const bool one = l < l_end && gocc[l] != 0;
+        bool one = false;
+        if (l < l_end) {
+          int b, x, y, z;
+          site_of(l, b, x, y, z);
+          one = occ[G.addr(b, x, y, z)] != 0;
+        }
         const unsigned m = __ballot_sync(0xffffffffu, one);
         if (one) q[qn + __popc(m & ((1u << lane) - 1u))] = l;
         qn += __popc(m);
         __syncwarp();
-        if (qn >= 32) {
+        if (qn >= 64) {
           eval_site(q[lane]);
+          eval_site(q[32 + lane]);
           __syncwarp();
-          if (lane < qn - 32) q[lane] = q[32 + lane];
-          qn -= 32;
+          if (lane < qn - 64) q[lane] = q[64 + lane];
+          qn -= 64;
           __syncwarp();
         }
       }
       if (lane < qn) eval_site(q[lane]);
+      if (lane + 32 < qn) eval_site(q[lane + 32]);
       long long *rd_l = reinterpret_cast<long long *>(red);
       for (int off = 16; off; off >>= 1) {
         n1 += __shfl_xor_sync(0xffffffffu, n1, off);
@@ -1389,10 +1410,24 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
   }
   // ---- write back
-  for (int l = tid; l < n_sites; l += nth) {
-    int b, x, y, z;
-    site_of(l, b, x, y, z);
-    P.occ[R.occ_offset + l] = occ[G.addr(b, x, y, z)];
+  if (vec16) {
+    uint4 *g16 = reinterpret_cast<uint4 *>(P.occ + R.occ_offset);
+    for (int v = tid; v < n_sites / 16; v += nth) {
+      uint32_t words[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        int b, x, y, z;
+        site_of(16 * v + k, b, x, y, z);
+        words[k >> 2] |= (uint32_t)(uint8_t)occ[G.addr(b, x, y, z)] << (8 * (k & 3));
+      }
+      g16[v] = make_uint4(words[0], words[1], words[2], words[3]);
+    }
+  } else {
+    for (int l = tid; l < n_sites; l += nth) {
+      int b, x, y, z;
+      site_of(l, b, x, y, z);
+      P.occ[R.occ_offset + l] = occ[G.addr(b, x, y, z)];
+    }
   }
   if (tid == 0) {
     S.energy = energy;
