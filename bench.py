@@ -332,13 +332,15 @@ def run_gb300(args):
     bytes_per_prop = 2 * (1 + z) + 2 * p_acc
     achieved = props * bytes_per_prop / (kernel_ms / 1e3) / 1e9
     clocks = clk.summary()
+    # DRAM bytes of one k_sweep launch from the committed ncu capture (the
+    # replica stays in shared memory: only the staging read reaches DRAM)
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "k_sweep_fcc24_canonical_dram.json")
+    prof = os.path.join(ROOT, "profiles", "k_sweep_fcc24_canonical_ncu.md")
     if os.path.exists(prof):
-        try:
-            traffic = json.load(open(prof)).get("dram_bytes_per_launch_scaled")
-        except (OSError, ValueError):
-            traffic = None
+        import re
+
+        m = re.search(r"^dram_bytes_per_launch: (\d+)$", open(prof).read(), re.M)
+        traffic = int(m.group(1)) if m else None
     line = {
         "metric": "proposals/s", "value": value, "unit": "proposals/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
