@@ -555,6 +555,58 @@ def run_learned_comparison(args):
     return 0
 
 
+def run_nfold_comparison(args):
+    """n-fold way against the plain Metropolis sweep on one semi-grand
+    canonical batch (128 replicas of 24^3 FCC A/B, configuration 0's CE) at a
+    low temperature, where most Metropolis proposals are rejected: events/s of
+    the n-fold kernel, its Metropolis-equivalent trials/s (sum of residence
+    weights / time) and the sweep's proposals/s on the same states."""
+    import torch
+
+    from casmcode_clexmonte_gb300 import build as B
+
+    B.build()
+    from casmcode_clexmonte_gb300 import calculator as cm
+    from casmcode_clexmonte_gb300 import workloads
+
+    w = workloads.config(0)
+    sysd = cm.System(w.ce)
+    n, L, T = 128, (24, 24, 24), args.nfold_temperature
+    rng = np.random.default_rng(5)
+    b = cm.ReplicaBatch(sysd, "semigrand_canonical", [L] * n)
+    for i in range(n):
+        b.set_conditions(i, T, np.array([0.0]))
+        b.set_seed(i, 4242 + i)
+        b.set_occupation(i, rng.integers(0, 2, 24 ** 3).astype(np.int8))
+    b.run(200, 0)  # equilibrate with the sweep
+    b.run(args.steps, 0)
+    b.synchronize()
+    sweep_ms = b.kernel_ms()
+    st = [b.stats(i) for i in range(n)]
+    acc = sum(s["n_accepted"] for s in st) / max(1, sum(s["n_proposed"] for s in st))
+    props = sum(s["n_proposed"] for s in st)
+    sweep_rate = props / (sweep_ms / 1e3)  # over the whole run; stats cover it
+    b.nfold_run(200, 0)  # warm-up
+    torch.cuda.synchronize()
+    n_ev = args.nfold_events
+    b.nfold_run(n_ev, 0)
+    nf_ms = b.kernel_ms()
+    weight = sum(b.stats(i)["n_samples"] for i in range(n))
+    line = {
+        "metric": "events/s", "value": n * n_ev / (nf_ms / 1e3), "unit": "events/s",
+        "n_gpus": 1, "steps": n_ev, "warmup": 200, "higher_is_better": True,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "fcc_binary_24I_sgc_x128_nfold", "replicas": n,
+                   "temperature_K": T, "param_chem_pot": 0.0},
+        "metropolis_equivalent_trials_per_s": weight / (nf_ms / 1e3),
+        "sweep_proposals_per_s": sweep_rate, "sweep_acceptance": acc,
+        "sweep_accepted_per_s": sweep_rate * acc,
+        "gpu_launches": 1,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -564,11 +616,17 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", type=int, default=WORKLOAD_INDEX, choices=[0, 1, 2, 3, 4])
     ap.add_argument("--learned-passes", type=int, default=40)
+    ap.add_argument("--nfold", action="store_true",
+                    help="n-fold way vs Metropolis sweep (semi-grand canonical, low T)")
+    ap.add_argument("--nfold-temperature", type=float, default=150.0)
+    ap.add_argument("--nfold-events", type=int, default=20000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.nfold:
+        return run_nfold_comparison(args)
     if args.workload == 3:
         return run_learned_comparison(args)
     if args.workload != WORKLOAD_INDEX:

@@ -52,7 +52,7 @@ EXPORTS = [
     "cem_replicas_create", "cem_replicas_destroy", "cem_n_sites", "cem_set_conditions",
     "cem_set_seed", "cem_set_occupation", "cem_get_occupation", "cem_set_occupation_all",
     "cem_get_occupation_all", "cem_host_alloc", "cem_host_free", "cem_energy",
-    "cem_delta_energy", "cem_replay", "cem_enforce_composition", "cem_run", "cem_get_stats", "cem_get_samples",
+    "cem_delta_energy", "cem_replay", "cem_enforce_composition", "cem_nfold_run", "cem_run", "cem_get_stats", "cem_get_samples",
     "cem_reset_stats", "cem_synchronize", "cem_last_kernel_ms", "cem_smem_bandwidth",
     "cem_set_option", "cem_get_option", "cem_delta_energy_noalloc",
     "cem_mlp_info", "cem_mlp_create", "cem_mlp_destroy", "cem_mlp_get_params",
@@ -96,6 +96,7 @@ def load(path: str = LIB):
     L.cem_replay.argtypes = [P, C.c_int, C.c_uint64, C.c_int64, vp, vp, vp,
                              C.POINTER(C.c_int64), C.POINTER(C.c_uint64)]
     L.cem_enforce_composition.argtypes = [P, _dp, C.c_uint64, C.POINTER(C.c_int64)]
+    L.cem_nfold_run.argtypes = [P, C.c_int64, C.c_int64, C.c_int64, vp, vp, vp]
     L.cem_run.argtypes = [P, C.c_int64, C.c_int64, C.c_int]
     L.cem_get_stats.argtypes = [P, C.c_int, C.POINTER(Stats)]
     L.cem_get_samples.argtypes = [P, C.c_int, vp, vp, C.c_int64, C.POINTER(C.c_int64)]

@@ -159,6 +159,19 @@ class ReplicaBatch:
                                                int(mt_seed), flips.ctypes.data_as(C.POINTER(C.c_int64))))
         return flips
 
+    def nfold_run(self, n_events: int, n_equil: int = 0, record: int = 0):
+        """n-fold way (rejection-free) events on every replica (semi-grand
+        canonical). Statistics become residence-time weighted. With
+        ``record`` > 0 returns the first ``record`` events of each replica:
+        site, new occupant and residence weight arrays of shape (n, record)."""
+        n = len(self.L)
+        site = np.zeros((n, record), dtype=np.int64) if record else None
+        occ = np.zeros((n, record), dtype=np.int32) if record else None
+        dt = np.zeros((n, record)) if record else None
+        check(self.lib.cem_nfold_run(self.handle, int(n_events), int(n_equil), int(record),
+                                     ptr(site), ptr(occ), ptr(dt)))
+        return dict(site=site, occ=occ, dt=dt) if record else None
+
     def run(self, n_passes: int, n_equil: int = 0, record_samples: bool = False):
         check(self.lib.cem_run(self.handle, int(n_passes), int(n_equil), int(bool(record_samples))))
 

@@ -129,6 +129,9 @@ struct cem_replicas {
   unsigned long long *d_trees = nullptr; // two sum trees per replica
   double *d_lsamples = nullptr;          // [rep][cap][3]
   long long lsample_capacity = 0, lsamples_recorded = 0;
+  // n-fold way: per-replica rate trees
+  double *d_nftree = nullptr;
+  long long *d_nftree_off = nullptr;
   ~cem_replicas() {
     cudaFree(sstate.halo);
     cudaFree(sstate.acc);
@@ -137,6 +140,8 @@ struct cem_replicas {
     cudaFree(d_lw);
     cudaFree(d_trees);
     cudaFree(d_lsamples);
+    cudaFree(d_nftree);
+    cudaFree(d_nftree_off);
     cudaFree(d_reps);
     cudaFree(d_stats);
     cudaFree(d_occ);
@@ -412,7 +417,35 @@ int cem_system_create(const cem_system_desc *d, cem_system **out) {
     uint8_t *dlut = dev_copy(lut);
     float *dwhi = dev_copy(whi), *dwlo = dev_copy(wlo);
     double *dw = dev_copy(s->w);
-    s->owned = {dpb, ddu, dlo, dlut, dwhi, dwlo, dw};
+    // distinct flower partners per sublattice (the sites whose events see a
+    // change of the centre site)
+    std::vector<int> fp((size_t)d->n_sublat * MAX_FP * 4, 0);
+    for (int b = 0; b < d->n_sublat; ++b) {
+      int n = 0;
+      for (int c = T.fl_begin[b][0]; c < T.fl_begin[b][T.n_orbits]; ++c)
+        for (int q = 0; q < 3; ++q) {
+          const int p = s->fl_pb[c * 3 + q];
+          if (p < 0) continue;
+          const int *u = &s->fl_du[c * 9 + q * 3];
+          bool seen = false;
+          for (int k = 0; k < n && !seen; ++k) {
+            const int *e = &fp[((size_t)b * MAX_FP + k) * 4];
+            seen = e[0] == p && e[1] == u[0] && e[2] == u[1] && e[3] == u[2];
+          }
+          if (seen) continue;
+          require(n < MAX_FP, "too many distinct flower partners", CEM_ERR_UNSUPPORTED);
+          int *e = &fp[((size_t)b * MAX_FP + n) * 4];
+          e[0] = p;
+          e[1] = u[0];
+          e[2] = u[1];
+          e[3] = u[2];
+          ++n;
+        }
+      T.n_fp[b] = n;
+    }
+    int *dfp = dev_copy(fp);
+    T.fp = dfp;
+    s->owned = {dpb, ddu, dlo, dlut, dwhi, dwlo, dw, dfp};
     T.cl_pb = dpb;
     T.cl_du = ddu;
     T.cl_lut = dlo;
@@ -771,6 +804,119 @@ int cem_reset_stats(cem_replicas *r) {
   return guard([&] {
     require(r != nullptr, "null handle");
     init_stats(r);
+  });
+}
+
+// Zero the sampled moments of every replica (keeps energy, species counts and
+// the pass / event counters).
+static void reset_moments(cem_replicas *r) {
+  std::vector<ReplicaStats> st(r->n);
+  CUDA_OK(cudaMemcpyAsync(st.data(), r->d_stats, sizeof(ReplicaStats) * r->n,
+                          cudaMemcpyDeviceToHost, r->stream));
+  CUDA_OK(cudaStreamSynchronize(r->stream));
+  for (auto &x : st) {
+    x.n_samples = 0;
+    x.sum_e = x.sum_e2 = x.sum_f = 0;
+    for (int k = 0; k < 3; ++k) x.sum_x[k] = x.sum_ex[k] = 0;
+    for (int k = 0; k < 9; ++k) x.sum_xx[k] = 0;
+    x.status = 0;
+  }
+  CUDA_OK(cudaMemcpyAsync(r->d_stats, st.data(), sizeof(ReplicaStats) * r->n,
+                          cudaMemcpyHostToDevice, r->stream));
+}
+
+int cem_nfold_run(cem_replicas *r, int64_t n_events, int64_t n_equil, int64_t record_capacity,
+                  int64_t *rec_site, int32_t *rec_occ, double *rec_dt) {
+  return guard([&] {
+    require(r != nullptr, "null handle");
+    require(r->ensemble == CEM_SEMIGRAND_CANONICAL,
+            "the n-fold way runs semi-grand canonical replicas");
+    require(n_events >= 0 && n_equil >= 0 && record_capacity >= 0, "counts must be >= 0");
+    require(record_capacity == 0 || (rec_site && rec_occ && rec_dt), "null record buffers");
+    const CeTables &T = r->sys->T;
+    int dev = 0, maxsm = 0;
+    CUDA_OK(cudaGetDevice(&dev));
+    CUDA_OK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    // generated evaluator when every replica has the 24^3 or 10^3 pitch
+    int pitch = 0;
+    if (r->sys->fcc_generated) {
+      const int p0 = r->reps[0].L[0] + 4;
+      bool same = p0 == 28 || p0 == 14;
+      for (const Replica &R : r->reps)
+        same = same && R.L[0] + 4 == p0 && R.L[1] + 4 == p0;
+      if (same) pitch = p0;
+    }
+    int smem = 0;
+    for (const Replica &R : r->reps)
+      smem = std::max(smem, nfold_smem_bytes(T, R.L[0], R.L[1], R.L[2], pitch));
+    require(smem <= maxsm, "supercell does not fit in shared memory for the n-fold kernel",
+            CEM_ERR_UNSUPPORTED);
+    if (!r->d_nftree) {
+      std::vector<long long> off(r->n);
+      long long total = 0;
+      for (int i = 0; i < r->n; ++i) {
+        off[i] = total;
+        total += rate_tree_size((long long)r->reps[i].n_sites * (T.n_occ - 1));
+      }
+      CUDA_OK(cudaMalloc(&r->d_nftree, sizeof(double) * (size_t)total));
+      CUDA_OK(cudaMalloc(&r->d_nftree_off, sizeof(long long) * r->n));
+      CUDA_OK(cudaMemcpy(r->d_nftree_off, off.data(), sizeof(long long) * r->n,
+                         cudaMemcpyHostToDevice));
+    }
+    r->upload_reps();
+    if (!r->stats_valid) init_stats(r);
+    reset_moments(r);
+    NfoldParams P{};
+    P.reps = r->d_reps;
+    P.stats = r->d_stats;
+    P.occ = r->d_occ;
+    P.tree = r->d_nftree;
+    P.tree_off = r->d_nftree_off;
+    P.n_events = n_events;
+    P.n_equil = n_equil;
+    P.rec_cap = record_capacity;
+    for (size_t k = 0; k < r->sys->RT.size() && k < 16; ++k) P.RT[k] = r->sys->RT[k];
+    long long *dsite = nullptr;
+    int *docc = nullptr;
+    double *ddt = nullptr;
+    auto cleanup = [&] {
+      cudaFree(dsite);
+      cudaFree(docc);
+      cudaFree(ddt);
+    };
+    try {
+      const size_t nrec = (size_t)record_capacity * r->n;
+      if (nrec) {
+        CUDA_OK(cudaMalloc(&dsite, sizeof(long long) * nrec));
+        CUDA_OK(cudaMalloc(&docc, sizeof(int) * nrec));
+        CUDA_OK(cudaMalloc(&ddt, sizeof(double) * nrec));
+        CUDA_OK(cudaMemsetAsync(dsite, 0xFF, sizeof(long long) * nrec, r->stream));
+      }
+      P.rec_site = dsite;
+      P.rec_occ = docc;
+      P.rec_dt = ddt;
+      CUDA_OK(cudaEventRecord(r->ev0, r->stream));
+      CUDA_OK(launch_nfold(T, P, r->n, smem, pitch, r->stream));
+      CUDA_OK(cudaEventRecord(r->ev1, r->stream));
+      if (nrec) {
+        CUDA_OK(cudaMemcpyAsync(rec_site, dsite, sizeof(long long) * nrec, cudaMemcpyDeviceToHost,
+                                r->stream));
+        CUDA_OK(cudaMemcpyAsync(rec_occ, docc, sizeof(int) * nrec, cudaMemcpyDeviceToHost,
+                                r->stream));
+        CUDA_OK(cudaMemcpyAsync(rec_dt, ddt, sizeof(double) * nrec, cudaMemcpyDeviceToHost,
+                                r->stream));
+      }
+      std::vector<ReplicaStats> st(r->n);
+      CUDA_OK(cudaMemcpyAsync(st.data(), r->d_stats, sizeof(ReplicaStats) * r->n,
+                              cudaMemcpyDeviceToHost, r->stream));
+      CUDA_OK(cudaStreamSynchronize(r->stream));
+      for (const auto &x : st)
+        if (x.status) throw Err(CEM_ERR_DEVICE, "no event has a non-zero rate (zero temperature in a local minimum)");
+    } catch (...) {
+      cleanup();
+      throw;
+    }
+    cleanup();
   });
 }
 

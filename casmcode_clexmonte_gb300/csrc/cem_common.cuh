@@ -30,6 +30,7 @@ constexpr int MAX_PARTNERS = 3;  // clusters of up to 4 sites
 constexpr int MAX_NB = 16;       // nearest-neighbour displacements per sublattice
 constexpr int MAX_COLOURS = 8;   // per axis
 constexpr int MAX_L = 128;       // per axis
+constexpr int MAX_FP = 128;      // distinct flower partners per sublattice
 
 // Cluster-expansion tables in device memory (built once per system).
 struct CeTables {
@@ -63,6 +64,10 @@ struct CeTables {
   int wq[MAX_ORBITS];
   float wr[MAX_ORBITS];
   float wq_scale;
+  // distinct partner sites of each sublattice's flower clusters (the sites
+  // whose energy changes see a change of the centre): (sublattice, du[3])
+  int n_fp[MAX_SUBLAT];
+  const int *fp;  // [n_sublat][MAX_FP][4]
   // owned clusters use index n_fl + i in the cl_* arrays
 };
 
@@ -207,6 +212,59 @@ CEM_HD float cem_expf_neg(float x) {
   __builtin_memcpy(&scale, &bits, 4);
 #endif
   return FMUL(p, scale);
+}
+
+// exp(x) for x <= 0 in FP64, for n-fold rates: Cody-Waite reduction
+// x = n ln2 + r with the fdlibm split of ln2 (ln2_hi has 32 significant bits,
+// so n ln2_hi is exact), e^r by its degree-13 Taylor polynomial in Horner
+// form with fused multiply-adds (|r| <= ln2/2: truncation below 2^-56
+// relative), scaled by 2^n. Every operation is explicitly rounded, so host
+// and device give the same bits. x < -745 (or NaN) returns 0.
+#ifdef __CUDA_ARCH__
+#define DADD(a, b) __dadd_rn((a), (b))
+#define DSUB(a, b) __dsub_rn((a), (b))
+#define DMUL(a, b) __dmul_rn((a), (b))
+#define DDIV(a, b) __ddiv_rn((a), (b))
+#define DFMA(a, b, c) __fma_rn((a), (b), (c))
+#else
+#define DADD(a, b) ((double)((a) + (b)))
+#define DSUB(a, b) ((double)((a) - (b)))
+#define DMUL(a, b) ((double)((a) * (b)))
+#define DDIV(a, b) ((double)((a) / (b)))
+#define DFMA(a, b, c) std::fma((a), (b), (c))
+#endif
+
+CEM_HD double cem_exp_neg(double x) {
+  if (!(x >= -745.0)) return 0.0;
+  if (x > 0.0) x = 0.0;
+  const double log2e = 0x1.71547652b82fep+0;
+  const double ln2_hi = 0x1.62e42fee00000p-1;
+  const double ln2_lo = 0x1.a39ef35793c76p-33;
+#ifdef __CUDA_ARCH__
+  const double n = rint(DMUL(x, log2e));
+#else
+  const double n = std::nearbyint(DMUL(x, log2e));
+#endif
+  double r = DFMA(-n, ln2_hi, x);
+  r = DFMA(-n, ln2_lo, r);
+  const double c[14] = {0x1.0000000000000p+0, 0x1.0000000000000p+0, 0x1.0000000000000p-1,
+                        0x1.5555555555555p-3, 0x1.5555555555555p-5, 0x1.1111111111111p-7,
+                        0x1.6c16c16c16c17p-10, 0x1.a01a01a01a01ap-13, 0x1.a01a01a01a01ap-16,
+                        0x1.71de3a556c734p-19, 0x1.27e4fb7789f5cp-22, 0x1.ae64567f544e4p-26,
+                        0x1.1eed8eff8d898p-29, 0x1.6124613a86d09p-33};  // 1/k!
+  double p = c[13];
+  for (int k = 12; k >= 0; --k) p = DFMA(p, r, c[k]);
+#ifdef __CUDA_ARCH__
+  return ldexp(p, (int)n);
+#else
+  return std::ldexp(p, (int)n);
+#endif
+}
+
+// Uniform double in [0, 1) with 53 random bits from two Philox words.
+CEM_HD double u53(uint32_t a, uint32_t b) {
+  return DMUL(DADD(DMUL((double)(a >> 5), 67108864.0), (double)(b >> 6)),
+              0x1.0p-53);
 }
 
 // ------------------------------------------------------------ MT19937-64

@@ -109,4 +109,44 @@ cudaError_t learned_run(const CeTables &T, const Replica *reps, ReplicaStats *st
                         int n_sites, int n_replicas, int L, long long n_passes, long long n_equil,
                         double *samples, long long capacity, int pitch, cudaStream_t st);
 
+// n-fold way (cem_nfold.cu)
+// 32-ary sum tree over n leaves: level 0 = leaves, level k + 1 has
+// ceil(n_k / 32) nodes, the last level one node; levels stored back to back.
+struct RateTree {
+  int n_lev;
+  long long off[8], n[8];
+};
+__host__ __device__ inline void rate_tree_geo(long long n_leaves, RateTree &g) {
+  g.n_lev = 1;
+  g.off[0] = 0;
+  g.n[0] = n_leaves;
+  while (g.n[g.n_lev - 1] > 1 && g.n_lev < 8) {
+    const int k = g.n_lev;
+    g.off[k] = g.off[k - 1] + g.n[k - 1];
+    g.n[k] = (g.n[k - 1] + 31) / 32;
+    g.n_lev = k + 1;
+  }
+}
+__host__ __device__ inline long long rate_tree_size(long long n_leaves) {
+  RateTree g;
+  rate_tree_geo(n_leaves, g);
+  return g.off[g.n_lev - 1] + 1;
+}
+struct NfoldParams {
+  const Replica *reps;
+  ReplicaStats *stats;
+  int8_t *occ;
+  double *tree;               // per replica trees, back to back
+  const long long *tree_off;  // [n_rep] offset of each replica's tree
+  long long n_events, n_equil;
+  long long rec_cap;          // recorded events per replica (0: none)
+  long long *rec_site;
+  int *rec_occ;
+  double *rec_dt;
+  double RT[16];
+};
+int nfold_smem_bytes(const CeTables &T, int L0, int L1, int L2, int pitch);
+cudaError_t launch_nfold(const CeTables &T, const NfoldParams &P, int n_replicas, int smem,
+                         int pitch, cudaStream_t st);
+
 }  // namespace cem

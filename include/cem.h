@@ -188,6 +188,24 @@ int cem_replay(cem_replicas *r, int replica, uint64_t mt_seed, int64_t n_steps,
                uint8_t *accept_seq, double *dE_seq, int64_t *site_seq, int64_t *n_accept,
                uint64_t *n_draws);
 
+/* n-fold way (rejection-free semi-grand canonical Monte Carlo, Bortz-Kalos-
+ * Lebowitz): each replica draws n_equil + n_events events, an event being a
+ * single-site occupant change drawn with probability proportional to its
+ * Metropolis rate (1 if dE <= 0, else exp(-beta dE), dE the semi-grand
+ * canonical potential change), and applies it. After the n_equil first
+ * events, the state before each event enters the statistics with weight
+ * n_possible / (sum of rates), its expected residence time in Metropolis
+ * trials (n_possible = sites x n_occ x (n_occ - 1)); cem_get_stats then
+ * returns time-weighted moments (n_samples = total weight). Optional records
+ * per replica (record_capacity per replica, replica-major): changed site,
+ * new occupant and weight of each of the first events. Replaces
+ * clexmonte::nfold::Nfold::run (include/casm/clexmonte/nfold/nfold_impl.hh:20-108)
+ * and CompleteEventCalculator::calculate_rate
+ * (src/casm/clexmonte/nfold/nfold_events.cc:24-60). Semi-grand canonical
+ * batches only; CEM_ERR_DEVICE when a replica has no event of non-zero rate. */
+int cem_nfold_run(cem_replicas *r, int64_t n_events, int64_t n_equil, int64_t record_capacity,
+                  int64_t *rec_site, int32_t *rec_occ, double *rec_dt);
+
 /* Composition enforcement: greedy semi-grand canonical flips that move each
  * replica toward target_mol (n_occ values per replica, replica-major:
  * species count per unit cell, e.g. {1 - x, x} for a one-site binary cell)

@@ -760,6 +760,183 @@ i64 ora_enforce_composition(void *h, signed char *occ, const double *target, u64
   }
 }
 
+// ---- n-fold way (Bortz-Kalos-Lebowitz rejection-free semi-grand canonical
+// Monte Carlo; clexmonte::nfold::Nfold::run, include/casm/clexmonte/nfold/
+// nfold_impl.hh:20-108, rates as CompleteEventCalculator::calculate_rate,
+// src/casm/clexmonte/nfold/nfold_events.cc:24-60). Restated sequentially:
+// events are (site l, k-th other occupant), e = l (n_occ - 1) + k; rate =
+// 1 if dE <= 0 else exp(-beta dE) with dE = sum_f w_f dcount_f - dmu; a
+// 32-ary sum tree whose nodes are sequential sums of their children; each
+// step weights the current state by n_possible / total, draws a uniform
+// u53 from Philox4x32-10 (counter = event index, tag 3), descends the tree,
+// applies the event. All rates are recomputed after every event (the GPU
+// recomputes only the changed site's flower), so the comparison also checks
+// the GPU's impact lists.
+extern "C" void ora_philox4x32_10(const unsigned *ctr_in, const unsigned *key_in, unsigned *out);
+
+// exp(x) for x <= 0: Cody-Waite reduction with the fdlibm split of ln2,
+// degree-13 Taylor polynomial by fused multiply-adds, scaling by 2^n.
+static double exp_neg_restated(double x) {
+  if (!(x >= -745.0)) return 0.0;
+  if (x > 0.0) x = 0.0;
+  const double log2e = 0x1.71547652b82fep+0;
+  const double ln2_hi = 0x1.62e42fee00000p-1;
+  const double ln2_lo = 0x1.a39ef35793c76p-33;
+  const double n = std::nearbyint(x * log2e);
+  double r = std::fma(-n, ln2_hi, x);
+  r = std::fma(-n, ln2_lo, r);
+  static const double c[14] = {0x1.0000000000000p+0, 0x1.0000000000000p+0, 0x1.0000000000000p-1,
+                               0x1.5555555555555p-3, 0x1.5555555555555p-5, 0x1.1111111111111p-7,
+                               0x1.6c16c16c16c17p-10, 0x1.a01a01a01a01ap-13, 0x1.a01a01a01a01ap-16,
+                               0x1.71de3a556c734p-19, 0x1.27e4fb7789f5cp-22, 0x1.ae64567f544e4p-26,
+                               0x1.1eed8eff8d898p-29, 0x1.6124613a86d09p-33};
+  double p = c[13];
+  for (int k = 12; k >= 0; --k) p = std::fma(p, r, c[k]);
+  return std::ldexp(p, (int)n);
+}
+
+extern "C" double ora_exp_neg(double x) { return exp_neg_restated(x); }
+
+// stats_out: [0] total weight, [1] sum w ep, [2] sum w ep^2, [3] sum w ef,
+// [4..6] sum w x_k, [7..15] sum w x_k x_k', [16..18] sum w ep x_k.
+// Returns the number of events applied (-1 on error).
+extern "C" i64 ora_nfold(void *h, signed char *occ, double temperature, const double *mu,
+                         const double *w, u64 seed, i64 n_events, i64 n_equil, i64 rec_cap,
+                         i64 *rec_site, int *rec_occ, double *rec_dt, double *stats_out) {
+  try {
+    System &s = *(System *)h;
+    const int no = s.n_occ, N = s.n_sites;
+    const double kb = 8.617333262e-5;
+    const double beta = (std::fabs(temperature) < 1e-10) ? INFINITY : 1.0 / (kb * temperature);
+    std::vector<double> dmu(no * no, 0.0);
+    for (int oi = 0; oi < no; ++oi)
+      for (int of = 0; of < no; ++of) {
+        double t = 0.0;
+        for (int k = 0; k < no - 1; ++k) {
+          double x = s.RT[k * no + of] - s.RT[k * no + oi];
+          t += mu[k] * x;
+        }
+        dmu[oi * no + of] = t;
+      }
+    std::vector<i64> dc(s.n_funcs);
+    auto de_f = [&](int l, int of) {
+      std::fill(dc.begin(), dc.end(), 0);
+      site_delta_counts(s, occ, l, of, dc.data());
+      double d = 0.0;
+      for (int f = 1; f < s.n_funcs; ++f) d = d + w[f] * (double)dc[f];
+      return d;
+    };
+    const i64 n_ev = (i64)N * (no - 1);
+    // tree levels
+    std::vector<std::vector<double>> lev;
+    lev.push_back(std::vector<double>(n_ev));
+    while (lev.back().size() > 1) lev.push_back(std::vector<double>((lev.back().size() + 31) / 32));
+    auto rebuild = [&]() {
+      for (i64 e = 0; e < n_ev; ++e) {
+        const int l = (int)(e / (no - 1)), k = (int)(e % (no - 1));
+        const int oi = occ[l], of = k < oi ? k : k + 1;
+        const double de = de_f(l, of) - dmu[oi * no + of];
+        lev[0][e] = de <= 0.0 ? 1.0 : exp_neg_restated(-beta * de);
+      }
+      for (size_t L = 1; L < lev.size(); ++L)
+        for (size_t node = 0; node < lev[L].size(); ++node) {
+          double t = 0.0;
+          const size_t c1 = std::min(node * 32 + 32, lev[L - 1].size());
+          for (size_t c = node * 32; c < c1; ++c) t = t + lev[L - 1][c];
+          lev[L][node] = t;
+        }
+    };
+    // observables
+    std::vector<i64> nspec(no, 0);
+    for (int l = 0; l < N; ++l) nspec[occ[l]]++;
+    std::vector<i64> cnt(s.n_funcs);
+    all_counts(s, occ, cnt.data());
+    double energy = counts_to_energy(s, cnt.data());
+    for (int k = 0; k < 19; ++k) stats_out[k] = 0.0;
+    const double n_possible = (double)N * (double)(no * (no - 1));
+    const unsigned key[2] = {(unsigned)seed, (unsigned)(seed >> 32)};
+    rebuild();
+    i64 done = 0;
+    for (i64 it = 0; it < n_equil + n_events; ++it) {
+      const double total = lev.back()[0];
+      if (!(total > 0.0)) break;
+      const double dt = n_possible / total;
+      if (it >= n_equil) {
+        double x[3] = {0.0, 0.0, 0.0}, mux = 0.0;
+        for (int k = 0; k < no - 1; ++k) {
+          double t = 0.0;
+          for (int a = 0; a < no; ++a) {
+            const double c = (double)nspec[a] - (a == 0 ? (double)N : 0.0);
+            t = t + s.RT[k * no + a] * c;
+          }
+          x[k] = t / (double)s.n_uc;
+          mux = mux + mu[k] * x[k];
+        }
+        const double ef = energy / (double)s.n_uc;
+        const double ep = ef - mux;
+        stats_out[0] = stats_out[0] + dt;
+        stats_out[1] = stats_out[1] + dt * ep;
+        stats_out[2] = stats_out[2] + dt * (ep * ep);
+        stats_out[3] = stats_out[3] + dt * ef;
+        for (int k = 0; k < no - 1; ++k) {
+          stats_out[4 + k] = stats_out[4 + k] + dt * x[k];
+          stats_out[16 + k] = stats_out[16 + k] + dt * (ep * x[k]);
+          for (int k2 = 0; k2 < no - 1; ++k2)
+            stats_out[7 + k * 3 + k2] = stats_out[7 + k * 3 + k2] + dt * (x[k] * x[k2]);
+        }
+      }
+      const unsigned ctr[4] = {(unsigned)it, (unsigned)(it >> 32), 0u, 3u << 16};
+      unsigned rr[4];
+      ora_philox4x32_10(ctr, key, rr);
+      const double u = ((double)(rr[0] >> 5) * 67108864.0 + (double)(rr[1] >> 6)) * 0x1.0p-53;
+      double tgt = u * total;
+      i64 node = 0;
+      for (int L = (int)lev.size() - 1; L >= 1; --L) {
+        const auto &ch = lev[L - 1];
+        const i64 c0 = node * 32, c1 = std::min<i64>(c0 + 32, (i64)ch.size());
+        double cum = 0.0, last_before = 0.0;
+        i64 pick = -1, last = -1;
+        for (i64 c = c0; c < c1; ++c) {
+          const double v = ch[c];
+          const double nc = cum + v;
+          if (v > 0.0) {
+            if (tgt < nc) {
+              pick = c;
+              break;
+            }
+            last = c;
+            last_before = cum;
+          }
+          cum = nc;
+        }
+        if (pick < 0) {
+          pick = last;
+          cum = last_before;
+        }
+        tgt = tgt - cum;
+        node = pick;
+      }
+      const int l = (int)(node / (no - 1)), k = (int)(node % (no - 1));
+      const int oi = occ[l], of = k < oi ? k : k + 1;
+      if (it < rec_cap) {
+        rec_site[it] = l;
+        rec_occ[it] = of;
+        rec_dt[it] = dt;
+      }
+      energy = energy + de_f(l, of);
+      nspec[oi]--;
+      nspec[of]++;
+      occ[l] = (signed char)of;
+      rebuild();
+      ++done;
+    }
+    return done;
+  } catch (std::exception &e) {
+    g_err = e.what();
+    return -1;
+  }
+}
+
 // Many independent sequential chains on host threads (CPU baseline):
 // replica r uses occ + r*n_sites, seed + r, temperature[r], mu[r*(n_occ-1)].
 // Returns wall seconds; n_steps_out = total proposals.

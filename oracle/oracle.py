@@ -78,6 +78,11 @@ def lib():
         ]
         L.ora_enforce_composition.restype = C.c_int64
         L.ora_enforce_composition.argtypes = [P, i8p, f64p, C.c_uint64, u64p]
+        L.ora_exp_neg.restype = C.c_double
+        L.ora_exp_neg.argtypes = [C.c_double]
+        L.ora_nfold.restype = C.c_int64
+        L.ora_nfold.argtypes = [P, i8p, C.c_double, f64p, f64p, C.c_uint64, C.c_int64, C.c_int64,
+                                C.c_int64, i64p, i32p, f64p, f64p]
         L.ora_mt19937_64.argtypes = [C.c_uint64, C.c_int64, u64p]
         L.ora_std_uniform_int.argtypes = [C.c_uint64, C.c_int64, i64p, i64p, u64p]
         L.ora_std_uniform_real.argtypes = [C.c_uint64, C.c_int64, f64p]
@@ -217,6 +222,22 @@ class OracleSystem:
         if n < 0:
             raise RuntimeError(lib().ora_last_error().decode())
         return int(n), int(draws[0])
+
+    def nfold(self, occ, temperature, mu, w, seed, n_events, n_equil=0, record=0):
+        """n-fold way restated sequentially; ``occ`` is updated in place.
+        ``w`` are the per-function weights the GPU uses."""
+        assert occ.dtype == np.int8 and occ.flags.c_contiguous and occ.size == self.n_sites
+        rec_site = np.zeros(max(record, 1), dtype=np.int64)
+        rec_occ = np.zeros(max(record, 1), dtype=np.int32)
+        rec_dt = np.zeros(max(record, 1))
+        st = np.zeros(19)
+        n = lib().ora_nfold(self.h, occ, float(temperature), np.ascontiguousarray(mu, dtype=np.float64),
+                            np.ascontiguousarray(w, dtype=np.float64), int(seed), int(n_events),
+                            int(n_equil), int(record), rec_site, rec_occ, rec_dt, st)
+        if n < 0:
+            raise RuntimeError(lib().ora_last_error().decode())
+        return dict(n=int(n), site=rec_site[:record], occ=rec_occ[:record], dt=rec_dt[:record],
+                    stats=st)
 
     def run_threads(self, occ, ensemble, temps, mus, seed, n_passes, n_threads):
         nrep = len(temps)

@@ -54,3 +54,25 @@ def test_float_float_dot_within_1e10():
         exact = float(np.dot(w, dc))
         got = _ff_dot(w, dc)
         assert abs(got - exact) <= 1e-10 * max(abs(exact), 1e-3)
+
+
+def test_exp64_restatement_matches_oracle_and_libm(tmp_path, oracle_mod):
+    """The FP64 exp of the n-fold rates: the product's host build and the
+    oracle's restatement give the same bits, within 1 ulp of libm."""
+    exe = str(tmp_path / "probe64")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off",
+                    os.path.join(HERE, "host_exp64_probe.cc"), "-o", exe], check=True)
+    rng = np.random.default_rng(5)
+    x = np.concatenate([-rng.uniform(0, 1, 2000), -rng.uniform(0, 50, 2000),
+                        -rng.uniform(0, 745, 2000), [0.0, -0.0, -1e-300, -744.0, -745.5, -800.0]])
+    out = subprocess.run([exe], input="\n".join(float(v).hex() for v in x),
+                         capture_output=True, text=True, check=True).stdout.split()
+    got = np.array([int(v, 16) for v in out], dtype=np.uint64).view(np.float64)
+    lib = oracle_mod.lib()
+    ora = np.array([lib.ora_exp_neg(float(v)) for v in x])
+    np.testing.assert_array_equal(got, ora)
+    ref = np.exp(x)
+    normal = ref > 1e-300
+    ulp = np.spacing(ref[normal])
+    assert np.max(np.abs(got[normal] - ref[normal]) / ulp) <= 1.0
+    assert np.all(got[x < -745.2] == 0.0)
