@@ -579,13 +579,16 @@ def run_nfold_comparison(args):
         b.set_seed(i, 4242 + i)
         b.set_occupation(i, rng.integers(0, 2, 24 ** 3).astype(np.int8))
     b.run(200, 0)  # equilibrate with the sweep
+    b.synchronize()
+    st0 = [b.stats(i) for i in range(n)]
     b.run(args.steps, 0)
     b.synchronize()
     sweep_ms = b.kernel_ms()
     st = [b.stats(i) for i in range(n)]
-    acc = sum(s["n_accepted"] for s in st) / max(1, sum(s["n_proposed"] for s in st))
-    props = sum(s["n_proposed"] for s in st)
-    sweep_rate = props / (sweep_ms / 1e3)  # over the whole run; stats cover it
+    props = sum(s["n_proposed"] - s0["n_proposed"] for s, s0 in zip(st, st0))
+    accs = sum(s["n_accepted"] - s0["n_accepted"] for s, s0 in zip(st, st0))
+    acc = accs / max(1, props)
+    sweep_rate = props / (sweep_ms / 1e3)
     b.nfold_run(200, 0)  # warm-up
     torch.cuda.synchronize()
     n_ev = args.nfold_events
