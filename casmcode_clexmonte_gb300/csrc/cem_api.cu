@@ -136,6 +136,7 @@ struct cem_replicas {
     cudaFree(sstate.halo);
     cudaFree(sstate.acc);
     cudaFree(sstate.run);
+    cudaFree(sstate.sched);
     if (sstate.exec) cudaGraphExecDestroy(sstate.exec);
     cudaFree(d_lw);
     cudaFree(d_trees);

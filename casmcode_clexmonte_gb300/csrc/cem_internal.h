@@ -79,6 +79,8 @@ struct StreamState {
   int8_t *halo = nullptr;        // [n_rep][halo bytes]
   long long *acc = nullptr;      // [n_rep][16]
   StreamRun *run = nullptr;      // device
+  int2 *sched = nullptr;         // [n_rep][n_sub] schedule of the current pass
+  int sched_cap = 0;             // entries allocated per replica
   cudaGraphExec_t exec = nullptr;
   int key = -1;
 };

@@ -25,60 +25,54 @@ struct StreamParams {
   long long halo_stride;
   long long *acc;          // [n_rep][16] pass accumulators
   const StreamRun *run;
-  int sub, n_classes, n_pair_sw, n_local_sw;
+  int2 *sched;             // [n_rep][n_sub]: (class, parameters) of each sub-step
+  int sub, n_sub, n_classes, n_pair_sw, n_local_sw;
   double RT[16];
 };
 
-// Class and parameters of sub-step `sub` of the pass (the schedule of the
-// shared-memory sweep: rank of the class key within its sweep).
-__device__ __forceinline__ void stream_schedule(const Replica &R, const CeTables &T, int ensemble,
-                                                long long pass, int sub, int n_classes,
-                                                int n_pair_sw, int &cls, uint32_t &par) {
+// Schedule of a pass (the shared-memory sweep's: class order by key rank
+// within each sweep, parameters per class): one CTA per replica, one thread
+// per (sweep, class).
+__global__ void k_stream_sched(const __grid_constant__ CeTables T,
+                               const __grid_constant__ StreamParams SP) {
+  const int rep = blockIdx.x;
+  const Replica &R = SP.reps[rep];
+  const long long pass = SP.stats[rep].pass;
   const uint32_t k0 = (uint32_t)R.seed, k1 = (uint32_t)(R.seed >> 32);
   const uint32_t plo = (uint32_t)pass, phi = (uint32_t)(pass >> 32) & 0xFFFFu;
-  const int sw = sub / n_classes, want = sub - sw * n_classes;
-  uint32_t keys[64];
-  for (int c = 0; c < n_classes; ++c) {
-    const int e = sw * n_classes + c;
-    keys[c] = philox4x32_10(U4{0xFFFFFFFFu - (uint32_t)e, 0u, plo, phi | (TAG_SCHED << 16)}, k0, k1).x;
-  }
-  cls = 0;
-  for (int c = 0; c < n_classes; ++c) {
+  const int nc = SP.n_classes;
+  const int dims[3] = {R.L[0] / 2, R.L[1] / 2, R.L[2] / 2};
+  for (int e = threadIdx.x; e < SP.n_sub; e += blockDim.x) {
+    const int sw = e / nc, c = e - sw * nc;
+    const U4 r = philox4x32_10(U4{0xFFFFFFFFu - (uint32_t)e, 0u, plo, phi | (TAG_SCHED << 16)}, k0, k1);
     int rank = 0;
-    for (int c2 = 0; c2 < n_classes; ++c2)
-      rank += (keys[c2] < keys[c]) || (keys[c2] == keys[c] && c2 < c);
-    if (rank == want) cls = c;
+    for (int c2 = 0; c2 < nc; ++c2) {
+      const uint32_t k2 = philox4x32_10(
+          U4{0xFFFFFFFFu - (uint32_t)(sw * nc + c2), 0u, plo, phi | (TAG_SCHED << 16)}, k0, k1).x;
+      rank += (k2 < r.x) || (k2 == r.x && c2 < c);
+    }
+    const uint32_t par = sched_param(r, R.ensemble, sw, SP.n_pair_sw, dims, T.n_nb[0]);
+    SP.sched[(long long)rep * SP.n_sub + sw * nc + rank] = make_int2(c, (int)par);
   }
-  const int e = sw * n_classes + cls;
-  const U4 r = philox4x32_10(U4{0xFFFFFFFFu - (uint32_t)e, 0u, plo, phi | (TAG_SCHED << 16)}, k0, k1);
-  const int half = R.L[0] / 2;
-  const int dims[3] = {half, R.L[1] / 2, R.L[2] / 2};
-  par = sched_param(r, ensemble, sw, n_pair_sw, dims, T.n_nb[0]);
 }
 
+// One colour sub-step of every replica; the class's candidates are split
+// into contiguous chunks, one per CTA. Canonical sub-steps compact the
+// candidate pairs whose occupants differ (the proposals) per warp, then
+// spread them over the CTA, as the shared-memory sweep does.
 template <int PITCH>
 __global__ void __launch_bounds__(256) k_stream_sub(const __grid_constant__ CeTables T,
                                                     const __grid_constant__ StreamParams SP) {
+  extern __shared__ int s_list[];  // kept candidates of this CTA
+  __shared__ int s_kept[8];
+  __shared__ long long s_red[8][16];
   const int rep = blockIdx.y;
   const Replica &R = SP.reps[rep];
-  __shared__ int s_cls;
-  __shared__ uint32_t s_par;
-  __shared__ long long s_red[8][16];
-  __shared__ float whi[MAX_FUNCS], wlo[MAX_FUNCS];
   const long long pass = SP.stats[rep].pass;
   const int ensemble = R.ensemble;
-  if (threadIdx.x == 0) {
-    int c;
-    uint32_t par;
-    stream_schedule(R, T, ensemble, pass, SP.sub, SP.n_classes, SP.n_pair_sw, c, par);
-    s_cls = c;
-    s_par = par;
-  }
-  for (int f = threadIdx.x; f < T.n_funcs; f += blockDim.x) {
-    whi[f] = T.w_hi[f];
-    wlo[f] = T.w_lo[f];
-  }
-  __syncthreads();
+  const int2 sc = SP.sched[(long long)rep * SP.n_sub + SP.sub];
+  const int c = sc.x;
+  const uint32_t par = (uint32_t)sc.y;
   Geo G;
   G.L0 = R.L[0];
   G.L1 = R.L[1];
@@ -87,11 +81,8 @@ __global__ void __launch_bounds__(256) k_stream_sub(const __grid_constant__ CeTa
   G.W = G.H = PITCH;
   G.V = PITCH * PITCH * (G.L2 + 4);
   int8_t *occ = SP.halo + (long long)rep * SP.halo_stride;
-  const int n_uc = G.L0 * G.L1 * G.L2;
-  const int c = s_cls;
-  const uint32_t par = s_par;
-  const int cc[3] = {c & 1, (c >> 1) & 1, (c >> 2) & 1};  // class = parities (p = 2, even L)
-  const int dims[3] = {G.L0 / 2, G.L1 / 2, G.L2 / 2};
+  const int cc0 = c & 1, cc1 = (c >> 1) & 1, cc2 = (c >> 2) & 1;  // class = parities (p = 2, even L)
+  const int d0 = G.L0 / 2, d1 = G.L1 / 2, d2 = G.L2 / 2;
   const uint32_t k0 = (uint32_t)R.seed, k1 = (uint32_t)(R.seed >> 32);
   const uint32_t plo = (uint32_t)pass, phi = (uint32_t)(pass >> 32) & 0xFFFFu;
   const uint32_t ctr_sub = (uint32_t)SP.sub;
@@ -99,16 +90,19 @@ __global__ void __launch_bounds__(256) k_stream_sub(const __grid_constant__ CeTa
   const int sw = SP.sub / SP.n_classes;
   const SiteEval<2, PITCH> ev{&T, nullptr, nullptr, nullptr};
   EnergyAcc<2> eacc;
-  int n_prop = 0, n_acc = 0, d1 = 0;
-  int dsub[4] = {0, 0, 0, 0};
-  auto cxf = [&](int a, int i) { return 2 * i + cc[a]; };
-  const int nthreads = gridDim.x * blockDim.x;
-  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  int n_prop = 0, n_acc = 0, d1sum = 0;
+  RegCounts<4> dsub;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  auto wrap_lt2 = [](int v, int L) { return v >= L ? v - L : v; };  // v < 2L
   if (ensemble == 0) {
-    const int n = dims[0] * dims[1] * dims[2];
-    for (int q = t0; q < n; q += nthreads) {
-      const int ix = q % dims[0], iy = (q / dims[0]) % dims[1], iz = q / (dims[0] * dims[1]);
-      const int x = cxf(0, ix), y = cxf(1, iy), z = cxf(2, iz);
+    // ---------------- flips: every class site is a proposal
+    const int n = d0 * d1 * d2;
+    const int per = (n + gridDim.x - 1) / gridDim.x;
+    const int q0 = blockIdx.x * per, q1 = min(n, q0 + per);
+    const FastDiv f0(d0), f1(d1);
+    for (int q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
+      const int t = f0.div(q), iz = f1.div(t);
+      const int x = 2 * (q - t * d0) + cc0, y = 2 * (t - iz * d1) + cc1, z = 2 * iz + cc2;
       const int ad = G.addr(0, x, y, z);
       const int o_i = occ[ad];
       const int l = x + G.L0 * (y + G.L1 * z);
@@ -118,89 +112,128 @@ __global__ void __launch_bounds__(256) k_stream_sub(const __grid_constant__ CeTa
       acc.zero();
       ev.add(0, o_i, o_f, occ, ad, acc);
       FF d;
-      const float de = sweep_de<2>(T, acc, whi, wlo, R.dmu_hi[o_i * 2 + o_f], R.dmu_lo[o_i * 2 + o_f], d);
+      const float de = sweep_de<2>(T, acc, nullptr, nullptr, R.dmu_hi[o_i * 2 + o_f],
+                                   R.dmu_lo[o_i * 2 + o_f], d);
       ++n_prop;
       if (accept_de(de, beta_f, u24(r.x))) {
         ++n_acc;
         put_site(occ, G, 0, x, y, z, (int8_t)o_f);
         eacc.add(acc, d, 0.0);
-        d1 += o_f - o_i;
-        dsub[sc_sublattice(x, y, z)] += o_f - o_i;
-      }
-    }
-  } else if (sw < SP.n_pair_sw) {
-    if (par != 0xFFFFFFFFu) {
-      const int a = par & 3, m = (par >> 2) & 255, rot = par >> 10;
-      const int na = dims[a];
-      const int half = (na / (2 * m)) * m;
-      int e3[3] = {dims[0], dims[1], dims[2]};
-      e3[a] = half;
-      const int n = e3[0] * e3[1] * e3[2];
-      for (int q = t0; q < n; q += nthreads) {
-        int ia[3] = {q % e3[0], (q / e3[0]) % e3[1], q / (e3[0] * e3[1])};
-        int ib[3] = {ia[0], ia[1], ia[2]};
-        const int jj = ia[a];
-        const int u = 2 * m * (jj / m) + (jj % m);
-        ia[a] = (u + rot) % na;
-        ib[a] = (u + m + rot) % na;
-        const int xa = cxf(0, ia[0]), ya = cxf(1, ia[1]), za = cxf(2, ia[2]);
-        const int xb = cxf(0, ib[0]), yb = cxf(1, ib[1]), zb = cxf(2, ib[2]);
-        const int ada = G.addr(0, xa, ya, za), adb = G.addr(0, xb, yb, zb);
-        const int oa = occ[ada], ob = occ[adb];
-        if (oa == ob) continue;
-        const int la = xa + G.L0 * (ya + G.L1 * za);
-        const U4 r = philox4x32_10(U4{(uint32_t)la, ctr_sub, plo, phi | (TAG_SITE << 16)}, k0, k1);
-        Acc<2> acc;
-        acc.zero();
-        ev.add(0, oa, ob, occ, ada, acc);
-        ev.add(0, ob, oa, occ, adb, acc);
-        FF d;
-        const float de = sweep_de<2>(T, acc, whi, wlo, 0.f, 0.f, d);
-        ++n_prop;
-        if (accept_de(de, beta_f, u24(r.x))) {
-          ++n_acc;
-          put_site(occ, G, 0, xa, ya, za, (int8_t)ob);
-          put_site(occ, G, 0, xb, yb, zb, (int8_t)oa);
-          eacc.add(acc, d, 0.0);
-        }
+        d1sum += o_f - o_i;
+        dsub.add(sc_sublattice(x, y, z), o_f - o_i);
       }
     }
   } else {
-    const int parity = par & 7, dlt = (par >> 3) & 15;
-    const int rots[3] = {(int)((par >> 7) & 127), (int)((par >> 14) & 127), (int)((par >> 21) & 127)};
-    if (T.n_nb[0] > 0) {
-      const int *du = T.nb_du[0][dlt];
-      int h[3];
-      for (int a = 0; a < 3; ++a) h[a] = dims[a] / 2;
-      const int n = h[0] * h[1] * h[2];
-      for (int q = t0; q < n; q += nthreads) {
-        const int t[3] = {q % h[0], (q / h[0]) % h[1], q / (h[0] * h[1])};
-        int ii[3];
-        for (int a = 0; a < 3; ++a) ii[a] = (rots[a] + ((parity >> a) & 1) + 2 * t[a]) % dims[a];
-        const int xa = cxf(0, ii[0]), ya = cxf(1, ii[1]), za = cxf(2, ii[2]);
-        const int xb = wrapc(xa + du[0], G.L0), yb = wrapc(ya + du[1], G.L1), zb = wrapc(za + du[2], G.L2);
-        const int ada = G.addr(0, xa, ya, za), adb = G.addr(0, xb, yb, zb);
-        const int oa = occ[ada], ob = occ[adb];
-        if (oa == ob) continue;
-        const int la = xa + G.L0 * (ya + G.L1 * za);
-        const U4 r = philox4x32_10(U4{(uint32_t)la, ctr_sub, plo, phi | (TAG_SITE << 16)}, k0, k1);
-        Acc<2> acc;
-        acc.zero();
-        ev.add(0, oa, ob, occ, ada, acc);
-        put_site(occ, G, 0, xa, ya, za, (int8_t)ob);
-        ev.add(0, ob, oa, occ, adb, acc);
-        FF d;
-        const float de = sweep_de<2>(T, acc, whi, wlo, 0.f, 0.f, d);
-        ++n_prop;
-        if (accept_de(de, beta_f, u24(r.x))) {
-          ++n_acc;
-          put_site(occ, G, 0, xb, yb, zb, (int8_t)oa);
-          eacc.add(acc, d, 0.0);
-          dsub[sc_sublattice(xa, ya, za)] += ob - oa;
-          dsub[sc_sublattice(xb, yb, zb)] += oa - ob;
-        } else {
-          put_site(occ, G, 0, xa, ya, za, (int8_t)oa);
+    // ---------------- canonical: pairs inside the class or neighbour swaps
+    const bool local = sw >= SP.n_pair_sw;
+    int n = 0, g0 = 1, g1 = 1, pa = 0, pm = 1, prot = 0, pna = 1;
+    int parity = 0, r0 = 0, r1 = 0, r2 = 0, du0 = 0, du1 = 0, du2 = 0;
+    if (!local) {
+      if (par != 0xFFFFFFFFu) {
+        pa = par & 3;
+        pm = (par >> 2) & 255;
+        prot = (int)(par >> 10);
+        pna = pa == 0 ? d0 : (pa == 1 ? d1 : d2);
+        const int half = (pna / (2 * pm)) * pm;
+        g0 = pa == 0 ? half : d0;
+        g1 = pa == 1 ? half : d1;
+        n = g0 * g1 * (pa == 2 ? half : d2);
+      }
+    } else if (T.n_nb[0] > 0) {
+      parity = par & 7;
+      const int dlt = (par >> 3) & 15;
+      r0 = (int)((par >> 7) & 127);
+      r1 = (int)((par >> 14) & 127);
+      r2 = (int)((par >> 21) & 127);
+      du0 = T.nb_du[0][dlt][0];
+      du1 = T.nb_du[0][dlt][1];
+      du2 = T.nb_du[0][dlt][2];
+      g0 = d0 / 2;
+      g1 = d1 / 2;
+      n = g0 * g1 * (d2 / 2);
+    }
+    const FastDiv fe0(g0), fe1(g1), fpm(pm);
+    auto sites_of = [&](int q, int &xa, int &ya, int &za, int &xb, int &yb, int &zb) {
+      const int t = fe0.div(q), i2 = fe1.div(t);
+      const int i0 = q - t * g0, i1 = t - i2 * g1;
+      if (!local) {
+        const int jj = pa == 0 ? i0 : (pa == 1 ? i1 : i2);
+        const int jq = fpm.div(jj);
+        const int u = 2 * pm * jq + (jj - jq * pm);
+        const int ja = wrap_lt2(u + prot, pna), jb = wrap_lt2(u + pm + prot, pna);
+        xa = 2 * (pa == 0 ? ja : i0) + cc0;
+        xb = 2 * (pa == 0 ? jb : i0) + cc0;
+        ya = 2 * (pa == 1 ? ja : i1) + cc1;
+        yb = 2 * (pa == 1 ? jb : i1) + cc1;
+        za = 2 * (pa == 2 ? ja : i2) + cc2;
+        zb = 2 * (pa == 2 ? jb : i2) + cc2;
+      } else {
+        xa = 2 * wrap_lt2(r0 + (parity & 1) + 2 * i0, d0) + cc0;
+        ya = 2 * wrap_lt2(r1 + ((parity >> 1) & 1) + 2 * i1, d1) + cc1;
+        za = 2 * wrap_lt2(r2 + ((parity >> 2) & 1) + 2 * i2, d2) + cc2;
+        xb = wrapc(xa + du0, G.L0);
+        yb = wrapc(ya + du1, G.L1);
+        zb = wrapc(za + du2, G.L2);
+      }
+    };
+    // phase A: this CTA's chunk, split between its warps, compacted in order
+    const int per = (n + gridDim.x - 1) / gridDim.x;
+    const int q0 = blockIdx.x * per, q1 = min(n, q0 + per);
+    const int nw = blockDim.x >> 5;
+    const int wper = (per + nw - 1) / nw;
+    const int wq0 = q0 + warp * wper, wq1 = min(q1, wq0 + wper);
+    int kept = 0;
+    for (int qb = wq0; qb < wq1; qb += 32) {
+      const int q = qb + lane;
+      bool act = false;
+      if (q < wq1) {
+        int xa, ya, za, xb, yb, zb;
+        sites_of(q, xa, ya, za, xb, yb, zb);
+        act = occ[G.addr(0, xa, ya, za)] != occ[G.addr(0, xb, yb, zb)];
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, act);
+      if (act) s_list[warp * wper + kept + __popc(m & ((1u << lane) - 1u))] = q;
+      kept += __popc(m);
+    }
+    if (lane == 0) s_kept[warp] = kept;
+    __syncthreads();
+    // phase B: kept pair i of the CTA goes to thread i mod block size
+    int total = 0;
+    for (int w = 0; w < nw; ++w) total += s_kept[w];
+    for (int i = threadIdx.x; i < total; i += blockDim.x) {
+      int wsel = 0, bsel = 0, run = 0;
+      for (int w = 0; w < nw; ++w) {
+        const int k = s_kept[w];
+        if (i >= run) {
+          wsel = w;
+          bsel = run;
         }
+        run += k;
+      }
+      const int q = s_list[wsel * wper + (i - bsel)];
+      int xa, ya, za, xb, yb, zb;
+      sites_of(q, xa, ya, za, xb, yb, zb);
+      const int ada = G.addr(0, xa, ya, za), adb = G.addr(0, xb, yb, zb);
+      const int oa = occ[ada], ob = occ[adb];
+      const int la = xa + G.L0 * (ya + G.L1 * za);
+      const U4 r = philox4x32_10(U4{(uint32_t)la, ctr_sub, plo, phi | (TAG_SITE << 16)}, k0, k1);
+      Acc<2> acc;
+      acc.zero();
+      ev.add(0, oa, ob, occ, ada, acc);
+      if (local) put_site(occ, G, 0, xa, ya, za, (int8_t)ob);  // first change applied
+      ev.add(0, ob, oa, occ, adb, acc);
+      FF d;
+      const float de = sweep_de<2>(T, acc, nullptr, nullptr, 0.f, 0.f, d);
+      ++n_prop;
+      if (accept_de(de, beta_f, u24(r.x))) {
+        ++n_acc;
+        if (!local) put_site(occ, G, 0, xa, ya, za, (int8_t)ob);
+        put_site(occ, G, 0, xb, yb, zb, (int8_t)oa);
+        eacc.add(acc, d, 0.0);
+        dsub.add(sc_sublattice(xa, ya, za), ob - oa);
+        dsub.add(sc_sublattice(xb, yb, zb), oa - ob);
+      } else if (local) {
+        put_site(occ, G, 0, xa, ya, za, (int8_t)oa);
       }
     }
   }
@@ -209,10 +242,10 @@ __global__ void __launch_bounds__(256) k_stream_sub(const __grid_constant__ CeTa
   for (int k = 0; k < 16; ++k) vals[k] = 0;
   vals[0] = n_prop;
   vals[1] = n_acc;
-  vals[2] = d1;
-  for (int k = 0; k < 4; ++k) vals[4 + k] = dsub[k];
+  vals[2] = d1sum;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) vals[4 + k] = dsub.v[k];
   for (int g = 0; g < MAX_ORBITS; ++g) vals[8 + g] = eacc.dc[g];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < 16; ++k)
     for (int off = 16; off; off >>= 1) vals[k] += __shfl_xor_sync(0xffffffffu, vals[k], off);
@@ -224,7 +257,6 @@ __global__ void __launch_bounds__(256) k_stream_sub(const __grid_constant__ CeTa
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_red[w][threadIdx.x];
     if (t) atomicAdd((unsigned long long *)&SP.acc[rep * 16 + threadIdx.x], (unsigned long long)t);
   }
-  (void)n_uc;
 }
 
 // End of pass: one thread per replica.
@@ -343,6 +375,14 @@ static cudaError_t stream_run_t(const CeTables &T, StreamState &st, const Replic
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   const int n_sub = (n_pair_sw + n_local_sw) * n_classes;
   const int key = n_sub * 1000 + n_classes * 10 + n_pair_sw;
+  if (st.sched_cap < n_sub) {
+    cudaFree(st.sched);
+    st.sched = nullptr;
+    if ((e = cudaMalloc(&st.sched, sizeof(int2) * n_sub * n_rep)) != cudaSuccess) return e;
+    st.sched_cap = n_sub;
+    if (st.exec) cudaGraphExecDestroy(st.exec);
+    st.exec = nullptr;
+  }
   if (!st.exec || st.key != key) {
     if (st.exec) cudaGraphExecDestroy(st.exec);
     st.exec = nullptr;
@@ -353,16 +393,26 @@ static cudaError_t stream_run_t(const CeTables &T, StreamState &st, const Replic
     SP.halo_stride = stride;
     SP.acc = st.acc;
     SP.run = st.run;
+    SP.sched = st.sched;
+    SP.n_sub = n_sub;
     SP.n_classes = n_classes;
     SP.n_pair_sw = n_pair_sw;
     SP.n_local_sw = n_local_sw;
     for (int k = 0; k < 16; ++k) SP.RT[k] = RT[k];
     cudaGraph_t graph;
     if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
-    const int blocks = 304;  // 2 x 152 SMs of CTAs per replica and sub-step
+    const int blocks = 304;  // 2 x 152 SMs of CTAs per sub-step, over all replicas
+    // candidates per CTA: at most (L/2)^3 per class, split into bx chunks
+    // of at most 8192 (their list stays below 48 KB of shared memory), plus
+    // rounding of the per-warp chunks
+    const long long half = L2 / 2, n_max = half * half * half;
+    int bx = blocks / n_rep > 0 ? blocks / n_rep : 1;
+    if (bx < (n_max + 8191) / 8192) bx = (int)((n_max + 8191) / 8192);
+    const int smem = (int)(4 * ((n_max + bx - 1) / bx + 8));
+    k_stream_sched<<<n_rep, 64, 0, s>>>(T, SP);
     for (int sub = 0; sub < n_sub; ++sub) {
       SP.sub = sub;
-      k_stream_sub<PITCH><<<dim3(blocks / n_rep > 0 ? blocks / n_rep : 1, n_rep), 256, 0, s>>>(T, SP);
+      k_stream_sub<PITCH><<<dim3(bx, n_rep), 256, smem, s>>>(T, SP);
     }
     k_stream_end<<<(n_rep + 63) / 64, 64, 0, s>>>(T, SP, n_rep);
     if ((e = cudaStreamEndCapture(s, &graph)) != cudaSuccess) return e;
