@@ -96,6 +96,32 @@ def render(ce, name="gen_fcc") -> str:
         L.append(f"  n[{g}] = {expr};")
     L.append("}")
     L.append("")
+    # owned clusters: anchored at the site (its lexicographically smallest
+    # point), so every periodic cluster is counted once over all sites
+    index = {tuple(d): k for k, d in enumerate(nbs)}
+    owned = [[] for _ in orbits]
+    for c in ce.owned[0]:
+        owned[c.orbit].append(tuple(index[tuple(du)] for _, du in c.partners))
+    used = sorted({k for cl in owned for c in cl for k in c})
+    L.append("// owned[g] = number of clusters of orbit g anchored at this site (its")
+    L.append("// lexicographically smallest point) whose other sites are all 1")
+    L.append("template <int P>")
+    L.append("__device__ __forceinline__ void owned_counts(const int8_t *__restrict__ c,")
+    L.append("                                             int (&n)[N_ORBITS]) {")
+    for k in used:
+        d = nbs[k]
+        L.append(f"  const int v{k} = c[({d[0]}) + P * ({d[1]}) + P * P * ({d[2]})];")
+    for g, cl in enumerate(owned):
+        if orbits[g][0] == 1:
+            L.append(f"  n[{g}] = 1;")
+            continue
+        terms = []
+        for c in cl:
+            terms.append(" & ".join(f"v{k}" for k in c) if len(c) > 1 else f"v{c[0]}")
+        expr = " + ".join(f"({t})" if "&" in t else t for t in terms) if terms else "0"
+        L.append(f"  n[{g}] = {expr};")
+    L.append("}")
+    L.append("")
     L.append(f"}}  // namespace {name}")
     L.append("}  // namespace cem")
     return "\n".join(L) + "\n"

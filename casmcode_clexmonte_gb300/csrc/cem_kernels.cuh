@@ -1024,10 +1024,19 @@ __global__ void __launch_bounds__(THREADS, 1)
       auto eval_site = [&](int l) {
         int b, x, y, z;
         site_of(l, b, x, y, z);
-        Acc<2> acc;
-        acc.zero();
-        ev.add(b, 0, 1, occ, G.addr(b, x, y, z), acc);
-        for (int g = 0; g < MAX_ORBITS; ++g) cnt[g] += acc.c[g];
+        if constexpr (PITCH > 0) {
+          // clusters anchored at the site, each counted once: scale by the
+          // orbit size for the division below
+          int nn[gen_fcc::N_ORBITS];
+          gen_fcc::owned_counts<PITCH>(occ + G.addr(b, x, y, z), nn);
+#pragma unroll
+          for (int g = 0; g < gen_fcc::N_ORBITS; ++g) cnt[g] += nn[g] * T.orb_size[g];
+        } else {
+          Acc<2> acc;
+          acc.zero();
+          ev.add(b, 0, 1, occ, G.addr(b, x, y, z), acc);
+          for (int g = 0; g < MAX_ORBITS; ++g) cnt[g] += acc.c[g];
+        }
         ++n1;
         sub[sc_sublattice(x, y, z)]++;
       };
