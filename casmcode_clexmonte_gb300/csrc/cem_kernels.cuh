@@ -876,6 +876,104 @@ __device__ __forceinline__ void compact_pairs(const PairGeom &pg, const Geo &G, 
   if (lane == 0) wk[warp] = kept;
 }
 
+// Exact initial statistics of a binary replica staged in shared memory,
+// written to S: count_g = number of clusters of orbit g with every site
+// occupant 1. Kept out of line, so that the sweep loop's register allocation
+// does not depend on it.
+template <int PITCH, int NW>
+__device__ __noinline__ void init_binary_stats(const CeTables &T, const int8_t *occ,
+                                               const Geo &G, const SiteIndex &site_of,
+                                               const SiteEval<2, PITCH> &ev, int n_sites,
+                                               int n_uc, int *qbase, unsigned char *red,
+                                               ReplicaStats &S) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // exact initial state: every cluster of orbit g with all sites occupant 1
+  // is seen from each of its size_g sites, so count_g = sum over sites with
+  // occupant 1 of its flower count / size_g
+  // Occupied sites are queued per warp and evaluated 64 at a time (two
+  // independent sites per lane), so no lane idles on an empty site.
+  long long cnt[MAX_ORBITS];
+  for (int g = 0; g < MAX_ORBITS; ++g) cnt[g] = 0;
+  long long n1 = 0, sub[4] = {0, 0, 0, 0};
+  int *q = qbase + warp * 96;
+  int qn = 0;
+  auto eval_site = [&](int l) {
+    int b, x, y, z;
+    site_of(l, b, x, y, z);
+    if constexpr (PITCH > 0) {
+      // clusters anchored at the site, each counted once: scale by the
+      // orbit size for the division below
+      int nn[gen_fcc::N_ORBITS];
+      gen_fcc::owned_counts<PITCH>(occ + G.addr(b, x, y, z), nn);
+#pragma unroll
+      for (int g = 0; g < gen_fcc::N_ORBITS; ++g) cnt[g] += nn[g] * T.orb_size[g];
+    } else {
+      Acc<2> acc;
+      acc.zero();
+      ev.add(b, 0, 1, occ, G.addr(b, x, y, z), acc);
+      for (int g = 0; g < MAX_ORBITS; ++g) cnt[g] += acc.c[g];
+    }
+    ++n1;
+    sub[sc_sublattice(x, y, z)]++;
+  };
+  const int per_warp = (n_sites + NW - 1) / NW;
+  const int l_begin = warp * per_warp, l_end = min(n_sites, l_begin + per_warp);
+  for (int l0 = l_begin; l0 < l_end; l0 += 32) {
+    const int l = l0 + lane;
+    bool one = false;
+    if (l < l_end) {
+      int b, x, y, z;
+      site_of(l, b, x, y, z);
+      one = occ[G.addr(b, x, y, z)] != 0;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, one);
+    if (one) q[qn + __popc(m & ((1u << lane) - 1u))] = l;
+    qn += __popc(m);
+    __syncwarp();
+    if (qn >= 64) {
+      eval_site(q[lane]);
+      eval_site(q[32 + lane]);
+      __syncwarp();
+      if (lane < qn - 64) q[lane] = q[64 + lane];
+      qn -= 64;
+      __syncwarp();
+    }
+  }
+  if (lane < qn) eval_site(q[lane]);
+  if (lane + 32 < qn) eval_site(q[lane + 32]);
+  long long *rd_l = reinterpret_cast<long long *>(red);
+  for (int off = 16; off; off >>= 1) {
+    n1 += __shfl_xor_sync(0xffffffffu, n1, off);
+    for (int g = 0; g < MAX_ORBITS; ++g) cnt[g] += __shfl_xor_sync(0xffffffffu, cnt[g], off);
+    for (int k = 0; k < 4; ++k) sub[k] += __shfl_xor_sync(0xffffffffu, sub[k], off);
+  }
+  if (lane == 0) {
+    for (int g = 0; g < MAX_ORBITS; ++g) rd_l[warp * 16 + g] = cnt[g];
+    rd_l[warp * 16 + 8] = n1;
+    for (int k = 0; k < 4; ++k) rd_l[warp * 16 + 9 + k] = sub[k];
+  }
+  __syncthreads();
+  if (tid == 0) {
+    long long tot[13] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int w = 0; w < NW; ++w)
+      for (int k = 0; k < 13; ++k) tot[k] += rd_l[w * 16 + k];
+    double e = T.w[0] * n_uc;
+    for (int g = 0; g < T.n_orbits; ++g)
+      e += T.w[T.orb_func_base[g]] * (double)(tot[g] / T.orb_size[g]);
+    const long long pass = S.pass, np = S.n_proposed, na = S.n_accepted;
+    unsigned char *raw = reinterpret_cast<unsigned char *>(&S);
+    for (int q = 0; q < (int)sizeof(ReplicaStats); ++q) raw[q] = 0;
+    S.energy = e;
+    S.n_species[0] = n_sites - tot[8];
+    S.n_species[1] = tot[8];
+    for (int k = 0; k < 4; ++k) S.n_sub[k] = tot[9 + k];
+    S.pass = pass;
+    S.n_proposed = np;
+    S.n_accepted = na;
+  }
+  __syncthreads();
+}
+
 template <int NOCC, int PITCH, int THREADS = SWEEP_THREADS>
 __global__ void __launch_bounds__(THREADS, 1)
     k_sweep(const __grid_constant__ CeTables T, const __grid_constant__ SweepParams P) {
@@ -1008,95 +1106,11 @@ __global__ void __launch_bounds__(THREADS, 1)
                     // image of one core site: L >= 2 reach + 1 on every axis)
 
   const SiteEval<NOCC, PITCH> ev{&T, cl_off, lutoff, lut};
-  const int lane = tid & 31, warp = tid >> 5, nwarp = NW;
+  const int lane = tid & 31, warp = tid >> 5;
   if constexpr (NOCC == 2) {
-    if (P.init) {
-      // exact initial state: every cluster of orbit g with all sites occupant 1
-      // is seen from each of its size_g sites, so count_g = sum over sites with
-      // occupant 1 of its flower count / size_g
-      // Occupied sites are queued per warp and evaluated 64 at a time (two
-      // independent sites per lane), so no lane idles on an empty site.
-      long long cnt[MAX_ORBITS];
-      for (int g = 0; g < MAX_ORBITS; ++g) cnt[g] = 0;
-      long long n1 = 0, sub[4] = {0, 0, 0, 0};
-      int *q = reinterpret_cast<int *>(smem + lay.initq) + warp * 96;
-      int qn = 0;
-      auto eval_site = [&](int l) {
-        int b, x, y, z;
-        site_of(l, b, x, y, z);
-        if constexpr (PITCH > 0) {
-          // clusters anchored at the site, each counted once: scale by the
-          // orbit size for the division below
-          int nn[gen_fcc::N_ORBITS];
-          gen_fcc::owned_counts<PITCH>(occ + G.addr(b, x, y, z), nn);
-#pragma unroll
-          for (int g = 0; g < gen_fcc::N_ORBITS; ++g) cnt[g] += nn[g] * T.orb_size[g];
-        } else {
-          Acc<2> acc;
-          acc.zero();
-          ev.add(b, 0, 1, occ, G.addr(b, x, y, z), acc);
-          for (int g = 0; g < MAX_ORBITS; ++g) cnt[g] += acc.c[g];
-        }
-        ++n1;
-        sub[sc_sublattice(x, y, z)]++;
-      };
-      const int per_warp = (n_sites + NW - 1) / NW;
-      const int l_begin = warp * per_warp, l_end = min(n_sites, l_begin + per_warp);
-      for (int l0 = l_begin; l0 < l_end; l0 += 32) {
-        const int l = l0 + lane;
-        bool one = false;
-        if (l < l_end) {
-          int b, x, y, z;
-          site_of(l, b, x, y, z);
-          one = occ[G.addr(b, x, y, z)] != 0;
-        }
-        const unsigned m = __ballot_sync(0xffffffffu, one);
-        if (one) q[qn + __popc(m & ((1u << lane) - 1u))] = l;
-        qn += __popc(m);
-        __syncwarp();
-        if (qn >= 64) {
-          eval_site(q[lane]);
-          eval_site(q[32 + lane]);
-          __syncwarp();
-          if (lane < qn - 64) q[lane] = q[64 + lane];
-          qn -= 64;
-          __syncwarp();
-        }
-      }
-      if (lane < qn) eval_site(q[lane]);
-      if (lane + 32 < qn) eval_site(q[lane + 32]);
-      long long *rd_l = reinterpret_cast<long long *>(red);
-      for (int off = 16; off; off >>= 1) {
-        n1 += __shfl_xor_sync(0xffffffffu, n1, off);
-        for (int g = 0; g < MAX_ORBITS; ++g) cnt[g] += __shfl_xor_sync(0xffffffffu, cnt[g], off);
-        for (int k = 0; k < 4; ++k) sub[k] += __shfl_xor_sync(0xffffffffu, sub[k], off);
-      }
-      if (lane == 0) {
-        for (int g = 0; g < MAX_ORBITS; ++g) rd_l[warp * 16 + g] = cnt[g];
-        rd_l[warp * 16 + 8] = n1;
-        for (int k = 0; k < 4; ++k) rd_l[warp * 16 + 9 + k] = sub[k];
-      }
-      __syncthreads();
-      if (tid == 0) {
-        long long tot[13] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-        for (int w = 0; w < nwarp; ++w)
-          for (int k = 0; k < 13; ++k) tot[k] += rd_l[w * 16 + k];
-        double e = T.w[0] * n_uc;
-        for (int g = 0; g < T.n_orbits; ++g)
-          e += T.w[T.orb_func_base[g]] * (double)(tot[g] / T.orb_size[g]);
-        const long long pass = S.pass, np = S.n_proposed, na = S.n_accepted;
-        unsigned char *raw = reinterpret_cast<unsigned char *>(&S);
-        for (int q = 0; q < (int)sizeof(ReplicaStats); ++q) raw[q] = 0;
-        S.energy = e;
-        S.n_species[0] = n_sites - tot[8];
-        S.n_species[1] = tot[8];
-        for (int k = 0; k < 4; ++k) S.n_sub[k] = tot[9 + k];
-        S.pass = pass;
-        S.n_proposed = np;
-        S.n_accepted = na;
-      }
-      __syncthreads();
-    }
+    if (P.init)
+      init_binary_stats<PITCH, NW>(T, occ, G, site_of, ev, n_sites, n_uc,
+                                   reinterpret_cast<int *>(smem + lay.initq), red, S);
   }
   double energy = S.energy;
   long long nspec[8], nsub[4];
