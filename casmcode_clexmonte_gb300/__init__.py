@@ -20,6 +20,7 @@ from .casm_io import (  # noqa: F401
     SummaryWriter,
     read_cluster_expansion,
     read_prim,
+    read_system,
     write_eci_json,
 )
 

@@ -32,7 +32,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import CEM_CANONICAL, CEM_SEMIGRAND_CANONICAL, check, ptr
-from .system import KB, ClusterExpansion, composition_RT, system_arrays
+from .system import KB, ClusterExpansion, param_RT_of, system_arrays
 
 METHODS = {"semigrand_canonical": CEM_SEMIGRAND_CANONICAL, "canonical": CEM_CANONICAL}
 
@@ -51,7 +51,7 @@ class System:
         self.handle = h
         self.n_occ = ce.prim.n_occ
         self.n_funcs = ce.n_funcs
-        self.RT = composition_RT(ce.prim.n_basis, ce.prim.n_occ)
+        self.RT = param_RT_of(ce)
 
     def __del__(self):
         h = getattr(self, "handle", None)
@@ -259,13 +259,16 @@ class ReplicaBatch:
 
 
 def mol_composition(system: "System", param_composition) -> np.ndarray:
-    """Species per unit cell for a parametric composition on the standard
-    axes (origin: every site occupant 0; end member k: every site occupant k)."""
+    """Species per unit cell for a parametric composition on the system's
+    composition axes (origin: every site occupant 0; mol = origin + Q x with
+    Q the pseudo-inverse of the axes' R^T)."""
     nb = system.ce.prim.n_basis
     x = np.atleast_1d(np.asarray(param_composition, dtype=np.float64))
     if x.size != system.n_occ - 1:
         raise ValueError(f"param_composition must have {system.n_occ - 1} components")
-    return np.concatenate([[nb * (1.0 - x.sum())], nb * x])
+    origin = np.zeros(system.n_occ)
+    origin[0] = nb
+    return origin + np.linalg.pinv(system.RT) @ x
 
 
 def enforce_composition(state: "MonteCarloState", target_mol_composition, system: "System",

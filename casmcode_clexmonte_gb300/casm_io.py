@@ -1,5 +1,7 @@
 """Reference-format input and results output.
 
+* ``read_system``: a CASM ``system.json`` (prim, composition axes, the
+  formation-energy basis set and its coefficients).
 * ``read_prim`` / ``read_cluster_expansion``: CASM ``prim.json`` and the basis
   set / ECI JSON (``formation_energy_eci.json``: ``bspecs`` with
   ``orbit_branch_specs`` max lengths, ``orbits`` with ``mult`` and
@@ -101,6 +103,58 @@ def read_cluster_expansion(prim_src, eci_src, sparse_eci=None) -> ClusterExpansi
         for idx, val in sp:
             eci[int(idx)] = float(val)
     ce.eci = eci
+    return ce
+
+
+def composition_axes_RT(axes: dict, occupants) -> np.ndarray:
+    """R^T (independent axes x components, in the prim's occupant order) of
+    CASM composition axes (``origin`` and one end member per axis, species
+    per unit cell, over ``components``). The samplers count the composition
+    from the state where every site holds occupant 0, so the origin must be
+    that state."""
+    comps = list(axes["components"])
+    if sorted(comps) != sorted(occupants):
+        raise ValueError(f"composition components {comps} differ from the occupants {list(occupants)}")
+    order = [comps.index(o) for o in occupants]
+    origin = np.asarray(axes["origin"], dtype=np.float64)[order]
+    names = [k for k in "abcdefghijklmnopqrstuvwxyz" if k in axes]
+    if len(names) != len(occupants) - 1:
+        raise ValueError(f"expected {len(occupants) - 1} independent composition axes, found {len(names)}")
+    Q = np.stack([np.asarray(axes[k], dtype=np.float64)[order] - origin for k in names], axis=1)
+    n_basis = origin.sum()
+    expect = np.zeros(len(occupants))
+    expect[0] = n_basis
+    if not np.allclose(origin, expect):
+        raise ValueError("composition axes whose origin is not 'every site occupant 0' are not supported")
+    return np.ascontiguousarray(np.linalg.pinv(Q))
+
+
+def read_system(path: str) -> ClusterExpansion:
+    """Formation-energy cluster expansion of a CASM ``system.json``
+    (``System_json_io.cc:491-538``): ``prim``, ``composition_axes``,
+    ``clex.formation_energy`` = (basis set, coefficients). The basis set's
+    functions are rebuilt from its ``bspecs`` (the generated Clexulator
+    source is not compiled) and checked orbit by orbit against the
+    coefficients file, or against the basis set's ``basis.json`` when the
+    coefficients are a sparse ``[[index, value]]`` list."""
+    base = os.path.dirname(os.path.abspath(path))
+    d = json.load(open(path))
+    clex = d["clex"]["formation_energy"]
+    bset = d["basis_sets"][clex["basis_set"]]
+    bdir = os.path.dirname(os.path.join(base, bset["source"]))
+    coef = json.load(open(os.path.join(base, clex["coefficients"])))
+    if isinstance(coef, dict):
+        doc = dict(coef)
+        if "bspecs" not in doc:
+            doc["bspecs"] = json.load(open(os.path.join(bdir, "bspecs.json")))
+        ce = read_cluster_expansion(d["prim"], doc)
+    else:
+        basis = json.load(open(os.path.join(bdir, "basis.json")))
+        if "bspecs" not in basis:
+            basis["bspecs"] = json.load(open(os.path.join(bdir, "bspecs.json")))
+        ce = read_cluster_expansion(d["prim"], basis, sparse_eci=coef)
+    if "composition_axes" in d:
+        ce.param_RT = composition_axes_RT(d["composition_axes"], ce.prim.occupants)
     return ce
 
 

@@ -219,6 +219,9 @@ class ClusterExpansion:
         self.eci = np.zeros(self.n_funcs) if eci is None else np.asarray(eci, float)
         if self.eci.shape != (self.n_funcs,):
             raise ValueError(f"eci must have {self.n_funcs} entries")
+        # R^T of the parametric composition axes; None = the standard axes
+        # (origin: every site occupant 0; end member k: every site occupant k)
+        self.param_RT = None
 
     # ---- symmetry
     def _check_symmetry(self):
@@ -601,6 +604,15 @@ def composition_RT(n_basis: int, n_occ: int) -> np.ndarray:
     return np.ascontiguousarray(np.linalg.pinv(Q))
 
 
+def param_RT_of(ce: ClusterExpansion) -> np.ndarray:
+    """R^T of the cluster expansion's composition axes (standard axes unless
+    set from a CASM system file)."""
+    rt = getattr(ce, "param_RT", None)
+    if rt is None:
+        return composition_RT(ce.prim.n_basis, ce.prim.n_occ)
+    return np.ascontiguousarray(rt, dtype=np.float64)
+
+
 def system_arrays(ce: ClusterExpansion) -> dict:
     """Flat arrays of the C ABI's ``cem_system_desc`` for a cluster expansion."""
     n_sf = ce.n_sf
@@ -615,7 +627,7 @@ def system_arrays(ce: ClusterExpansion) -> dict:
         orbit_func_begin=np.array([o.func_begin for o in orbits], dtype=np.int32),
         orbit_n_funcs=np.array([o.n_funcs for o in orbits], dtype=np.int32),
         weights=np.ascontiguousarray(ce.weights(), dtype=np.float64),
-        param_RT=composition_RT(ce.prim.n_basis, ce.prim.n_occ).reshape(-1),
+        param_RT=param_RT_of(ce).reshape(-1),
     )
     for name, table in (("flower", ce.flowers), ("owned", ce.owned)):
         sub, orb, psub, pdu, lut = [], [], [], [], []

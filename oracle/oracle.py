@@ -125,7 +125,8 @@ class OracleSystem:
         ml = np.zeros(5)
         for k, v in ce.max_length.items():
             ml[k] = v
-        self.RT = composition_RT(prim.n_basis, prim.n_occ)
+        rt = getattr(ce, "param_RT", None)
+        self.RT = composition_RT(prim.n_basis, prim.n_occ) if rt is None else np.asarray(rt, dtype=np.float64)
         h = lib().ora_system_create(
             prim.n_basis,
             np.ascontiguousarray(prim.lattice.reshape(-1), dtype=np.int64),

@@ -216,3 +216,62 @@ def test_summary_layout(method, components, convergence, tmp_path):
         ms = data["analysis"]["mol_susc"]
         assert ms["B,B"][0] == pytest.approx(4 * ps["a,a"][0])
         assert ms["A,A"][0] == pytest.approx(4 * 2 * ps["a,a"][0])
+
+
+def _write_project(tmp_path, sparse: bool, axes=None):
+    """A CASM project directory in the reference's layout (system.json,
+    basis_sets/bset.default/{bspecs,basis}.json, coefficients)."""
+    prim, eci, facts = _fcc_ternary_docs()
+    bdir = tmp_path / "basis_sets" / "bset.default"
+    bdir.mkdir(parents=True)
+    json.dump(eci["bspecs"], open(bdir / "bspecs.json", "w"))
+    basis = json.loads(json.dumps(eci))
+    for o in basis["orbits"]:
+        for f in o["cluster_functions"]:
+            f.pop("eci", None)
+    json.dump(basis, open(bdir / "basis.json", "w"))
+    if sparse:
+        json.dump(facts["sparse_eci"], open(tmp_path / "eci.json", "w"))
+    else:
+        json.dump(eci, open(tmp_path / "eci.json", "w"))
+    system = {
+        "prim": prim,
+        "composition_axes": axes or {"components": ["A", "B", "Va"], "origin": [1.0, 0.0, 0.0],
+                                     "a": [0.0, 1.0, 0.0], "b": [0.0, 0.0, 1.0],
+                                     "independent_compositions": 2},
+        "basis_sets": {"default": {"source": "basis_sets/bset.default/FCC_Clexulator_default.cc"}},
+        "clex": {"formation_energy": {"basis_set": "default", "coefficients": "eci.json"}},
+    }
+    json.dump(system, open(tmp_path / "system.json", "w"))
+    return str(tmp_path / "system.json"), facts
+
+
+@pytest.mark.parametrize("sparse", [False, True])
+def test_read_system_json(sparse, tmp_path):
+    path, facts = _write_project(tmp_path, sparse)
+    ce = casm_io.read_system(path)
+    want = np.zeros(ce.n_funcs)
+    for i, v in facts["sparse_eci"]:
+        want[i] = v
+    np.testing.assert_array_equal(ce.eci, want)
+    from casmcode_clexmonte_gb300.system import composition_RT, system_arrays
+
+    np.testing.assert_allclose(ce.param_RT, composition_RT(1, 3))
+    np.testing.assert_allclose(system_arrays(ce)["param_RT"], composition_RT(1, 3).reshape(-1))
+
+
+def test_read_system_composition_axes(tmp_path):
+    # axes listed in another component order and with the end members swapped
+    axes = {"components": ["Va", "A", "B"], "origin": [0.0, 1.0, 0.0],
+            "a": [1.0, 0.0, 0.0], "b": [0.0, 0.0, 1.0]}
+    path, _ = _write_project(tmp_path, False, axes)
+    ce = casm_io.read_system(path)
+    # a = Va content, b = B content: rows of R^T select those species
+    RT = ce.param_RT
+    x = RT @ (np.array([0.5, 0.2, 0.3]) - np.array([1.0, 0.0, 0.0]))  # A, B, Va per unit cell
+    np.testing.assert_allclose(x, [0.3, 0.2])
+    bad = {"components": ["A", "B", "Va"], "origin": [0.0, 1.0, 0.0],
+           "a": [1.0, 0.0, 0.0], "b": [0.0, 0.0, 1.0]}
+    path2, _ = _write_project(tmp_path / "p2", False, bad)
+    with pytest.raises(ValueError, match="origin"):
+        casm_io.read_system(path2)
