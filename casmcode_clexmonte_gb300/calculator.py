@@ -175,6 +175,15 @@ class ReplicaBatch:
     def run(self, n_passes: int, n_equil: int = 0, record_samples: bool = False):
         check(self.lib.cem_run(self.handle, int(n_passes), int(n_equil), int(bool(record_samples))))
 
+    def autotune(self, trial_passes: int = 20) -> dict:
+        """Pick the fastest launch schedule (threads per replica, replica
+        order) by timing trial passes from the current state; the state is
+        restored afterwards."""
+        ms = C.c_double()
+        check(self.lib.cem_autotune(self.handle, int(trial_passes), C.byref(ms)))
+        return dict(threads=self.get_option("threads"), cta_order=self.get_option("cta_order"),
+                    trial_ms=ms.value)
+
     def set_option(self, key: str, value: int):
         check(self.lib.cem_set_option(self.handle, key.encode(), int(value)))
 

@@ -115,6 +115,9 @@ struct cem_replicas {
   int max_classes = 1, sweep_smem = 0, pitch = 0, generic_smem = 0;
   int n_pair_sweeps = 2, n_local_sweeps = 1;
   int threads = SWEEP_THREADS;
+  // replica -> CTA schedule: 0 = CTA i runs replica i, 1 = largest replicas first
+  int cta_order = 0;
+  int *d_cta_rep = nullptr;
   bool reps_dirty = true, stats_valid = false;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -142,6 +145,7 @@ struct cem_replicas {
     cudaFree(d_trees);
     cudaFree(d_lsamples);
     cudaFree(d_nftree);
+    cudaFree(d_cta_rep);
     cudaFree(d_nftree_off);
     cudaFree(d_reps);
     cudaFree(d_stats);
@@ -808,6 +812,24 @@ int cem_reset_stats(cem_replicas *r) {
   });
 }
 
+// Replica -> CTA schedule of the shared-memory sweep. Mode 1 launches the
+// largest replicas first (stable in replica order), so that a batch of uneven
+// supercells does not end on a few large replicas; the results do not depend
+// on the schedule.
+static void set_cta_order(cem_replicas *r, int mode) {
+  require(mode == 0 || mode == 1, "cta_order must be 0 (replica order) or 1 (largest first)");
+  cudaFree(r->d_cta_rep);
+  r->d_cta_rep = nullptr;
+  r->cta_order = mode;
+  if (mode == 0) return;
+  std::vector<int> order(r->n);
+  for (int i = 0; i < r->n; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return r->reps[a].n_sites > r->reps[b].n_sites; });
+  CUDA_OK(cudaMalloc(&r->d_cta_rep, sizeof(int) * r->n));
+  CUDA_OK(cudaMemcpy(r->d_cta_rep, order.data(), sizeof(int) * r->n, cudaMemcpyHostToDevice));
+}
+
 // Zero the sampled moments of every replica (keeps energy, species counts and
 // the pass / event counters).
 static void reset_moments(cem_replicas *r) {
@@ -1049,6 +1071,7 @@ int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_sampl
     P.max_classes = r->max_classes;
     P.n_pair_sweeps = r->n_pair_sweeps;
     P.n_local_sweeps = r->n_local_sweeps;
+    P.cta_rep = r->d_cta_rep;
     const CeTables &T = r->sys->T;
     for (size_t k = 0; k < r->sys->RT.size() && k < 16; ++k) P.RT[k] = r->sys->RT[k];
     if (record_samples) {
@@ -1142,6 +1165,63 @@ int cem_smem_bandwidth(double *gbs) {
   });
 }
 
+int cem_autotune(cem_replicas *r, int64_t trial_passes, double *best_ms) {
+  return guard([&] {
+    require(r != nullptr, "null handle");
+    require(trial_passes > 0, "trial_passes must be > 0");
+    if (best_ms) *best_ms = 0.0;
+    if (r->streamed) return;  // one fixed graph per pass
+    int8_t *occ_save = nullptr;
+    ReplicaStats *st_save = nullptr;
+    auto cleanup = [&] {
+      cudaFree(occ_save);
+      cudaFree(st_save);
+    };
+    try {
+      CUDA_OK(cudaMalloc(&occ_save, (size_t)r->total_sites + 16));
+      CUDA_OK(cudaMalloc(&st_save, sizeof(ReplicaStats) * r->n));
+      CUDA_OK(cudaMemcpyAsync(occ_save, r->d_occ, (size_t)r->total_sites, cudaMemcpyDeviceToDevice,
+                              r->stream));
+      CUDA_OK(cudaMemcpyAsync(st_save, r->d_stats, sizeof(ReplicaStats) * r->n,
+                              cudaMemcpyDeviceToDevice, r->stream));
+      const bool valid0 = r->stats_valid;
+      auto restore = [&] {
+        CUDA_OK(cudaMemcpyAsync(r->d_occ, occ_save, (size_t)r->total_sites,
+                                cudaMemcpyDeviceToDevice, r->stream));
+        CUDA_OK(cudaMemcpyAsync(r->d_stats, st_save, sizeof(ReplicaStats) * r->n,
+                                cudaMemcpyDeviceToDevice, r->stream));
+        r->stats_valid = valid0;
+      };
+      double best = 1e300;
+      int bt = r->threads, bo = r->cta_order;
+      for (int th : {SWEEP_THREADS, 256})
+        for (int order : {0, 1}) {
+          restore();
+          r->threads = th;
+          set_cta_order(r, order);
+          if (cem_run(r, trial_passes, 0, 0) != CEM_OK) throw Err(CEM_ERR_CUDA, cem_last_error());
+          CUDA_OK(cudaEventSynchronize(r->ev1));
+          float ms = 0.f;
+          CUDA_OK(cudaEventElapsedTime(&ms, r->ev0, r->ev1));
+          if (ms < best) {
+            best = ms;
+            bt = th;
+            bo = order;
+          }
+        }
+      restore();
+      r->threads = bt;
+      set_cta_order(r, bo);
+      CUDA_OK(cudaStreamSynchronize(r->stream));
+      if (best_ms) *best_ms = best;
+    } catch (...) {
+      cleanup();
+      throw;
+    }
+    cleanup();
+  });
+}
+
 int cem_set_option(cem_replicas *r, const char *key, int64_t value) {
   return guard([&] {
     require(r && key, "null argument");
@@ -1159,6 +1239,11 @@ int cem_set_option(cem_replicas *r, const char *key, int64_t value) {
       require(sp != 0, "this batch has no HBM-streamed kernel", CEM_ERR_UNSUPPORTED);
       r->streamed = true;
       r->stream_pitch = sp;
+    } else if (k == "threads") {
+      require(value == 512 || value == 256, "threads must be 512 or 256 (two replicas per SM)");
+      r->threads = (int)value;
+    } else if (k == "cta_order") {
+      set_cta_order(r, (int)value);
     } else if (k == "generic_evaluator") {
       if (value) {
         r->pitch = 0;
@@ -1183,6 +1268,7 @@ int cem_get_option(cem_replicas *r, const char *key, int64_t *value) {
     else if (k == "colour_classes") *value = r->max_classes;
     else if (k == "streamed") *value = r->streamed ? 1 : 0;
     else if (k == "threads") *value = r->threads;
+    else if (k == "cta_order") *value = r->cta_order;
     else throw Err(CEM_ERR_INVALID, "unknown option '" + k + "'");
   });
 }

@@ -40,6 +40,7 @@ struct SweepParams {
   int max_classes;
   int n_pair_sweeps, n_local_sweeps;  // canonical pass composition
   int init;                    // binary systems: compute the exact initial stats in-kernel
+  const int *cta_rep;          // replica of each CTA (null: CTA i runs replica i)
   double RT[16];               // (n_occ-1) x n_occ
 };
 

@@ -975,10 +975,10 @@ __device__ __noinline__ void init_binary_stats(const CeTables &T, const int8_t *
 }
 
 template <int NOCC, int PITCH, int THREADS = SWEEP_THREADS>
-__global__ void __launch_bounds__(THREADS, 1)
+__global__ void __launch_bounds__(THREADS, 512 / THREADS)
     k_sweep(const __grid_constant__ CeTables T, const __grid_constant__ SweepParams P) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int rep = blockIdx.x;
+  const int rep = P.cta_rep ? P.cta_rep[blockIdx.x] : blockIdx.x;
   const Replica &R = P.reps[rep];
   ReplicaStats &Sg = P.stats[rep];
   constexpr int NW = THREADS / 32;

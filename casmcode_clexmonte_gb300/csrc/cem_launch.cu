@@ -31,6 +31,17 @@ CEM_EXTERN_PITCH(28)
 CEM_EXTERN_PITCH(36)
 CEM_EXTERN_PITCH(52)
 CEM_EXTERN_PITCH(64)
+// 256-thread variants (two replicas per SM), cem_k256a.cu / cem_k256b.cu
+#define CEM_EXTERN_256(N, P)                                                                 \
+  extern template cudaError_t launch_sweep_t<N, P, 256>(const CeTables &, const SweepParams &, \
+                                                        int, int, cudaStream_t);
+CEM_EXTERN_256(2, 14)
+CEM_EXTERN_256(2, 28)
+CEM_EXTERN_256(2, 36)
+CEM_EXTERN_256(2, 52)
+CEM_EXTERN_256(2, 64)
+CEM_EXTERN_256(2, 0)
+CEM_EXTERN_256(3, 0)
 
 cudaError_t launch_energy(const CeTables &T, const int8_t *occ, int L0, int L1, int L2,
                           unsigned long long *counts, cudaStream_t st) {
@@ -63,17 +74,24 @@ int sweep_smem_bytes(const CeTables &T, int L0, int L1, int L2, int n_classes, i
   return sweep_smem_bytes_impl(T, L0, L1, L2, n_classes, pitch);
 }
 
+template <int TH>
+static cudaError_t launch_sweep_th(const CeTables &T, const SweepParams &P, int n_replicas,
+                                   int smem, int pitch, cudaStream_t st) {
+  if (pitch == 14) return launch_sweep_t<2, 14, TH>(T, P, n_replicas, smem, st);
+  if (pitch == 28) return launch_sweep_t<2, 28, TH>(T, P, n_replicas, smem, st);
+  if (pitch == 36) return launch_sweep_t<2, 36, TH>(T, P, n_replicas, smem, st);
+  if (pitch == 52) return launch_sweep_t<2, 52, TH>(T, P, n_replicas, smem, st);
+  if (pitch == 64) return launch_sweep_t<2, 64, TH>(T, P, n_replicas, smem, st);
+  if (pitch != 0) return cudaErrorInvalidValue;
+  if (T.n_occ == 2) return launch_sweep_t<2, 0, TH>(T, P, n_replicas, smem, st);
+  if (T.n_occ == 3) return launch_sweep_t<3, 0, TH>(T, P, n_replicas, smem, st);
+  return cudaErrorInvalidValue;
+}
+
 cudaError_t launch_sweep(const CeTables &T, const SweepParams &P, int n_replicas, int smem,
                          int pitch, int threads, cudaStream_t st) {
-  if (threads != SWEEP_THREADS) return cudaErrorInvalidValue;
-  if (pitch == 14) return launch_sweep_t<2, 14, SWEEP_THREADS>(T, P, n_replicas, smem, st);
-  if (pitch == 28) return launch_sweep_t<2, 28, SWEEP_THREADS>(T, P, n_replicas, smem, st);
-  if (pitch == 36) return launch_sweep_t<2, 36, SWEEP_THREADS>(T, P, n_replicas, smem, st);
-  if (pitch == 52) return launch_sweep_t<2, 52, SWEEP_THREADS>(T, P, n_replicas, smem, st);
-  if (pitch == 64) return launch_sweep_t<2, 64, SWEEP_THREADS>(T, P, n_replicas, smem, st);
-  if (pitch != 0) return cudaErrorInvalidValue;
-  if (T.n_occ == 2) return launch_sweep_t<2, 0, SWEEP_THREADS>(T, P, n_replicas, smem, st);
-  if (T.n_occ == 3) return launch_sweep_t<3, 0, SWEEP_THREADS>(T, P, n_replicas, smem, st);
+  if (threads == SWEEP_THREADS) return launch_sweep_th<SWEEP_THREADS>(T, P, n_replicas, smem, pitch, st);
+  if (threads == 256) return launch_sweep_th<256>(T, P, n_replicas, smem, pitch, st);
   return cudaErrorInvalidValue;
 }
 

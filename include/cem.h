@@ -227,6 +227,17 @@ int cem_enforce_composition(cem_replicas *r, const double *target_mol, uint64_t 
  * SemiGrandCanonicalCalculator.cc:423-466). */
 int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_samples);
 
+/* Autotuner of the shared-memory sweep's launch schedule: times trial_passes
+ * passes with each of {512 threads per replica, 256 threads (two replicas per
+ * SM)} x {replica order, largest replicas first}, from the same saved state,
+ * then restores the state and keeps the fastest (options "threads" and
+ * "cta_order"). The chain does not depend on the schedule (for binary systems
+ * bit for bit; ternary running energies may differ in the last bits, their
+ * FP64 sums being reduced in another order). No-op for HBM-streamed batches.
+ * Replaces no reference function (the reference has no GPU launch
+ * schedule). */
+int cem_autotune(cem_replicas *r, int64_t trial_passes, double *best_ms);
+
 /* Run options of a batch (canonical pass composition and evaluator):
  *   "pair_sweeps"  (default 2): sweeps of swaps between sites of one colour
  *                  class per pass;
@@ -237,7 +248,10 @@ int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_sampl
  *   "streamed" (1): keep the occupations in HBM and run one kernel per colour
  *                  sub-step over many CTAs per replica (a captured CUDA graph
  *                  per pass); chosen automatically when a supercell does not
- *                  fit in shared memory (binary FCC, equal even supercells).
+ *                  fit in shared memory (binary FCC, equal even supercells);
+ *   "threads" (512 or 256): threads per replica of the shared-memory sweep
+ *                  (256: two replicas per SM);
+ *   "cta_order" (0 or 1): replica -> CTA schedule (1: largest first).
  * cem_get_option also reads "pitch", "smem_bytes", "colour_classes" and
  * "streamed". */
 int cem_set_option(cem_replicas *r, const char *key, int64_t value);
