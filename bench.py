@@ -278,15 +278,20 @@ def run_gb300(args):
     props_all = reduce_sum(dist, props)
     value = props_all / t_dev
     # effective independent samples of the potential energy per pass
-    n_eff = 0.0
+    n_eff = n_eff_op = 0.0
     taus = []
     for i in range(w.n_replicas):
         pot, _ = batch.samples(i, args.steps)
+        op = batch.order_samples(i, args.steps)
         t = tau_int(pot) if pot.size > 16 else float("nan")
+        t_op = tau_int(op) if op.size > 16 else float("nan")
         taus.append(t)
         if np.isfinite(t):
             n_eff += pot.size / (2.0 * t)
+        if np.isfinite(t_op):
+            n_eff_op += op.size / (2.0 * t_op)
     n_eff = reduce_sum(dist, n_eff)
+    n_eff_op = reduce_sum(dist, n_eff_op)
 
     # end-to-end through the C ABI with pinned host buffers: two replica
     # batches (each with its own stream) alternate, so one batch's host <->
@@ -331,6 +336,13 @@ def run_gb300(args):
     for hp in hps:
         _lib.check(lib.cem_host_free(hp))
 
+    # drift of the running energy (integer delta-count bookkeeping) against a
+    # fresh full recompute of the final states
+    drift = 0.0
+    for i in range(0, w.n_replicas, max(1, w.n_replicas // 8)):
+        e_run = batch.stats(i)["energy"]
+        e_fresh, _ = batch.energy(i)
+        drift = max(drift, abs(e_run - e_fresh) / max(abs(e_fresh), 1e-300))
     p_acc = accs / max(props, 1)
     z = 42  # distinct flower sites of an FCC site (12 + 6 + 24)
     bytes_per_prop = 2 * (1 + z) + 2 * p_acc
@@ -360,6 +372,8 @@ def run_gb300(args):
         }),
         "proposals": int(props_all), "acceptance": p_acc,
         "effective_samples_per_s": n_eff / t_dev,
+        "effective_samples_per_s_order_parameter": n_eff_op / t_dev,
+        "running_energy_rel_drift_vs_recompute": drift,
         "tau_int_potential_median": float(np.nanmedian(taus)),
         "host_wall_s": t1 - t0,
         "e2e": {"value": e2e_props / e2e_time, "unit": "proposals/s",
@@ -513,7 +527,9 @@ def run_learned_comparison(args):
         taus_p.append((te, to))
         neff_e += e.size / (2 * te)
         neff_op += op.size / (2 * to)
-    mean_e_plain = float(np.mean([plain.stats(i)["mean_potential"] for i in range(n_rep)]))
+    e_rep_plain = np.array([plain.stats(i)["mean_potential"] for i in range(n_rep)])
+    mean_e_plain = float(e_rep_plain.mean())
+    sig_plain = float(e_rep_plain.std(ddof=1) / np.sqrt(n_rep))
     # 3. train the proposal network on plain-sampler snapshots (1e6 environments)
     X, t = [], []
     for i in range(n_rep):
@@ -540,7 +556,10 @@ def run_learned_comparison(args):
         taus_l.append((te, to))
         neff_e_l += e.size / (2 * te)
         neff_op_l += op.size / (2 * to)
-    mean_e_learned = float(np.mean([plain.learned_samples(i, lp)[0].mean() for i in range(n_rep)]))
+    e_rep_learned = np.array([plain.learned_samples(i, lp)[0].mean() for i in range(n_rep)])
+    mean_e_learned = float(e_rep_learned.mean())
+    sig_learned = float(e_rep_learned.std(ddof=1) / np.sqrt(n_rep))
+    sig_diff = float(np.hypot(sig_plain, sig_learned))
     line = {
         "metric": "effective samples/s (learned vs plain GPU Metropolis, same <E>)",
         "workload": w.name, "T_c_scan_K": tc, "temperature_K": T,
@@ -549,16 +568,20 @@ def run_learned_comparison(args):
                   "tau_int_E_median": float(np.median([a for a, _ in taus_p])),
                   "tau_int_order_median": float(np.median([b for _, b in taus_p])),
                   "eff_samples_per_s_E": neff_e / t_plain,
-                  "eff_samples_per_s_order": neff_op / t_plain, "mean_E": mean_e_plain},
+                  "eff_samples_per_s_order": neff_op / t_plain, "mean_E": mean_e_plain,
+                  "mean_E_sigma": sig_plain},
         "learned": {"passes": lp, "seconds": t_learned,
                     "proposals_per_s": n_rep * lp * int(w.n_sites[0]) / t_learned,
                     "tau_int_E_median": float(np.median([a for a, _ in taus_l])),
                     "tau_int_order_median": float(np.median([b for _, b in taus_l])),
                     "eff_samples_per_s_E": neff_e_l / t_learned,
                     "eff_samples_per_s_order": neff_op_l / t_learned, "mean_E": mean_e_learned,
+                    "mean_E_sigma": sig_learned,
                     "train_seconds": train_s, "train_loss": [float(x) for x in losses]},
         "ratio_learned_over_plain_E": (neff_e_l / t_learned) / (neff_e / t_plain),
         "ratio_learned_over_plain_order": (neff_op_l / t_learned) / (neff_op / t_plain),
+        "same_E_within_2sigma": bool(abs(mean_e_learned - mean_e_plain) <= 2 * sig_diff),
+        "E_difference_over_sigma": abs(mean_e_learned - mean_e_plain) / sig_diff if sig_diff > 0 else None,
     }
     print(json.dumps(line), flush=True)
     return 0
