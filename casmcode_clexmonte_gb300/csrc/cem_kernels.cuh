@@ -529,7 +529,7 @@ constexpr int MAX_SWEEPS = 8;
 struct SweepSmem {
   // carved from dynamic shared memory; offsets in bytes
   int occ, cl_off, lutoff, lut, whi, wlo, dmu, ax, sched, red, clist, wkept, stats, desc, initq,
-      total;
+      bar, total;
 };
 
 __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
@@ -566,16 +566,20 @@ __host__ __device__ inline void sweep_layout(const CeTables &T, int L0, int L1, 
   o += align16(3 * MAX_SWEEPS * n_classes_max * 4);
   s.red = o;  // block reduction scratch: 32 warps x 16 slots of 8 bytes
   o += 32 * 16 * 8;
+  s.stats = o;  // the replica's running statistics, resident for the launch
+  o += align16((int)sizeof(ReplicaStats));
+  // [clist, bar): unused while the replica is staged in and written back,
+  // so the bulk copies go through it
   s.clist = o;  // kept canonical candidates (u16), two buffers: a class holds <= n_uc / 8 sites
   o += 2 * align16(2 * clist_capacity(L0, L1, L2));
   s.wkept = o;  // kept candidates per warp, two buffers
   o += 2 * 32 * 4;
-  s.stats = o;  // the replica's running statistics, resident for the launch
-  o += align16((int)sizeof(ReplicaStats));
   s.desc = o;  // decoded sub-steps of the current pass
   o += MAX_SWEEPS * n_classes_max * 80;
   s.initq = o;  // per-warp queues of occupied sites (initial energy)
   o += 32 * 96 * 4;
+  s.bar = o;  // two mbarriers of the staging copies
+  o += 16;
   s.total = o;
 }
 
@@ -584,6 +588,45 @@ inline int sweep_smem_bytes_impl(const CeTables &T, int L0, int L1, int L2, int 
   SweepSmem s;
   sweep_layout(T, L0, L1, L2, n_classes, pitch, s);
   return s.total;
+}
+
+// ------------------------------------------------------------ bulk copies
+// One-dimensional TMA bulk copies (cp.async.bulk) between global and shared
+// memory, completing on an mbarrier (loads) or a bulk group (stores). Both
+// addresses must be 16-byte aligned and the size a multiple of 16 bytes.
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// Bounded wait for the completion of the mbarrier phase with this parity.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int max_iter) {
+  const uint32_t a = smem_u32(bar);
+  for (int i = 0; i < max_iter; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void bulk_store(void *dst_gmem, const void *src_smem, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst_gmem),
+               "r"(smem_u32(src_smem)), "r"(bytes)
+               : "memory");
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
 }
 
 // floor(n / d) for a block-uniform divisor d >= 1 and numerators n >= 0 with
@@ -876,6 +919,81 @@ __device__ __forceinline__ void compact_pairs(const PairGeom &pg, const Geo &G, 
   if (lane == 0) wk[warp] = kept;
 }
 
+// Replica staging through a shared-memory buffer of cap bytes (a multiple
+// of 16): each round, one thread issues bulk copies of up to 32 KB for as
+// much of the replica as fits, all completing on one mbarrier; then every
+// thread scatters the round into the halo'd layout. Returns false, with no
+// copy in flight, when a round did not complete within the wait limit.
+static __device__ __noinline__ bool stage_replica_bulk(const int8_t *gocc, int n_sites, int8_t *occ,
+                                                       const Geo &G, const SiteIndex &site_of,
+                                                       uint8_t *buf, int cap, uint64_t *bar) {
+  const int tid = threadIdx.x, nth = blockDim.x;
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  int round = 0;
+  for (int off0 = 0; off0 < n_sites; off0 += cap, ++round) {
+    const int bytes = min(cap, n_sites - off0);
+    if (tid == 0) {
+      if (round) fence_proxy_async_smem();
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                   "r"((uint32_t)bytes)
+                   : "memory");
+      for (int o = 0; o < bytes; o += 32768) {
+        const uint32_t piece = (uint32_t)min(32768, bytes - o);
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+                "r"(smem_u32(buf + o)),
+            "l"(gocc + off0 + o), "r"(piece), "r"(smem_u32(bar))
+            : "memory");
+      }
+    }
+    const bool ok = mbar_wait(bar, (uint32_t)(round & 1), 1 << 22);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) mbar_wait(bar, (uint32_t)(round & 1), 1 << 22);  // let the copies land
+      __syncthreads();
+      return false;
+    }
+    for (int i = tid; i < bytes; i += nth) {
+      int b, x, y, z;
+      site_of(off0 + i, b, x, y, z);
+      put_site(occ, G, b, x, y, z, (int8_t)buf[i]);
+    }
+    __syncthreads();
+  }
+  return true;
+}
+
+// Occupations back to global memory: each round gathers as much of the
+// replica as fits in the buffer from the halo'd layout, then one thread
+// issues bulk stores of up to 32 KB and waits until they have read the
+// buffer.
+static __device__ __noinline__ void writeback_replica_bulk(int8_t *gout, int n_sites,
+                                                           const int8_t *occ, const Geo &G,
+                                                           const SiteIndex &site_of, uint8_t *buf,
+                                                           int cap) {
+  const int tid = threadIdx.x, nth = blockDim.x;
+  for (int off0 = 0; off0 < n_sites; off0 += cap) {
+    const int bytes = min(cap, n_sites - off0);
+    for (int i = tid; i < bytes; i += nth) {
+      int b, x, y, z;
+      site_of(off0 + i, b, x, y, z);
+      buf[i] = (uint8_t)occ[G.addr(b, x, y, z)];
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      for (int o = 0; o < bytes; o += 32768)
+        bulk_store(gout + off0 + o, buf + o, (uint32_t)min(32768, bytes - o));
+      asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+    }
+    __syncthreads();
+  }
+  if (tid == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
 // Exact initial statistics of a binary replica staged in shared memory,
 // written to S: count_g = number of clusters of orbit g with every site
 // occupant 1. Kept out of line, so that the sweep loop's register allocation
@@ -1082,18 +1200,16 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
   // 16-byte loads when the replica's occupations are 16-byte aligned (the
   // loads of a thread are issued together, then scattered into the halo'd
   // layout); byte loads otherwise
+  // bulk (TMA) copies when the replica's occupations are 16-byte aligned,
+  // byte loads otherwise
   const bool vec16 = ((R.occ_offset | n_sites) & 15) == 0;
+  uint8_t *stg = smem + lay.clist;
+  const int stg_cap = ((lay.bar - lay.clist) / 16) * 16;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + lay.bar);
   if (vec16) {
-    const uint4 *g16 = reinterpret_cast<const uint4 *>(gocc);
-    for (int v = tid; v < n_sites / 16; v += nth) {
-      const uint4 w = g16[v];
-      const uint32_t words[4] = {w.x, w.y, w.z, w.w};
-#pragma unroll
-      for (int k = 0; k < 16; ++k) {
-        int b, x, y, z;
-        site_of(16 * v + k, b, x, y, z);
-        put_site(occ, G, b, x, y, z, (int8_t)((words[k >> 2] >> (8 * (k & 3))) & 0xFF));
-      }
+    if (!stage_replica_bulk(gocc, n_sites, occ, G, site_of, stg, stg_cap, bar)) {
+      if (tid == 0) Sg.status = 5;  // a staging copy did not complete: replica left unchanged
+      return;
     }
   } else {
     for (int l = tid; l < n_sites; l += nth) {
@@ -1434,17 +1550,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
   }
   // ---- write back
   if (vec16) {
-    uint4 *g16 = reinterpret_cast<uint4 *>(P.occ + R.occ_offset);
-    for (int v = tid; v < n_sites / 16; v += nth) {
-      uint32_t words[4] = {0u, 0u, 0u, 0u};
-#pragma unroll
-      for (int k = 0; k < 16; ++k) {
-        int b, x, y, z;
-        site_of(16 * v + k, b, x, y, z);
-        words[k >> 2] |= (uint32_t)(uint8_t)occ[G.addr(b, x, y, z)] << (8 * (k & 3));
-      }
-      g16[v] = make_uint4(words[0], words[1], words[2], words[3]);
-    }
+    writeback_replica_bulk(P.occ + R.occ_offset, n_sites, occ, G, site_of, stg, stg_cap);
   } else {
     for (int l = tid; l < n_sites; l += nth) {
       int b, x, y, z;
