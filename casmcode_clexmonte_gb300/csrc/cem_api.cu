@@ -1113,6 +1113,9 @@ int cem_get_stats(cem_replicas *r, int i, cem_stats *out) {
     ReplicaStats S;
     CUDA_OK(cudaMemcpyAsync(&S, r->d_stats + i, sizeof(S), cudaMemcpyDeviceToHost, r->stream));
     CUDA_OK(cudaStreamSynchronize(r->stream));
+    if (S.status == 5)
+      throw Err(CEM_ERR_DEVICE,
+                "a shared-memory staging copy did not complete; the replica was left unchanged");
     std::memset(out, 0, sizeof(*out));
     const int nc = r->sys->T.n_occ - 1;
     out->n_samples = S.n_samples;
