@@ -304,16 +304,13 @@ def run_gb300(args):
     for i in range(w.n_replicas):
         batches[1].set_conditions(i, float(w.temperature[i]))
         batches[1].set_seed(i, int(w.seeds[i]) + 7919 * rank + 104729)
-    hps, hosts = [], []
+    hosts = []
     for b in batches:
-        hp = C.c_void_p()
-        _lib.check(lib.cem_host_alloc(nbytes, C.byref(hp)))
-        hps.append(hp)
-        hosts.append(np.ctypeslib.as_array((C.c_int8 * nbytes).from_address(hp.value)))
+        hosts.append(b.pinned_buffer())
         batch.get_occupation_all(hosts[-1])
-    batches[1].set_occupation_all(hosts[1])  # first launch of the second batch
-    batches[1].run(1, 0)
-    batches[1].get_occupation_all(hosts[1])
+    for b, h in zip(batches, hosts):  # capture each batch's step graph
+        b.step_async(h, h, 1)
+        b.synchronize()
     e2e_steps = max(4, min(args.steps, 400))
 
     def n_proposed():
@@ -325,16 +322,13 @@ def run_gb300(args):
     for s in range(e2e_steps):
         b, h = batches[s % 2], hosts[s % 2]
         if s >= 2:
-            b.get_occupation_all(h)  # result of step s - 2
-        b.set_occupation_all(h)
-        b.run(1, 0)
-    for s in range(e2e_steps - 2, e2e_steps):
-        batches[s % 2].get_occupation_all(hosts[s % 2])
+            b.synchronize()  # step s - 2 has written its result to h
+        b.step_async(h, h, 1)  # graph: h -> device, one pass, device -> h
+    for b in batches:
+        b.synchronize()
     t3 = time.perf_counter()
     e2e_props = reduce_sum(dist, n_proposed() - e_before)
     e2e_time = reduce_max(dist, t3 - t2)
-    for hp in hps:
-        _lib.check(lib.cem_host_free(hp))
 
     # drift of the running energy (integer delta-count bookkeeping) against a
     # fresh full recompute of the final states
@@ -379,8 +373,8 @@ def run_gb300(args):
         "e2e": {"value": e2e_props / e2e_time, "unit": "proposals/s",
                 "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                 "steps": e2e_steps,
-                "pipeline": "two replica batches on two streams alternate; each step = "
-                            "upload occupations, one pass, read occupations back"},
+                "pipeline": "two replica batches on two streams alternate; each step = one "
+                            "CUDA graph: upload occupations, one pass, read occupations back"},
         "roofline": {"bound": "smem", "achieved": achieved, "peak": smem_gbs, "unit": "GB/s",
                      "frac": achieved / smem_gbs, "traffic": traffic,
                      "peak_source": "measured in this run by cem_smem_bandwidth "

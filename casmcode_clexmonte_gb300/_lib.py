@@ -54,7 +54,7 @@ EXPORTS = [
     "cem_get_occupation_all", "cem_host_alloc", "cem_host_free", "cem_energy",
     "cem_delta_energy", "cem_replay", "cem_enforce_composition", "cem_nfold_run", "cem_run", "cem_get_stats", "cem_get_samples",
     "cem_reset_stats", "cem_synchronize", "cem_last_kernel_ms", "cem_smem_bandwidth",
-    "cem_set_option", "cem_get_option", "cem_autotune", "cem_delta_energy_noalloc",
+    "cem_set_option", "cem_get_option", "cem_autotune", "cem_step_async", "cem_delta_energy_noalloc",
     "cem_mlp_info", "cem_mlp_create", "cem_mlp_destroy", "cem_mlp_get_params",
     "cem_mlp_set_params", "cem_mlp_forward", "cem_mlp_gradient", "cem_mlp_train",
     "cem_learned_features", "cem_learned_run", "cem_learned_samples", "cem_get_order_samples",
@@ -99,6 +99,7 @@ def load(path: str = LIB):
     L.cem_nfold_run.argtypes = [P, C.c_int64, C.c_int64, C.c_int64, vp, vp, vp]
     L.cem_run.argtypes = [P, C.c_int64, C.c_int64, C.c_int]
     L.cem_autotune.argtypes = [P, C.c_int64, C.POINTER(C.c_double)]
+    L.cem_step_async.argtypes = [P, vp, vp, C.c_int64]
     L.cem_get_stats.argtypes = [P, C.c_int, C.POINTER(Stats)]
     L.cem_get_samples.argtypes = [P, C.c_int, vp, vp, C.c_int64, C.POINTER(C.c_int64)]
     L.cem_reset_stats.argtypes = [P]

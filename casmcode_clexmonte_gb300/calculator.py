@@ -83,6 +83,9 @@ class ReplicaBatch:
         if h is not None and h.value:
             self.lib.cem_replicas_destroy(h)
             self.handle = None
+        for hp in getattr(self, "_pinned", []):
+            self.lib.cem_host_free(hp)
+        self._pinned = []
 
     def set_conditions(self, i: int, temperature: float, param_chem_pot=None):
         mu = None
@@ -174,6 +177,20 @@ class ReplicaBatch:
 
     def run(self, n_passes: int, n_equil: int = 0, record_samples: bool = False):
         check(self.lib.cem_run(self.handle, int(n_passes), int(n_equil), int(bool(record_samples))))
+
+    def step_async(self, host_in: np.ndarray, host_out: np.ndarray, n_passes: int = 1):
+        """Copy the packed occupations in, run ``n_passes`` passes, copy them
+        out, as one CUDA graph on the batch's stream (page-locked int8
+        buffers of all sites, e.g. from ``pinned_buffer``)."""
+        check(self.lib.cem_step_async(self.handle, ptr(host_in), ptr(host_out), int(n_passes)))
+
+    def pinned_buffer(self) -> np.ndarray:
+        """Page-locked int8 buffer of all replicas' sites (freed with the batch)."""
+        nbytes = int(self.offsets[-1])
+        hp = C.c_void_p()
+        check(self.lib.cem_host_alloc(nbytes, C.byref(hp)))
+        self._pinned = getattr(self, "_pinned", []) + [hp]
+        return np.ctypeslib.as_array((C.c_int8 * nbytes).from_address(hp.value))
 
     def autotune(self, trial_passes: int = 20) -> dict:
         """Pick the fastest launch schedule (threads per replica, replica

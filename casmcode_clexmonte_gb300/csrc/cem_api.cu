@@ -126,6 +126,12 @@ struct cem_replicas {
   bool streamed = false;
   int stream_pitch = 0;
   StreamState sstate;
+  // end-to-end step graph (copy in, passes, copy out), captured per key
+  cudaGraphExec_t step_exec = nullptr;
+  const void *step_in = nullptr;
+  void *step_out = nullptr;
+  long long step_passes = -1;
+  int step_threads = 0, step_order = -1, step_pitch = -1;
   long long stream_pass = 0;
   // learned-proposal state
   long long *d_lw = nullptr;             // per-site integer weights
@@ -141,6 +147,7 @@ struct cem_replicas {
     cudaFree(sstate.run);
     cudaFree(sstate.sched);
     if (sstate.exec) cudaGraphExecDestroy(sstate.exec);
+    if (step_exec) cudaGraphExecDestroy(step_exec);
     cudaFree(d_lw);
     cudaFree(d_trees);
     cudaFree(d_lsamples);
@@ -985,6 +992,74 @@ int cem_enforce_composition(cem_replicas *r, const double *target_mol, uint64_t 
       if (res[3 * i + 2] != 0) throw Err(CEM_ERR_DEVICE, "composition enforcement did not terminate");
       if (n_flips) n_flips[i] = res[3 * i];
     }
+  });
+}
+
+int cem_step_async(cem_replicas *r, const int8_t *host_in, int8_t *host_out, int64_t n_passes) {
+  return guard([&] {
+    require(r && host_in && host_out, "null argument");
+    require(n_passes >= 1, "n_passes must be >= 1");
+    require(!r->streamed, "HBM-streamed batches run through cem_run", CEM_ERR_UNSUPPORTED);
+    for (const void *p : {(const void *)host_in, (const void *)host_out}) {
+      cudaPointerAttributes a{};
+      CUDA_OK(cudaPointerGetAttributes(&a, p));
+      require(a.type == cudaMemoryTypeHost,
+              "cem_step_async needs page-locked host buffers (cem_host_alloc)");
+    }
+    int dev = 0, maxsm = 0;
+    CUDA_OK(cudaGetDevice(&dev));
+    CUDA_OK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    require(r->sweep_smem <= maxsm, "supercell does not fit in shared memory", CEM_ERR_UNSUPPORTED);
+    r->upload_reps();
+    const bool same = r->step_exec && r->step_in == host_in && r->step_out == host_out &&
+                      r->step_passes == n_passes && r->step_threads == r->threads &&
+                      r->step_order == r->cta_order && r->step_pitch == r->pitch;
+    if (!same) {
+      if (r->step_exec) cudaGraphExecDestroy(r->step_exec);
+      r->step_exec = nullptr;
+      const CeTables &T = r->sys->T;
+      SweepParams P{};
+      P.reps = r->d_reps;
+      P.stats = r->d_stats;
+      P.occ = r->d_occ;
+      P.n_passes = n_passes;
+      P.n_equil = 0;
+      P.max_classes = r->max_classes;
+      P.n_pair_sweeps = r->n_pair_sweeps;
+      P.n_local_sweeps = r->n_local_sweeps;
+      P.cta_rep = r->d_cta_rep;
+      P.init = T.n_occ == 2 ? 1 : 0;
+      for (size_t k = 0; k < r->sys->RT.size() && k < 16; ++k) P.RT[k] = r->sys->RT[k];
+      int max_sites = 0;
+      for (const Replica &R : r->reps) max_sites = std::max(max_sites, R.n_sites);
+      cudaGraph_t graph;
+      CUDA_OK(cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
+      cudaError_t e = cudaMemcpyAsync(r->d_occ, host_in, (size_t)r->total_sites,
+                                      cudaMemcpyHostToDevice, r->stream);
+      if (e == cudaSuccess && !P.init)
+        e = launch_init_stats(T, r->d_reps, r->d_stats, r->d_occ, r->n, max_sites, r->stream);
+      if (e == cudaSuccess)
+        e = launch_sweep(T, P, r->n, r->sweep_smem, r->pitch, r->threads, r->stream);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(host_out, r->d_occ, (size_t)r->total_sites, cudaMemcpyDeviceToHost,
+                            r->stream);
+      const cudaError_t e2 = cudaStreamEndCapture(r->stream, &graph);
+      CUDA_OK(e);
+      CUDA_OK(e2);
+      e = cudaGraphInstantiate(&r->step_exec, graph, 0);
+      cudaGraphDestroy(graph);
+      CUDA_OK(e);
+      r->step_in = host_in;
+      r->step_out = host_out;
+      r->step_passes = n_passes;
+      r->step_threads = r->threads;
+      r->step_order = r->cta_order;
+      r->step_pitch = r->pitch;
+    }
+    CUDA_OK(cudaEventRecord(r->ev0, r->stream));
+    CUDA_OK(cudaGraphLaunch(r->step_exec, r->stream));
+    CUDA_OK(cudaEventRecord(r->ev1, r->stream));
+    r->stats_valid = true;
   });
 }
 

@@ -238,6 +238,17 @@ int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_sampl
  * schedule). */
 int cem_autotune(cem_replicas *r, int64_t trial_passes, double *best_ms);
 
+/* One end-to-end step of a batch as a CUDA graph: copy the packed
+ * occupations of all replicas in from host_in, run n_passes passes (the
+ * exact initial statistics recomputed on the device), copy the occupations
+ * out to host_out. The graph is captured at the first call for these buffers
+ * and pass count and replayed afterwards. Host buffers must be page-locked
+ * (cem_host_alloc); asynchronous on the batch's stream (cem_synchronize
+ * waits). Shared-memory batches only. Replaces no single reference function:
+ * it is the batch form of set state -> run -> read state
+ * (CanonicalCalculator.cc:413-462). */
+int cem_step_async(cem_replicas *r, const int8_t *host_in, int8_t *host_out, int64_t n_passes);
+
 /* Run options of a batch (canonical pass composition and evaluator):
  *   "pair_sweeps"  (default 2): sweeps of swaps between sites of one colour
  *                  class per pass;
