@@ -131,7 +131,7 @@ struct cem_replicas {
   const void *step_in = nullptr;
   void *step_out = nullptr;
   long long step_passes = -1;
-  int step_threads = 0, step_order = -1, step_pitch = -1;
+  int step_threads = 0, step_order = -1, step_pitch = -1, step_pair = -1, step_local = -1;
   long long stream_pass = 0;
   // learned-proposal state
   long long *d_lw = nullptr;             // per-site integer weights
@@ -1013,7 +1013,8 @@ int cem_step_async(cem_replicas *r, const int8_t *host_in, int8_t *host_out, int
     r->upload_reps();
     const bool same = r->step_exec && r->step_in == host_in && r->step_out == host_out &&
                       r->step_passes == n_passes && r->step_threads == r->threads &&
-                      r->step_order == r->cta_order && r->step_pitch == r->pitch;
+                      r->step_order == r->cta_order && r->step_pitch == r->pitch &&
+                      r->step_pair == r->n_pair_sweeps && r->step_local == r->n_local_sweeps;
     if (!same) {
       if (r->step_exec) cudaGraphExecDestroy(r->step_exec);
       r->step_exec = nullptr;
@@ -1055,6 +1056,8 @@ int cem_step_async(cem_replicas *r, const int8_t *host_in, int8_t *host_out, int
       r->step_threads = r->threads;
       r->step_order = r->cta_order;
       r->step_pitch = r->pitch;
+      r->step_pair = r->n_pair_sweeps;
+      r->step_local = r->n_local_sweeps;
     }
     CUDA_OK(cudaEventRecord(r->ev0, r->stream));
     CUDA_OK(cudaGraphLaunch(r->step_exec, r->stream));
