@@ -365,6 +365,7 @@ def run_gb300(args):
                          "picked_by": "autotuner (10 timed trial passes per candidate)"},
         }),
         "proposals": int(props_all), "acceptance": p_acc,
+        "proposals_per_s_per_replica": value / (w.n_replicas * ws),
         "effective_samples_per_s": n_eff / t_dev,
         "effective_samples_per_s_order_parameter": n_eff_op / t_dev,
         "running_energy_rel_drift_vs_recompute": drift,
