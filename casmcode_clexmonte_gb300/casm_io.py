@@ -25,7 +25,8 @@ import os
 
 import numpy as np
 
-from .system import KB, ClusterExpansion, Prim
+from .crystal import Crystal, CrystalClusterExpansion
+from .system import KB, ClusterExpansion, Prim, cubic_point_group
 
 
 def _integer_grid(lattice: np.ndarray, basis_cart: np.ndarray, tol: float = 1e-6):
@@ -63,6 +64,34 @@ def read_prim(src) -> Prim:
     )
 
 
+def read_crystal(src) -> Crystal:
+    """Any CASM ``prim.json``: lattice, basis (fractional or Cartesian) and
+    the occupants of every basis site."""
+    d = json.load(open(src)) if isinstance(src, (str, os.PathLike)) else src
+    lat = np.array(d["lattice_vectors"], dtype=float)
+    mode = d.get("coordinate_mode", "Fractional").lower()
+    coords = np.array([b["coordinate"] for b in d["basis"]], dtype=float)
+    frac = coords if mode.startswith("frac") else coords @ np.linalg.inv(lat)
+    return Crystal(d.get("title", "prim"), lat, frac, [tuple(b["occupants"]) for b in d["basis"]])
+
+
+def _cubic_prim(d: dict):
+    """The cubic builder's ``Prim`` when every site allows the same (two or
+    more) occupants, the sites lie on an integer grid and the cubic point
+    group maps the crystal onto itself; None otherwise."""
+    occs = [tuple(b["occupants"]) for b in d["basis"]]
+    if len(occs[0]) < 2 or any(o != occs[0] for o in occs):
+        return None
+    try:
+        prim = read_prim(d)
+        for op in cubic_point_group():
+            for b in range(prim.n_basis):
+                prim.site_of(prim.basis[b] @ op.T)
+    except ValueError:
+        return None
+    return prim
+
+
 def _max_lengths(bspecs: dict) -> dict:
     br = bspecs["cluster_specs"]["params"]["orbit_branch_specs"]
     return {int(k): float(v["max_length"]) for k, v in br.items() if int(k) >= 2}
@@ -71,14 +100,22 @@ def _max_lengths(bspecs: dict) -> dict:
 def read_cluster_expansion(prim_src, eci_src, sparse_eci=None) -> ClusterExpansion:
     """Cluster expansion from CASM files; ECI from ``eci_src`` (its
     ``cluster_functions[*].eci``) or from a sparse list ``[[index, value]]``."""
-    prim = read_prim(prim_src)
+    pd = json.load(open(prim_src)) if isinstance(prim_src, (str, os.PathLike)) else prim_src
     d = json.load(open(eci_src)) if isinstance(eci_src, (str, os.PathLike)) else eci_src
     basis = d.get("bspecs", {}).get("basis_function_specs", {})
     site_bf = basis.get("dof_specs", {}).get("occ", {}).get("site_basis_functions", "OCCUPATION")
     if str(site_bf).upper() != "OCCUPATION":
         raise ValueError(f"site basis functions '{site_bf}' are not supported (occupation only)")
-    ce = ClusterExpansion(prim, _max_lengths(d["bspecs"]))
     orbits = d["orbits"]
+    prim = _cubic_prim(pd)
+    if prim is not None:
+        ce = ClusterExpansion(prim, _max_lengths(d["bspecs"]))
+    else:
+        protos = None
+        if all("prototype" in o and "sites" in o["prototype"] for o in orbits):
+            protos = [[(int(x[0]), tuple(int(v) for v in x[1:])) for x in o["prototype"]["sites"]]
+                      for o in orbits]
+        ce = CrystalClusterExpansion(read_crystal(pd), _max_lengths(d["bspecs"]), orbit_order=protos)
     if len(orbits) != len(ce.orbits) + 1:
         raise ValueError(f"file has {len(orbits)} orbits, built {len(ce.orbits) + 1}")
     eci = np.zeros(ce.n_funcs)
@@ -106,27 +143,38 @@ def read_cluster_expansion(prim_src, eci_src, sparse_eci=None) -> ClusterExpansi
     return ce
 
 
-def composition_axes_RT(axes: dict, occupants) -> np.ndarray:
-    """R^T (independent axes x components, in the prim's occupant order) of
+def composition_axes_RT(axes: dict, occupants, fixed=None) -> np.ndarray:
+    """R^T (independent axes x occupants, in the prim's occupant order) of
     CASM composition axes (``origin`` and one end member per axis, species
-    per unit cell, over ``components``). The samplers count the composition
-    from the state where every site holds occupant 0, so the origin must be
-    that state."""
+    per unit cell, over ``components``). ``occupants`` are the species of the
+    sublattices with a degree of freedom; ``fixed`` maps the species of the
+    single-occupant sublattices to their count per unit cell. The samplers
+    count the composition from the state where every site with a degree of
+    freedom holds occupant 0, so the origin must be that state, and no axis
+    may change a species that only the fixed sublattices hold."""
+    fixed = dict(fixed or {})
     comps = list(axes["components"])
-    if sorted(comps) != sorted(occupants):
-        raise ValueError(f"composition components {comps} differ from the occupants {list(occupants)}")
-    order = [comps.index(o) for o in occupants]
-    origin = np.asarray(axes["origin"], dtype=np.float64)[order]
+    species = list(occupants) + [c for c in fixed if c not in occupants]
+    if sorted(comps) != sorted(species):
+        raise ValueError(f"composition components {comps} differ from the species {species}")
+    origin = np.asarray(axes["origin"], dtype=np.float64).reshape(-1)
     names = [k for k in "abcdefghijklmnopqrstuvwxyz" if k in axes]
     if len(names) != len(occupants) - 1:
         raise ValueError(f"expected {len(occupants) - 1} independent composition axes, found {len(names)}")
-    Q = np.stack([np.asarray(axes[k], dtype=np.float64)[order] - origin for k in names], axis=1)
-    n_basis = origin.sum()
-    expect = np.zeros(len(occupants))
-    expect[0] = n_basis
+    Q = np.stack([np.asarray(axes[k], dtype=np.float64).reshape(-1) - origin for k in names], axis=1)
+    n_dof = origin[[comps.index(o) for o in occupants]].sum() - sum(
+        fixed.get(o, 0) for o in occupants)
+    expect = np.zeros(len(comps))
+    for c, n in fixed.items():
+        expect[comps.index(c)] += n
+    expect[comps.index(occupants[0])] += n_dof
     if not np.allclose(origin, expect):
         raise ValueError("composition axes whose origin is not 'every site occupant 0' are not supported")
-    return np.ascontiguousarray(np.linalg.pinv(Q))
+    for c in comps:
+        if c not in occupants and np.any(np.abs(Q[comps.index(c)]) > 1e-12):
+            raise ValueError(f"a composition axis changes {c}, which no site can take or lose")
+    RT = np.linalg.pinv(Q)
+    return np.ascontiguousarray(RT[:, [comps.index(o) for o in occupants]])
 
 
 def read_system(path: str) -> ClusterExpansion:
@@ -154,12 +202,33 @@ def read_system(path: str) -> ClusterExpansion:
             basis["bspecs"] = json.load(open(os.path.join(bdir, "bspecs.json")))
         ce = read_cluster_expansion(d["prim"], basis, sparse_eci=coef)
     if "composition_axes" in d:
-        ce.param_RT = composition_axes_RT(d["composition_axes"], ce.prim.occupants)
+        cr = getattr(ce, "crystal", None)
+        ce.param_RT = composition_axes_RT(d["composition_axes"], ce.prim.occupants,
+                                          cr.fixed_counts() if cr is not None else None)
     return ce
 
 
-def write_eci_json(ce: ClusterExpansion, path: str):
+def _prim_doc(ce) -> dict:
+    cr = getattr(ce, "crystal", None)
+    if cr is not None:
+        return {
+            "title": cr.title,
+            "coordinate_mode": "Fractional",
+            "lattice_vectors": cr.lattice.tolist(),
+            "basis": [{"coordinate": cr.frac[b].tolist(), "occupants": list(cr.occupants[b])}
+                      for b in range(cr.n_basis)],
+        }
     p = ce.prim
+    return {
+        "title": p.title,
+        "coordinate_mode": "Cartesian",
+        "lattice_vectors": (p.lattice * p.grid).tolist(),
+        "basis": [{"coordinate": (b * p.grid).tolist(), "occupants": list(p.occupants)}
+                  for b in p.basis],
+    }
+
+
+def write_eci_json(ce: ClusterExpansion, path: str):
     orbits = [{
         "linear_orbit_index": 0, "mult": 1,
         "cluster_functions": [{"linear_function_index": 0, "eci": float(ce.eci[0])}],
@@ -189,13 +258,7 @@ def write_eci_json(ce: ClusterExpansion, path: str):
                               "params": {"orbit_branch_specs": branch}},
         },
         "orbits": orbits,
-        "prim": {
-            "title": p.title,
-            "coordinate_mode": "Cartesian",
-            "lattice_vectors": (p.lattice * p.grid).tolist(),
-            "basis": [{"coordinate": (b * p.grid).tolist(), "occupants": list(p.occupants)}
-                      for b in p.basis],
-        },
+        "prim": _prim_doc(ce),
     }
     with open(path, "w") as f:
         json.dump(doc, f, indent=1)

@@ -1,12 +1,31 @@
 #!/bin/bash
-# Compile the reference's generated FCC Clexulator, where it lies in the
+# Compile a generated Clexulator of the reference, where it lies in the
 # reference tree, against the shim in oracle/ref_shim, into oracle/_ref/.
 # Needs the reference sources (present only where they are mounted).
+#   build_ref.sh        FCC_binary_vacancy bset.default (one sublattice)
+#   build_ref.sh zro    Clex_ZrO_Occ bset.formation_energy (hcp Zr + O/Va)
+# Prints the path of the built probe on its last line.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 REF="${REFERENCE_ROOT:-/root/reference}"
-SRC="$REF/tests/unit/clexmonte/data/FCC_binary_vacancy/basis_sets/bset.default/FCC_binary_vacancy_Clexulator_default.cc"
-[ -f "$SRC" ] || { echo "reference sources not found: $SRC" >&2; exit 2; }
+DATA="$REF/tests/unit/clexmonte/data"
 mkdir -p "$HERE/_ref"
-g++ -O1 -std=c++17 -I "$HERE/ref_shim" "$SRC" "$HERE/ref_probe_fcc.cc" -o "$HERE/_ref/fcc_clexulator_probe"
-echo "$HERE/_ref/fcc_clexulator_probe"
+case "${1:-fcc}" in
+  fcc)
+    SRC="$DATA/FCC_binary_vacancy/basis_sets/bset.default/FCC_binary_vacancy_Clexulator_default.cc"
+    [ -f "$SRC" ] || { echo "reference sources not found: $SRC" >&2; exit 2; }
+    g++ -O1 -std=c++17 -I "$HERE/ref_shim" "$SRC" "$HERE/ref_probe_fcc.cc" -o "$HERE/_ref/fcc_clexulator_probe"
+    echo "$HERE/_ref/fcc_clexulator_probe"
+    ;;
+  zro)
+    SRC="$DATA/Clex_ZrO_Occ/basis_sets/bset.formation_energy/ZrO_Clexulator_formation_energy.cc"
+    [ -f "$SRC" ] || { echo "reference sources not found: $SRC" >&2; exit 2; }
+    g++ -O1 -std=c++17 -I "$HERE/ref_shim" -DPROBE_FACTORY=make_ZrO_Clexulator_formation_energy \
+      "$SRC" "$HERE/ref_probe_xtal.cc" -o "$HERE/_ref/zro_clexulator_probe"
+    echo "$HERE/_ref/zro_clexulator_probe"
+    ;;
+  *)
+    echo "unknown probe: $1" >&2
+    exit 2
+    ;;
+esac

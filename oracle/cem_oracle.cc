@@ -26,7 +26,10 @@
 // Clusters are enumerated here from the lattice and the per-size maximum
 // lengths, and each decorated cluster is identified by a geometric invariant
 // (sorted edge list with squared lengths and species pairs), not by the
-// product's symmetry tables. Orbit multiplicities are counted here.
+// product's symmetry tables. Orbit multiplicities are counted here. Crystals
+// whose orbits such invariants do not separate (several sublattices, e.g.
+// the reference's Clex_ZrO_Occ prim) go through ora_system_create_xtal: the
+// factor group is searched here and clusters are keyed by canonical forms.
 
 #include <algorithm>
 #include <array>
@@ -134,6 +137,8 @@ inline int site_index(const System &s, int b, i64 i, i64 j, i64 k) {
   auto m = [](i64 a, int n) { return (int)(((a % n) + n) % n); };
   return b * s.n_uc + m(i, s.L[0]) + s.L[0] * (m(j, s.L[1]) + s.L[1] * m(k, s.L[2]));
 }
+
+void finish_build(System &s, const std::vector<double> &orbit_count);
 
 void build(System &s, const double *max_length /*[5], index = size*/,
            const int *func_size, const i64 *func_pts /*n_funcs*4*3*/,
@@ -262,6 +267,12 @@ void build(System &s, const double *max_length /*[5], index = size*/,
       }
     }
   }
+  finish_build(s, orbit_count);
+}
+
+// Multiplicities, weights, supercell clusters and their incidence lists, from
+// the anchored cluster types of every basis site.
+void finish_build(System &s, const std::vector<double> &orbit_count) {
   // 3. multiplicities, weights
   s.mult.assign(s.n_funcs, 1.0);
   s.weight.assign(s.n_funcs, 0.0);
@@ -331,6 +342,279 @@ void build(System &s, const double *max_length /*[5], index = size*/,
     s.inc[e].pos = s.inc_pos[e];
     for (int q = 0; q < 4; ++q) s.inc[e].sites[q] = k.sites[q];
   }
+}
+
+// ---- general crystals (any lattice; several sublattices, each with its own
+// occupant list). Written independently of the product's table builder:
+// the factor group is searched here from the lattice and the basis, and
+// clusters are identified by their canonical form under it (the smallest,
+// over the operations, of the sorted integral sites (i, j, k, b, label)
+// translated so that the first site is in cell 0), since distance lists do
+// not separate the orbits of such crystals.
+struct XOp {
+  int R[3][3];
+  std::vector<int> perm;
+  std::vector<std::array<i64, 3>> d;
+};
+
+std::vector<XOp> xtal_factor_group(const double *lat, int nb, const double *frac, const int *kind,
+                                   double tol) {
+  double G[3][3];
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) {
+      G[a][b] = 0;
+      for (int c = 0; c < 3; ++c) G[a][b] += lat[a * 3 + c] * lat[b * 3 + c];
+    }
+  double scale = 1.0;
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) scale = std::max(scale, std::fabs(G[a][b]));
+  std::vector<XOp> ops;
+  for (int code = 0; code < 19683; ++code) {
+    int R[3][3], c = code;
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) {
+        R[a][b] = c % 3 - 1;
+        c /= 3;
+      }
+    const int det = R[0][0] * (R[1][1] * R[2][2] - R[1][2] * R[2][1]) -
+                    R[0][1] * (R[1][0] * R[2][2] - R[1][2] * R[2][0]) +
+                    R[0][2] * (R[1][0] * R[2][1] - R[1][1] * R[2][0]);
+    if (det != 1 && det != -1) continue;
+    bool metric = true;  // R^T G R == G
+    for (int a = 0; a < 3 && metric; ++a)
+      for (int b = 0; b < 3 && metric; ++b) {
+        double v = 0;
+        for (int p = 0; p < 3; ++p)
+          for (int q = 0; q < 3; ++q) v += R[p][a] * G[p][q] * R[q][b];
+        if (std::fabs(v - G[a][b]) > tol * scale) metric = false;
+      }
+    if (!metric) continue;
+    std::vector<std::array<double, 3>> rf(nb);
+    for (int b = 0; b < nb; ++b)
+      for (int a = 0; a < 3; ++a)
+        rf[b][a] = R[a][0] * frac[b * 3] + R[a][1] * frac[b * 3 + 1] + R[a][2] * frac[b * 3 + 2];
+    for (int b1 = 0; b1 < nb; ++b1) {
+      if (kind[b1] != kind[0]) continue;
+      double t[3];
+      for (int a = 0; a < 3; ++a) t[a] = frac[b1 * 3 + a] - rf[0][a];
+      XOp op;
+      std::memcpy(op.R, R, sizeof(R));
+      bool ok = true;
+      for (int b = 0; b < nb && ok; ++b) {
+        int hit = -1;
+        std::array<i64, 3> dd{};
+        for (int b2 = 0; b2 < nb && hit < 0; ++b2) {
+          if (kind[b2] != kind[b]) continue;
+          bool same = true;
+          for (int a = 0; a < 3; ++a) {
+            const double x = rf[b][a] + t[a] - frac[b2 * 3 + a];
+            if (std::fabs(x - std::nearbyint(x)) > tol) same = false;
+            dd[a] = (i64)std::nearbyint(x);
+          }
+          if (same) hit = b2;
+        }
+        if (hit < 0) ok = false;
+        op.perm.push_back(hit);
+        op.d.push_back(dd);
+      }
+      if (ok) ops.push_back(op);
+    }
+  }
+  return ops;
+}
+
+struct XSite {
+  int b;  // prim sublattice
+  i64 u[3];
+};
+
+std::vector<i64> xtal_key(const std::vector<XOp> &ops, const std::vector<XSite> &sites,
+                          const std::vector<int> &lab) {
+  std::vector<i64> best;
+  const int n = (int)sites.size();
+  std::vector<std::array<i64, 5>> m(n);
+  for (const XOp &op : ops) {
+    for (int q = 0; q < n; ++q) {
+      const XSite &s = sites[q];
+      for (int a = 0; a < 3; ++a)
+        m[q][a] = op.R[a][0] * s.u[0] + op.R[a][1] * s.u[1] + op.R[a][2] * s.u[2] + op.d[s.b][a];
+      m[q][3] = op.perm[s.b];
+      m[q][4] = lab[q];
+    }
+    std::sort(m.begin(), m.end());
+    std::vector<i64> key;
+    key.reserve(5 * n);
+    for (int q = 0; q < n; ++q)
+      for (int a = 0; a < 5; ++a) key.push_back(a < 3 ? m[q][a] - m[0][a] : m[q][a]);
+    if (best.empty() || key < best) best = key;
+  }
+  return best;
+}
+
+// func_sites: per function 4 sites (prim sublattice, i, j, k); func_occ: the
+// occupant (1-based site-function index + 1) on each site.
+void build_xtal(System &s, const double *lat, int nb_all, const double *frac, const int *kind,
+                const int *dof, const double *max_length, const int *func_size,
+                const i64 *func_sites, const int *func_occ) {
+  const double tol = 1e-5;
+  std::vector<XOp> ops = xtal_factor_group(lat, nb_all, frac, kind, tol);
+  if (ops.empty()) throw std::runtime_error("empty factor group");
+  std::vector<int> kb(nb_all, -1), dof_b;
+  for (int b = 0; b < nb_all; ++b)
+    if (dof[b]) {
+      kb[b] = (int)dof_b.size();
+      dof_b.push_back(b);
+    }
+  if ((int)dof_b.size() != s.n_basis) throw std::runtime_error("n_basis != sublattices with dof");
+  auto cart = [&](int b, const i64 *u, double *c) {
+    for (int a = 0; a < 3; ++a) {
+      c[a] = 0;
+      for (int r = 0; r < 3; ++r) c[a] += ((double)u[r] + frac[b * 3 + r]) * lat[r * 3 + a];
+    }
+  };
+  // 1. functions and orbits by canonical form
+  std::map<std::vector<i64>, int> fmap, omap;
+  s.func_orbit.assign(s.n_funcs, -1);
+  for (int f = 1; f < s.n_funcs; ++f) {
+    const int n = func_size[f];
+    std::vector<XSite> p(n);
+    std::vector<int> o(n), z(n, 0);
+    for (int i = 0; i < n; ++i) {
+      const i64 *q = func_sites + (f * 4 + i) * 4;
+      p[i].b = (int)q[0];
+      p[i].u[0] = q[1];
+      p[i].u[1] = q[2];
+      p[i].u[2] = q[3];
+      o[i] = func_occ[f * 4 + i];
+    }
+    auto key = xtal_key(ops, p, o);
+    if (fmap.count(key)) throw std::runtime_error("two functions share a canonical form");
+    fmap[key] = f;
+    auto okey = xtal_key(ops, p, z);
+    if (!omap.count(okey)) {
+      const int id = (int)omap.size();
+      omap[okey] = id;
+    }
+    s.func_orbit[f] = omap[okey];
+  }
+  const int n_orbit = (int)omap.size();
+  std::vector<double> orbit_count(n_orbit, 0.0);
+  double rmax = 0;
+  for (int n = 2; n <= 4; ++n) rmax = std::max(rmax, max_length[n]);
+  // search box: |u_a| <= rmax * |column a of the inverse lattice| + 2
+  double inv[3][3];
+  {
+    const double *A = lat;
+    const double det = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+                       A[2] * (A[3] * A[7] - A[4] * A[6]);
+    inv[0][0] = (A[4] * A[8] - A[5] * A[7]) / det;
+    inv[0][1] = (A[2] * A[7] - A[1] * A[8]) / det;
+    inv[0][2] = (A[1] * A[5] - A[2] * A[4]) / det;
+    inv[1][0] = (A[5] * A[6] - A[3] * A[8]) / det;
+    inv[1][1] = (A[0] * A[8] - A[2] * A[6]) / det;
+    inv[1][2] = (A[2] * A[3] - A[0] * A[5]) / det;
+    inv[2][0] = (A[3] * A[7] - A[4] * A[6]) / det;
+    inv[2][1] = (A[1] * A[6] - A[0] * A[7]) / det;
+    inv[2][2] = (A[0] * A[4] - A[1] * A[3]) / det;
+  }
+  int box[3];
+  for (int a = 0; a < 3; ++a) {
+    const double nrm = std::sqrt(inv[0][a] * inv[0][a] + inv[1][a] * inv[1][a] + inv[2][a] * inv[2][a]);
+    box[a] = (int)std::ceil(rmax * nrm) + 2;
+  }
+  s.types.assign(s.n_basis, {});
+  for (int b : dof_b) {
+    const i64 zero[3] = {0, 0, 0};
+    double c0[3];
+    cart(b, zero, c0);
+    struct Nb {
+      XSite site;
+      double c[3];
+    };
+    std::vector<Nb> nb;
+    for (i64 u0 = -box[0]; u0 <= box[0]; ++u0)
+      for (i64 u1 = -box[1]; u1 <= box[1]; ++u1)
+        for (i64 u2 = -box[2]; u2 <= box[2]; ++u2)
+          for (int bb : dof_b) {
+            Nb e;
+            e.site.b = bb;
+            e.site.u[0] = u0;
+            e.site.u[1] = u1;
+            e.site.u[2] = u2;
+            cart(bb, e.site.u, e.c);
+            double d2 = 0;
+            for (int a = 0; a < 3; ++a) d2 += (e.c[a] - c0[a]) * (e.c[a] - c0[a]);
+            if (d2 > 0 && std::sqrt(d2) <= rmax + tol) nb.push_back(e);
+          }
+    auto dist = [](const double *a, const double *b) {
+      double d2 = 0;
+      for (int k = 0; k < 3; ++k) d2 += (a[k] - b[k]) * (a[k] - b[k]);
+      return std::sqrt(d2);
+    };
+    auto site_less = [](const XSite &x, const XSite &y) {  // by (i, j, k, b)
+      for (int a = 0; a < 3; ++a)
+        if (x.u[a] != y.u[a]) return x.u[a] < y.u[a];
+      return x.b < y.b;
+    };
+    XSite centre{b, {0, 0, 0}};
+    auto add_type = [&](const std::vector<int> &idx) {
+      const int n = (int)idx.size() + 1;
+      const double lim = max_length[n] + tol;
+      std::vector<XSite> p(n);
+      std::vector<const double *> c(n);
+      p[0] = centre;
+      c[0] = c0;
+      for (int i = 1; i < n; ++i) {
+        p[i] = nb[idx[i - 1]].site;
+        c[i] = nb[idx[i - 1]].c;
+      }
+      for (int i = 0; i < n; ++i)
+        for (int j = i + 1; j < n; ++j)
+          if (dist(c[i], c[j]) > lim) return;
+      for (int i = 1; i < n; ++i)
+        if (site_less(p[i], p[0])) return;  // anchor = the smallest site
+      std::vector<int> z(n, 0);
+      auto it = omap.find(xtal_key(ops, p, z));
+      if (it == omap.end()) return;
+      AnchorType t;
+      t.size = n;
+      t.orbit = it->second;
+      for (int i = 0; i < n; ++i) {
+        t.b[i] = kb[p[i].b];
+        for (int a = 0; a < 3; ++a) t.du[i][a] = p[i].u[a];
+      }
+      int ncode = 1;
+      for (int i = 0; i < n; ++i) ncode *= s.n_occ;
+      t.lut.assign(ncode, -1);
+      std::vector<int> occ(n);
+      for (int code = 0; code < ncode; ++code) {
+        int cc = code;
+        bool all_nonref = true;
+        for (int i = 0; i < n; ++i) {
+          occ[i] = cc % s.n_occ;
+          cc /= s.n_occ;
+          if (occ[i] == 0) all_nonref = false;
+        }
+        if (!all_nonref) continue;
+        auto f = fmap.find(xtal_key(ops, p, occ));
+        if (f == fmap.end()) throw std::runtime_error("decorated cluster has no function");
+        t.lut[code] = f->second;
+      }
+      orbit_count[t.orbit] += 1.0;
+      s.types[kb[b]].push_back(t);
+    };
+    add_type({});
+    const int m = (int)nb.size();
+    for (int i = 0; i < m; ++i) {
+      if (max_length[2] > 0) add_type({i});
+      for (int j = i + 1; j < m; ++j) {
+        if (max_length[3] > 0) add_type({i, j});
+        if (max_length[4] > 0)
+          for (int k = j + 1; k < m; ++k) add_type({i, j, k});
+      }
+    }
+  }
+  finish_build(s, orbit_count);
 }
 
 inline int cluster_code(const System &s, int c, const signed char *occ, int site, int site_occ) {
@@ -512,6 +796,33 @@ void *ora_system_create(int n_basis, const i64 *lattice, const i64 *basis, doubl
     s->coeff.assign(coeff, coeff + n_funcs);
     s->RT.assign(RT, RT + (n_occ - 1) * n_occ);
     build(*s, max_length, func_size, func_pts, func_occ);
+    return s.release();
+  } catch (std::exception &e) {
+    g_err = e.what();
+    return nullptr;
+  }
+}
+
+void *ora_system_create_xtal(int n_basis_all, const double *lattice, const double *frac,
+                             const int *site_kind, const int *site_dof, int n_occ,
+                             const double *max_length, int n_funcs, const int *func_size,
+                             const i64 *func_sites, const int *func_occ, const double *eci,
+                             const double *coeff, const double *RT, int Lx, int Ly, int Lz) {
+  try {
+    auto s = std::make_unique<System>();
+    int nd = 0;
+    for (int b = 0; b < n_basis_all; ++b) nd += site_dof[b] ? 1 : 0;
+    s->n_basis = nd;
+    s->n_occ = n_occ;
+    s->L[0] = Lx;
+    s->L[1] = Ly;
+    s->L[2] = Lz;
+    s->n_funcs = n_funcs;
+    s->eci.assign(eci, eci + n_funcs);
+    s->coeff.assign(coeff, coeff + n_funcs);
+    s->RT.assign(RT, RT + (n_occ - 1) * n_occ);
+    build_xtal(*s, lattice, n_basis_all, frac, site_kind, site_dof, max_length, func_size,
+               func_sites, func_occ);
     return s.release();
   } catch (std::exception &e) {
     g_err = e.what();

@@ -53,6 +53,11 @@ def lib():
             C.c_int, i64p, i64p, C.c_double, C.c_int, f64p, C.c_int, i32p, i64p, i32p,
             f64p, f64p, f64p, C.c_int, C.c_int, C.c_int,
         ]
+        L.ora_system_create_xtal.restype = P
+        L.ora_system_create_xtal.argtypes = [
+            C.c_int, f64p, f64p, i32p, i32p, C.c_int, f64p, C.c_int, i32p, i64p, i32p,
+            f64p, f64p, f64p, C.c_int, C.c_int, C.c_int,
+        ]
         L.ora_system_destroy.argtypes = [P]
         L.ora_n_sites.argtypes = [P]
         L.ora_n_clusters.argtypes = [P]
@@ -115,34 +120,52 @@ class OracleSystem:
         self.L = tuple(int(x) for x in L)
         nf = ce.n_funcs
         size = np.zeros(nf, dtype=np.int32)
-        pts = np.zeros((nf, 4, 3), dtype=np.int64)
         occ = np.zeros((nf, 4), dtype=np.int32)
         for f in range(1, nf):
             o = ce.orbits[ce.func_orbit[f]]
             size[f] = o.size
-            pts[f, : o.size] = o.prototype
             occ[f, : o.size] = np.array(ce.func_rep[f]) + 1
         ml = np.zeros(5)
         for k, v in ce.max_length.items():
             ml[k] = v
         rt = getattr(ce, "param_RT", None)
         self.RT = composition_RT(prim.n_basis, prim.n_occ) if rt is None else np.asarray(rt, dtype=np.float64)
-        h = lib().ora_system_create(
-            prim.n_basis,
-            np.ascontiguousarray(prim.lattice.reshape(-1), dtype=np.int64),
-            np.ascontiguousarray(prim.basis.reshape(-1), dtype=np.int64),
-            float(prim.grid),
-            prim.n_occ,
-            ml,
-            nf,
-            size,
-            np.ascontiguousarray(pts.reshape(-1)),
-            np.ascontiguousarray(occ.reshape(-1)),
+        common = (
             np.ascontiguousarray(ce.eci, dtype=np.float64),
             np.ascontiguousarray(ce.func_coeff, dtype=np.float64),
             np.ascontiguousarray(self.RT.reshape(-1)),
             *self.L,
         )
+        cr = getattr(ce, "crystal", None)
+        if cr is not None:
+            # general crystal: prototypes as integral sites (prim sublattice, cell)
+            sites = np.zeros((nf, 4, 4), dtype=np.int64)
+            for f in range(1, nf):
+                for q, (b, u) in enumerate(ce.orbits[ce.func_orbit[f]].proto_sites):
+                    sites[f, q] = (b, *u)
+            kinds = {o: k for k, o in enumerate(dict.fromkeys(cr.occupants))}
+            h = lib().ora_system_create_xtal(
+                cr.n_basis,
+                np.ascontiguousarray(cr.lattice.reshape(-1)),
+                np.ascontiguousarray(cr.frac.reshape(-1)),
+                np.array([kinds[o] for o in cr.occupants], dtype=np.int32),
+                np.array([1 if len(o) > 1 else 0 for o in cr.occupants], dtype=np.int32),
+                prim.n_occ, ml, nf, size, np.ascontiguousarray(sites.reshape(-1)),
+                np.ascontiguousarray(occ.reshape(-1)), *common,
+            )
+        else:
+            pts = np.zeros((nf, 4, 3), dtype=np.int64)
+            for f in range(1, nf):
+                o = ce.orbits[ce.func_orbit[f]]
+                pts[f, : o.size] = o.prototype
+            h = lib().ora_system_create(
+                prim.n_basis,
+                np.ascontiguousarray(prim.lattice.reshape(-1), dtype=np.int64),
+                np.ascontiguousarray(prim.basis.reshape(-1), dtype=np.int64),
+                float(prim.grid), prim.n_occ, ml, nf, size,
+                np.ascontiguousarray(pts.reshape(-1)), np.ascontiguousarray(occ.reshape(-1)),
+                *common,
+            )
         if not h:
             raise RuntimeError(lib().ora_last_error().decode())
         self.h = h

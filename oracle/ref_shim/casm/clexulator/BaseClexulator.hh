@@ -55,6 +55,7 @@ class BaseClexulator {
 
   std::set<xtal::UnitCell> const &neighborhood() const { return m_neighborhood; }
   long weight(int r, int c) const { return m_weight_matrix.v[r][c]; }
+  std::set<int> const &sublat_indices() const { return m_sublat_indices; }
 
   virtual ClexParamPack const &param_pack() const = 0;
   virtual ClexParamPack &param_pack() = 0;
