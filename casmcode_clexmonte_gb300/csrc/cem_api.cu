@@ -91,6 +91,7 @@ struct cem_system {
   std::vector<int> fl_sub, fl_pb, fl_du;
   int nb_reach = 0;
   bool fcc_generated = false;  // flower matches the generated binary FCC evaluator
+  bool big = false;            // more orbits than the register accumulators hold
   std::vector<void *> owned;
   ~cem_system() {
     for (void *p : owned) cudaFree(p);
@@ -284,7 +285,7 @@ int cem_system_create(const cem_system_desc *d, cem_system **out) {
     require(d->n_occ >= 2 && d->n_occ <= 3, "n_occ must be 2 or 3", CEM_ERR_UNSUPPORTED);
     require(d->n_funcs >= 1 && d->n_funcs <= MAX_FUNCS, "n_funcs out of range",
             CEM_ERR_UNSUPPORTED);
-    require(d->n_orbits >= 1 && d->n_orbits <= MAX_ORBITS, "n_orbits out of range",
+    require(d->n_orbits >= 1 && d->n_orbits <= MAX_ORBITS_ALL, "n_orbits out of range",
             CEM_ERR_UNSUPPORTED);
     auto s = std::make_unique<cem_system>();
     CeTables &T = s->T;
@@ -312,10 +313,10 @@ int cem_system_create(const cem_system_desc *d, cem_system **out) {
     std::vector<int> pb(ncl * 3), du(ncl * 9), lutoff(ncl);
     std::vector<uint8_t> lut((size_t)ncl * stride, 0);
     auto load = [&](int base, int n, const int *sub, const int *orb, const int *psub,
-                    const int *pdu, const int16_t *plut, int begin[MAX_SUBLAT][MAX_ORBITS + 1]) {
+                    const int *pdu, const int16_t *plut, int begin[MAX_SUBLAT][MAX_ORBITS_ALL + 1]) {
       int prev_b = 0, prev_g = 0;
       for (int b = 0; b < MAX_SUBLAT; ++b)
-        for (int g = 0; g <= MAX_ORBITS; ++g) begin[b][g] = -1;
+        for (int g = 0; g <= MAX_ORBITS_ALL; ++g) begin[b][g] = -1;
       for (int c = 0; c < n; ++c) {
         const int b = sub[c], g = orb[c];
         require(b >= 0 && b < d->n_sublat && g >= 0 && g < d->n_orbits, "bad cluster entry");
@@ -350,7 +351,7 @@ int cem_system_create(const cem_system_desc *d, cem_system **out) {
         }
       require(c == n, "clusters are not grouped by sublattice then orbit");
       for (int b = d->n_sublat; b < MAX_SUBLAT; ++b)
-        for (int g = 0; g <= MAX_ORBITS; ++g) begin[b][g] = n;
+        for (int g = 0; g <= MAX_ORBITS_ALL; ++g) begin[b][g] = n;
     };
     load(0, d->n_flower, d->flower_sublat, d->flower_orbit, d->flower_partner_sublat,
          d->flower_partner_du, d->flower_lut, T.fl_begin);
@@ -395,7 +396,8 @@ int cem_system_create(const cem_system_desc *d, cem_system **out) {
       T.wr[g] = 0.f;
     }
     T.wq_scale = 1.f;
-    if (d->n_occ == 2) {
+    s->big = T.n_orbits > MAX_ORBITS;
+    if (d->n_occ == 2 && !s->big) {
       double wmax = 0.0;
       long long dcmax[MAX_ORBITS] = {0};
       for (int g = 0; g < T.n_orbits; ++g) {
@@ -550,9 +552,10 @@ int cem_replicas_create(const cem_system *sys, int n, const int *L, int ensemble
       if (pitch) smem = std::max(smem, sweep_smem_bytes(sys->T, Li[0], Li[1], Li[2], max_cls, pitch));
     }
     if (pitch && smem > maxsm) pitch = 0;  // generated layout does not fit: run-time tables
+    if (sys->big) pitch = -1;               // run-time tables, one orbit at a time
     r->pitch = pitch;
     r->generic_smem = gsmem;
-    r->sweep_smem = pitch ? smem : gsmem;
+    r->sweep_smem = pitch > 0 ? smem : gsmem;
     if (r->sweep_smem > maxsm && stream_pitch_for(*sys, r->reps)) {
       r->streamed = true;
       r->stream_pitch = stream_pitch_for(*sys, r->reps);
@@ -861,6 +864,8 @@ int cem_nfold_run(cem_replicas *r, int64_t n_events, int64_t n_equil, int64_t re
     require(r != nullptr, "null handle");
     require(r->ensemble == CEM_SEMIGRAND_CANONICAL,
             "the n-fold way runs semi-grand canonical replicas");
+    require(!r->sys->big, "the n-fold way supports cluster expansions of at most 8 orbits",
+            CEM_ERR_UNSUPPORTED);
     require(n_events >= 0 && n_equil >= 0 && record_capacity >= 0, "counts must be >= 0");
     require(record_capacity == 0 || (rec_site && rec_occ && rec_dt), "null record buffers");
     const CeTables &T = r->sys->T;
@@ -955,6 +960,9 @@ int cem_enforce_composition(cem_replicas *r, const double *target_mol, uint64_t 
   return guard([&] {
     require(r != nullptr, "null replica batch");
     require(target_mol != nullptr, "null target composition");
+    require(!r->sys->big,
+            "composition enforcement supports cluster expansions of at most 8 orbits",
+            CEM_ERR_UNSUPPORTED);
     const int nocc = r->sys->T.n_occ;
     for (int i = 0; i < r->n * nocc; ++i)
       require(std::isfinite(target_mol[i]), "target composition must be finite");
@@ -1029,7 +1037,7 @@ int cem_step_async(cem_replicas *r, const int8_t *host_in, int8_t *host_out, int
       P.n_pair_sweeps = r->n_pair_sweeps;
       P.n_local_sweeps = r->n_local_sweeps;
       P.cta_rep = r->d_cta_rep;
-      P.init = T.n_occ == 2 ? 1 : 0;
+      P.init = (T.n_occ == 2 && r->pitch >= 0) ? 1 : 0;
       for (size_t k = 0; k < r->sys->RT.size() && k < 16; ++k) P.RT[k] = r->sys->RT[k];
       int max_sites = 0;
       for (const Replica &R : r->reps) max_sites = std::max(max_sites, R.n_sites);
@@ -1136,7 +1144,8 @@ int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_sampl
       return;
     }
     // binary systems compute the exact initial stats inside the sweep kernel
-    const bool fused_init = !r->stats_valid && r->sys->T.n_occ == 2;
+    // (the orbit-at-a-time kernel has no fused initial energy)
+    const bool fused_init = !r->stats_valid && r->sys->T.n_occ == 2 && r->pitch >= 0;
     if (!r->stats_valid && !fused_init) init_stats(r);
     SweepParams P{};
     P.init = fused_init ? 1 : 0;
@@ -1277,6 +1286,7 @@ int cem_autotune(cem_replicas *r, int64_t trial_passes, double *best_ms) {
       int bt = r->threads, bo = r->cta_order;
       for (int th : {SWEEP_THREADS, 256})
         for (int order : {0, 1}) {
+          if (th != SWEEP_THREADS && r->sys->big) continue;
           restore();
           r->threads = th;
           set_cta_order(r, order);
@@ -1322,12 +1332,22 @@ int cem_set_option(cem_replicas *r, const char *key, int64_t value) {
       r->stream_pitch = sp;
     } else if (k == "threads") {
       require(value == 512 || value == 256, "threads must be 512 or 256 (two replicas per SM)");
+      require(value == 512 || !r->sys->big,
+              "cluster expansions with more than 8 orbits run 512 threads per replica",
+              CEM_ERR_UNSUPPORTED);
       r->threads = (int)value;
     } else if (k == "cta_order") {
       set_cta_order(r, (int)value);
+    } else if (k == "orbit_walk") {
+      // run-time tables walked one orbit at a time (the kernel that large
+      // cluster expansions need), also for small ones
+      require(value == 1, "orbit_walk can only be switched on");
+      r->pitch = -1;
+      r->sweep_smem = r->generic_smem;
+      r->threads = SWEEP_THREADS;
     } else if (k == "generic_evaluator") {
       if (value) {
-        r->pitch = 0;
+        r->pitch = r->sys->big ? -1 : 0;
         r->sweep_smem = r->generic_smem;
       } else {
         throw Err(CEM_ERR_INVALID, "generic_evaluator can only be switched on");

@@ -24,26 +24,28 @@
 namespace cem {
 
 constexpr int MAX_SUBLAT = 4;
-constexpr int MAX_ORBITS = 8;    // non-empty orbits
-constexpr int MAX_FUNCS = 64;
+constexpr int MAX_ORBITS = 8;        // orbits held in register accumulators
+constexpr int MAX_ORBITS_ALL = 128;  // non-empty orbits of a system (more than
+                                     // MAX_ORBITS: one orbit at a time)
+constexpr int MAX_FUNCS = 128;
 constexpr int MAX_PARTNERS = 3;  // clusters of up to 4 sites
 constexpr int MAX_NB = 16;       // nearest-neighbour displacements per sublattice
 constexpr int MAX_COLOURS = 8;   // per axis
 constexpr int MAX_L = 128;       // per axis
-constexpr int MAX_FP = 128;      // distinct flower partners per sublattice
+constexpr int MAX_FP = 256;      // distinct flower partners per sublattice
 
 // Cluster-expansion tables in device memory (built once per system).
 struct CeTables {
   int n_sublat, n_occ, n_sf, n_funcs, n_orbits;
-  int orb_func_base[MAX_ORBITS];
-  int orb_n_funcs[MAX_ORBITS];
-  int orb_size[MAX_ORBITS];
+  int orb_func_base[MAX_ORBITS_ALL];
+  int orb_n_funcs[MAX_ORBITS_ALL];
+  int orb_size[MAX_ORBITS_ALL];
   // flower clusters, grouped by centre sublattice then orbit:
   // clusters of (b, g) are [fl_begin[b][g], fl_begin[b][g+1])
-  int fl_begin[MAX_SUBLAT][MAX_ORBITS + 1];
+  int fl_begin[MAX_SUBLAT][MAX_ORBITS_ALL + 1];
   int n_fl;
   // owned clusters (each periodic cluster counted once), same grouping
-  int ow_begin[MAX_SUBLAT][MAX_ORBITS + 1];
+  int ow_begin[MAX_SUBLAT][MAX_ORBITS_ALL + 1];
   int n_ow;
   int reach;  // max |cell offset component| over flower partners
   // neighbour displacements per sublattice (canonical local swaps)

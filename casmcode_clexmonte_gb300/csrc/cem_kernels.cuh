@@ -19,6 +19,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <type_traits>
 
 #include "cem_common.cuh"
 #include "cem_internal.h"
@@ -44,8 +45,79 @@ struct Acc<2> {
   }
 };
 
+// Delta counts of one orbit for one changed site (centre of sublattice b,
+// o_i -> o_f): binary systems an integer count change, other systems packed
+// 8-bit counts of the decorations gained (p) and lost (m) per local function.
+// rd(c, j) returns the occupant of partner j of cluster c.
+template <int NOCC>
+struct OrbAcc {
+  unsigned long long p = 0ull, m = 0ull;
+};
+template <>
+struct OrbAcc<2> {
+  int c = 0;
+};
+
+template <int NOCC, class Reader>
+__device__ __forceinline__ void orbit_site(const CeTables &T, int b, int g, int o_i, int o_f,
+                                           const int *__restrict__ lutoff,
+                                           const uint8_t *__restrict__ lut, Reader rd,
+                                           OrbAcc<NOCC> &a) {
+  const int c0 = T.fl_begin[b][g], c1 = T.fl_begin[b][g + 1];
+  const int size = T.orb_size[g];
+  if constexpr (NOCC == 2) {
+    int cnt = 0;
+    if (size == 1) {
+      cnt = c1 - c0;
+    } else if (size == 2) {
+      for (int c = c0; c < c1; ++c) cnt += rd(c, 0);
+    } else if (size == 3) {
+      for (int c = c0; c < c1; ++c) cnt += rd(c, 0) & rd(c, 1);
+    } else {
+      for (int c = c0; c < c1; ++c) cnt += rd(c, 0) & rd(c, 1) & rd(c, 2);
+    }
+    a.c += (o_f - o_i) * cnt;
+  } else {
+    constexpr int NSF = NOCC - 1;
+    for (int c = c0; c < c1; ++c) {
+      int code = 0, mul = NSF;
+      bool ok = true;
+      for (int j = 0; j < size - 1; ++j) {
+        int v = rd(c, j);
+        ok = ok && (v != 0);
+        code += (v - 1) * mul;
+        mul *= NSF;
+      }
+      if (ok) {
+        const int base = lutoff[c] + code;
+        if (o_f) a.p += 1ull << (8 * lut[base + o_f - 1]);
+        if (o_i) a.m += 1ull << (8 * lut[base + o_i - 1]);
+      }
+    }
+  }
+}
+
+// Add the float-float terms W_f dC_f of orbit g's functions to r (functions
+// in increasing order; binary systems add the orbit's one term even when it is
+// zero, other systems skip zero terms).
+template <int NOCC>
+__device__ __forceinline__ void orbit_fold(const CeTables &T, int g, const OrbAcc<NOCC> &a,
+                                           const float *__restrict__ whi,
+                                           const float *__restrict__ wlo, FF &r) {
+  const int base = T.orb_func_base[g];
+  if constexpr (NOCC == 2) {
+    ff_add_term(r, whi[base], wlo[base], a.c);
+  } else {
+    const int nf = T.orb_n_funcs[g];
+    for (int fl = 0; fl < nf; ++fl) {
+      const int dc = (int)((a.p >> (8 * fl)) & 255ull) - (int)((a.m >> (8 * fl)) & 255ull);
+      if (dc) ff_add_term(r, whi[base + fl], wlo[base + fl], dc);
+    }
+  }
+}
+
 // Add the delta counts of changing the centre site of sublattice b from o_i
-// to o_f. rd(c, j) returns the occupant of partner j of cluster c.
+// to o_f, for the first MAX_ORBITS orbits (register accumulators).
 template <int NOCC, class Reader>
 __device__ __forceinline__ void accumulate_site(const CeTables &T, int b, int o_i, int o_f,
                                                 const int *__restrict__ lutoff,
@@ -54,37 +126,13 @@ __device__ __forceinline__ void accumulate_site(const CeTables &T, int b, int o_
 #pragma unroll
   for (int g = 0; g < MAX_ORBITS; ++g) {
     if (g < T.n_orbits) {
-      const int c0 = T.fl_begin[b][g], c1 = T.fl_begin[b][g + 1];
-      const int size = T.orb_size[g];
+      OrbAcc<NOCC> a;
+      orbit_site<NOCC>(T, b, g, o_i, o_f, lutoff, lut, rd, a);
       if constexpr (NOCC == 2) {
-        int cnt = 0;
-        if (size == 1) {
-          cnt = c1 - c0;
-        } else if (size == 2) {
-          for (int c = c0; c < c1; ++c) cnt += rd(c, 0);
-        } else if (size == 3) {
-          for (int c = c0; c < c1; ++c) cnt += rd(c, 0) & rd(c, 1);
-        } else {
-          for (int c = c0; c < c1; ++c) cnt += rd(c, 0) & rd(c, 1) & rd(c, 2);
-        }
-        acc.c[g] += (o_f - o_i) * cnt;
+        acc.c[g] += a.c;
       } else {
-        constexpr int NSF = NOCC - 1;
-        for (int c = c0; c < c1; ++c) {
-          int code = 0, mul = NSF;
-          bool ok = true;
-          for (int j = 0; j < size - 1; ++j) {
-            int v = rd(c, j);
-            ok = ok && (v != 0);
-            code += (v - 1) * mul;
-            mul *= NSF;
-          }
-          if (ok) {
-            const int base = lutoff[c] + code;
-            if (o_f) acc.p[g] += 1ull << (8 * lut[base + o_f - 1]);
-            if (o_i) acc.m[g] += 1ull << (8 * lut[base + o_i - 1]);
-          }
-        }
+        acc.p[g] += a.p;
+        acc.m[g] += a.m;
       }
     }
   }
@@ -255,36 +303,57 @@ __global__ void k_delta(const __grid_constant__ CeTables T, const int8_t *__rest
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n_events) return;
   const int n_uc = L0 * L1 * L2;
-  Acc<NOCC> acc;
-  acc.zero();
   double mu_term = 0.0;
-  int ov_site[4], ov_val[4];
+  // sequential semantics: site s sees the changes of sites 0 .. s-1
+  int ov_site[4], ov_val[4], sb[4], si[4], sj[4], sk[4], soi[4], sof[4];
   for (int s = 0; s < k_sites; ++s) {
     const int l = (int)sites[e * k_sites + s];
     const int b = l / n_uc, uc = l - b * n_uc;
-    const int i = uc % L0, j = (uc / L0) % L1, k = uc / (L0 * L1);
+    sb[s] = b;
+    si[s] = uc % L0;
+    sj[s] = (uc / L0) % L1;
+    sk[s] = uc / (L0 * L1);
     int o_i = occ[l];
     for (int q = 0; q < s; ++q)
       if (ov_site[q] == l) o_i = ov_val[q];
-    const int o_f = new_occ[e * k_sites + s];
-    auto rd = [&](int c, int jj) -> int {
-      const int pb = T.cl_pb[c * 3 + jj];
-      const int *du = T.cl_du + c * 9 + jj * 3;
-      const int site = pb * n_uc + wrapc(i + du[0], L0) +
-                       L0 * (wrapc(j + du[1], L1) + L1 * wrapc(k + du[2], L2));
-      int v = occ[site];
-      for (int q = 0; q < s; ++q)
-        if (ov_site[q] == site) v = ov_val[q];
-      return v;
-    };
-    accumulate_site<NOCC>(T, b, o_i, o_f, T.cl_lut, T.lut, rd, acc);
-    if (dmu) mu_term += dmu[o_i * NOCC + o_f];
+    soi[s] = o_i;
+    sof[s] = new_occ[e * k_sites + s];
+    if (dmu) mu_term += dmu[o_i * NOCC + sof[s]];
     ov_site[s] = l;
-    ov_val[s] = o_f;
+    ov_val[s] = sof[s];
   }
-  FF d = acc_dot<NOCC>(T, acc, T.w_hi, T.w_lo);
+  FF d{0.f, 0.f};
+  long long *dc_out = dcount ? dcount + (long long)e * T.n_funcs : nullptr;
+  if (dc_out) dc_out[0] = 0;
+  for (int g = 0; g < T.n_orbits; ++g) {
+    OrbAcc<NOCC> a;
+    for (int s = 0; s < k_sites; ++s) {
+      const int i = si[s], j = sj[s], k = sk[s];
+      auto rd = [&](int c, int jj) -> int {
+        const int pb = T.cl_pb[c * 3 + jj];
+        const int *du = T.cl_du + c * 9 + jj * 3;
+        const int site = pb * n_uc + wrapc(i + du[0], L0) +
+                         L0 * (wrapc(j + du[1], L1) + L1 * wrapc(k + du[2], L2));
+        int v = occ[site];
+        for (int q = 0; q < s; ++q)
+          if (ov_site[q] == site) v = ov_val[q];
+        return v;
+      };
+      orbit_site<NOCC>(T, sb[s], g, soi[s], sof[s], T.cl_lut, T.lut, rd, a);
+    }
+    orbit_fold<NOCC>(T, g, a, T.w_hi, T.w_lo, d);
+    if (dc_out) {
+      const int base = T.orb_func_base[g];
+      if constexpr (NOCC == 2) {
+        dc_out[base] = a.c;
+      } else {
+        for (int fl = 0; fl < T.orb_n_funcs[g]; ++fl)
+          dc_out[base + fl] =
+              (int)((a.p >> (8 * fl)) & 255ull) - (int)((a.m >> (8 * fl)) & 255ull);
+      }
+    }
+  }
   dE[e] = ((double)d.s + (double)d.e) - mu_term;
-  if (dcount) acc_store<NOCC>(T, acc, dcount + (long long)e * T.n_funcs);
 }
 
 // ------------------------------------------------------------ replay
@@ -414,71 +483,91 @@ __global__ void k_replay(const __grid_constant__ CeTables T, ReplayParams P) {
     }
     __syncwarp();
     if (ev_stop) break;
-    // ---- delta correlations: lanes split each centre's flower clusters
-    Acc<NOCC> acc;
-    acc.zero();
+    // ---- delta correlations: lanes split each centre's flower clusters;
+    // one orbit at a time, both changed sites, folded into the float-float
+    // energy change in function order. The first change is applied before
+    // any cluster is read: a site's own flower never contains the site, so
+    // site 0 sees the original state and site 1 sees site 0 changed (the
+    // reference's sequential semantics).
     const int n = ev_n;
     int saved = 0;
+    if (n > 1) {
+      if (lane == 0) {
+        saved = occ[ev_site[0]];
+        occ[ev_site[0]] = (int8_t)ev_new[0];
+      }
+      __syncwarp();
+    }
+    int sb[2], si[2], sj[2], sk[2], soi[2], sof[2];
     for (int s = 0; s < n; ++s) {
       const int l = (int)ev_site[s];
       const int b = l / n_uc, uc = l - b * n_uc;
-      const int i = uc % L0, j = (uc / L0) % L1, k = uc / (L0 * L1);
-      const int o_i = occ[l], o_f = ev_new[s];
-      if (lane == 0 && s == 0) saved = o_i;
-#pragma unroll
-      for (int g = 0; g < MAX_ORBITS; ++g) {
-        if (g < T.n_orbits) {
-          const int c0 = T.fl_begin[b][g], c1 = T.fl_begin[b][g + 1];
-          const int size = T.orb_size[g];
-          int cnt = 0;
-          unsigned long long pp = 0ull, mm = 0ull;
-          for (int c = c0 + lane; c < c1; c += 32) {
-            int code = 0, mul = NOCC - 1, prod = 1;
-            bool ok = true;
-            for (int q = 0; q < size - 1; ++q) {
-              const int pb = T.cl_pb[c * 3 + q];
-              const int *du = T.cl_du + c * 9 + q * 3;
-              const int site = pb * n_uc + wrapc(i + du[0], L0) +
-                               L0 * (wrapc(j + du[1], L1) + L1 * wrapc(k + du[2], L2));
-              const int v = occ[site];
-              prod &= v;
-              ok = ok && (v != 0);
-              code += (v - 1) * mul;
-              mul *= (NOCC - 1);
-            }
-            if constexpr (NOCC == 2) {
-              cnt += prod;
-            } else {
-              if (ok) {
-                const int base = T.cl_lut[c] + code;
-                if (o_f) pp += 1ull << (8 * T.lut[base + o_f - 1]);
-                if (o_i) mm += 1ull << (8 * T.lut[base + o_i - 1]);
-              }
-            }
+      sb[s] = b;
+      si[s] = uc % L0;
+      sj[s] = (uc / L0) % L1;
+      sk[s] = uc / (L0 * L1);
+      soi[s] = (s == 0 && n > 1) ? __shfl_sync(0xffffffffu, saved, 0) : (int)occ[l];
+      sof[s] = ev_new[s];
+    }
+    FF d{0.f, 0.f};
+    for (int g = 0; g < T.n_orbits; ++g) {
+      const int size = T.orb_size[g];
+      int cnt_tot = 0;
+      unsigned long long p_tot = 0ull, m_tot = 0ull;
+      for (int s = 0; s < n; ++s) {
+        const int b = sb[s], i = si[s], j = sj[s], k = sk[s], o_i = soi[s], o_f = sof[s];
+        const int c0 = T.fl_begin[b][g], c1 = T.fl_begin[b][g + 1];
+        int cnt = 0;
+        unsigned long long pp = 0ull, mm = 0ull;
+        for (int c = c0 + lane; c < c1; c += 32) {
+          int code = 0, mul = NOCC - 1, prod = 1;
+          bool ok = true;
+          for (int q = 0; q < size - 1; ++q) {
+            const int pb = T.cl_pb[c * 3 + q];
+            const int *du = T.cl_du + c * 9 + q * 3;
+            const int site = pb * n_uc + wrapc(i + du[0], L0) +
+                             L0 * (wrapc(j + du[1], L1) + L1 * wrapc(k + du[2], L2));
+            const int v = occ[site];
+            prod &= v;
+            ok = ok && (v != 0);
+            code += (v - 1) * mul;
+            mul *= (NOCC - 1);
           }
           if constexpr (NOCC == 2) {
-            for (int off = 16; off; off >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
-            acc.c[g] += (o_f - o_i) * cnt;
+            cnt += prod;
           } else {
-            for (int off = 16; off; off >>= 1) {
-              pp += __shfl_xor_sync(0xffffffffu, pp, off);
-              mm += __shfl_xor_sync(0xffffffffu, mm, off);
+            if (ok) {
+              const int base = T.cl_lut[c] + code;
+              if (o_f) pp += 1ull << (8 * T.lut[base + o_f - 1]);
+              if (o_i) mm += 1ull << (8 * T.lut[base + o_i - 1]);
             }
-            acc.p[g] += pp;
-            acc.m[g] += mm;
           }
         }
+        if constexpr (NOCC == 2) {
+          for (int off = 16; off; off >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
+          cnt_tot += (o_f - o_i) * cnt;
+        } else {
+          for (int off = 16; off; off >>= 1) {
+            pp += __shfl_xor_sync(0xffffffffu, pp, off);
+            mm += __shfl_xor_sync(0xffffffffu, mm, off);
+          }
+          p_tot += pp;
+          m_tot += mm;
+        }
       }
-      __syncwarp();
-      if (s + 1 < n) {  // sequential semantics: apply this change first
-        if (lane == 0) occ[l] = (int8_t)o_f;
-        __syncwarp();
+      OrbAcc<NOCC> a;
+      if constexpr (NOCC == 2) {
+        a.c = cnt_tot;
+      } else {
+        a.p = p_tot;
+        a.m = m_tot;
       }
+      orbit_fold<NOCC>(T, g, a, T.w_hi, T.w_lo, d);
     }
+    __syncwarp();
     // ---- dE, acceptance and application (lane 0)
     if (lane == 0) {
       if (n > 1) occ[ev_site[0]] = (int8_t)saved;
-      FF d = acc_dot<NOCC>(T, acc, T.w_hi, T.w_lo);
       double de = (double)d.s + (double)d.e;
       if (P.ensemble == 0) de -= P.dmu[occ[ev_site[0]] * NOCC + ev_new[0]];
       bool accept = true;
@@ -542,9 +631,9 @@ __host__ __device__ inline int clist_capacity(int L0, int L1, int L2) {
 __host__ __device__ inline void sweep_layout(const CeTables &T, int L0, int L1, int L2,
                                              int n_classes_max, int pitch, SweepSmem &s) {
   const int R = T.reach;
-  const int W = pitch ? pitch : L0 + 2 * R, H = pitch ? pitch : L1 + 2 * R;
+  const int W = pitch > 0 ? pitch : L0 + 2 * R, H = pitch > 0 ? pitch : L1 + 2 * R;
   const int V = W * H * (L2 + 2 * R);
-  const bool tables = (pitch == 0);
+  const bool tables = (pitch <= 0);
   int o = 0;
   s.occ = o;
   o += align16(T.n_sublat * V);
@@ -809,7 +898,9 @@ __device__ __forceinline__ uint32_t sched_param(const U4 &r, int ensemble, int s
 }
 
 // Site evaluation policy: PITCH > 0 uses the generated binary FCC evaluator
-// (compile-time neighbour offsets); PITCH == 0 walks the run-time tables.
+// (compile-time neighbour offsets); PITCH == 0 walks the run-time tables with
+// register accumulators for up to MAX_ORBITS orbits; PITCH == -1 walks them
+// one orbit at a time (any number of orbits).
 template <int NOCC, int PITCH>
 struct SiteEval {
   const CeTables *T;
@@ -828,6 +919,20 @@ struct SiteEval {
       auto rd = [&](int cl, int j) -> int { return occ[ad + cl_off[cl * 3 + j]]; };
       accumulate_site<NOCC>(*T, b, o_i, o_f, lutoff, lut, rd, acc);
     }
+  }
+  __device__ __forceinline__ void orbit(int b, int g, int o_i, int o_f, const int8_t *occ, int ad,
+                                        OrbAcc<NOCC> &a) const {
+    auto rd = [&](int cl, int j) -> int { return occ[ad + cl_off[cl * 3 + j]]; };
+    orbit_site<NOCC>(*T, b, g, o_i, o_f, lutoff, lut, rd, a);
+  }
+};
+
+// running energy as an FP64 sum of accepted energy changes (any system)
+struct EnergyAccF64 {
+  double de = 0.0;
+  template <class A>
+  __device__ __forceinline__ void add(const A &, const FF &d, double extra) {
+    de += (double)d.s + (double)d.e + extra;
   }
 };
 
@@ -1106,8 +1211,11 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
   G.L1 = R.L[1];
   G.L2 = R.L[2];
   G.R = T.reach;
-  G.W = PITCH ? PITCH : G.L0 + 2 * G.R;
-  G.H = PITCH ? PITCH : G.L1 + 2 * G.R;
+  G.W = PITCH > 0 ? PITCH : G.L0 + 2 * G.R;
+  G.H = PITCH > 0 ? PITCH : G.L1 + 2 * G.R;
+  // binary systems with generated or register-accumulated tables keep exact
+  // integer delta correlations per orbit for the running energy
+  constexpr bool EXACT = (NOCC == 2 && PITCH >= 0);
   G.V = G.W * G.H * (G.L2 + 2 * G.R);
   const int n_uc = G.L0 * G.L1 * G.L2;
   const int nsl = T.n_sublat;
@@ -1146,7 +1254,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
     ax_coord[a] = ax_cnt[a] + MAX_COLOURS;
   }
   // ---- stage tables
-  if constexpr (PITCH == 0) {
+  if constexpr (PITCH <= 0) {
     for (int c = tid; c < T.n_fl; c += nth) {
       int cb = 0;
       for (int b = 0; b < nsl; ++b)
@@ -1223,7 +1331,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
 
   const SiteEval<NOCC, PITCH> ev{&T, cl_off, lutoff, lut};
   const int lane = tid & 31, warp = tid >> 5;
-  if constexpr (NOCC == 2) {
+  if constexpr (EXACT) {
     if (P.init)
       init_binary_stats<PITCH, NW>(T, occ, G, site_of, ev, n_sites, n_uc,
                                    reinterpret_cast<int *>(smem + lay.initq), red, S);
@@ -1328,7 +1436,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
     }
     __syncthreads();
 
-    EnergyAcc<NOCC> eacc;
+    std::conditional_t<EXACT, EnergyAcc<NOCC>, EnergyAccF64> eacc;
     RegCounts<NOCC> dspec;
     RegCounts<4> dsub;  // binary FCC only (PITCH > 0)
     int n_prop = 0, n_acc = 0;
@@ -1360,11 +1468,23 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
             o_f = alt < o_i ? alt : alt + 1;
           }
           Acc<NOCC> acc;
-          acc.zero();
-          ev.add(cb, o_i, o_f, occ, ad, acc);
           FF d;
-          const float de = sweep_de<NOCC>(T, acc, whi, wlo, dmu_hi[o_i * NOCC + o_f],
-                                          dmu_lo[o_i * NOCC + o_f], d);
+          float de;
+          if constexpr (PITCH >= 0) {
+            acc.zero();
+            ev.add(cb, o_i, o_f, occ, ad, acc);
+            de = sweep_de<NOCC>(T, acc, whi, wlo, dmu_hi[o_i * NOCC + o_f],
+                                dmu_lo[o_i * NOCC + o_f], d);
+          } else {
+            d = FF{0.f, 0.f};
+            for (int g = 0; g < T.n_orbits; ++g) {
+              OrbAcc<NOCC> a;
+              ev.orbit(cb, g, o_i, o_f, occ, ad, a);
+              orbit_fold<NOCC>(T, g, a, whi, wlo, d);
+            }
+            ff_add_ff(d, -dmu_hi[o_i * NOCC + o_f], -dmu_lo[o_i * NOCC + o_f]);
+            de = FADD(d.s, d.e);
+          }
           ++n_prop;
           if (accept_de(de, beta_f, u24(r.x))) {
             ++n_acc;
@@ -1417,12 +1537,28 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
           const int la = cb * n_uc + xa + G.L0 * (ya + G.L1 * za);
           const U4 r = philox4x32_10(U4{(uint32_t)la, ctr_sub, plo, phi | (TAG_SITE << 16)}, k0, k1);
           Acc<NOCC> acc;
-          acc.zero();
-          ev.add(cb, oa, ob, occ, ada, acc);
-          if (local) put_site(occ, G, cb, xa, ya, za, (int8_t)ob);  // first change applied
-          ev.add(bb, ob, oa, occ, adb, acc);
           FF d;
-          const float de = sweep_de<NOCC>(T, acc, whi, wlo, 0.f, 0.f, d);
+          float de;
+          if constexpr (PITCH >= 0) {
+            acc.zero();
+            ev.add(cb, oa, ob, occ, ada, acc);
+            if (local) put_site(occ, G, cb, xa, ya, za, (int8_t)ob);  // first change applied
+            ev.add(bb, ob, oa, occ, adb, acc);
+            de = sweep_de<NOCC>(T, acc, whi, wlo, 0.f, 0.f, d);
+          } else {
+            // the first change is applied before any cluster is read: a
+            // site's own flower never contains it, so a sees the original
+            // state and b sees a changed
+            if (local) put_site(occ, G, cb, xa, ya, za, (int8_t)ob);
+            d = FF{0.f, 0.f};
+            for (int g = 0; g < T.n_orbits; ++g) {
+              OrbAcc<NOCC> a;
+              ev.orbit(cb, g, oa, ob, occ, ada, a);
+              ev.orbit(bb, g, ob, oa, occ, adb, a);
+              orbit_fold<NOCC>(T, g, a, whi, wlo, d);
+            }
+            de = FADD(d.s, d.e);
+          }
           ++n_prop;
           if (accept_de(de, beta_f, u24(r.x))) {
             ++n_acc;
@@ -1468,7 +1604,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
         for (int k = 0; k < 4; ++k) vals[4 + k] = dsub.v[k];
       }
       double dsum = 0.0;
-      if constexpr (NOCC == 2) {
+      if constexpr (EXACT) {
 #pragma unroll
         for (int g = 0; g < MAX_ORBITS; ++g) vals[8 + g] = eacc.dc[g];
       } else {
@@ -1477,7 +1613,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
 #pragma unroll
       for (int k = 0; k < 16; ++k)
         for (int off = 16; off; off >>= 1) vals[k] += __shfl_xor_sync(0xffffffffu, vals[k], off);
-      if constexpr (NOCC != 2)
+      if constexpr (!EXACT)
         for (int off = 16; off; off >>= 1) dsum += __shfl_xor_sync(0xffffffffu, dsum, off);
       int *rd_i = reinterpret_cast<int *>(red);                   // [NW][16]
       double *rd_d = reinterpret_cast<double *>(red + NW * 64);  // [NW]
@@ -1501,7 +1637,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
         for (int k = 0; k < 16; ++k) tot[k] = __shfl_sync(0xffffffffu, v, k);
         double dtot = __shfl_sync(0xffffffffu, dv, 16);
         if (lane == 0) {
-          if constexpr (NOCC == 2) {
+          if constexpr (EXACT) {
             dtot = 0.0;
             for (int g = 0; g < T.n_orbits; ++g)
               dtot += T.w[T.orb_func_base[g]] * (double)tot[8 + g];

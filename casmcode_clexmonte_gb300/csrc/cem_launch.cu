@@ -42,6 +42,13 @@ CEM_EXTERN_256(2, 52)
 CEM_EXTERN_256(2, 64)
 CEM_EXTERN_256(2, 0)
 CEM_EXTERN_256(3, 0)
+// one orbit at a time (cem_kbig.cu)
+extern template cudaError_t launch_sweep_t<2, -1, SWEEP_THREADS>(const CeTables &,
+                                                                 const SweepParams &, int, int,
+                                                                 cudaStream_t);
+extern template cudaError_t launch_sweep_t<3, -1, SWEEP_THREADS>(const CeTables &,
+                                                                 const SweepParams &, int, int,
+                                                                 cudaStream_t);
 
 cudaError_t launch_energy(const CeTables &T, const int8_t *occ, int L0, int L1, int L2,
                           unsigned long long *counts, cudaStream_t st) {
@@ -90,6 +97,12 @@ static cudaError_t launch_sweep_th(const CeTables &T, const SweepParams &P, int 
 
 cudaError_t launch_sweep(const CeTables &T, const SweepParams &P, int n_replicas, int smem,
                          int pitch, int threads, cudaStream_t st) {
+  if (pitch == -1) {  // one orbit at a time, 512 threads
+    if (threads != SWEEP_THREADS) return cudaErrorInvalidValue;
+    if (T.n_occ == 2) return launch_sweep_t<2, -1, SWEEP_THREADS>(T, P, n_replicas, smem, st);
+    if (T.n_occ == 3) return launch_sweep_t<3, -1, SWEEP_THREADS>(T, P, n_replicas, smem, st);
+    return cudaErrorInvalidValue;
+  }
   if (threads == SWEEP_THREADS) return launch_sweep_th<SWEEP_THREADS>(T, P, n_replicas, smem, pitch, st);
   if (threads == 256) return launch_sweep_th<256>(T, P, n_replicas, smem, pitch, st);
   return cudaErrorInvalidValue;

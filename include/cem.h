@@ -48,10 +48,15 @@ typedef struct cem_replicas cem_replicas;
  * the number of clusters whose decoration is in class f and
  * weights[f] = eci_f * coeff_f / mult_f. */
 typedef struct cem_system_desc {
-  int n_sublat;               /* basis sites per unit cell, 1..4 */
+  int n_sublat;               /* sublattices with an occupation degree of
+                                 freedom per unit cell, 1..4 (single-occupant
+                                 sublattices are left out) */
   int n_occ;                  /* occupants per site, 2 or 3 */
-  int n_funcs;                /* functions including the empty function */
-  int n_orbits;               /* non-empty orbits, 1..8, in function order */
+  int n_funcs;                /* functions including the empty function, <= 128 */
+  int n_orbits;               /* non-empty orbits, 1..128, in function order
+                                 (more than 8: the sweep walks the tables one
+                                 orbit at a time; the n-fold way, composition
+                                 enforcement and the HBM-streamed mode need <= 8) */
   const int *orbit_size;      /* [n_orbits] sites per cluster, 1..4 */
   const int *orbit_func_begin;/* [n_orbits] first function index */
   const int *orbit_n_funcs;   /* [n_orbits] number of functions */
@@ -256,6 +261,10 @@ int cem_step_async(cem_replicas *r, const int8_t *host_in, int8_t *host_out, int
  *                  neighbour per pass (these move atoms between classes);
  *   "generic_evaluator" (1): use the run-time cluster tables even where the
  *                  generated binary FCC evaluator applies;
+ *   "orbit_walk" (1): walk the run-time tables one orbit at a time, the
+ *                  kernel that cluster expansions with more than 8 orbits
+ *                  (real CASM basis sets) always use; running energy as an
+ *                  FP64 sum of accepted changes; 512 threads per replica;
  *   "streamed" (1): keep the occupations in HBM and run one kernel per colour
  *                  sub-step over many CTAs per replica (a captured CUDA graph
  *                  per pass); chosen automatically when a supercell does not
@@ -263,7 +272,8 @@ int cem_step_async(cem_replicas *r, const int8_t *host_in, int8_t *host_out, int
  *   "threads" (512 or 256): threads per replica of the shared-memory sweep
  *                  (256: two replicas per SM);
  *   "cta_order" (0 or 1): replica -> CTA schedule (1: largest first).
- * cem_get_option also reads "pitch", "smem_bytes", "colour_classes" and
+ * cem_get_option also reads "pitch" (> 0 generated evaluator, 0 run-time
+ * tables, -1 one orbit at a time), "smem_bytes", "colour_classes" and
  * "streamed". */
 int cem_set_option(cem_replicas *r, const char *key, int64_t value);
 int cem_get_option(cem_replicas *r, const char *key, int64_t *value);
