@@ -637,6 +637,89 @@ def run_nfold_comparison(args):
     return 0
 
 
+def run_zro(args):
+    """A real CASM basis set on the GPU: the reference's Clex_ZrO_Occ system
+    (hcp Zr, O/Va on the octahedral sites; 73 orbits, 1591 clusters per O
+    site), semi-grand canonical, 152 replicas of 12 x 12 x 8 prim cells
+    (2304 O/Va sites each) over a temperature x chemical-potential grid.
+    Proposals/s of the orbit-at-a-time sweep kernel, and the oracle (CPU
+    restatement of the reference loop) on the same system beside it."""
+    import torch
+
+    from casmcode_clexmonte_gb300 import build as B
+
+    B.build()
+    from casmcode_clexmonte_gb300 import calculator as cm
+    from tests.zro_fixture import zro_ce
+
+    ce = zro_ce()
+    n, L = 152, (12, 12, 8)
+    temps = np.linspace(1000.0, 2500.0, n)
+    mus = np.linspace(-1.0, 0.0, n)[np.random.default_rng(3).permutation(n)]
+    rng = np.random.default_rng(17)
+    n_sites = 2 * int(np.prod(L))
+    occ = [(rng.random(n_sites) < 0.5).astype(np.int8) for _ in range(n)]
+    sysd = cm.System(ce)
+
+    def measure(walk, passes):
+        b = cm.ReplicaBatch(sysd, "semigrand_canonical", [L] * n)
+        if walk:
+            b.set_option("orbit_walk", walk)
+        for i in range(n):
+            b.set_conditions(i, float(temps[i]), np.array([mus[i]]))
+            b.set_seed(i, 5150 + i)
+        b.set_occupation_all(np.concatenate(occ))
+        b.run(args.warmup, 0)
+        b.synchronize()
+        st0 = [b.stats(i) for i in range(n)]
+        torch.cuda.synchronize()
+        b.run(passes, 0)
+        b.synchronize()
+        ms = b.kernel_ms()
+        st = [b.stats(i) for i in range(n)]
+        props = sum(s["n_proposed"] - s0["n_proposed"] for s, s0 in zip(st, st0))
+        accs = sum(s["n_accepted"] - s0["n_accepted"] for s, s0 in zip(st, st0))
+        drift = max(abs(b.stats(i)["energy"] - b.energy(i)[0]) / max(1.0, abs(b.energy(i)[0]))
+                    for i in range(0, n, 19))
+        return b, props, accs, ms, drift
+
+    b, props, accs, ms, drift = measure(0, args.zro_passes)
+    value = props / (ms / 1e3)
+    _, props1, _, ms1, _ = measure(1, max(2, args.zro_passes // 8))
+    line = {
+        "metric": "proposals/s", "value": value, "unit": "proposals/s", "n_gpus": 1,
+        "steps": args.zro_passes, "warmup": args.warmup, "ms_per_step": ms / args.zro_passes,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "reference basis set and ECI (Clex_ZrO_Occ); seeded random initial states",
+        "config": {"workload": "zro_hcp_12x12x8_sgc_x152", "replicas": n, "sites_per_replica": n_sites,
+                   "orbits": len(ce.orbits), "clusters_per_site": len(ce.flowers[0]),
+                   "pitch": b.get_option("pitch"), "colour_classes": b.get_option("colour_classes"),
+                   "smem_bytes": b.get_option("smem_bytes"),
+                   "temperatures_K": [1000.0, 2500.0], "param_chem_pot": [-1.0, 0.0]},
+        "acceptance": accs / max(1, props),
+        "running_energy_rel_drift_vs_recompute": drift,
+        "thread_per_site_orbit_walk_proposals_per_s": props1 / (ms1 / 1e3),
+        "gpu_launches": 1,
+    }
+    if not args.no_cpu_baseline:
+        from oracle import oracle
+
+        oracle.build_oracle()
+        o = oracle.OracleSystem(ce, L)
+        nt = min(os.cpu_count() or 1, n)
+        occ_s = np.concatenate(occ[:nt]).astype(np.int8)
+        secs, steps = o.run_threads(occ_s.copy(), 0, temps[:nt].copy(), mus[:nt, None].copy(), 7, 1, nt)
+        passes = max(1, int(12.0 * (steps / max(secs, 1e-9)) / (nt * n_sites)))
+        secs, steps = o.run_threads(occ_s.copy(), 0, temps[:nt].copy(), mus[:nt, None].copy(), 9,
+                                    passes, nt)
+        line["cpu_baseline"] = {
+            "value": steps / secs, "unit": "proposals/s", "cores": nt, "kind": "port",
+            "sample": f"{nt} replicas x {passes} passes of the same system, one sequential "
+                      f"std::mt19937_64 chain per host thread ({secs:.1f} s)"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -650,6 +733,9 @@ def main():
                     help="n-fold way vs Metropolis sweep (semi-grand canonical, low T)")
     ap.add_argument("--nfold-temperature", type=float, default=150.0)
     ap.add_argument("--nfold-events", type=int, default=20000)
+    ap.add_argument("--zro", action="store_true",
+                    help="the reference's Clex_ZrO_Occ basis set (73 orbits), semi-grand canonical")
+    ap.add_argument("--zro-passes", type=int, default=40)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -657,6 +743,8 @@ def main():
         return run_reference(args)
     if args.nfold:
         return run_nfold_comparison(args)
+    if args.zro:
+        return run_zro(args)
     if args.workload == 3:
         return run_learned_comparison(args)
     if args.workload != WORKLOAD_INDEX:

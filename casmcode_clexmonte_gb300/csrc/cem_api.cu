@@ -92,6 +92,8 @@ struct cem_system {
   int nb_reach = 0;
   bool fcc_generated = false;  // flower matches the generated binary FCC evaluator
   bool big = false;            // more orbits than the register accumulators hold
+  bool coop = false;           // big binary system for the warp-cooperative sweep
+  bool split_ok = false;       // binary, split weights exist, orbits sorted by size
   std::vector<void *> owned;
   ~cem_system() {
     for (void *p : owned) cudaFree(p);
@@ -228,6 +230,15 @@ int choose_colouring(const cem_system &s, const int L[3], int ensemble) {
     if (ok) return p;
   }
   throw Err(CEM_ERR_UNSUPPORTED, "no valid site colouring for this supercell");
+}
+
+// dynamic shared memory of the sweep kernel for a batch at a given pitch
+// (the layout of the run-time tables depends on the evaluator)
+int batch_smem(const cem_replicas *r, int pitch) {
+  int smem = 0;
+  for (const Replica &R : r->reps)
+    smem = std::max(smem, sweep_smem_bytes(r->sys->T, R.L[0], R.L[1], R.L[2], r->max_classes, pitch));
+  return smem;
 }
 
 void check_rep(const cem_replicas *r, int i) {
@@ -397,35 +408,50 @@ int cem_system_create(const cem_system_desc *d, cem_system **out) {
     }
     T.wq_scale = 1.f;
     s->big = T.n_orbits > MAX_ORBITS;
-    if (d->n_occ == 2 && !s->big) {
+    std::vector<int> wq_all(T.n_orbits, 0);
+    std::vector<float> wr_all(T.n_orbits, 0.f);
+    if (d->n_occ == 2) {
       double wmax = 0.0;
-      long long dcmax[MAX_ORBITS] = {0};
+      std::vector<long long> dcmax(T.n_orbits, 0);
       for (int g = 0; g < T.n_orbits; ++g) {
         wmax = std::max(wmax, std::fabs(s->w[T.orb_func_base[g]]));
         for (int b = 0; b < T.n_sublat; ++b)
           dcmax[g] = std::max<long long>(dcmax[g], 2 * (T.fl_begin[b][g + 1] - T.fl_begin[b][g]));
       }
+      bool ok = wmax == 0.0;
       if (wmax > 0.0) {
         for (int bits = 13; bits >= 0; --bits) {
           const double q = std::ldexp(1.0, std::ilogb(wmax) - bits);
           long long bound = 0;
-          long long A[MAX_ORBITS] = {0};
+          std::vector<long long> A(T.n_orbits, 0);
           for (int g = 0; g < T.n_orbits; ++g) {
             A[g] = std::llround(s->w[T.orb_func_base[g]] / q);
             bound += std::llabs(A[g]) * dcmax[g];
           }
-          if (bound < (1ll << 24) || bits == 0) {
-            require(bound < (1ll << 24), "cluster expansion too large for the binary sweep weights",
-                    CEM_ERR_UNSUPPORTED);
+          if (bound < (1ll << 24)) {
+            ok = true;
             T.wq_scale = (float)q;
             for (int g = 0; g < T.n_orbits; ++g) {
-              T.wq[g] = (int)A[g];
-              T.wr[g] = (float)(s->w[T.orb_func_base[g]] - (double)A[g] * q);
+              wq_all[g] = (int)A[g];
+              wr_all[g] = (float)(s->w[T.orb_func_base[g]] - (double)A[g] * q);
             }
             break;
           }
         }
       }
+      // small systems: the register sweep needs the split; large ones fall
+      // back to the orbit walk without it
+      require(ok || s->big, "cluster expansion too large for the binary sweep weights",
+              CEM_ERR_UNSUPPORTED);
+      bool sorted = true;
+      for (int g = 1; g < T.n_orbits; ++g) sorted = sorted && T.orb_size[g] >= T.orb_size[g - 1];
+      s->split_ok = ok && sorted;
+      s->coop = s->big && s->split_ok;
+      if (!s->big)
+        for (int g = 0; g < T.n_orbits; ++g) {
+          T.wq[g] = wq_all[g];
+          T.wr[g] = wr_all[g];
+        }
     }
     int *dpb = dev_copy(pb), *ddu = dev_copy(du), *dlo = dev_copy(lutoff);
     uint8_t *dlut = dev_copy(lut);
@@ -459,7 +485,11 @@ int cem_system_create(const cem_system_desc *d, cem_system **out) {
     }
     int *dfp = dev_copy(fp);
     T.fp = dfp;
-    s->owned = {dpb, ddu, dlo, dlut, dwhi, dwlo, dw, dfp};
+    int *dwq = dev_copy(wq_all);
+    float *dwr = dev_copy(wr_all);
+    T.wq_all = dwq;
+    T.wr_all = dwr;
+    s->owned = {dpb, ddu, dlo, dlut, dwhi, dwlo, dw, dfp, dwq, dwr};
     T.cl_pb = dpb;
     T.cl_du = ddu;
     T.cl_lut = dlo;
@@ -552,10 +582,10 @@ int cem_replicas_create(const cem_system *sys, int n, const int *L, int ensemble
       if (pitch) smem = std::max(smem, sweep_smem_bytes(sys->T, Li[0], Li[1], Li[2], max_cls, pitch));
     }
     if (pitch && smem > maxsm) pitch = 0;  // generated layout does not fit: run-time tables
-    if (sys->big) pitch = -1;               // run-time tables, one orbit at a time
+    if (sys->big) pitch = sys->coop ? -2 : -1;  // one warp per site / one orbit at a time
     r->pitch = pitch;
     r->generic_smem = gsmem;
-    r->sweep_smem = pitch > 0 ? smem : gsmem;
+    r->sweep_smem = pitch > 0 ? smem : batch_smem(r.get(), pitch);
     if (r->sweep_smem > maxsm && stream_pitch_for(*sys, r->reps)) {
       r->streamed = true;
       r->stream_pitch = stream_pitch_for(*sys, r->reps);
@@ -1339,16 +1369,19 @@ int cem_set_option(cem_replicas *r, const char *key, int64_t value) {
     } else if (k == "cta_order") {
       set_cta_order(r, (int)value);
     } else if (k == "orbit_walk") {
-      // run-time tables walked one orbit at a time (the kernel that large
-      // cluster expansions need), also for small ones
-      require(value == 1, "orbit_walk can only be switched on");
-      r->pitch = -1;
-      r->sweep_smem = r->generic_smem;
+      // the kernels of large cluster expansions, also for small ones:
+      // 1 = one thread per site walking the tables one orbit at a time,
+      // 2 = one warp per site change (binary, orbits sorted by size)
+      require(value == 1 || value == 2, "orbit_walk must be 1 or 2");
+      require(value == 1 || r->sys->split_ok,
+              "orbit_walk 2 needs a binary system with split weights", CEM_ERR_UNSUPPORTED);
+      r->pitch = value == 1 ? -1 : -2;
+      r->sweep_smem = batch_smem(r, r->pitch);
       r->threads = SWEEP_THREADS;
     } else if (k == "generic_evaluator") {
       if (value) {
-        r->pitch = r->sys->big ? -1 : 0;
-        r->sweep_smem = r->generic_smem;
+        r->pitch = r->sys->big ? (r->sys->coop ? -2 : -1) : 0;
+        r->sweep_smem = batch_smem(r, r->pitch);
       } else {
         throw Err(CEM_ERR_INVALID, "generic_evaluator can only be switched on");
       }

@@ -66,6 +66,9 @@ struct CeTables {
   int wq[MAX_ORBITS];
   float wr[MAX_ORBITS];
   float wq_scale;
+  // the same split for every orbit (binary systems of any size), device arrays
+  const int *wq_all;    // [n_orbits]
+  const float *wr_all;  // [n_orbits]
   // distinct partner sites of each sublattice's flower clusters (the sites
   // whose energy changes see a change of the centre): (sublattice, du[3])
   int n_fp[MAX_SUBLAT];

@@ -641,8 +641,8 @@ __host__ __device__ inline void sweep_layout(const CeTables &T, int L0, int L1, 
   o += tables ? align16(T.n_fl * 3 * 4) : 0;
   s.lutoff = o;
   o += tables ? align16(T.n_fl * 4) : 0;
-  s.lut = o;
-  o += tables ? align16(T.n_fl * (T.n_sf * T.n_sf * T.n_sf * T.n_sf)) : 0;
+  s.lut = o;  // pitch -2: per-cluster f32 remainder weights instead
+  o += tables ? align16(pitch == -2 ? T.n_fl * 4 : T.n_fl * (T.n_sf * T.n_sf * T.n_sf * T.n_sf)) : 0;
   s.whi = o;
   o += align16(T.n_funcs * 4);
   s.wlo = o;
@@ -802,6 +802,48 @@ __device__ __forceinline__ float sweep_de(const CeTables &T, const Acc<NOCC> &ac
     d = acc_dot<NOCC>(T, acc, whi, wlo);
     ff_add_ff(d, -mu_hi, -mu_lo);
     return FADD(d.s, d.e);
+  }
+}
+
+// Warp-cooperative energy change of one binary site change (PITCH -2):
+// the lanes split the centre's flower clusters (points, pairs, triplets,
+// quadruplets: seg[0..4] bounds in the size-sorted flower); every cluster
+// carries its orbit's weight split w = A q + r (A integer, |r| <= q/2), so a
+// lane sums A * product exactly in int32 and r * product in an f32 FMA chain.
+// Returns the lane's partial sums (the caller reduces over the warp).
+__device__ __forceinline__ void coop_site(const int8_t *__restrict__ occ, int ad,
+                                          const int *__restrict__ cl_off,
+                                          const int *__restrict__ cw_a,
+                                          const float *__restrict__ cw_r, const int *seg,
+                                          int lane, int &n, float &r) {
+  for (int c = seg[0] + lane; c < seg[1]; c += 32) {
+    n += cw_a[c];
+    r = FADD(r, cw_r[c]);
+  }
+  for (int c = seg[1] + lane; c < seg[2]; c += 32) {
+    const int v = occ[ad + cl_off[c * 3]];
+    n += v * cw_a[c];
+    r = FFMA(cw_r[c], (float)v, r);
+  }
+  for (int c = seg[2] + lane; c < seg[3]; c += 32) {
+    const int v = occ[ad + cl_off[c * 3]] & occ[ad + cl_off[c * 3 + 1]];
+    n += v * cw_a[c];
+    r = FFMA(cw_r[c], (float)v, r);
+  }
+  for (int c = seg[3] + lane; c < seg[4]; c += 32) {
+    const int v = occ[ad + cl_off[c * 3]] & occ[ad + cl_off[c * 3 + 1]] & occ[ad + cl_off[c * 3 + 2]];
+    n += v * cw_a[c];
+    r = FFMA(cw_r[c], (float)v, r);
+  }
+}
+
+// Sum over the warp (butterfly: every lane ends with the same bits, float
+// addition being commutative).
+__device__ __forceinline__ void warp_sum_nr(int &n, float &r) {
+#pragma unroll
+  for (int off = 16; off; off >>= 1) {
+    n += __shfl_xor_sync(0xffffffffu, n, off);
+    r = FADD(r, __shfl_xor_sync(0xffffffffu, r, off));
   }
 }
 
@@ -1216,6 +1258,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
   // binary systems with generated or register-accumulated tables keep exact
   // integer delta correlations per orbit for the running energy
   constexpr bool EXACT = (NOCC == 2 && PITCH >= 0);
+  static_assert(PITCH != -2 || NOCC == 2, "the warp-cooperative evaluator is binary");
   G.V = G.W * G.H * (G.L2 + 2 * G.R);
   const int n_uc = G.L0 * G.L1 * G.L2;
   const int nsl = T.n_sublat;
@@ -1254,6 +1297,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
     ax_coord[a] = ax_cnt[a] + MAX_COLOURS;
   }
   // ---- stage tables
+  int *seg = reinterpret_cast<int *>(smem + lay.initq);  // PITCH -2: [n_sublat][5]
   if constexpr (PITCH <= 0) {
     for (int c = tid; c < T.n_fl; c += nth) {
       int cb = 0;
@@ -1264,10 +1308,19 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
         const int *du = T.cl_du + c * 9 + q * 3;
         cl_off[c * 3 + q] = (pb < 0) ? 0 : (pb - cb) * G.V + du[0] + G.W * (du[1] + G.H * du[2]);
       }
-      lutoff[c] = T.cl_lut[c];
+      if constexpr (PITCH == -2) {
+        int g = 0;  // the cluster's orbit: fl_begin[cb][g] <= c < fl_begin[cb][g + 1]
+        while (g + 1 < T.n_orbits && c >= T.fl_begin[cb][g + 1]) ++g;
+        lutoff[c] = T.wq_all[g];
+        reinterpret_cast<float *>(lut)[c] = T.wr_all[g];
+      } else {
+        lutoff[c] = T.cl_lut[c];
+      }
     }
-    const int lut_n = T.n_fl * (T.n_sf * T.n_sf * T.n_sf * T.n_sf);
-    for (int i = tid; i < lut_n; i += nth) lut[i] = T.lut[i];
+    if constexpr (PITCH != -2) {
+      const int lut_n = T.n_fl * (T.n_sf * T.n_sf * T.n_sf * T.n_sf);
+      for (int i = tid; i < lut_n; i += nth) lut[i] = T.lut[i];
+    }
   }
   for (int f = tid; f < T.n_funcs; f += nth) {
     whi[f] = T.w_hi[f];
@@ -1328,6 +1381,17 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
   }
   __syncthreads();  // core and periodic halo images (every halo cell is the
                     // image of one core site: L >= 2 reach + 1 on every axis)
+  if constexpr (PITCH == -2) {
+    // flower bounds by cluster size (orbits are sorted by size), written after
+    // the staging copies, which pass through this area; the schedule's
+    // barriers order them before the first sub-step
+    for (int i = tid; i < nsl * 5; i += nth) {
+      const int b = i / 5, sz = i - 5 * b;  // sz = 0..4: first cluster of size > sz
+      int g = 0;
+      while (g < T.n_orbits && T.orb_size[g] <= sz) ++g;
+      seg[i] = T.fl_begin[b][g];
+    }
+  }
 
   const SiteEval<NOCC, PITCH> ev{&T, cl_off, lutoff, lut};
   const int lane = tid & 31, warp = tid >> 5;
@@ -1451,6 +1515,40 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
       const uint32_t ctr_sub = (uint32_t)sub;
       const FastDiv fe0(D.g0, (uint32_t)D.m0), fe1(D.g1, (uint32_t)D.m1);
       if (D.mode == 0) {
+       if constexpr (PITCH == -2) {
+        // ---------------- flips, one warp per site (binary, any size)
+        const int *sg = seg + 5 * cb;
+        const int *cw_a = lutoff;
+        const float *cw_r = reinterpret_cast<const float *>(lut);
+        for (int q = warp; q < D.n; q += NW) {
+          const int t = fe0.div(q), iz = fe1.div(t);
+          const int ix = q - t * d0, iy = t - iz * d1;
+          const int x = cx[ix], y = cy[iy], z = cz[iz];
+          const int ad = G.addr(cb, x, y, z);
+          const int o_i = occ[ad], o_f = 1 - o_i;
+          const int l = cb * n_uc + x + G.L0 * (y + G.L1 * z);
+          const U4 r = philox4x32_10(U4{(uint32_t)l, ctr_sub, plo, phi | (TAG_SITE << 16)}, k0, k1);
+          int nq = 0;
+          float rr = 0.f;
+          coop_site(occ, ad, cl_off, cw_a, cw_r, sg, lane, nq, rr);
+          warp_sum_nr(nq, rr);
+          const int dd = o_f - o_i;
+          nq *= dd;
+          rr = dd > 0 ? rr : -rr;
+          const float de = FADD(FADD(FFMA((float)nq, T.wq_scale, rr), -dmu_hi[o_i * NOCC + o_f]),
+                                -dmu_lo[o_i * NOCC + o_f]);
+          if (lane == 0) {
+            ++n_prop;
+            if (accept_de(de, beta_f, u24(r.x))) {
+              ++n_acc;
+              put_site(occ, G, cb, x, y, z, (int8_t)o_f);
+              eacc.de += (double)nq * (double)T.wq_scale + (double)rr;
+              dspec.add(o_i, -1);
+              dspec.add(o_f, 1);
+            }
+          }
+        }
+       } else {
         // ---------------- flips of every site of the class
         for (int q = tid; q < D.n; q += nth) {
           const int t = fe0.div(q), iz = fe1.div(t);
@@ -1495,6 +1593,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
             if constexpr (PITCH > 0) dsub.add(sc_sublattice(x, y, z), o_f - o_i);
           }
         }
+       }
       } else {
         // ---------------- canonical swaps: pairs inside the class (mode 1)
         // or a site with a neighbour (mode 2, sequential dE).
@@ -1518,7 +1617,60 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
         int total = 0;
 #pragma unroll
         for (int w = 0; w < NW; ++w) total += wk[w];
-        for (int i = tid; i < total; i += nth) {
+        if constexpr (PITCH == -2) {
+          // one warp per pair (binary, any size); the first change is applied
+          // before any cluster is read (a site's own flower never contains
+          // it): a sees the original state, b sees a changed
+          const int *cw_a = lutoff;
+          const float *cw_r = reinterpret_cast<const float *>(lut);
+          for (int i = warp; i < total; i += NW) {
+            int wsel = 0, bsel = 0, run = 0;
+#pragma unroll
+            for (int w = 0; w < NW; ++w) {
+              const int k = wk[w];
+              if (i >= run) {
+                wsel = w;
+                bsel = run;
+              }
+              run += k;
+            }
+            const int q = cl[wsel * chunk + (i - bsel)];
+            int xa, ya, za, xb, yb, zb;
+            pg.sites(q, G, xa, ya, za, xb, yb, zb);
+            const int ada = G.addr(cb, xa, ya, za), adb = G.addr(bb, xb, yb, zb);
+            const int oa = occ[ada], ob = occ[adb];
+            const int la = cb * n_uc + xa + G.L0 * (ya + G.L1 * za);
+            const U4 r =
+                philox4x32_10(U4{(uint32_t)la, ctr_sub, plo, phi | (TAG_SITE << 16)}, k0, k1);
+            __syncwarp();
+            if (local && lane == 0) put_site(occ, G, cb, xa, ya, za, (int8_t)ob);
+            __syncwarp();
+            int na = 0, nb = 0;
+            float ra = 0.f, rb = 0.f;
+            coop_site(occ, ada, cl_off, cw_a, cw_r, seg + 5 * cb, lane, na, ra);
+            coop_site(occ, adb, cl_off, cw_a, cw_r, seg + 5 * bb, lane, nb, rb);
+            int nq = na - nb;
+            float rr = FADD(ra, -rb);
+            warp_sum_nr(nq, rr);
+            const int dd = ob - oa;  // a: oa -> ob, b: ob -> oa
+            nq *= dd;
+            rr = dd > 0 ? rr : -rr;
+            const float de = FFMA((float)nq, T.wq_scale, rr);
+            __syncwarp();
+            if (lane == 0) {
+              ++n_prop;
+              if (accept_de(de, beta_f, u24(r.x))) {
+                ++n_acc;
+                if (!local) put_site(occ, G, cb, xa, ya, za, (int8_t)ob);
+                put_site(occ, G, bb, xb, yb, zb, (int8_t)oa);
+                eacc.de += (double)nq * (double)T.wq_scale + (double)rr;
+              } else if (local) {
+                put_site(occ, G, cb, xa, ya, za, (int8_t)oa);
+              }
+            }
+          }
+        }
+        for (int i = tid; PITCH != -2 && i < total; i += nth) {
           int wsel = 0, bsel = 0, run = 0;
 #pragma unroll
           for (int w = 0; w < NW; ++w) {  // last warp whose kept range starts at or before i

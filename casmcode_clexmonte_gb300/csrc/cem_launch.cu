@@ -49,6 +49,9 @@ extern template cudaError_t launch_sweep_t<2, -1, SWEEP_THREADS>(const CeTables 
 extern template cudaError_t launch_sweep_t<3, -1, SWEEP_THREADS>(const CeTables &,
                                                                  const SweepParams &, int, int,
                                                                  cudaStream_t);
+extern template cudaError_t launch_sweep_t<2, -2, SWEEP_THREADS>(const CeTables &,
+                                                                 const SweepParams &, int, int,
+                                                                 cudaStream_t);
 
 cudaError_t launch_energy(const CeTables &T, const int8_t *occ, int L0, int L1, int L2,
                           unsigned long long *counts, cudaStream_t st) {
@@ -97,6 +100,10 @@ static cudaError_t launch_sweep_th(const CeTables &T, const SweepParams &P, int 
 
 cudaError_t launch_sweep(const CeTables &T, const SweepParams &P, int n_replicas, int smem,
                          int pitch, int threads, cudaStream_t st) {
+  if (pitch == -2) {  // binary, one warp per site change, 512 threads
+    if (threads != SWEEP_THREADS || T.n_occ != 2) return cudaErrorInvalidValue;
+    return launch_sweep_t<2, -2, SWEEP_THREADS>(T, P, n_replicas, smem, st);
+  }
   if (pitch == -1) {  // one orbit at a time, 512 threads
     if (threads != SWEEP_THREADS) return cudaErrorInvalidValue;
     if (T.n_occ == 2) return launch_sweep_t<2, -1, SWEEP_THREADS>(T, P, n_replicas, smem, st);

@@ -44,7 +44,7 @@ def _close(a, b):
 def test_zro_energy_and_delta_match_oracle(ce, cm, oracle_mod):
     sysd = cm.System(ce)
     b = cm.ReplicaBatch(sysd, "semigrand_canonical", [L])
-    assert b.get_option("pitch") == -1  # one orbit at a time
+    assert b.get_option("pitch") == -2  # binary: one warp per site change
     o = oracle_mod.OracleSystem(ce, L)
     rng = np.random.default_rng(3)
     mu = np.array([-0.4])
@@ -134,13 +134,16 @@ def test_orbit_walk_matches_register_sweep_ternary(ens, cm):
         assert abs(sa["energy"] - sb["energy"]) <= 1e-9 * abs(sb["energy"]) + 1e-9
 
 
-def test_orbit_walk_binary_running_energy(cm):
-    """Binary FCC through the orbit-at-a-time kernel: the FP64 running energy
+@pytest.mark.parametrize("walk", [1, 2])
+def test_orbit_walk_binary_running_energy(walk, cm):
+    """Binary FCC through the large-expansion kernels (1: one thread per site,
+    orbit by orbit; 2: one warp per site change): the FP64 running energy
     equals a fresh recompute; canonical composition is kept."""
     ce = workloads.fcc_binary_ce(5)
     sysd = cm.System(ce)
     b = cm.ReplicaBatch(sysd, "canonical", [(12, 12, 12)] * 3)
-    b.set_option("orbit_walk", 1)
+    b.set_option("orbit_walk", walk)
+    assert b.get_option("pitch") == -walk
     rng = np.random.default_rng(2)
     occs = []
     for i in range(3):
@@ -158,11 +161,14 @@ def test_orbit_walk_binary_running_energy(cm):
         assert int(b.get_occupation(i).sum()) == int(occs[i].sum())
 
 
+@pytest.mark.parametrize("walk", [0, 1])
 @pytest.mark.parametrize("ens", ["semigrand_canonical", "canonical"])
-def test_zro_sweep_running_energy_and_invariants(ens, ce, cm):
+def test_zro_sweep_running_energy_and_invariants(ens, walk, ce, cm):
     sysd = cm.System(ce)
     Ls = [(8, 8, 8), (9, 9, 8), (12, 12, 8)]
     b = cm.ReplicaBatch(sysd, ens, Ls)
+    if walk:
+        b.set_option("orbit_walk", walk)
     rng = np.random.default_rng(31)
     occs = []
     for i, x in enumerate(Ls):
@@ -184,8 +190,10 @@ def test_zro_sweep_running_energy_and_invariants(ens, ce, cm):
             assert int(new.sum()) == int(occs[i].sum())
 
 
-def test_zro_equilibrium_matches_oracle(ce, cm, oracle_mod):
-    """<potential energy> and <x> of the parallel sampler against the
+@pytest.mark.parametrize("walk", [0, 1])
+def test_zro_equilibrium_matches_oracle(walk, ce, cm, oracle_mod):
+    """<potential energy> and <x> of the parallel sampler (default: one warp
+    per site change; 1: one thread per site, orbit by orbit) against the
     sequential oracle chain (semi-grand canonical), within 4 combined
     standard errors."""
     T, mu = 2500.0, np.array([-0.6])
@@ -199,6 +207,8 @@ def test_zro_equilibrium_matches_oracle(ce, cm, oracle_mod):
     sysd = cm.System(ce)
     nrep = 16
     b = cm.ReplicaBatch(sysd, "semigrand_canonical", [L] * nrep)
+    if walk:
+        b.set_option("orbit_walk", walk)
     for i in range(nrep):
         b.set_conditions(i, T, mu)
         b.set_seed(i, 300 + i)
