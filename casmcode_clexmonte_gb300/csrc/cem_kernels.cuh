@@ -811,27 +811,34 @@ __device__ __forceinline__ float sweep_de(const CeTables &T, const Acc<NOCC> &ac
 // carries its orbit's weight split w = A q + r (A integer, |r| <= q/2), so a
 // lane sums A * product exactly in int32 and r * product in an f32 FMA chain.
 // Returns the lane's partial sums (the caller reduces over the warp).
+// Partner offsets are stored partner-major (off0[c], off1[c], off2[c] at
+// stride n_fl), so each warp-wide load reads 32 consecutive words: one
+// shared-memory wavefront instead of three for a 12-byte record per cluster.
 __device__ __forceinline__ void coop_site(const int8_t *__restrict__ occ, int ad,
-                                          const int *__restrict__ cl_off,
+                                          const int *__restrict__ cl_off, int n_fl,
                                           const int *__restrict__ cw_a,
                                           const float *__restrict__ cw_r, const int *seg,
                                           int lane, int &n, float &r) {
+  const int *off0 = cl_off, *off1 = cl_off + n_fl, *off2 = cl_off + 2 * n_fl;
   for (int c = seg[0] + lane; c < seg[1]; c += 32) {
     n += cw_a[c];
     r = FADD(r, cw_r[c]);
   }
+#pragma unroll 2
   for (int c = seg[1] + lane; c < seg[2]; c += 32) {
-    const int v = occ[ad + cl_off[c * 3]];
+    const int v = occ[ad + off0[c]];
     n += v * cw_a[c];
     r = FFMA(cw_r[c], (float)v, r);
   }
+#pragma unroll 4
   for (int c = seg[2] + lane; c < seg[3]; c += 32) {
-    const int v = occ[ad + cl_off[c * 3]] & occ[ad + cl_off[c * 3 + 1]];
+    const int v = occ[ad + off0[c]] & occ[ad + off1[c]];
     n += v * cw_a[c];
     r = FFMA(cw_r[c], (float)v, r);
   }
+#pragma unroll 4
   for (int c = seg[3] + lane; c < seg[4]; c += 32) {
-    const int v = occ[ad + cl_off[c * 3]] & occ[ad + cl_off[c * 3 + 1]] & occ[ad + cl_off[c * 3 + 2]];
+    const int v = occ[ad + off0[c]] & occ[ad + off1[c]] & occ[ad + off2[c]];
     n += v * cw_a[c];
     r = FFMA(cw_r[c], (float)v, r);
   }
@@ -1306,7 +1313,8 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
       for (int q = 0; q < 3; ++q) {
         const int pb = T.cl_pb[c * 3 + q];
         const int *du = T.cl_du + c * 9 + q * 3;
-        cl_off[c * 3 + q] = (pb < 0) ? 0 : (pb - cb) * G.V + du[0] + G.W * (du[1] + G.H * du[2]);
+        const int off = (pb < 0) ? 0 : (pb - cb) * G.V + du[0] + G.W * (du[1] + G.H * du[2]);
+        cl_off[PITCH == -2 ? q * T.n_fl + c : c * 3 + q] = off;  // -2: partner-major
       }
       if constexpr (PITCH == -2) {
         int g = 0;  // the cluster's orbit: fl_begin[cb][g] <= c < fl_begin[cb][g + 1]
@@ -1530,7 +1538,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
           const U4 r = philox4x32_10(U4{(uint32_t)l, ctr_sub, plo, phi | (TAG_SITE << 16)}, k0, k1);
           int nq = 0;
           float rr = 0.f;
-          coop_site(occ, ad, cl_off, cw_a, cw_r, sg, lane, nq, rr);
+          coop_site(occ, ad, cl_off, T.n_fl, cw_a, cw_r, sg, lane, nq, rr);
           warp_sum_nr(nq, rr);
           const int dd = o_f - o_i;
           nq *= dd;
@@ -1647,8 +1655,8 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
             __syncwarp();
             int na = 0, nb = 0;
             float ra = 0.f, rb = 0.f;
-            coop_site(occ, ada, cl_off, cw_a, cw_r, seg + 5 * cb, lane, na, ra);
-            coop_site(occ, adb, cl_off, cw_a, cw_r, seg + 5 * bb, lane, nb, rb);
+            coop_site(occ, ada, cl_off, T.n_fl, cw_a, cw_r, seg + 5 * cb, lane, na, ra);
+            coop_site(occ, adb, cl_off, T.n_fl, cw_a, cw_r, seg + 5 * bb, lane, nb, rb);
             int nq = na - nb;
             float rr = FADD(ra, -rb);
             warp_sum_nr(nq, rr);
