@@ -894,8 +894,6 @@ int cem_nfold_run(cem_replicas *r, int64_t n_events, int64_t n_equil, int64_t re
     require(r != nullptr, "null handle");
     require(r->ensemble == CEM_SEMIGRAND_CANONICAL,
             "the n-fold way runs semi-grand canonical replicas");
-    require(!r->sys->big, "the n-fold way supports cluster expansions of at most 8 orbits",
-            CEM_ERR_UNSUPPORTED);
     require(n_events >= 0 && n_equil >= 0 && record_capacity >= 0, "counts must be >= 0");
     require(record_capacity == 0 || (rec_site && rec_occ && rec_dt), "null record buffers");
     const CeTables &T = r->sys->T;
@@ -990,9 +988,6 @@ int cem_enforce_composition(cem_replicas *r, const double *target_mol, uint64_t 
   return guard([&] {
     require(r != nullptr, "null replica batch");
     require(target_mol != nullptr, "null target composition");
-    require(!r->sys->big,
-            "composition enforcement supports cluster expansions of at most 8 orbits",
-            CEM_ERR_UNSUPPORTED);
     const int nocc = r->sys->T.n_occ;
     for (int i = 0; i < r->n * nocc; ++i)
       require(std::isfinite(target_mol[i]), "target composition must be finite");

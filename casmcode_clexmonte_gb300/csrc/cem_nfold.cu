@@ -48,6 +48,24 @@ __device__ __forceinline__ double de_fp64(const CeTables &T, const Acc<NOCC> &ac
   return d;
 }
 
+// The same sum one orbit at a time (any number of orbits): adds orbit g's
+// terms to d in function-index order.
+template <int NOCC>
+__device__ __forceinline__ double orbit_fold_fp64(const CeTables &T, int g, const OrbAcc<NOCC> &a,
+                                                  double d) {
+  const int base = T.orb_func_base[g];
+  if constexpr (NOCC == 2) {
+    return DADD(d, DMUL(T.w[base], (double)a.c));
+  } else {
+    const int nf = T.orb_n_funcs[g];
+    for (int fl = 0; fl < nf; ++fl) {
+      const int dc = (int)((a.p >> (8 * fl)) & 255ull) - (int)((a.m >> (8 * fl)) & 255ull);
+      d = DADD(d, DMUL(T.w[base + fl], (double)dc));
+    }
+    return d;
+  }
+}
+
 struct NfoldLayout {
   int occ, cl_off, lutoff, lut, stats, imp, misc, total;
 };
@@ -133,6 +151,25 @@ __global__ void __launch_bounds__(NF_THREADS)
 
   const SiteEval<NOCC, PITCH> ev{&T, cl_off, lutoff, lut};
   const double beta = R.beta;
+  // FP64 formation-energy change of one site change: the generated evaluator
+  // with register counts, or the run-time tables one orbit at a time (the
+  // same terms in the same order, for expansions of any size)
+  auto site_de = [&](int b, int o_i, int o_f, int ad) -> double {
+    if constexpr (PITCH > 0) {
+      Acc<NOCC> acc;
+      acc.zero();
+      ev.add(b, o_i, o_f, occ, ad, acc);
+      return de_fp64<NOCC>(T, acc);
+    } else {
+      double d = 0.0;
+      for (int g = 0; g < T.n_orbits; ++g) {
+        OrbAcc<NOCC> a;
+        ev.orbit(b, g, o_i, o_f, occ, ad, a);
+        d = orbit_fold_fp64<NOCC>(T, g, a, d);
+      }
+      return d;
+    }
+  };
   // rate of event e = l (n_occ - 1) + k: site l to its k-th other occupant
   auto rate_of = [&](long long e) -> double {
     const int l = (int)(e / (NOCC - 1)), k = (int)(e - (long long)l * (NOCC - 1));
@@ -141,10 +178,7 @@ __global__ void __launch_bounds__(NF_THREADS)
     const int ad = G.addr(b, x, y, z);
     const int o_i = occ[ad];
     const int o_f = k < o_i ? k : k + 1;
-    Acc<NOCC> acc;
-    acc.zero();
-    ev.add(b, o_i, o_f, occ, ad, acc);
-    const double de = DSUB(de_fp64<NOCC>(T, acc), R.dmu[o_i * NOCC + o_f]);
+    const double de = DSUB(site_de(b, o_i, o_f, ad), R.dmu[o_i * NOCC + o_f]);
     return de <= 0.0 ? 1.0 : cem_exp_neg(DMUL(-beta, de));
   };
   // sum tree over the events: level 0 = rates, node = sum of its 32 children
@@ -252,10 +286,7 @@ __global__ void __launch_bounds__(NF_THREADS)
       const int ad = G.addr(b, x, y, z);
       const int o_i = occ[ad];
       const int o_f = kk < o_i ? kk : kk + 1;
-      Acc<NOCC> acc;
-      acc.zero();
-      ev.add(b, o_i, o_f, occ, ad, acc);
-      energy = DADD(energy, de_fp64<NOCC>(T, acc));
+      energy = DADD(energy, site_de(b, o_i, o_f, ad));
       nspec[o_i] -= 1;
       nspec[o_f] += 1;
       put_site(occ, G, b, x, y, z, (int8_t)o_f);

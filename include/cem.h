@@ -54,9 +54,11 @@ typedef struct cem_system_desc {
   int n_occ;                  /* occupants per site, 2 or 3 */
   int n_funcs;                /* functions including the empty function, <= 128 */
   int n_orbits;               /* non-empty orbits, 1..128, in function order
-                                 (more than 8: the sweep walks the tables one
-                                 orbit at a time; the n-fold way, composition
-                                 enforcement and the HBM-streamed mode need <= 8) */
+                                 (more than 8: the sweep, the n-fold way, the
+                                 delta and replay kernels walk the tables one
+                                 orbit at a time; the HBM-streamed mode and the
+                                 learned proposal need the generated binary FCC
+                                 topology) */
   const int *orbit_size;      /* [n_orbits] sites per cluster, 1..4 */
   const int *orbit_func_begin;/* [n_orbits] first function index */
   const int *orbit_n_funcs;   /* [n_orbits] number of functions */

@@ -219,3 +219,56 @@ def test_zro_equilibrium_matches_oracle(walk, ce, cm, oracle_mod):
     e_g, se_g = pots.mean(), pots.std(ddof=1) / np.sqrt(nrep)
     assert abs(e_g - e_o) < 4.0 * np.hypot(se_g, se_o), (e_g, se_g, e_o, se_o)
     assert abs(xs.mean() - x_o) < 4.0 * np.hypot(xs.std(ddof=1) / np.sqrt(nrep), sx_o)
+
+
+def test_zro_nfold_matches_oracle_event_for_event(ce, cm, oracle_mod):
+    """The n-fold way on the ZrO basis set (run-time tables walked one orbit
+    at a time): event sequence, residence weights and final occupation equal
+    the oracle's, which recomputes every rate after every event."""
+    rng = np.random.default_rng(29)
+    Ls = (7, 7, 7)
+    sysd = cm.System(ce)
+    b = cm.ReplicaBatch(sysd, "semigrand_canonical", [Ls])
+    T, mu = 1800.0, np.array([-0.5])
+    b.set_conditions(0, T, mu)
+    seed = 0x5EED0F2
+    b.set_seed(0, seed)
+    occ = (rng.random(2 * 343) < 0.4).astype(np.int8)
+    b.set_occupation(0, occ)
+    n_events, n_equil = 120, 20
+    rec = b.nfold_run(n_events, n_equil, record=n_events + n_equil)
+    o = oracle_mod.OracleSystem(ce, Ls)
+    occ_o = occ.copy()
+    ref = o.nfold(occ_o, T, mu, sysd.arrays["weights"], seed, n_events, n_equil,
+                  record=n_events + n_equil)
+    np.testing.assert_array_equal(rec["site"][0], ref["site"])
+    np.testing.assert_array_equal(rec["occ"][0], ref["occ"])
+    np.testing.assert_array_equal(rec["dt"][0], ref["dt"])
+    np.testing.assert_array_equal(b.get_occupation(0), occ_o)
+    e_now, _ = b.energy(0)
+    assert b.stats(0)["energy"] == pytest.approx(e_now, rel=1e-9, abs=1e-9)
+
+
+def test_zro_enforce_matches_oracle(ce, cm, oracle_mod):
+    """Composition enforcement on the O/Va sublattices: same flips as the
+    oracle's restatement of clexmonte::enforce_composition."""
+    Ls = [(8, 8, 8), (12, 12, 8)]
+    sysd = cm.System(ce)
+    b = cm.ReplicaBatch(sysd, "canonical", Ls)
+    rng = np.random.default_rng(4)
+    occs, targets = [], []
+    for i, L in enumerate(Ls):
+        n = 2 * L[0] * L[1] * L[2]
+        occ = (rng.random(n) < 0.2).astype(np.int8)
+        b.set_occupation(i, occ)
+        occs.append(occ)
+        x = 0.3 + 0.4 * i  # O per O/Va site
+        targets.append(np.array([2 * (1 - x), 2 * x]))  # Va, O per unit cell
+    seed = 0xBEEF
+    flips = b.enforce_composition(np.array(targets), seed)
+    for i, L in enumerate(Ls):
+        o = oracle_mod.OracleSystem(ce, L)
+        ref = occs[i].copy()
+        nf, _ = o.enforce_composition(ref, targets[i], seed + i)
+        assert flips[i] == nf > 0
+        np.testing.assert_array_equal(b.get_occupation(i), ref)
