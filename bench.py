@@ -178,11 +178,17 @@ def cpu_baseline(w, n_threads: int, target_s: float = 12.0) -> dict:
     rate = steps / max(secs, 1e-9)
     passes = max(1, int(target_s * rate / (n * int(w.n_sites[0]))))
     secs, steps = o.run_threads(occ.copy(), 1, temps, mus, 11, passes, n)
+    # one chain on one core (a bounded sample of about 3 s)
+    n1 = int(w.n_sites[0])
+    p1 = max(1, int(3.0 * rate / n / n1))
+    s1, st1 = o.run_threads(occ[:n1].copy(), 1, temps[:1].copy(), mus[:1].copy(), 13, p1, 1)
     return {
         "value": steps / secs, "unit": "proposals/s", "cores": n, "kind": "port",
         "sample": f"{n} replicas x {passes} passes of the 24^3 canonical workload, one "
                   f"sequential std::mt19937_64 chain per host thread ({secs:.1f} s)",
         "seconds": secs,
+        "single_core": {"value": st1 / s1, "unit": "proposals/s",
+                        "sample": f"1 replica x {p1} passes on one thread ({s1:.1f} s)"},
     }
 
 
