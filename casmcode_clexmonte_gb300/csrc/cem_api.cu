@@ -115,7 +115,7 @@ struct cem_replicas {
   long long sample_capacity = 0;
   int sample_width = 1;
   long long n_samples_recorded = 0;
-  int max_classes = 1, sweep_smem = 0, pitch = 0, generic_smem = 0;
+  int max_classes = 1, sweep_smem = 0, pitch = 0;
   int n_pair_sweeps = 2, n_local_sweeps = 1;
   int threads = SWEEP_THREADS;
   // replica -> CTA schedule: 0 = CTA i runs replica i, 1 = largest replicas first
@@ -232,12 +232,19 @@ int choose_colouring(const cem_system &s, const int L[3], int ensemble) {
   throw Err(CEM_ERR_UNSUPPORTED, "no valid site colouring for this supercell");
 }
 
+// sub-steps of one pass (sweeps x colour classes): the size of the sweep
+// kernel's per-pass schedule
+int sub_steps(const cem_replicas *r) {
+  const int sweeps = r->ensemble == CEM_CANONICAL ? r->n_pair_sweeps + r->n_local_sweeps : 1;
+  return sweeps * r->max_classes;
+}
+
 // dynamic shared memory of the sweep kernel for a batch at a given pitch
 // (the layout of the run-time tables depends on the evaluator)
 int batch_smem(const cem_replicas *r, int pitch) {
   int smem = 0;
   for (const Replica &R : r->reps)
-    smem = std::max(smem, sweep_smem_bytes(r->sys->T, R.L[0], R.L[1], R.L[2], r->max_classes, pitch));
+    smem = std::max(smem, sweep_smem_bytes(r->sys->T, R.L[0], R.L[1], R.L[2], sub_steps(r), pitch));
   return smem;
 }
 
@@ -575,17 +582,10 @@ int cem_replicas_create(const cem_system *sys, int n, const int *L, int ensemble
         break;
       }
     }
-    int smem = 0, gsmem = 0;
-    for (int i = 0; i < n; ++i) {
-      const int *Li = r->reps[i].L;
-      gsmem = std::max(gsmem, sweep_smem_bytes(sys->T, Li[0], Li[1], Li[2], max_cls, 0));
-      if (pitch) smem = std::max(smem, sweep_smem_bytes(sys->T, Li[0], Li[1], Li[2], max_cls, pitch));
-    }
-    if (pitch && smem > maxsm) pitch = 0;  // generated layout does not fit: run-time tables
+    if (pitch && batch_smem(r.get(), pitch) > maxsm) pitch = 0;  // generated layout does not fit
     if (sys->big) pitch = sys->coop ? -2 : -1;  // one warp per site / one orbit at a time
     r->pitch = pitch;
-    r->generic_smem = gsmem;
-    r->sweep_smem = pitch > 0 ? smem : batch_smem(r.get(), pitch);
+    r->sweep_smem = batch_smem(r.get(), pitch);
     if (r->sweep_smem > maxsm && stream_pitch_for(*sys, r->reps)) {
       r->streamed = true;
       r->stream_pitch = stream_pitch_for(*sys, r->reps);
@@ -1059,6 +1059,7 @@ int cem_step_async(cem_replicas *r, const int8_t *host_in, int8_t *host_out, int
       P.n_passes = n_passes;
       P.n_equil = 0;
       P.max_classes = r->max_classes;
+    P.max_sub = sub_steps(r);
       P.n_pair_sweeps = r->n_pair_sweeps;
       P.n_local_sweeps = r->n_local_sweeps;
       P.cta_rep = r->d_cta_rep;
@@ -1181,6 +1182,7 @@ int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_sampl
     P.n_passes = n_passes;
     P.n_equil = n_equil;
     P.max_classes = r->max_classes;
+    P.max_sub = sub_steps(r);
     P.n_pair_sweeps = r->n_pair_sweeps;
     P.n_local_sweeps = r->n_local_sweeps;
     P.cta_rep = r->d_cta_rep;
@@ -1371,18 +1373,18 @@ int cem_set_option(cem_replicas *r, const char *key, int64_t value) {
       require(value == 1 || r->sys->split_ok,
               "orbit_walk 2 needs a binary system with split weights", CEM_ERR_UNSUPPORTED);
       r->pitch = value == 1 ? -1 : -2;
-      r->sweep_smem = batch_smem(r, r->pitch);
       r->threads = SWEEP_THREADS;
     } else if (k == "generic_evaluator") {
       if (value) {
         r->pitch = r->sys->big ? (r->sys->coop ? -2 : -1) : 0;
-        r->sweep_smem = batch_smem(r, r->pitch);
       } else {
         throw Err(CEM_ERR_INVALID, "generic_evaluator can only be switched on");
       }
     } else {
       throw Err(CEM_ERR_INVALID, "unknown option '" + k + "'");
     }
+    // the evaluator and the sweep counts set the kernel's shared-memory layout
+    r->sweep_smem = batch_smem(r, r->pitch);
   });
 }
 

@@ -38,6 +38,7 @@ struct SweepParams {
   int sample_width;
   long long n_passes, n_equil;
   int max_classes;
+  int max_sub;  // sub-steps per pass (sweeps x colour classes): sizes the schedule
   int n_pair_sweeps, n_local_sweeps;  // canonical pass composition
   int init;                    // binary systems: compute the exact initial stats in-kernel
   const int *cta_rep;          // replica of each CTA (null: CTA i runs replica i)
@@ -59,7 +60,7 @@ cudaError_t launch_enforce(int n_occ, const Replica *reps, int n_reps, int8_t *o
 cudaError_t launch_init_stats(const CeTables &T, const Replica *reps, ReplicaStats *stats,
                               const int8_t *occ, int n_replicas, int max_sites, cudaStream_t st);
 cudaError_t smem_bandwidth(double *gbs, cudaStream_t st);
-int sweep_smem_bytes(const CeTables &T, int L0, int L1, int L2, int n_classes, int pitch);
+int sweep_smem_bytes(const CeTables &T, int L0, int L1, int L2, int n_sub, int pitch);
 // pitch 0: run-time tables; otherwise the generated binary FCC evaluator with
 // that x/y pitch (one of SWEEP_PITCHES)
 cudaError_t launch_sweep(const CeTables &T, const SweepParams &P, int n_replicas, int smem,

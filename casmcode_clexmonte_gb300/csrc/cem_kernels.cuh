@@ -171,16 +171,6 @@ __device__ __forceinline__ FF acc_dot(const CeTables &T, const Acc<NOCC> &acc,
   return r;
 }
 
-template <int NOCC>
-__device__ void acc_store(const CeTables &T, const Acc<NOCC> &acc, long long *out) {
-  for (int f = 0; f < T.n_funcs; ++f) out[f] = 0;
-  for (int g = 0; g < T.n_orbits; ++g) {
-    const int base = T.orb_func_base[g];
-    const int nf = T.orb_n_funcs[g];
-    for (int fl = 0; fl < nf; ++fl) out[base + fl] = acc_dc<NOCC>(acc, g, fl);
-  }
-}
-
 __device__ __forceinline__ int wrapc(int x, int L) {
   x = (x < 0) ? x + L : x;
   return (x >= L) ? x - L : x;
@@ -629,7 +619,7 @@ __host__ __device__ inline int clist_capacity(int L0, int L1, int L2) {
 
 // pitch > 0: fixed x/y pitch of the generated evaluator; 0: L + 2 reach
 __host__ __device__ inline void sweep_layout(const CeTables &T, int L0, int L1, int L2,
-                                             int n_classes_max, int pitch, SweepSmem &s) {
+                                             int n_sub_max, int pitch, SweepSmem &s) {
   const int R = T.reach;
   const int W = pitch > 0 ? pitch : L0 + 2 * R, H = pitch > 0 ? pitch : L1 + 2 * R;
   const int V = W * H * (L2 + 2 * R);
@@ -651,8 +641,8 @@ __host__ __device__ inline void sweep_layout(const CeTables &T, int L0, int L1, 
   o += 128;
   s.ax = o;  // per axis: begin[MAX_COLOURS], cnt[MAX_COLOURS], coord[MAX_L]
   o += align16(3 * (2 * MAX_COLOURS + MAX_L) * 4);
-  s.sched = o;  // key[n], par[n], order[n] (u32 each), n = MAX_SWEEPS * n_classes
-  o += align16(3 * MAX_SWEEPS * n_classes_max * 4);
+  s.sched = o;  // key[n], par[n], order[n] (u32 each), n = sub-steps per pass
+  o += align16(3 * n_sub_max * 4);
   s.red = o;  // block reduction scratch: 32 warps x 16 slots of 8 bytes
   o += 32 * 16 * 8;
   s.stats = o;  // the replica's running statistics, resident for the launch
@@ -664,7 +654,7 @@ __host__ __device__ inline void sweep_layout(const CeTables &T, int L0, int L1, 
   s.wkept = o;  // kept candidates per warp, two buffers
   o += 2 * 32 * 4;
   s.desc = o;  // decoded sub-steps of the current pass
-  o += MAX_SWEEPS * n_classes_max * 80;
+  o += n_sub_max * 80;
   s.initq = o;  // per-warp queues of occupied sites (initial energy)
   o += 32 * 96 * 4;
   s.bar = o;  // two mbarriers of the staging copies
@@ -672,10 +662,10 @@ __host__ __device__ inline void sweep_layout(const CeTables &T, int L0, int L1, 
   s.total = o;
 }
 
-inline int sweep_smem_bytes_impl(const CeTables &T, int L0, int L1, int L2, int n_classes,
+inline int sweep_smem_bytes_impl(const CeTables &T, int L0, int L1, int L2, int n_sub,
                                  int pitch) {
   SweepSmem s;
-  sweep_layout(T, L0, L1, L2, n_classes, pitch, s);
+  sweep_layout(T, L0, L1, L2, n_sub, pitch, s);
   return s.total;
 }
 
@@ -1275,7 +1265,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
   const int ensemble = R.ensemble;
   const float beta_f = R.beta_f;
   SweepSmem lay;
-  sweep_layout(T, G.L0, G.L1, G.L2, P.max_classes, PITCH, lay);
+  sweep_layout(T, G.L0, G.L1, G.L2, P.max_sub, PITCH, lay);
   int8_t *occ = reinterpret_cast<int8_t *>(smem + lay.occ);
   int *cl_off = reinterpret_cast<int *>(smem + lay.cl_off);
   int *lutoff = reinterpret_cast<int *>(smem + lay.lutoff);

@@ -80,8 +80,8 @@ cudaError_t launch_replay(const CeTables &T, const ReplayParams &P, cudaStream_t
   return cudaErrorInvalidValue;
 }
 
-int sweep_smem_bytes(const CeTables &T, int L0, int L1, int L2, int n_classes, int pitch) {
-  return sweep_smem_bytes_impl(T, L0, L1, L2, n_classes, pitch);
+int sweep_smem_bytes(const CeTables &T, int L0, int L1, int L2, int n_sub, int pitch) {
+  return sweep_smem_bytes_impl(T, L0, L1, L2, n_sub, pitch);
 }
 
 template <int TH>
