@@ -1690,9 +1690,12 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
           FF d;
           float de;
           if constexpr (PITCH >= 0) {
+            // the first change is applied before either flower is read (a
+            // site's own flower never contains it, so a sees the original
+            // state and b sees a changed); the two gathers can then overlap
             acc.zero();
+            if (local) put_site(occ, G, cb, xa, ya, za, (int8_t)ob);
             ev.add(cb, oa, ob, occ, ada, acc);
-            if (local) put_site(occ, G, cb, xa, ya, za, (int8_t)ob);  // first change applied
             ev.add(bb, ob, oa, occ, adb, acc);
             de = sweep_de<NOCC>(T, acc, whi, wlo, 0.f, 0.f, d);
           } else {
