@@ -561,6 +561,15 @@ def run_learned_comparison(args):
     mean_e_learned = float(e_rep_learned.mean())
     sig_learned = float(e_rep_learned.std(ddof=1) / np.sqrt(n_rep))
     sig_diff = float(np.hypot(sig_plain, sig_learned))
+    # 5. the plain sampler again, from the learned chain's final states (its global
+    # swaps have removed the antiphase boundaries the plain chain was still
+    # coarsening): both chains then sample the same equilibrium state
+    plain.run(args.steps, 0, record_samples=True)
+    plain.synchronize()
+    e_rep_plain2 = np.array([plain.stats(i)["mean_potential"] for i in range(n_rep)])
+    mean_e_plain2 = float(e_rep_plain2.mean())
+    sig_plain2 = float(e_rep_plain2.std(ddof=1) / np.sqrt(n_rep))
+    sig_diff2 = float(np.hypot(sig_plain2, sig_learned))
     line = {
         "metric": "effective samples/s (learned vs plain GPU Metropolis, same <E>)",
         "workload": w.name, "T_c_scan_K": tc, "temperature_K": T,
@@ -583,6 +592,11 @@ def run_learned_comparison(args):
         "ratio_learned_over_plain_order": (neff_op_l / t_learned) / (neff_op / t_plain),
         "same_E_within_2sigma": bool(abs(mean_e_learned - mean_e_plain) <= 2 * sig_diff),
         "E_difference_over_sigma": abs(mean_e_learned - mean_e_plain) / sig_diff if sig_diff > 0 else None,
+        "plain_from_learned_states": {
+            "passes": args.steps, "mean_E": mean_e_plain2, "mean_E_sigma": sig_plain2,
+            "same_E_within_2sigma": bool(abs(mean_e_learned - mean_e_plain2) <= 2 * sig_diff2),
+            "E_difference_over_sigma": abs(mean_e_learned - mean_e_plain2) / sig_diff2
+            if sig_diff2 > 0 else None},
     }
     print(json.dumps(line), flush=True)
     return 0

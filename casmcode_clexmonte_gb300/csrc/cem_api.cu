@@ -94,6 +94,7 @@ struct cem_system {
   bool big = false;            // more orbits than the register accumulators hold
   bool coop = false;           // big binary system for the warp-cooperative sweep
   bool split_ok = false;       // binary, split weights exist, orbits sorted by size
+  std::vector<int> wq_host;    // split weights' integer parts per orbit
   std::vector<void *> owned;
   ~cem_system() {
     for (void *p : owned) cudaFree(p);
@@ -116,6 +117,7 @@ struct cem_replicas {
   int sample_width = 1;
   long long n_samples_recorded = 0;
   int max_classes = 1, sweep_smem = 0, pitch = 0;
+  bool wide_records = false;  // cooperative sweep: keep 32-bit cluster records
   int n_pair_sweeps = 2, n_local_sweeps = 1;
   int threads = SWEEP_THREADS;
   // replica -> CTA schedule: 0 = CTA i runs replica i, 1 = largest replicas first
@@ -237,6 +239,30 @@ int choose_colouring(const cem_system &s, const int L[3], int ensemble) {
 int sub_steps(const cem_replicas *r) {
   const int sweeps = r->ensemble == CEM_CANONICAL ? r->n_pair_sweeps + r->n_local_sweeps : 1;
   return sweeps * r->max_classes;
+}
+
+// the cooperative sweep's 16-bit cluster records: every partner offset in
+// every replica's halo'd layout and every integer weight fits in int16
+bool fits_pack16(const cem_replicas *r) {
+  const cem_system &s = *r->sys;
+  const CeTables &T = s.T;
+  if (!s.split_ok) return false;
+  for (int a : s.wq_host)
+    if (a < -32768 || a > 32767) return false;
+  for (const Replica &R : r->reps) {
+    const long long W = R.L[0] + 2 * T.reach, H = R.L[1] + 2 * T.reach;
+    const long long V = W * H * (R.L[2] + 2 * T.reach);
+    for (int b = 0; b < T.n_sublat; ++b)
+      for (int c = T.fl_begin[b][0]; c < T.fl_begin[b][T.n_orbits]; ++c)
+        for (int q = 0; q < 3; ++q) {
+          const int pb = s.fl_pb[c * 3 + q];
+          if (pb < 0) continue;
+          const int *du = &s.fl_du[c * 9 + q * 3];
+          const long long off = (pb - b) * V + du[0] + W * (du[1] + H * du[2]);
+          if (off < -32768 || off > 32767) return false;
+        }
+  }
+  return true;
 }
 
 // dynamic shared memory of the sweep kernel for a batch at a given pitch
@@ -453,6 +479,7 @@ int cem_system_create(const cem_system_desc *d, cem_system **out) {
       bool sorted = true;
       for (int g = 1; g < T.n_orbits; ++g) sorted = sorted && T.orb_size[g] >= T.orb_size[g - 1];
       s->split_ok = ok && sorted;
+      s->wq_host = wq_all;
       s->coop = s->big && s->split_ok;
       if (!s->big)
         for (int g = 0; g < T.n_orbits; ++g) {
@@ -1059,7 +1086,8 @@ int cem_step_async(cem_replicas *r, const int8_t *host_in, int8_t *host_out, int
       P.n_passes = n_passes;
       P.n_equil = 0;
       P.max_classes = r->max_classes;
-    P.max_sub = sub_steps(r);
+      P.max_sub = sub_steps(r);
+      P.pack16 = (r->pitch == -2 && !r->wide_records && fits_pack16(r)) ? 1 : 0;
       P.n_pair_sweeps = r->n_pair_sweeps;
       P.n_local_sweeps = r->n_local_sweeps;
       P.cta_rep = r->d_cta_rep;
@@ -1183,6 +1211,7 @@ int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_sampl
     P.n_equil = n_equil;
     P.max_classes = r->max_classes;
     P.max_sub = sub_steps(r);
+    P.pack16 = (r->pitch == -2 && !r->wide_records && fits_pack16(r)) ? 1 : 0;
     P.n_pair_sweeps = r->n_pair_sweeps;
     P.n_local_sweeps = r->n_local_sweeps;
     P.cta_rep = r->d_cta_rep;
@@ -1374,6 +1403,12 @@ int cem_set_option(cem_replicas *r, const char *key, int64_t value) {
               "orbit_walk 2 needs a binary system with split weights", CEM_ERR_UNSUPPORTED);
       r->pitch = value == 1 ? -1 : -2;
       r->threads = SWEEP_THREADS;
+    } else if (k == "wide_records") {
+      // the cooperative sweep's 32-bit cluster records even where 16-bit
+      // ones fit (same sums, same chain)
+      r->wide_records = value != 0;
+      if (r->step_exec) cudaGraphExecDestroy(r->step_exec);  // captured with the old layout
+      r->step_exec = nullptr;
     } else if (k == "generic_evaluator") {
       if (value) {
         r->pitch = r->sys->big ? (r->sys->coop ? -2 : -1) : 0;

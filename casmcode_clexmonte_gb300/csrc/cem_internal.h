@@ -41,6 +41,7 @@ struct SweepParams {
   int max_sub;  // sub-steps per pass (sweeps x colour classes): sizes the schedule
   int n_pair_sweeps, n_local_sweeps;  // canonical pass composition
   int init;                    // binary systems: compute the exact initial stats in-kernel
+  int pack16;                  // cooperative sweep: 16-bit partner offsets and weights
   const int *cta_rep;          // replica of each CTA (null: CTA i runs replica i)
   double RT[16];               // (n_occ-1) x n_occ
 };

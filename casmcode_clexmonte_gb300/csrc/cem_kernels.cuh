@@ -834,6 +834,47 @@ __device__ __forceinline__ void coop_site(const int8_t *__restrict__ occ, int ad
   }
 }
 
+// The same with 16-bit records (batches whose partner offsets and integer
+// weights fit in int16): pk0[c] = off0 | off1 << 16, pk1[c] = off2 | A << 16,
+// one word fewer per triplet and two fewer per quadruplet than the 32-bit
+// records (the kernel is bound by shared-memory load wavefronts).
+__device__ __forceinline__ int lo16(int w) { return (int)(int16_t)(w & 0xFFFF); }
+__device__ __forceinline__ int hi16(int w) { return w >> 16; }  // arithmetic shift
+__device__ __forceinline__ int pack16(int lo, int hi) {
+  return (int)(((unsigned)lo & 0xFFFFu) | ((unsigned)hi << 16));
+}
+
+__device__ __forceinline__ void coop_site16(const int8_t *__restrict__ occ, int ad,
+                                            const int *__restrict__ pk0,
+                                            const int *__restrict__ pk1,
+                                            const float *__restrict__ cw_r, const int *seg,
+                                            int lane, int &n, float &r) {
+  for (int c = seg[0] + lane; c < seg[1]; c += 32) {
+    n += hi16(pk1[c]);
+    r = FADD(r, cw_r[c]);
+  }
+#pragma unroll 2
+  for (int c = seg[1] + lane; c < seg[2]; c += 32) {
+    const int v = occ[ad + lo16(pk0[c])];
+    n += v * hi16(pk1[c]);
+    r = FFMA(cw_r[c], (float)v, r);
+  }
+#pragma unroll 4
+  for (int c = seg[2] + lane; c < seg[3]; c += 32) {
+    const int w0 = pk0[c];
+    const int v = occ[ad + lo16(w0)] & occ[ad + hi16(w0)];
+    n += v * hi16(pk1[c]);
+    r = FFMA(cw_r[c], (float)v, r);
+  }
+#pragma unroll 4
+  for (int c = seg[3] + lane; c < seg[4]; c += 32) {
+    const int w0 = pk0[c], w1 = pk1[c];
+    const int v = occ[ad + lo16(w0)] & occ[ad + hi16(w0)] & occ[ad + lo16(w1)];
+    n += v * hi16(w1);
+    r = FFMA(cw_r[c], (float)v, r);
+  }
+}
+
 // Sum over the warp (butterfly: every lane ends with the same bits, float
 // addition being commutative).
 __device__ __forceinline__ void warp_sum_nr(int &n, float &r) {
@@ -1300,16 +1341,23 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
       int cb = 0;
       for (int b = 0; b < nsl; ++b)
         if (c >= T.fl_begin[b][0]) cb = b;
+      int off[3];
       for (int q = 0; q < 3; ++q) {
         const int pb = T.cl_pb[c * 3 + q];
         const int *du = T.cl_du + c * 9 + q * 3;
-        const int off = (pb < 0) ? 0 : (pb - cb) * G.V + du[0] + G.W * (du[1] + G.H * du[2]);
-        cl_off[PITCH == -2 ? q * T.n_fl + c : c * 3 + q] = off;  // -2: partner-major
+        off[q] = (pb < 0) ? 0 : (pb - cb) * G.V + du[0] + G.W * (du[1] + G.H * du[2]);
+        if (PITCH != -2) cl_off[c * 3 + q] = off[q];
       }
       if constexpr (PITCH == -2) {
         int g = 0;  // the cluster's orbit: fl_begin[cb][g] <= c < fl_begin[cb][g + 1]
         while (g + 1 < T.n_orbits && c >= T.fl_begin[cb][g + 1]) ++g;
-        lutoff[c] = T.wq_all[g];
+        if (P.pack16) {  // the host checked that offsets and weights fit in int16
+          cl_off[c] = pack16(off[0], off[1]);
+          cl_off[T.n_fl + c] = pack16(off[2], T.wq_all[g]);
+        } else {  // partner-major 32-bit offsets
+          for (int q = 0; q < 3; ++q) cl_off[q * T.n_fl + c] = off[q];
+          lutoff[c] = T.wq_all[g];
+        }
         reinterpret_cast<float *>(lut)[c] = T.wr_all[g];
       } else {
         lutoff[c] = T.cl_lut[c];
@@ -1528,7 +1576,10 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
           const U4 r = philox4x32_10(U4{(uint32_t)l, ctr_sub, plo, phi | (TAG_SITE << 16)}, k0, k1);
           int nq = 0;
           float rr = 0.f;
-          coop_site(occ, ad, cl_off, T.n_fl, cw_a, cw_r, sg, lane, nq, rr);
+          if (P.pack16)
+            coop_site16(occ, ad, cl_off, cl_off + T.n_fl, cw_r, sg, lane, nq, rr);
+          else
+            coop_site(occ, ad, cl_off, T.n_fl, cw_a, cw_r, sg, lane, nq, rr);
           warp_sum_nr(nq, rr);
           const int dd = o_f - o_i;
           nq *= dd;
@@ -1645,8 +1696,13 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
             __syncwarp();
             int na = 0, nb = 0;
             float ra = 0.f, rb = 0.f;
-            coop_site(occ, ada, cl_off, T.n_fl, cw_a, cw_r, seg + 5 * cb, lane, na, ra);
-            coop_site(occ, adb, cl_off, T.n_fl, cw_a, cw_r, seg + 5 * bb, lane, nb, rb);
+            if (P.pack16) {
+              coop_site16(occ, ada, cl_off, cl_off + T.n_fl, cw_r, seg + 5 * cb, lane, na, ra);
+              coop_site16(occ, adb, cl_off, cl_off + T.n_fl, cw_r, seg + 5 * bb, lane, nb, rb);
+            } else {
+              coop_site(occ, ada, cl_off, T.n_fl, cw_a, cw_r, seg + 5 * cb, lane, na, ra);
+              coop_site(occ, adb, cl_off, T.n_fl, cw_a, cw_r, seg + 5 * bb, lane, nb, rb);
+            }
             int nq = na - nb;
             float rr = FADD(ra, -rb);
             warp_sum_nr(nq, rr);

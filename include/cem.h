@@ -267,6 +267,10 @@ int cem_step_async(cem_replicas *r, const int8_t *host_in, int8_t *host_out, int
  *                  kernel that cluster expansions with more than 8 orbits
  *                  (real CASM basis sets) always use; running energy as an
  *                  FP64 sum of accepted changes; 512 threads per replica;
+ *   "wide_records" (0 or 1): 1 keeps the cooperative binary sweep's 32-bit
+ *                  cluster records where 16-bit ones (partner offsets and
+ *                  integer weights packed two per word) would fit; the
+ *                  chain is the same, the 16-bit records are faster;
  *   "streamed" (1): keep the occupations in HBM and run one kernel per colour
  *                  sub-step over many CTAs per replica (a captured CUDA graph
  *                  per pass); chosen automatically when a supercell does not

@@ -272,3 +272,27 @@ def test_zro_enforce_matches_oracle(ce, cm, oracle_mod):
         nf, _ = o.enforce_composition(ref, targets[i], seed + i)
         assert flips[i] == nf > 0
         np.testing.assert_array_equal(b.get_occupation(i), ref)
+
+
+@pytest.mark.parametrize("ens", ["semigrand_canonical", "canonical"])
+def test_zro_16bit_records_match_32bit(ens, ce, cm):
+    """The cooperative sweep's 16-bit cluster records (offsets and integer
+    weights packed two per word) give the same sums as the 32-bit records:
+    identical chains."""
+    sysd = cm.System(ce)
+    Ls = [(8, 8, 8), (10, 10, 8)]
+    rng = np.random.default_rng(8)
+    occs = [(rng.random(2 * int(np.prod(x))) < 0.45).astype(np.int8) for x in Ls]
+    out = []
+    for wide in (0, 1):
+        b = cm.ReplicaBatch(sysd, ens, Ls)
+        b.set_option("wide_records", wide)
+        for i in range(len(Ls)):
+            b.set_conditions(i, 1500.0 + 500 * i, np.array([-0.4]) if ens != "canonical" else None)
+            b.set_seed(i, 61 + i)
+            b.set_occupation(i, occs[i])
+        b.run(12, 2)
+        out.append([(b.get_occupation(i), b.stats(i)) for i in range(len(Ls))])
+    for (oa, sa), (ob, sb) in zip(*out):
+        np.testing.assert_array_equal(oa, ob)
+        assert sa["n_accepted"] == sb["n_accepted"] and sa["energy"] == sb["energy"]
