@@ -105,6 +105,33 @@ def test_learned_sampler_equilibrium_matches_oracle(trained, cm, oracle_mod):
     assert occ.sum() == occ0.sum()
 
 
+def test_learned_sampler_ordered_phase_matches_oracle(cm, oracle_mod):
+    """The same check in the L1_2-ordered phase (90 K, 0.9 T_c of this
+    expansion), where the trained weights are far from uniform: <E> of the
+    learned chain against the oracle's uniform-swap chain within 4 standard
+    errors."""
+    L, T, nrep = 10, 90.0, 16
+    ce = workloads.fcc_binary_ce(3, nn1=0.08)
+    rng = np.random.default_rng(19)
+    occ0 = workloads.fixed_composition(rng, L ** 3, 0.25)
+    o = oracle_mod.OracleSystem(ce, (L, L, L))
+    ref = o.run(occ0.copy(), 1, T, np.zeros(1), 91, 6000)
+    e_o, se_o = batch_means(ref["energy"][1500:])
+    sysd = cm.System(ce)
+    _, _, _, X, t = _snapshot_features(cm, T=T, passes=300)
+    net = cm.LearnedProposal(seed=6)
+    net.train(X, t, epochs=8, batch=512, lr=3e-3, seed=2)
+    b = cm.ReplicaBatch(sysd, "canonical", [(L, L, L)] * nrep)
+    for i in range(nrep):
+        b.set_conditions(i, T)
+        b.set_seed(i, 1900 + i)
+        b.set_occupation(i, occ0)
+    b.learned_run(net, 500, 150, record_samples=True)
+    means = np.array([b.learned_samples(i, 350)[0].mean() for i in range(nrep)])
+    e_g, se_g = means.mean(), means.std(ddof=1) / np.sqrt(nrep)
+    assert abs(e_g - e_o) < 4.0 * np.hypot(se_g, se_o), (e_g, se_g, e_o, se_o)
+
+
 def test_trained_network_raises_acceptance(cm):
     """What the network gains over the uniform proposal: a higher acceptance
     rate per proposal at the same conditions (and, reported, tau_int)."""
