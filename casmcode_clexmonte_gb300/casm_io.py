@@ -304,11 +304,16 @@ class SummaryWriter:
     "row,col"; "S" names the energy). Statistics carry the mean and the
     calculated precision = z(confidence) x the standard error corrected by the
     integrated autocorrelation time; with requested precisions, completion
-    results add the convergence and equilibration fields.
+    results add the convergence and equilibration fields. Mol compositions
+    follow CASM composition axes when given (``composition_axes``: the
+    system.json entry, e.g. Zr(2)Va(2-2a)O(2a) with a fixed Zr sublattice),
+    else the standard axes (origin every site occupant 0, end member k every
+    site occupant k).
     """
 
     def __init__(self, path: str, method: str, component_names, n_sites_per_uc: int,
-                 comp_var_names=None, confidence: float = 0.95, requested_precision=None):
+                 comp_var_names=None, confidence: float = 0.95, requested_precision=None,
+                 composition_axes=None):
         if method not in ("canonical", "semigrand_canonical"):
             raise ValueError(f"unknown method '{method}'")
         self.path = path
@@ -316,6 +321,16 @@ class SummaryWriter:
         self.components = list(component_names)
         self.n_basis = int(n_sites_per_uc)
         self.comp_vars = list(comp_var_names or "abcdefgh"[: len(self.components) - 1])
+        self.axes = None
+        if composition_axes is not None:
+            ax = composition_axes
+            names = [k for k in "abcdefghijklmnopqrstuvwxyz" if k in ax]
+            origin = np.asarray(ax["origin"], dtype=np.float64).reshape(-1)
+            Q = np.stack([np.asarray(ax[k], dtype=np.float64).reshape(-1) - origin for k in names],
+                         axis=1)
+            self.components = list(ax["components"])
+            self.comp_vars = names
+            self.axes = (origin, Q)
         self.z = _z(confidence)
         self.requested = dict(requested_precision or {})
         self.data = {"analysis": {}, "completion_check_results": {}, "conditions": {},
@@ -324,6 +339,8 @@ class SummaryWriter:
     # composition axes: origin = every site occupant 0, end member k = every
     # site occupant k (mol = origin + Q x)
     def _Q(self):
+        if self.axes is not None:
+            return self.axes[1]
         nc = len(self.comp_vars)
         Q = np.zeros((nc + 1, nc))
         for k in range(nc):
@@ -332,6 +349,8 @@ class SummaryWriter:
         return Q
 
     def _mol(self, x):
+        if self.axes is not None:
+            return self.axes[0] + self.axes[1] @ np.asarray(x, dtype=np.float64)
         origin = np.zeros(len(self.components))
         origin[0] = self.n_basis
         return origin + self._Q() @ np.asarray(x, dtype=np.float64)

@@ -162,3 +162,21 @@ def test_eci_json_round_trip_zro(ce, tmp_path):
     assert back.n_funcs == ce.n_funcs
     np.testing.assert_array_equal(back.eci, ce.eci)
     assert [(o.size, o.mult) for o in back.orbits] == [(o.size, o.mult) for o in ce.orbits]
+
+
+def test_summary_writer_follows_zro_composition_axes(tmp_path):
+    """mol_composition in summary.json over Zr, Va, O from the system's
+    composition axes (Zr(2)Va(2-2a)O(2a))."""
+    _, _, axes = documents()
+    path = str(tmp_path / "summary.json")
+    w = casm_io.SummaryWriter(path, "semigrand_canonical", ["Va", "O"], n_sites_per_uc=2,
+                              composition_axes=axes)
+    stats = {"mean_potential": -1.0, "mean_formation": -1.1, "var_potential": 1e-4,
+             "mean_comp": [0.25], "cov_comp": [[1e-4]], "cov_e_comp": [1e-5],
+             "n_samples": 100.0, "n_accepted": 40, "n_proposed": 100}
+    w.append(temperature=1200.0, n_unitcells=512, stats=stats, param_chem_pot=[-0.5])
+    w.write()
+    data = json.load(open(path))
+    mc = data["statistics"]["mol_composition"]
+    assert mc["component_names"] == ["Zr", "Va", "O"]
+    assert [mc[c]["mean"][0] for c in ("Zr", "Va", "O")] == pytest.approx([2.0, 1.5, 0.5])
