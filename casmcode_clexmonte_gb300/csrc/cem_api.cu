@@ -104,6 +104,7 @@ struct cem_system {
 struct cem_replicas {
   const cem_system *sys = nullptr;
   int n = 0, ensemble = 0;
+  int device = 0;  // the device current when the batch was created
   std::vector<Replica> reps;
   std::vector<ReplicaStats> stats_host;
   Replica *d_reps = nullptr;
@@ -552,6 +553,7 @@ int cem_replicas_create(const cem_system *sys, int n, const int *L, int ensemble
     r->sys = sys;
     r->n = n;
     r->ensemble = ensemble;
+    CUDA_OK(cudaGetDevice(&r->device));
     r->reps.resize(n);
     std::map<std::vector<int>, int> pcache;
     int64_t off = 0;
@@ -1259,6 +1261,10 @@ int cem_get_stats(cem_replicas *r, int i, cem_stats *out) {
     if (S.status == 5)
       throw Err(CEM_ERR_DEVICE,
                 "a shared-memory staging copy did not complete; the replica was left unchanged");
+    if (S.status == 6)
+      throw Err(CEM_ERR_DEVICE,
+                "a shared-memory staging copy did not complete and was still in flight when the "
+                "kernel gave up waiting; the replica was left unchanged");
     std::memset(out, 0, sizeof(*out));
     const int nc = r->sys->T.n_occ - 1;
     out->n_samples = S.n_samples;
@@ -1537,13 +1543,16 @@ int cem_last_kernel_ms(cem_replicas *r, double *ms) {
 // until the process exits), instead of allocating per call.
 //
 // Limits: at most CEM_NOALLOC_MAX_EVENTS events of at most
-// CEM_NOALLOC_MAX_SITES sites per call; larger calls are rejected.
+// CEM_NOALLOC_MAX_SITES sites per call; larger calls are rejected. The array
+// is CEM_NOALLOC_SCRATCH_BYTES bytes (cem.h; checked below against its
+// layout), dominated by the delta-correlation section sized for MAX_FUNCS
+// functions per event.
 // All calls share the array and it keeps the last call's contents; calls that
 // overlap on the GPU (different streams or batches at the same time) race.
 namespace {
 
-constexpr int NOALLOC_MAX_EVENTS = 4096;
-constexpr int NOALLOC_MAX_SITES = 4;
+constexpr int NOALLOC_MAX_EVENTS = CEM_NOALLOC_MAX_EVENTS;
+constexpr int NOALLOC_MAX_SITES = CEM_NOALLOC_MAX_SITES;
 constexpr size_t NA_SITES = 0;                                                   // int64
 constexpr size_t NA_NEW = NA_SITES + 8ull * NOALLOC_MAX_EVENTS * NOALLOC_MAX_SITES;  // int32
 constexpr size_t NA_DE = NA_NEW + 4ull * NOALLOC_MAX_EVENTS * NOALLOC_MAX_SITES;    // double
@@ -1552,6 +1561,8 @@ constexpr size_t NA_DMU = NA_DC + 8ull * NOALLOC_MAX_EVENTS * MAX_FUNCS;        
 constexpr size_t NA_BYTES = NA_DMU + 8 * 16;
 static_assert(NA_NEW % 256 == 0 && NA_DE % 256 == 0 && NA_DC % 256 == 0 && NA_DMU % 256 == 0,
               "scratch sections are 256-byte aligned");
+static_assert(NA_BYTES == CEM_NOALLOC_SCRATCH_BYTES,
+              "the scratch size stated in cem.h is the size of the array");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
 
@@ -1559,11 +1570,17 @@ constexpr int NA_MAX_DEVICES = 64;
 std::mutex g_noalloc_mutex;
 unsigned char *g_noalloc_ptr[NA_MAX_DEVICES] = {nullptr};
 
-// Device address of the scratch array for the current device; resolved once
+// Device address of the scratch array on the batch's device; resolved once
 // per device (the host-side name is only a stand-in, not a device address).
-unsigned char *noalloc_scratch() {
+// The batch's device must be the calling thread's current device: the
+// address, the batch's stream and its occupations all belong to it.
+unsigned char *noalloc_scratch(const cem_replicas *r) {
   int dev = 0;
   CUDA_OK(cudaGetDevice(&dev));
+  require(dev == r->device,
+          "cem_delta_energy_noalloc: the current device (" + std::to_string(dev) +
+              ") is not the device the batch was created on (" + std::to_string(r->device) +
+              "); make that device current first");
   require(dev >= 0 && dev < NA_MAX_DEVICES, "device index out of range", CEM_ERR_UNSUPPORTED);
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
   if (!g_noalloc_ptr[dev]) {
@@ -1587,7 +1604,7 @@ extern "C" int cem_delta_energy_noalloc(cem_replicas *r, int i, int n_events, in
                 " events per call (got " + std::to_string(n_events) + ")",
             CEM_ERR_UNSUPPORTED);
     require(sites && new_occ && dE, "null argument");
-    unsigned char *base = noalloc_scratch();  // first call on a device resolves the address
+    unsigned char *base = noalloc_scratch(r);  // first call on a device resolves the address
     if (n_events == 0) return;
     const Replica &R = r->reps[i];
     const CeTables &T = r->sys->T;

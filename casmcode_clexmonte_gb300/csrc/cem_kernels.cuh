@@ -1107,11 +1107,19 @@ __device__ __forceinline__ void compact_pairs(const PairGeom &pg, const Geo &G, 
 // Replica staging through a shared-memory buffer of cap bytes (a multiple
 // of 16): each round, one thread issues bulk copies of up to 32 KB for as
 // much of the replica as fits, all completing on one mbarrier; then every
-// thread scatters the round into the halo'd layout. Returns false, with no
-// copy in flight, when a round did not complete within the wait limit.
-static __device__ __noinline__ bool stage_replica_bulk(const int8_t *gocc, int n_sites, int8_t *occ,
-                                                       const Geo &G, const SiteIndex &site_of,
-                                                       uint8_t *buf, int cap, uint64_t *bar) {
+// thread scatters the round into the halo'd layout. Returns 0 when every
+// round completed (the mbarrier is then invalidated, so its word can be
+// reused as ordinary shared memory); STAGE_TIMEOUT when a round did not
+// complete within the wait limit but a second bounded wait saw its copies
+// land (nothing in flight); STAGE_IN_FLIGHT when that second wait ran out
+// too, so copies may still be writing into this CTA's shared memory.
+constexpr int STAGE_TIMEOUT = 5, STAGE_IN_FLIGHT = 6;
+__device__ __forceinline__ void mbar_inval(uint64_t *bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+static __device__ __noinline__ int stage_replica_bulk(const int8_t *gocc, int n_sites, int8_t *occ,
+                                                      const Geo &G, const SiteIndex &site_of,
+                                                      uint8_t *buf, int cap, uint64_t *bar) {
   const int tid = threadIdx.x, nth = blockDim.x;
   if (tid == 0) {
     mbar_init(bar, 1);
@@ -1137,9 +1145,9 @@ static __device__ __noinline__ bool stage_replica_bulk(const int8_t *gocc, int n
     }
     const bool ok = mbar_wait(bar, (uint32_t)(round & 1), 1 << 22);
     if (__syncthreads_or(!ok)) {
-      if (tid == 0) mbar_wait(bar, (uint32_t)(round & 1), 1 << 22);  // let the copies land
-      __syncthreads();
-      return false;
+      bool landed = true;
+      if (tid == 0) landed = mbar_wait(bar, (uint32_t)(round & 1), 1 << 22);  // let the copies land
+      return __syncthreads_or(!landed) ? STAGE_IN_FLIGHT : STAGE_TIMEOUT;
     }
     for (int i = tid; i < bytes; i += nth) {
       int b, x, y, z;
@@ -1148,7 +1156,9 @@ static __device__ __noinline__ bool stage_replica_bulk(const int8_t *gocc, int n
     }
     __syncthreads();
   }
-  return true;
+  if (tid == 0) mbar_inval(bar);
+  __syncthreads();
+  return 0;
 }
 
 // Occupations back to global memory: each round gathers as much of the
@@ -1404,9 +1414,6 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
   const int8_t *gocc = P.occ + R.occ_offset;
   const int n_sites = n_uc * nsl;
   const SiteIndex site_of(n_uc, G.L0, G.L1);
-  // 16-byte loads when the replica's occupations are 16-byte aligned (the
-  // loads of a thread are issued together, then scattered into the halo'd
-  // layout); byte loads otherwise
   // bulk (TMA) copies when the replica's occupations are 16-byte aligned,
   // byte loads otherwise
   const bool vec16 = ((R.occ_offset | n_sites) & 15) == 0;
@@ -1414,8 +1421,11 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
   const int stg_cap = ((lay.bar - lay.clist) / 16) * 16;
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem + lay.bar);
   if (vec16) {
-    if (!stage_replica_bulk(gocc, n_sites, occ, G, site_of, stg, stg_cap, bar)) {
-      if (tid == 0) Sg.status = 5;  // a staging copy did not complete: replica left unchanged
+    const int st = stage_replica_bulk(gocc, n_sites, occ, G, site_of, stg, stg_cap, bar);
+    if (st) {
+      // a staging copy did not complete: the replica is left unchanged
+      // (STAGE_IN_FLIGHT: its copies may also still have been in flight)
+      if (tid == 0) Sg.status = st;
       return;
     }
   } else {

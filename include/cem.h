@@ -172,13 +172,19 @@ int cem_delta_energy(cem_replicas *r, int replica, int n_events, int sites_per_e
  * to another framework's pool, or a per-event Monte Carlo loop that cannot
  * afford the device-wide synchronisation cudaMalloc and cudaFree imply.
  * Events and results are staged in one fixed array in device memory that is
- * part of the library (about 2.3 MB, held by every device that loads the
- * library until the process exits). At most 4096 events of at most 4 sites
- * per call; larger calls return CEM_ERR_UNSUPPORTED. The first call on a
- * device looks up the array's device address for that device, so make that
- * first call before any stream capture. All calls share the array and it
- * keeps the last call's contents; calls that overlap on the GPU (from
- * different streams or batches at the same time) race. */
+ * part of the library (CEM_NOALLOC_SCRATCH_BYTES = 4 423 808 bytes, about
+ * 4.4 MB, held by every device that loads the library until the process
+ * exits). At most CEM_NOALLOC_MAX_EVENTS events of at most
+ * CEM_NOALLOC_MAX_SITES sites per call; larger calls return
+ * CEM_ERR_UNSUPPORTED. The batch's device must be current (CEM_ERR_INVALID
+ * otherwise). The first call on a device looks up the array's device address
+ * for that device, so make that first call before any stream capture. All
+ * calls share the array and it keeps the last call's contents; calls that
+ * overlap on the GPU (from different streams or batches at the same time)
+ * race. */
+#define CEM_NOALLOC_MAX_EVENTS 4096
+#define CEM_NOALLOC_MAX_SITES 4
+#define CEM_NOALLOC_SCRATCH_BYTES 4423808
 int cem_delta_energy_noalloc(cem_replicas *r, int replica, int n_events, int sites_per_event,
                              const int64_t *sites, const int32_t *new_occ, int potential,
                              double *dE, int64_t *dcount);

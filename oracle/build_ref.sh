@@ -7,7 +7,13 @@
 # Prints the path of the built probe on its last line.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+# The reference tree: $REFERENCE_ROOT, else the read-only mount of the
+# reference sources in the build container. Exit status 2 when absent.
 REF="${REFERENCE_ROOT:-/root/reference}"
+if [ ! -d "$REF" ]; then
+  echo "reference sources not found at $REF (set REFERENCE_ROOT)" >&2
+  exit 2
+fi
 DATA="$REF/tests/unit/clexmonte/data"
 mkdir -p "$HERE/_ref"
 case "${1:-fcc}" in

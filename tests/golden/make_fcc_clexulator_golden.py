@@ -20,7 +20,11 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
+# the reference tree: $REFERENCE_ROOT, else its read-only mount in the
+# container that generates the fixtures
 REF = os.environ.get("REFERENCE_ROOT", "/root/reference")
+if not os.path.isdir(REF):
+    sys.exit(f"reference sources not found at {REF}: set REFERENCE_ROOT to the reference tree")
 
 
 def main():

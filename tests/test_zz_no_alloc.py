@@ -36,24 +36,30 @@ def env():
     return lib, cm, workloads, _lib
 
 
-def _noalloc(lib, batch, sites, new_occ, potential, n_funcs):
+def _noalloc(lib, batch, sites, new_occ, potential, n_funcs, with_dcount=True):
     n_events, k = sites.shape
     dE = np.zeros(n_events)
-    dc = np.zeros((n_events, n_funcs), dtype=np.int64)
+    dc = np.zeros((n_events, n_funcs), dtype=np.int64) if with_dcount else None
     rc = lib.cem_delta_energy_noalloc(batch.handle, 0, n_events, k, sites.ctypes.data,
                                       new_occ.ctypes.data, int(potential), dE.ctypes.data,
-                                      dc.ctypes.data)
+                                      dc.ctypes.data if with_dcount else None)
     return rc, dE, dc
 
 
-@pytest.mark.parametrize("kind", ["fcc_binary_sgc", "bcc_ternary_sgc"])
+@pytest.mark.parametrize("kind", ["fcc_binary_sgc", "bcc_ternary_sgc", "zro_sgc"])
 def test_noalloc_delta_matches_allocating_entry_point(kind, env):
     lib, cm, workloads, _lib = env
     rng = np.random.default_rng(99)
     if kind == "fcc_binary_sgc":
         ce, L, mu = workloads.fcc_binary_ce(1), (10, 10, 10), np.array([0.03])
-    else:
+    elif kind == "bcc_ternary_sgc":
         ce, L, mu = workloads.bcc_ternary_ce(2), (6, 6, 6), np.array([0.1, -0.05])
+    else:
+        # the reference's Zr-O basis set: 74 functions, so every event's
+        # delta-correlation row in the scratch array is 74 entries wide
+        from tests.zro_fixture import zro_ce
+
+        ce, L, mu = zro_ce(), (8, 8, 8), np.array([-0.4])
     sysd = cm.System(ce)
     b = cm.ReplicaBatch(sysd, "semigrand_canonical", [L])
     b.set_conditions(0, 900.0, mu)
@@ -73,6 +79,14 @@ def test_noalloc_delta_matches_allocating_entry_point(kind, env):
         assert rc == 0, lib.cem_last_error().decode()
         np.testing.assert_array_equal(dc, ref_dc)
         assert np.all(np.abs(dE - ref_dE) <= 1e-10 * np.abs(ref_dE) + 1e-12)
+    # without a delta-correlation output the kernel skips that section
+    sites = np.ascontiguousarray(rng.integers(0, n, (700, 2)), dtype=np.int64)
+    new_occ = np.ascontiguousarray((occ[sites] + rng.integers(1, nocc, (700, 2))) % nocc,
+                                   dtype=np.int32)
+    ref_dE, _ = b.delta(0, sites, new_occ, potential=True)
+    rc, dE, _ = _noalloc(lib, b, sites, new_occ, True, ce.n_funcs, with_dcount=False)
+    assert rc == 0, lib.cem_last_error().decode()
+    assert np.all(np.abs(dE - ref_dE) <= 1e-10 * np.abs(ref_dE) + 1e-12)
 
 
 def test_noalloc_rejects_calls_above_the_limit(env):
