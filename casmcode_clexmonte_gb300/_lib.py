@@ -56,8 +56,9 @@ EXPORTS = [
     "cem_reset_stats", "cem_synchronize", "cem_last_kernel_ms", "cem_smem_bandwidth",
     "cem_set_option", "cem_get_option", "cem_autotune", "cem_step_async", "cem_delta_energy_noalloc",
     "cem_mlp_info", "cem_mlp_create", "cem_mlp_destroy", "cem_mlp_get_params",
-    "cem_mlp_set_params", "cem_mlp_forward", "cem_mlp_gradient", "cem_mlp_train",
-    "cem_learned_features", "cem_learned_run", "cem_learned_samples", "cem_get_order_samples",
+    "cem_mlp_set_params", "cem_mlp_forward", "cem_mlp_forward_tc", "cem_mlp_gradient", "cem_mlp_train",
+    "cem_learned_features", "cem_learned_run", "cem_learned_group_run", "cem_learned_samples",
+    "cem_get_order_samples",
     "cem_state_bytes", "cem_get_state", "cem_set_state",
 ]
 
@@ -117,10 +118,13 @@ def load(path: str = LIB):
     L.cem_mlp_get_params.argtypes = [P, vp]
     L.cem_mlp_set_params.argtypes = [P, vp]
     L.cem_mlp_forward.argtypes = [P, C.c_int64, vp, vp]
+    L.cem_mlp_forward_tc.argtypes = [P, C.c_int64, vp, vp]
     L.cem_mlp_gradient.argtypes = [P, C.c_int64, vp, vp, vp, C.POINTER(C.c_double)]
     L.cem_mlp_train.argtypes = [P, C.c_int64, vp, vp, C.c_int, C.c_int, C.c_float, C.c_uint64, vp]
     L.cem_learned_features.argtypes = [P, C.c_int, vp, vp]
     L.cem_learned_run.argtypes = [P, P, C.c_int64, C.c_int64, C.c_int]
+    L.cem_learned_group_run.argtypes = [P, P, C.c_int, C.c_int, C.c_int, C.c_int64, C.c_int64,
+                                        C.c_int]
     L.cem_learned_samples.argtypes = [P, C.c_int, vp, vp, C.c_int64, C.POINTER(C.c_int64)]
     L.cem_get_option.argtypes = [P, C.c_char_p, C.POINTER(C.c_int64)]
     _lib = L

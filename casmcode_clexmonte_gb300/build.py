@@ -16,7 +16,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libcem_gb300.so")
-SOURCES = ["cem_api.cu", "cem_launch.cu", "cem_k2.cu", "cem_k3.cu", "cem_kfcc.cu", "cem_kfcc_b.cu", "cem_learned.cu", "cem_stream.cu",
+SOURCES = ["cem_api.cu", "cem_launch.cu", "cem_k2.cu", "cem_k3.cu", "cem_kfcc.cu", "cem_kfcc_b.cu", "cem_learned.cu", "cem_lgroup.cu", "cem_stream.cu",
            "cem_enforce.cu", "cem_nfold.cu",
            "cem_k256a.cu", "cem_k256b.cu", "cem_kbig.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

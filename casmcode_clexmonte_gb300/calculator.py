@@ -245,6 +245,21 @@ class ReplicaBatch:
         check(self.lib.cem_learned_run(self.handle, h, int(n_passes), int(n_equil),
                                        int(bool(record_samples))))
 
+    GROUP_WEIGHTS = {"uniform": 0, "network": 1, "exact": 2}
+
+    def learned_group_run(self, proposal, n_passes: int, n_equil: int = 0,
+                          record_samples: bool = False, weights: str | None = None,
+                          rounds: int = 16, local_substeps: int = 8):
+        """Learned group sweep (cem_learned_group_run): ``weights`` is
+        "network" (default when ``proposal`` is given), "uniform" or "exact"
+        (the locally balanced weights the network is trained toward)."""
+        if weights is None:
+            weights = "uniform" if proposal is None else "network"
+        mode = self.GROUP_WEIGHTS[weights]
+        h = None if proposal is None else proposal.handle
+        check(self.lib.cem_learned_group_run(self.handle, h, mode, int(rounds), int(local_substeps),
+                                             int(n_passes), int(n_equil), int(bool(record_samples))))
+
     def learned_samples(self, i: int, capacity: int):
         e = np.zeros(capacity)
         op = np.zeros(capacity)
@@ -317,9 +332,11 @@ def enforce_composition(state: "MonteCarloState", target_mol_composition, system
 
 
 class LearnedProposal:
-    """The proposal network (43 -> 64 -> 64 -> 1, bf16 parameters) on the GPU."""
+    """The proposal network (42 neighbour occupants -> 64 -> 64 -> 1 logit,
+    bf16 parameters) on the GPU. A site holding A is weighted exp(z), one
+    holding B exp(-z)."""
 
-    N_IN = 43
+    N_IN = 42
     N_HIDDEN = 64
 
     def __init__(self, seed: int = 0):
@@ -351,6 +368,13 @@ class LearnedProposal:
         X = np.ascontiguousarray(X, dtype=np.int8)
         z = np.zeros(len(X), dtype=np.float32)
         check(self.lib.cem_mlp_forward(self.handle, len(X), ptr(X), ptr(z)))
+        return z
+
+    def forward_tc(self, X) -> np.ndarray:
+        """Logits on the tensor-core path of the group sweep."""
+        X = np.ascontiguousarray(X, dtype=np.int8)
+        z = np.zeros(len(X), dtype=np.float32)
+        check(self.lib.cem_mlp_forward_tc(self.handle, len(X), ptr(X), ptr(z)))
         return z
 
     def gradient(self, X, t):

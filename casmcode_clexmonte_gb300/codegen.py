@@ -96,6 +96,29 @@ def render(ce, name="gen_fcc") -> str:
         L.append(f"  n[{g}] = {expr};")
     L.append("}")
     L.append("")
+    L.append("// the same counts, and the neighbour occupants packed into env (bit k =")
+    L.append("// neighbour k), the input of the proposal network")
+    L.append("template <int P>")
+    L.append("__device__ __forceinline__ void counts_env(const int8_t *__restrict__ c, int (&n)[N_ORBITS],")
+    L.append("                                           unsigned long long &env) {")
+    for k, d in enumerate(nbs):
+        L.append(f"  const int v{k} = c[({d[0]}) + P * ({d[1]}) + P * P * ({d[2]})];")
+    for g, (size, cl) in enumerate(orbits):
+        if size == 1:
+            L.append(f"  n[{g}] = 1;")
+            continue
+        terms = []
+        for c in cl:
+            terms.append(" & ".join(f"v{k}" for k in c) if len(c) > 1 else f"v{c[0]}")
+        expr = " + ".join(f"({t})" if "&" in t else t for t in terms)
+        L.append(f"  n[{g}] = {expr};")
+    lo = " | ".join(f"((unsigned)v{k} << {k})" for k in range(min(32, len(nbs))))
+    hi = " | ".join(f"((unsigned)v{k} << {k - 32})" for k in range(32, len(nbs))) or "0u"
+    L.append(f"  const unsigned lo = {lo};")
+    L.append(f"  const unsigned hi = {hi};")
+    L.append("  env = ((unsigned long long)hi << 32) | lo;")
+    L.append("}")
+    L.append("")
     # owned clusters: anchored at the site (its lexicographically smallest
     # point), so every periodic cluster is counted once over all sites
     index = {tuple(d): k for k, d in enumerate(nbs)}

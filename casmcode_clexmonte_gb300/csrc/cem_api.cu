@@ -1746,6 +1746,29 @@ int cem_mlp_forward(cem_mlp *m, int64_t n, const int8_t *features, float *logits
   });
 }
 
+int cem_mlp_forward_tc(cem_mlp *m, int64_t n, const int8_t *features, float *logits) {
+  return guard([&] {
+    require(m && features && logits && n >= 0, "bad argument");
+    if (n == 0) return;
+    int8_t *dx = nullptr;
+    float *dz = nullptr;
+    try {
+      CUDA_OK(cudaMalloc(&dx, (size_t)n * MLP_IN));
+      CUDA_OK(cudaMalloc(&dz, (size_t)n * 4));
+      CUDA_OK(cudaMemcpyAsync(dx, features, (size_t)n * MLP_IN, cudaMemcpyHostToDevice, m->stream));
+      CUDA_OK(mlp_forward_tc(m->d_params, dx, n, dz, m->stream));
+      CUDA_OK(cudaMemcpyAsync(logits, dz, (size_t)n * 4, cudaMemcpyDeviceToHost, m->stream));
+      CUDA_OK(cudaStreamSynchronize(m->stream));
+    } catch (...) {
+      cudaFree(dx);
+      cudaFree(dz);
+      throw;
+    }
+    cudaFree(dx);
+    cudaFree(dz);
+  });
+}
+
 int cem_mlp_gradient(cem_mlp *m, int64_t n, const int8_t *features, const float *targets,
                      float *grad, double *loss) {
   return guard([&] {
@@ -1909,6 +1932,57 @@ int cem_learned_run(cem_replicas *r, const cem_mlp *m, int64_t n_passes, int64_t
     CUDA_OK(learned_run(r->sys->T, r->d_reps, r->d_stats, r->d_occ, m ? m->d_params : nullptr,
                         m ? 1 : 0, r->d_lw, n, r->d_trees, tsize, n, r->n, L, n_passes, n_equil,
                         samples, cap, pitch, r->stream));
+    CUDA_OK(cudaEventRecord(r->ev1, r->stream));
+    r->stats_valid = false;  // the sweep recomputes its own state next time
+  });
+}
+
+int cem_learned_group_run(cem_replicas *r, const cem_mlp *m, int weights, int rounds,
+                          int local_substeps, int64_t n_passes, int64_t n_equil,
+                          int record_samples) {
+  return guard([&] {
+    require(r != nullptr, "null handle");
+    require(n_passes >= 0 && n_equil >= 0, "pass counts must be >= 0");
+    require(weights >= 0 && weights <= 2, "weights must be 0 (uniform), 1 (network) or 2 (exact)");
+    require(weights != 1 || m != nullptr, "network weights need a network");
+    require(rounds >= 1 && rounds <= CEM_LGROUP_MAX_ROUNDS, "rounds must be 1..32");
+    require(local_substeps >= 1 && local_substeps <= CEM_LGROUP_MAX_LOCAL,
+            "local_substeps must be 1..64 (they keep the chain ergodic)");
+    require(r->sys->fcc_generated && r->ensemble == CEM_CANONICAL,
+            "the learned group sweep supports canonical binary FCC systems of the generated "
+            "topology",
+            CEM_ERR_UNSUPPORTED);
+    const int L = r->reps[0].L[0];
+    for (const Replica &R : r->reps)
+      require(R.L[0] == L && R.L[1] == L && R.L[2] == L && lgroup_supported(L),
+              "the learned group sweep needs equal cubic supercells of 12, 24, 36 or 48 cells",
+              CEM_ERR_UNSUPPORTED);
+    int dev = 0, maxsm = 0;
+    CUDA_OK(cudaGetDevice(&dev));
+    CUDA_OK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    require(lgroup_smem_bytes(L) <= maxsm, "supercell does not fit in shared memory",
+            CEM_ERR_UNSUPPORTED);
+    r->upload_reps();
+    const int n = r->reps[0].n_sites;
+    (void)n;
+    double *samples = nullptr;
+    long long cap = 0;
+    if (record_samples) {
+      cap = std::max<long long>(1, n_passes - n_equil);
+      if (cap > r->lsample_capacity) {
+        cudaFree(r->d_lsamples);
+        r->d_lsamples = nullptr;
+        CUDA_OK(cudaMalloc(&r->d_lsamples, sizeof(double) * 3 * cap * r->n));
+        r->lsample_capacity = cap;
+      }
+      samples = r->d_lsamples;
+      cap = r->lsample_capacity;
+      r->lsamples_recorded = std::max<long long>(0, n_passes - n_equil);
+    }
+    CUDA_OK(cudaEventRecord(r->ev0, r->stream));
+    CUDA_OK(lgroup_run(r->sys->T, r->d_reps, r->d_stats, r->d_occ,
+                       weights == 1 ? m->d_params : nullptr, weights, rounds, local_substeps, r->n,
+                       L, n_passes, n_equil, samples, cap, r->stream));
     CUDA_OK(cudaEventRecord(r->ev1, r->stream));
     r->stats_valid = false;  // the sweep recomputes its own state next time
   });

@@ -114,6 +114,16 @@ cudaError_t learned_run(const CeTables &T, const Replica *reps, ReplicaStats *st
                         int n_sites, int n_replicas, int L, long long n_passes, long long n_equil,
                         double *samples, long long capacity, int pitch, cudaStream_t st);
 
+// learned group sweep (cem_lgroup.cu)
+cudaError_t mlp_forward_tc(const __nv_bfloat16 *params, const int8_t *X, long long n, float *z,
+                           cudaStream_t st);
+bool lgroup_supported(int L);
+int lgroup_smem_bytes(int L);
+cudaError_t lgroup_run(const CeTables &T, const Replica *reps, ReplicaStats *stats, int8_t *occ,
+                       const __nv_bfloat16 *params, int mode, int rounds, int n_local,
+                       int n_replicas, int L, long long n_passes, long long n_equil,
+                       double *samples, long long capacity, cudaStream_t st);
+
 // n-fold way (cem_nfold.cu)
 // 32-ary sum tree over n leaves: level 0 = leaves, level k + 1 has
 // ceil(n_k / 32) nodes, the last level one node; levels stored back to back.

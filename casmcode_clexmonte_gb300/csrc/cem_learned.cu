@@ -121,9 +121,11 @@ __global__ void k_mlp_pack(const float *__restrict__ master, __nv_bfloat16 *__re
 
 // ---------------------------------------------------------------- features
 // Environment of every site of one binary FCC replica (42 neighbours in the
-// generated order, then the site's own occupant) and the training target:
-// half the log Metropolis weight of flipping the site,
-// t = clamp(-beta * dE_flip / 2, LOGIT_MIN, LOGIT_MAX).
+// generated order) and the training target: half the log Metropolis weight
+// of putting B on the site in that environment,
+// t = clamp(-beta * dE_AB / 2, LOGIT_MIN, LOGIT_MAX) (for a site holding A
+// that is half the log weight of flipping it; for a site holding B its
+// flip's is -t).
 __global__ void k_features(const int8_t *__restrict__ occ, int L, const double *__restrict__ w,
                            const int *__restrict__ orb_func, double beta,
                            int8_t *__restrict__ X, float *__restrict__ t) {
@@ -143,8 +145,6 @@ __global__ void k_features(const int8_t *__restrict__ occ, int L, const double *
       v[k] = occ[xx + L * (yy + L * zz)];
       X[(long long)l * MLP_IN + k] = (int8_t)v[k];
     }
-    const int o = occ[l];
-    X[(long long)l * MLP_IN + gen_fcc::N_NB] = (int8_t)o;
     int cnt[gen_fcc::N_ORBITS];
     for (int g = 0; g < gen_fcc::N_ORBITS; ++g) cnt[g] = 0;
     for (int c = 0; c < gen_fcc::N_CL; ++c) {
@@ -157,7 +157,6 @@ __global__ void k_features(const int8_t *__restrict__ occ, int L, const double *
     }
     double de = 0.0;
     for (int g = 0; g < gen_fcc::N_ORBITS; ++g) de += w[orb_func[g]] * cnt[g];
-    de *= (o == 0) ? 1.0 : -1.0;
     float tt = (float)(-0.5 * beta * de);
     t[l] = fminf(fmaxf(tt, LOGIT_MIN), LOGIT_MAX);
   }
@@ -244,21 +243,16 @@ __global__ void k_learned_init(const __nv_bfloat16 *__restrict__ params, int use
   for (int l = warp; l < n; l += nw) {
     const int x = l % L, y = (l / L) % L, z = l / (L * L);
     for (int k = lane; k < MLP_IN; k += 32) {
-      int val;
-      if (k < gen_fcc::N_NB) {
-        int xx = (x + gen_fcc::NB_D[k][0] + L) % L, yy = (y + gen_fcc::NB_D[k][1] + L) % L,
-            zz = (z + gen_fcc::NB_D[k][2] + L) % L;
-        val = occ[xx + L * (yy + L * zz)];
-      } else {
-        val = occ[l];
-      }
-      env[warp][k] = (int8_t)val;
+      int xx = (x + gen_fcc::NB_D[k][0] + L) % L, yy = (y + gen_fcc::NB_D[k][1] + L) % L,
+          zz = (z + gen_fcc::NB_D[k][2] + L) % L;
+      env[warp][k] = occ[xx + L * (yy + L * zz)];
     }
     __syncwarp();
     long long w = 1;
     if (use_mlp) {
       float h1[2], h2[2];
-      w = logit_weight(mlp_forward_warp(P, env[warp], h1, h2));
+      const float zz = mlp_forward_warp(P, env[warp], h1, h2);
+      w = logit_weight(occ[l] ? -zz : zz);
     }
     if (lane == 0) {
       wts[l] = w;
@@ -475,13 +469,13 @@ __global__ void __launch_bounds__(LEARNED_THREADS, 1)
         const int x = s % L, y = (s / L) % L, z = s / (L * L);
         const int ad = G.addr(0, x, y, z);
         int8_t *e = env + warp * 48;
-        for (int k = lane; k < MLP_IN; k += 32)
-          e[k] = (k < gen_fcc::N_NB) ? occ[ad + s_nboff[k]] : occ[ad];
+        for (int k = lane; k < MLP_IN; k += 32) e[k] = occ[ad + s_nboff[k]];
         __syncwarp();
         long long w = 1;
         if (LP.use_mlp) {
           float h1[2], h2[2];
-          w = logit_weight(mlp_forward_warp(P, e, h1, h2));
+          const float zz = mlp_forward_warp(P, e, h1, h2);
+          w = logit_weight(occ[ad] ? -zz : zz);  // the proposed state is applied
         }
         if (lane == 0) {
           aff_wnew[j] = w;

@@ -1,16 +1,20 @@
 // Learned proposal for canonical swaps: a small MLP scores each site's
-// environment (its 42 neighbours in the first three shells plus its own
-// occupant), site weights are kept in per-species sum trees, and swaps are
+// environment (its 42 neighbours in the first three shells), and swaps are
 // proposed by drawing one site of each species with probability proportional
 // to its weight. The Metropolis-Hastings ratio uses the exact forward and
-// reverse proposal probabilities, so the stationary distribution is the
-// canonical one whatever the network predicts.
+// reverse proposal probabilities, so the canonical distribution is sampled
+// whatever the network predicts.
 //
-// Network: 43 inputs -> 64 (ReLU) -> 64 (ReLU) -> 1 logit z. Parameters are
-// stored in bf16 for inference; training keeps fp32 master copies; every dot
-// product accumulates in fp32. Site weight: w = max(1, round(2^12 exp(z)))
-// with z clamped to [-12, 8], an integer, so the sum trees hold exact int64
-// totals and a drawn site has probability exactly w / W.
+// Network: 42 inputs (neighbour occupants 0/1) -> 64 (ReLU) -> 64 (ReLU) ->
+// 1 logit z(env), trained toward -beta dE_AB(env) / 2, where dE_AB is the
+// energy change of putting species B on the site in that environment. A site
+// holding A gets weight exp(z) and a site holding B weight exp(-z) (the
+// locally balanced weights sqrt(pi(flipped) / pi(current)) when the network
+// is exact), so one evaluation serves both species. Parameters are stored in
+// bf16 for inference; training keeps fp32 master copies; every dot product
+// accumulates in fp32. Integer site weight: w = max(1, round(2^12 exp(+-z)))
+// with z clamped to [-10, 10], so sums are exact integers and a drawn site
+// has probability exactly w / W.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -22,7 +26,7 @@
 
 namespace cem {
 
-constexpr int MLP_IN = 43;
+constexpr int MLP_IN = 42;
 constexpr int MLP_H = 64;
 // parameter block (fp32 masters / bf16 copies), offsets in elements
 constexpr int MLP_W1 = 0;                        // [MLP_IN][MLP_H]  (input-major)
@@ -33,10 +37,11 @@ constexpr int MLP_W3 = MLP_B2 + MLP_H;           // [MLP_H]
 constexpr int MLP_B3 = MLP_W3 + MLP_H;           // [1]
 constexpr int MLP_NPARAM = MLP_B3 + 1;
 
-constexpr float LOGIT_MIN = -12.f, LOGIT_MAX = 8.f;
+constexpr float LOGIT_MIN = -10.f, LOGIT_MAX = 10.f;
 constexpr float WEIGHT_SCALE = 4096.f;
 
-// Integer proposal weight of a logit.
+// Integer proposal weight of a logit (of a site holding A; a site holding B
+// uses -z).
 __host__ __device__ inline long long logit_weight(float z) {
   z = fminf(fmaxf(z, LOGIT_MIN), LOGIT_MAX);
 #ifdef __CUDA_ARCH__
@@ -48,7 +53,7 @@ __host__ __device__ inline long long logit_weight(float z) {
   return r < 1 ? 1 : r;
 }
 
-// Forward pass of one environment by one warp. x: 43 occupants (0/1) in
+// Forward pass of one environment by one warp. x: 42 occupants (0/1) in
 // shared memory; P: fp32 parameters in shared memory (converted from bf16).
 // Returns the logit on every lane; h1, h2 receive this lane's hidden units
 // (j and j + 32).

@@ -1,0 +1,651 @@
+// Learned group sweep: the canonical Metropolis-Hastings sampler of binary
+// FCC cluster expansions (generated topology) in which the proposal network
+// chooses which swaps to propose inside random groups of non-interacting
+// sites.
+//
+// A pass visits the colour classes of period 3 (sites whose cell coordinates
+// agree modulo 3; no two of them share a cluster, since every flower offset
+// has a component in {-2..2} \ {0}) in a random order. A class sub-step
+//   1. evaluates, for every member, the exact energy change dE_AB of putting
+//      B on the site (integer cluster counts, split ECI weights) and the
+//      network logit z of its 42-neighbour environment; neither depends on
+//      other members of the class, so both stay valid for the whole sub-step;
+//   2. splits the class into groups of 32 members by a random affine
+//      permutation of the member index (state independent, drawn per
+//      sub-step), one group per warp;
+//   3. runs `rounds` Metropolis-Hastings swaps inside each group: an A member
+//      drawn with probability w_A / W_A, a B member with w_B / W_B (integer
+//      weights of z, exact integer totals), accepted with
+//      min(1, exp(-beta dE) q_rev / q_fwd) with the exact reverse
+//      probabilities (the swapped members change their own weights only).
+// Members of one group do not interact, so dE of a swap is the sum of the
+// two members' flip energies. Classes of period 3 mix the four simple-cubic
+// sublattices of the L1_2 order, so group swaps create and remove antisite
+// pairs. `n_local` sub-steps of nearest-neighbour swaps per pass (plain
+// Metropolis, pairs at anchors 6 cells apart) move atoms between classes, so
+// the chain is ergodic in the canonical ensemble.
+//
+// Weights: mode 0 every weight 1 (uniform swaps inside groups), mode 1 the
+// network (w_A = round(2^12 exp(z)), w_B = round(2^12 exp(-z)), z clamped),
+// mode 2 the exact locally balanced weights z = -beta dE_AB / 2 that the
+// network is trained to predict.
+//
+// Network evaluation: the two dense layers of 32 environments at a time on
+// the tensor cores (mma.sync m16n8k16, bf16 operands, fp32 accumulation):
+// inputs (0/1, exact in bf16) x W1[42->48 padded][64], ReLU, x W2[64][64],
+// ReLU, dot w3; the accumulator fragments of layer 1 are the A fragments of
+// layer 2.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "cem_kernels.cuh"
+#include "cem_learned.cuh"
+
+namespace cem {
+
+constexpr int LG_THREADS = 512;
+constexpr int LG_NW = LG_THREADS / 32;
+constexpr int LG_CLASSES = 27;
+constexpr uint32_t TAG_LG_SCHED = 0x5u, TAG_LG_GROUP = 0x6u, TAG_LG_LOCAL = 0x7u;
+// fragment tables of the network: [k-step][n-tile][lane] (b0, b1)
+constexpr int LG_W1_FRAGS = 3 * 8 * 32, LG_W2_FRAGS = 4 * 8 * 32;
+
+struct LGroupParams {
+  const Replica *reps;
+  ReplicaStats *stats;
+  int8_t *occ;
+  const __nv_bfloat16 *params;
+  int mode;  // 0 uniform, 1 network, 2 exact local energies
+  int rounds, n_local;
+  long long n_passes, n_equil;
+  double *samples;  // [rep][capacity][3]: energy per unit cell, x_B, order parameter
+  long long sample_capacity;
+};
+
+__device__ __forceinline__ void mma_bf16_16816(float (&c)[4], uint32_t a0, uint32_t a1,
+                                               uint32_t a2, uint32_t a3, uint32_t b0,
+                                               uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// bf16 pair (lower half: element k) of bits k and k + 1 of a 0/1 mask.
+__device__ __forceinline__ uint32_t lg_bits2(unsigned long long e, int k) {
+  const uint32_t x = (uint32_t)(e >> k) & 3u;
+  return ((x & 1u) * 0x3F80u) | ((x >> 1) * 0x3F800000u);
+}
+
+__device__ __forceinline__ uint32_t lg_pack(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+__device__ __forceinline__ unsigned long long shfl64(unsigned long long v, int src) {
+  const uint32_t lo = __shfl_sync(0xffffffffu, (uint32_t)v, src);
+  const uint32_t hi = __shfl_sync(0xffffffffu, (uint32_t)(v >> 32), src);
+  return ((unsigned long long)hi << 32) | lo;
+}
+
+// Network tables in shared memory: B fragments of W1 (rows 42..47 zero) and
+// W2, and the fp32 biases and output weights.
+struct LgNet {
+  const uint2 *w1, *w2;
+  const float *b1, *b2, *w3;
+  float b3;
+};
+
+// Logit of the environment of each lane's site (all 32 lanes take part).
+__device__ __forceinline__ float lg_network(const LgNet &N, unsigned long long env, int lane) {
+  const int g = lane >> 2, tig = lane & 3;
+  float zout = 0.f;
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt) {
+    const unsigned long long e0 = shfl64(env, 16 * mt + g), e1 = shfl64(env, 16 * mt + g + 8);
+    float acc[8][4];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      const int k0 = 16 * s + 2 * tig;
+      const uint32_t a0 = lg_bits2(e0, k0), a1 = lg_bits2(e1, k0);
+      const uint32_t a2 = lg_bits2(e0, k0 + 8), a3 = lg_bits2(e1, k0 + 8);
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const uint2 b = N.w1[(s * 8 + t) * 32 + lane];
+        mma_bf16_16816(acc[t], a0, a1, a2, a3, b.x, b.y);
+      }
+    }
+    uint32_t A2[4][4];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const int c0 = 8 * t + 2 * tig;
+      const float v0 = fmaxf(acc[t][0] + N.b1[c0], 0.f), v1 = fmaxf(acc[t][1] + N.b1[c0 + 1], 0.f);
+      const float v2 = fmaxf(acc[t][2] + N.b1[c0], 0.f), v3 = fmaxf(acc[t][3] + N.b1[c0 + 1], 0.f);
+      A2[t >> 1][(t & 1) * 2 + 0] = lg_pack(v0, v1);
+      A2[t >> 1][(t & 1) * 2 + 1] = lg_pack(v2, v3);
+    }
+    float p0 = 0.f, p1 = 0.f;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      float c[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const uint2 b = N.w2[(j * 8 + t) * 32 + lane];
+        mma_bf16_16816(c, A2[j][0], A2[j][1], A2[j][2], A2[j][3], b.x, b.y);
+      }
+      const int c0 = 8 * t + 2 * tig;
+      p0 = fmaf(fmaxf(c[0] + N.b2[c0], 0.f), N.w3[c0], p0);
+      p0 = fmaf(fmaxf(c[1] + N.b2[c0 + 1], 0.f), N.w3[c0 + 1], p0);
+      p1 = fmaf(fmaxf(c[2] + N.b2[c0], 0.f), N.w3[c0], p1);
+      p1 = fmaf(fmaxf(c[3] + N.b2[c0 + 1], 0.f), N.w3[c0 + 1], p1);
+    }
+    p0 += __shfl_xor_sync(0xffffffffu, p0, 1);
+    p0 += __shfl_xor_sync(0xffffffffu, p0, 2);
+    p1 += __shfl_xor_sync(0xffffffffu, p1, 1);
+    p1 += __shfl_xor_sync(0xffffffffu, p1, 2);
+    const int r = lane - 16 * mt;  // this lane's row in the m-tile
+    const float q0 = __shfl_sync(0xffffffffu, p0, 4 * (r & 7));
+    const float q1 = __shfl_sync(0xffffffffu, p1, 4 * (r & 7));
+    if (r >= 0 && r < 16) zout = (r < 8 ? q0 : q1) + N.b3;
+  }
+  return zout;
+}
+
+// Network tables in shared memory from the bf16 parameter block: B
+// fragments of W1 (rows >= 42 zero) and W2, biases and output weights.
+__device__ __forceinline__ void lg_load_net(const __nv_bfloat16 *__restrict__ P, uint2 *fw1,
+                                            uint2 *fw2, float *fb, int tid, int nth) {
+  auto w1 = [&](int k, int j) -> __nv_bfloat16 {
+    return k < MLP_IN ? P[MLP_W1 + k * MLP_H + j] : __float2bfloat16_rn(0.f);
+  };
+  auto pair = [](__nv_bfloat16 lo, __nv_bfloat16 hi) -> uint32_t {
+    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+  };
+  for (int i = tid; i < LG_W1_FRAGS; i += nth) {
+    const int ln = i & 31, st = i >> 5, t = st & 7, s = st >> 3;
+    const int g = ln >> 2, tg = ln & 3, n = 8 * t + g, k = 16 * s + 2 * tg;
+    fw1[i] = make_uint2(pair(w1(k, n), w1(k + 1, n)), pair(w1(k + 8, n), w1(k + 9, n)));
+  }
+  const __nv_bfloat16 *W2 = P + MLP_W2;
+  for (int i = tid; i < LG_W2_FRAGS; i += nth) {
+    const int ln = i & 31, st = i >> 5, t = st & 7, s = st >> 3;
+    const int g = ln >> 2, tg = ln & 3, n = 8 * t + g, k = 16 * s + 2 * tg;
+    fw2[i] = make_uint2(pair(W2[k * MLP_H + n], W2[(k + 1) * MLP_H + n]),
+                        pair(W2[(k + 8) * MLP_H + n], W2[(k + 9) * MLP_H + n]));
+  }
+  for (int i = tid; i < MLP_H; i += nth) {
+    fb[i] = __bfloat162float(P[MLP_B1 + i]);
+    fb[64 + i] = __bfloat162float(P[MLP_B2 + i]);
+    fb[128 + i] = __bfloat162float(P[MLP_W3 + i]);
+  }
+  if (tid == 0) fb[192] = __bfloat162float(P[MLP_B3]);
+}
+
+// Inference of n environments (n x 42 occupants) on the tensor cores, the
+// path the group sweep uses: 32 environments per warp, layer-1 activations
+// rounded to bf16 as layer 2's operand.
+__global__ void k_mlp_forward_tc(const __nv_bfloat16 *__restrict__ params,
+                                 const int8_t *__restrict__ X, long long n, float *__restrict__ z) {
+  __shared__ uint2 fw1[LG_W1_FRAGS], fw2[LG_W2_FRAGS];
+  __shared__ float fb[200];
+  lg_load_net(params, fw1, fw2, fb, threadIdx.x, blockDim.x);
+  __syncthreads();
+  const LgNet net{fw1, fw2, fb, fb + 64, fb + 128, fb[192]};
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (long long tile = (long long)blockIdx.x * nw + warp; tile * 32 < n;
+       tile += (long long)gridDim.x * nw) {
+    const long long e = tile * 32 + lane;
+    unsigned long long env = 0ull;
+    if (e < n)
+      for (int k = 0; k < MLP_IN; ++k)
+        env |= (unsigned long long)(X[e * MLP_IN + k] != 0) << k;
+    const float zz = lg_network(net, env, lane);
+    if (e < n) z[e] = zz;
+  }
+}
+
+// a^-1 mod n for gcd(a, n) = 1 (extended Euclid)
+__device__ __forceinline__ uint32_t lg_inverse(uint32_t a, uint32_t n) {
+  long long t = 0, nt = 1, r = n, nr = a;
+  while (nr != 0) {
+    const long long q = r / nr;
+    long long tmp = t - q * nt;
+    t = nt;
+    nt = tmp;
+    tmp = r - q * nr;
+    r = nr;
+    nr = tmp;
+  }
+  if (t < 0) t += n;
+  return (uint32_t)t;
+}
+
+__device__ __forceinline__ uint32_t lg_gcd(uint32_t a, uint32_t b) {
+  while (b) {
+    const uint32_t t = a % b;
+    a = b;
+    b = t;
+  }
+  return a;
+}
+
+// Exact flip energy A -> B of a site from its cluster counts: int32 sum of the
+// integer weight multiples times the quantum, plus the f32 remainder chain.
+__device__ __forceinline__ float lg_eab(const CeTables &T, const int (&n)[gen_fcc::N_ORBITS]) {
+  int I = 0;
+  float r = 0.f;
+#pragma unroll
+  for (int g = 0; g < gen_fcc::N_ORBITS; ++g) {
+    I += T.wq[g] * n[g];
+    r = FFMA(T.wr[g], (float)n[g], r);
+  }
+  return FFMA((float)I, T.wq_scale, r);
+}
+
+template <int PITCH>
+__global__ void __launch_bounds__(LG_THREADS, 1)
+    k_lgroup(const __grid_constant__ CeTables T, const __grid_constant__ LGroupParams LP) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int L = PITCH - 4, RH = 2, M = L / 3;
+  static_assert(L % 6 == 0, "the learned group sweep needs L a multiple of 6");
+  constexpr int N_SITES = L * L * L, N_C = M * M * M, N_GROUPS = (N_C + 31) / 32;
+  constexpr int V = PITCH * PITCH * (L + 2 * RH);
+  const int rep = blockIdx.x;
+  const Replica &R = LP.reps[rep];
+  ReplicaStats &S = LP.stats[rep];
+  Geo G;
+  G.L0 = G.L1 = G.L2 = L;
+  G.R = RH;
+  G.W = G.H = PITCH;
+  G.V = V;
+  int8_t *occ = reinterpret_cast<int8_t *>(smem);
+  uint2 *fw1 = reinterpret_cast<uint2 *>(smem + align16(V));
+  uint2 *fw2 = fw1 + LG_W1_FRAGS;
+  float *fb = reinterpret_cast<float *>(fw2 + LG_W2_FRAGS);  // b1[64], b2[64], w3[64], b3
+  __shared__ int s_order[LG_CLASSES];
+  __shared__ uint32_t s_key[LG_CLASSES], s_ainv[LG_CLASSES], s_boff[LG_CLASSES];
+  __shared__ int s_local[64];  // class | parity << 5 | neighbour << 8
+  __shared__ int s_red[LG_NW][12];
+  __shared__ long long s_cnt[gen_fcc::N_ORBITS], s_sub[4], s_n1;
+  __shared__ double s_energy;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int mode = LP.mode;
+  const int rounds = LP.rounds, n_local = LP.n_local;
+  const float beta_f = R.beta_f;
+  const uint32_t k0 = (uint32_t)R.seed, k1 = (uint32_t)(R.seed >> 32);
+
+  if (mode == 1) lg_load_net(LP.params, fw1, fw2, fb, tid, LG_THREADS);
+  // ---- stage the replica with its periodic halo
+  const int8_t *gocc = LP.occ + R.occ_offset;
+  for (int l = tid; l < N_SITES; l += LG_THREADS) {
+    const int x = l % L, y = (l / L) % L, z = l / (L * L);
+    occ[G.addr(0, x, y, z)] = gocc[l];
+  }
+  __syncthreads();
+  for (int h = tid; h < V; h += LG_THREADS) {
+    const int xh = h % PITCH, yh = (h / PITCH) % PITCH, zh = h / (PITCH * PITCH);
+    const int x = xh - RH, y = yh - RH, z = zh - RH;
+    if (x >= 0 && x < L && y >= 0 && y < L && z >= 0 && z < L) continue;
+    occ[h] = occ[G.addr(0, wrapc(x, L), wrapc(y, L), wrapc(z, L))];
+  }
+  if (tid < gen_fcc::N_ORBITS) s_cnt[tid] = 0;
+  if (tid < 4) s_sub[tid] = 0;
+  if (tid == 0) s_n1 = 0;
+  __syncthreads();
+  // ---- exact initial energy (owned clusters) and species / sublattice counts
+  {
+    long long cnt[gen_fcc::N_ORBITS] = {0, 0, 0, 0, 0, 0};
+    long long sub[4] = {0, 0, 0, 0}, n1 = 0;
+    for (int l = tid; l < N_SITES; l += LG_THREADS) {
+      const int x = l % L, y = (l / L) % L, z = l / (L * L);
+      const int ad = G.addr(0, x, y, z);
+      if (!occ[ad]) continue;
+      int nn[gen_fcc::N_ORBITS];
+      gen_fcc::owned_counts<PITCH>(occ + ad, nn);
+      for (int g = 0; g < gen_fcc::N_ORBITS; ++g) cnt[g] += nn[g];
+      sub[sc_sublattice(x, y, z)]++;
+      ++n1;
+    }
+    for (int g = 0; g < gen_fcc::N_ORBITS; ++g)
+      atomicAdd((unsigned long long *)&s_cnt[g], (unsigned long long)cnt[g]);
+    for (int k = 0; k < 4; ++k) atomicAdd((unsigned long long *)&s_sub[k], (unsigned long long)sub[k]);
+    atomicAdd((unsigned long long *)&s_n1, (unsigned long long)n1);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double e = T.w[0] * (double)N_SITES;
+    for (int g = 0; g < T.n_orbits; ++g) e += T.w[T.orb_func_base[g]] * (double)s_cnt[g];
+    s_energy = e;
+    const long long pass = S.pass, np = S.n_proposed, na = S.n_accepted;
+    unsigned char *raw = reinterpret_cast<unsigned char *>(&S);
+    for (int q = 0; q < (int)sizeof(ReplicaStats); ++q) raw[q] = 0;
+    S.pass = pass;
+    S.n_proposed = np;
+    S.n_accepted = na;
+    S.n_species[0] = N_SITES - s_n1;
+    S.n_species[1] = s_n1;
+    for (int k = 0; k < 4; ++k) S.n_sub[k] = s_sub[k];
+  }
+  __syncthreads();
+
+  const LgNet net{fw1, fw2, fb, fb + 64, fb + 128, mode == 1 ? fb[192] : 0.f};
+  long long pass_global = S.pass;
+  long long nsub[4];
+  for (int k = 0; k < 4; ++k) nsub[k] = s_sub[k];
+  const long long n_b = s_n1;
+  for (long long ip = 0; ip < LP.n_passes; ++ip, ++pass_global) {
+    const uint32_t plo = (uint32_t)pass_global, phi = (uint32_t)(pass_global >> 32) & 0xFFFFu;
+    // ---- schedule: class order, group permutations, local sub-steps
+    if (tid < LG_CLASSES) {
+      const U4 r = philox4x32_10(U4{(uint32_t)tid, 0u, plo, phi | (TAG_LG_SCHED << 16)}, k0, k1);
+      s_key[tid] = r.x;
+      // multiplier coprime with N_C (bounded search; 1 always qualifies)
+      uint32_t a = 1u;
+      for (int tries = 0; tries < 8; ++tries) {
+        const U4 q = philox4x32_10(U4{(uint32_t)tid, 1u + (uint32_t)tries, plo, phi | (TAG_LG_SCHED << 16)},
+                                   k0, k1);
+        const uint32_t cand = 1u + q.x % (uint32_t)(N_C > 1 ? N_C - 1 : 1);
+        if (lg_gcd(cand, (uint32_t)N_C) == 1u) {
+          a = cand;
+          break;
+        }
+      }
+      s_ainv[tid] = N_C > 1 ? lg_inverse(a % (uint32_t)N_C, (uint32_t)N_C) : 0u;
+      s_boff[tid] = r.y % (uint32_t)N_C;
+    } else if (tid >= 32 && tid < 32 + n_local) {
+      const int j = tid - 32;
+      const U4 r = philox4x32_10(U4{(uint32_t)j, 2u, plo, phi | (TAG_LG_LOCAL << 16)}, k0, k1);
+      s_local[j] = (int)(r.x % LG_CLASSES) | (int)((r.y & 7u) << 5) | (int)((r.z % 12u) << 8);
+    }
+    __syncthreads();
+    if (tid < LG_CLASSES) {
+      int rank = 0;
+      for (int c2 = 0; c2 < LG_CLASSES; ++c2)
+        rank += (s_key[c2] < s_key[tid]) || (s_key[c2] == s_key[tid] && c2 < tid);
+      s_order[rank] = tid;
+    }
+    __syncthreads();
+
+    int n_prop = 0, n_acc = 0;
+    int dcn[gen_fcc::N_ORBITS] = {0, 0, 0, 0, 0, 0};
+    RegCounts<4> dsub;
+    // ---- group sub-steps
+    for (int sub = 0; sub < LG_CLASSES; ++sub) {
+      const int c = s_order[sub];
+      const int cx = c % 3, cy = (c / 3) % 3, cz = c / 9;
+      const uint32_t ainv = s_ainv[c], boff = s_boff[c];
+      for (int grp = warp; grp < N_GROUPS; grp += LG_NW) {
+        const int r = grp * 32 + lane;
+        const bool act = r < N_C;
+        int x = 0, y = 0, z = 0, ad = 0, o = 0;
+        int n[gen_fcc::N_ORBITS] = {0, 0, 0, 0, 0, 0};
+        unsigned long long env = 0ull;
+        if (act) {
+          const uint32_t q = (uint32_t)(((unsigned long long)ainv *
+                                         (unsigned long long)(((uint32_t)r + (uint32_t)N_C - boff) %
+                                                              (uint32_t)N_C)) %
+                                        (unsigned long long)N_C);
+          const int i = (int)(q % M), j = (int)((q / M) % M), k = (int)(q / (M * M));
+          x = cx + 3 * i;
+          y = cy + 3 * j;
+          z = cz + 3 * k;
+          ad = G.addr(0, x, y, z);
+          o = occ[ad];
+          gen_fcc::counts_env<PITCH>(occ + ad, n, env);
+        }
+        const float eab = lg_eab(T, n);
+        float zl = 0.f;
+        if (mode == 1) zl = lg_network(net, env, lane);
+        else if (mode == 2) zl = FMUL(-0.5f * beta_f, eab);
+        const uint32_t wA = mode ? (uint32_t)logit_weight(zl) : 1u;
+        const uint32_t wB = mode ? (uint32_t)logit_weight(-zl) : 1u;
+        const int o0 = o;
+        uint32_t wc = o ? wB : wA, wa = o ? wA : wB;
+        float eme = o ? -eab : eab;  // this member's flip energy in its current state
+        // this lane's round: two Philox blocks (64-bit uniforms for both
+        // draws, 24 bits for the acceptance)
+        unsigned long long ua_own = 0ull, ub_own = 0ull;
+        uint32_t uu_own = 0u;
+        if (lane < rounds) {
+          const uint32_t ctr = (uint32_t)grp | ((uint32_t)sub << 16);
+          const U4 p = philox4x32_10(U4{ctr, (uint32_t)lane, plo, phi | (TAG_LG_GROUP << 16)}, k0, k1);
+          const U4 p2 = philox4x32_10(U4{ctr, (uint32_t)lane | 0x100u, plo, phi | (TAG_LG_GROUP << 16)},
+                                      k0, k1);
+          ua_own = ((unsigned long long)p.x << 32) | p.y;
+          ub_own = ((unsigned long long)p.z << 32) | p.w;
+          uu_own = p2.x;
+        }
+        for (int t = 0; t < rounds; ++t) {
+          uint32_t sa = (act && o == 0) ? wc : 0u, sb = (act && o == 1) ? wc : 0u;
+#pragma unroll
+          for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t va = __shfl_up_sync(0xffffffffu, sa, off);
+            const uint32_t vb = __shfl_up_sync(0xffffffffu, sb, off);
+            if (lane >= off) {
+              sa += va;
+              sb += vb;
+            }
+          }
+          const uint32_t WA = __shfl_sync(0xffffffffu, sa, 31), WB = __shfl_sync(0xffffffffu, sb, 31);
+          if (WA == 0u || WB == 0u) break;  // one species absent from the group
+          const unsigned long long ua = shfl64(ua_own, t), ub = shfl64(ub_own, t);
+          const uint32_t uu = __shfl_sync(0xffffffffu, uu_own, t);
+          const uint32_t xa = (uint32_t)__umul64hi(ua, (unsigned long long)WA);
+          const uint32_t xb = (uint32_t)__umul64hi(ub, (unsigned long long)WB);
+          const int la = __ffs(__ballot_sync(0xffffffffu, sa > xa)) - 1;
+          const int lb = __ffs(__ballot_sync(0xffffffffu, sb > xb)) - 1;
+          const float ea = __shfl_sync(0xffffffffu, eme, la), eb = __shfl_sync(0xffffffffu, eme, lb);
+          const uint32_t wca = __shfl_sync(0xffffffffu, wc, la), waa = __shfl_sync(0xffffffffu, wa, la);
+          const uint32_t wcb = __shfl_sync(0xffffffffu, wc, lb), wab = __shfl_sync(0xffffffffu, wa, lb);
+          const uint32_t WA2 = WA - wca + wab, WB2 = WB - wcb + waa;
+          const float dE = FADD(ea, eb);
+          bool accept;
+          if (mode == 0) {
+            accept = accept_de(dE, beta_f, u24(uu));
+          } else {
+            // q_rev / q_fwd = (W_A W_B / (W_A' W_B')) (w'_a w'_b / (w_a w_b))
+            const float ratio = FMUL(FMUL(__fdiv_rn((float)WA, (float)WA2), __fdiv_rn((float)WB, (float)WB2)),
+                                     FMUL(__fdiv_rn((float)waa, (float)wca), __fdiv_rn((float)wab, (float)wcb)));
+            const float lr = FFMA(-beta_f, dE, logf(ratio));
+            accept = (lr >= 0.f) || (u24(uu) < cem_expf_neg(lr));
+          }
+          if (lane == 0) {
+            ++n_prop;
+            n_acc += accept ? 1 : 0;
+          }
+          if (accept && (lane == la || lane == lb)) {
+            o ^= 1;
+            eme = -eme;
+            const uint32_t tmp = wc;
+            wc = wa;
+            wa = tmp;
+          }
+        }
+        if (act && o != o0) {
+          put_site(occ, G, 0, x, y, z, (int8_t)o);
+          const int d = o - o0;
+#pragma unroll
+          for (int g = 0; g < gen_fcc::N_ORBITS; ++g) dcn[g] += d * n[g];
+          dsub.add(sc_sublattice(x, y, z), d);
+        }
+      }
+      __syncthreads();
+    }
+    // ---- nearest-neighbour swaps (plain Metropolis) between classes
+    constexpr int H = M / 2, N_ANCHOR = H * H * H;
+    for (int ls = 0; ls < n_local; ++ls) {
+      const int code = s_local[ls];
+      const int c = code & 31, par = (code >> 5) & 7, dl = code >> 8;
+      const int cx = c % 3, cy = (c / 3) % 3, cz = c / 9;
+      const int dx = gen_fcc::NB_D[dl][0], dy = gen_fcc::NB_D[dl][1], dz = gen_fcc::NB_D[dl][2];
+      for (int q = tid; q < N_ANCHOR; q += LG_THREADS) {
+        const int i = q % H, j = (q / H) % H, k = q / (H * H);
+        const int xa = cx + 3 * (2 * i + (par & 1)), ya = cy + 3 * (2 * j + ((par >> 1) & 1)),
+                  za = cz + 3 * (2 * k + ((par >> 2) & 1));
+        const int xb = wrapc(xa + dx, L), yb = wrapc(ya + dy, L), zb = wrapc(za + dz, L);
+        const int ada = G.addr(0, xa, ya, za), adb = G.addr(0, xb, yb, zb);
+        const int oa = occ[ada], ob = occ[adb];
+        if (oa == ob) continue;
+        const int la = xa + L * (ya + L * za);
+        const U4 rr = philox4x32_10(U4{(uint32_t)la, (uint32_t)(LG_CLASSES + ls), plo,
+                                       phi | (TAG_LG_LOCAL << 16)},
+                                    k0, k1);
+        // the first change is applied before either flower is read (a site's
+        // flower never contains the site): a sees the original state, b sees
+        // a changed, as for a sequence of two changes
+        put_site(occ, G, 0, xa, ya, za, (int8_t)ob);
+        int na[gen_fcc::N_ORBITS], nb[gen_fcc::N_ORBITS];
+        gen_fcc::counts<PITCH>(occ + ada, na);
+        gen_fcc::counts<PITCH>(occ + adb, nb);
+        const int d = ob - oa;  // a: oa -> ob, b: ob -> oa
+        int I = 0;
+        float rm = 0.f;
+        int dc[gen_fcc::N_ORBITS];
+#pragma unroll
+        for (int g = 0; g < gen_fcc::N_ORBITS; ++g) {
+          dc[g] = d * (na[g] - nb[g]);
+          I += T.wq[g] * dc[g];
+          rm = FFMA(T.wr[g], (float)dc[g], rm);
+        }
+        const float de = FFMA((float)I, T.wq_scale, rm);
+        ++n_prop;
+        if (accept_de(de, beta_f, u24(rr.x))) {
+          ++n_acc;
+          put_site(occ, G, 0, xb, yb, zb, (int8_t)oa);
+#pragma unroll
+          for (int g = 0; g < gen_fcc::N_ORBITS; ++g) dcn[g] += dc[g];
+          dsub.add(sc_sublattice(xa, ya, za), d);
+          dsub.add(sc_sublattice(xb, yb, zb), -d);
+        } else {
+          put_site(occ, G, 0, xa, ya, za, (int8_t)oa);
+        }
+      }
+      __syncthreads();
+    }
+    // ---- end of pass: reduce, update the exact running energy, sample
+    {
+      int vals[12];
+      vals[0] = n_prop;
+      vals[1] = n_acc;
+#pragma unroll
+      for (int g = 0; g < gen_fcc::N_ORBITS; ++g) vals[2 + g] = dcn[g];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) vals[8 + k] = dsub.v[k];
+#pragma unroll
+      for (int k = 0; k < 12; ++k)
+        for (int off = 16; off; off >>= 1) vals[k] += __shfl_xor_sync(0xffffffffu, vals[k], off);
+      if (lane == 0)
+        for (int k = 0; k < 12; ++k) s_red[warp][k] = vals[k];
+      __syncthreads();
+      if (tid == 0) {
+        long long tot[12];
+        for (int k = 0; k < 12; ++k) {
+          tot[k] = 0;
+          for (int w = 0; w < LG_NW; ++w) tot[k] += s_red[w][k];
+        }
+        double de = 0.0;
+        for (int g = 0; g < T.n_orbits; ++g) de += T.w[T.orb_func_base[g]] * (double)tot[2 + g];
+        s_energy += de;
+        S.n_proposed += tot[0];
+        S.n_accepted += tot[1];
+        for (int k = 0; k < 4; ++k) nsub[k] += tot[8 + k];
+        const double xb = (double)n_b / N_SITES;
+        double op = 0.0;
+        for (int k = 0; k < 4; ++k) {
+          const double cc = (double)nsub[k] / (0.25 * N_SITES) - xb;
+          op += cc * cc;
+        }
+        op = sqrt(op);
+        const double ef = s_energy / N_SITES;
+        if (ip >= LP.n_equil) {
+          S.n_samples += 1.0;
+          S.sum_e += ef;
+          S.sum_e2 += ef * ef;
+          S.sum_f += ef;
+          S.sum_x[0] += xb;
+          S.sum_xx[0] += xb * xb;
+          S.sum_ex[0] += ef * xb;
+          if (LP.samples) {
+            const long long si = (long long)S.n_samples - 1;
+            if (si < LP.sample_capacity) {
+              double *out = LP.samples + ((long long)rep * LP.sample_capacity + si) * 3;
+              out[0] = ef;
+              out[1] = xb;
+              out[2] = op;
+            }
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  // ---- write back
+  for (int l = tid; l < N_SITES; l += LG_THREADS) {
+    const int x = l % L, y = (l / L) % L, z = l / (L * L);
+    LP.occ[R.occ_offset + l] = occ[G.addr(0, x, y, z)];
+  }
+  if (tid == 0) {
+    S.energy = s_energy;
+    S.pass = pass_global;
+    for (int k = 0; k < 4; ++k) S.n_sub[k] = nsub[k];
+  }
+}
+
+cudaError_t mlp_forward_tc(const __nv_bfloat16 *params, const int8_t *X, long long n, float *z,
+                           cudaStream_t st) {
+  long long grid = (n + 255) / 256;
+  if (grid > 4096) grid = 4096;
+  if (grid < 1) grid = 1;
+  k_mlp_forward_tc<<<(int)grid, 256, 0, st>>>(params, X, n, z);
+  return cudaGetLastError();
+}
+
+int lgroup_smem_bytes(int L) {
+  const int pitch = L + 4;
+  return align16(pitch * pitch * pitch) + (LG_W1_FRAGS + LG_W2_FRAGS) * 8 + 200 * 4;
+}
+
+bool lgroup_supported(int L) { return L == 12 || L == 24 || L == 36 || L == 48; }
+
+cudaError_t lgroup_run(const CeTables &T, const Replica *reps, ReplicaStats *stats, int8_t *occ,
+                       const __nv_bfloat16 *params, int mode, int rounds, int n_local,
+                       int n_replicas, int L, long long n_passes, long long n_equil,
+                       double *samples, long long capacity, cudaStream_t st) {
+  LGroupParams LP{};
+  LP.reps = reps;
+  LP.stats = stats;
+  LP.occ = occ;
+  LP.params = params;
+  LP.mode = mode;
+  LP.rounds = rounds;
+  LP.n_local = n_local;
+  LP.n_passes = n_passes;
+  LP.n_equil = n_equil;
+  LP.samples = samples;
+  LP.sample_capacity = capacity;
+  const int smem = lgroup_smem_bytes(L);
+  cudaError_t e = cudaSuccess;
+  switch (L) {
+#define CEM_LGROUP_CASE(LL)                                                                      \
+  case LL:                                                                                       \
+    e = cudaFuncSetAttribute(k_lgroup<LL + 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem); \
+    if (e != cudaSuccess) return e;                                                              \
+    k_lgroup<LL + 4><<<n_replicas, LG_THREADS, smem, st>>>(T, LP);                               \
+    break;
+    CEM_LGROUP_CASE(12)
+    CEM_LGROUP_CASE(24)
+    CEM_LGROUP_CASE(36)
+    CEM_LGROUP_CASE(48)
+#undef CEM_LGROUP_CASE
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace cem

@@ -75,6 +75,64 @@ __device__ __forceinline__ void counts(const int8_t *__restrict__ c, int (&n)[N_
   n[5] = (v12 & v0) + (v12 & v1) + (v12 & v3) + (v12 & v4) + (v0 & v13) + (v0 & v4) + (v0 & v7) + (v1 & v14) + (v1 & v3) + (v1 & v8) + (v13 & v2) + (v13 & v5) + (v13 & v7) + (v2 & v14) + (v2 & v5) + (v2 & v6) + (v14 & v6) + (v14 & v8) + (v3 & v15) + (v3 & v10) + (v4 & v16) + (v4 & v11) + (v5 & v15) + (v5 & v9) + (v6 & v9) + (v6 & v16) + (v7 & v11) + (v7 & v17) + (v8 & v10) + (v8 & v17) + (v15 & v9) + (v15 & v10) + (v9 & v16) + (v16 & v11) + (v10 & v17) + (v11 & v17);
 }
 
+// the same counts, and the neighbour occupants packed into env (bit k =
+// neighbour k), the input of the proposal network
+template <int P>
+__device__ __forceinline__ void counts_env(const int8_t *__restrict__ c, int (&n)[N_ORBITS],
+                                           unsigned long long &env) {
+  const int v0 = c[(-1) + P * (0) + P * P * (0)];
+  const int v1 = c[(-1) + P * (0) + P * P * (1)];
+  const int v2 = c[(-1) + P * (1) + P * P * (0)];
+  const int v3 = c[(0) + P * (-1) + P * P * (0)];
+  const int v4 = c[(0) + P * (-1) + P * P * (1)];
+  const int v5 = c[(0) + P * (0) + P * P * (-1)];
+  const int v6 = c[(0) + P * (0) + P * P * (1)];
+  const int v7 = c[(0) + P * (1) + P * P * (-1)];
+  const int v8 = c[(0) + P * (1) + P * P * (0)];
+  const int v9 = c[(1) + P * (-1) + P * P * (0)];
+  const int v10 = c[(1) + P * (0) + P * P * (-1)];
+  const int v11 = c[(1) + P * (0) + P * P * (0)];
+  const int v12 = c[(-1) + P * (-1) + P * P * (1)];
+  const int v13 = c[(-1) + P * (1) + P * P * (-1)];
+  const int v14 = c[(-1) + P * (1) + P * P * (1)];
+  const int v15 = c[(1) + P * (-1) + P * P * (-1)];
+  const int v16 = c[(1) + P * (-1) + P * P * (1)];
+  const int v17 = c[(1) + P * (1) + P * P * (-1)];
+  const int v18 = c[(-2) + P * (0) + P * P * (1)];
+  const int v19 = c[(-2) + P * (1) + P * P * (0)];
+  const int v20 = c[(-2) + P * (1) + P * P * (1)];
+  const int v21 = c[(-1) + P * (-1) + P * P * (0)];
+  const int v22 = c[(-1) + P * (-1) + P * P * (2)];
+  const int v23 = c[(-1) + P * (0) + P * P * (-1)];
+  const int v24 = c[(-1) + P * (0) + P * P * (2)];
+  const int v25 = c[(-1) + P * (2) + P * P * (-1)];
+  const int v26 = c[(-1) + P * (2) + P * P * (0)];
+  const int v27 = c[(0) + P * (-2) + P * P * (1)];
+  const int v28 = c[(0) + P * (-1) + P * P * (-1)];
+  const int v29 = c[(0) + P * (-1) + P * P * (2)];
+  const int v30 = c[(0) + P * (1) + P * P * (-2)];
+  const int v31 = c[(0) + P * (1) + P * P * (1)];
+  const int v32 = c[(0) + P * (2) + P * P * (-1)];
+  const int v33 = c[(1) + P * (-2) + P * P * (0)];
+  const int v34 = c[(1) + P * (-2) + P * P * (1)];
+  const int v35 = c[(1) + P * (0) + P * P * (-2)];
+  const int v36 = c[(1) + P * (0) + P * P * (1)];
+  const int v37 = c[(1) + P * (1) + P * P * (-2)];
+  const int v38 = c[(1) + P * (1) + P * P * (0)];
+  const int v39 = c[(2) + P * (-1) + P * P * (-1)];
+  const int v40 = c[(2) + P * (-1) + P * P * (0)];
+  const int v41 = c[(2) + P * (0) + P * P * (-1)];
+  n[0] = 1;
+  n[1] = v0 + v1 + v2 + v3 + v4 + v5 + v6 + v7 + v8 + v9 + v10 + v11;
+  n[2] = v12 + v13 + v14 + v15 + v16 + v17;
+  n[3] = v18 + v19 + v20 + v21 + v22 + v23 + v24 + v25 + v26 + v27 + v28 + v29 + v30 + v31 + v32 + v33 + v34 + v35 + v36 + v37 + v38 + v39 + v40 + v41;
+  n[4] = (v0 & v1) + (v0 & v2) + (v0 & v3) + (v0 & v5) + (v1 & v2) + (v1 & v4) + (v1 & v6) + (v2 & v7) + (v2 & v8) + (v3 & v4) + (v3 & v5) + (v3 & v9) + (v4 & v6) + (v4 & v9) + (v5 & v7) + (v5 & v10) + (v6 & v8) + (v6 & v11) + (v7 & v8) + (v7 & v10) + (v8 & v11) + (v9 & v10) + (v9 & v11) + (v10 & v11);
+  n[5] = (v12 & v0) + (v12 & v1) + (v12 & v3) + (v12 & v4) + (v0 & v13) + (v0 & v4) + (v0 & v7) + (v1 & v14) + (v1 & v3) + (v1 & v8) + (v13 & v2) + (v13 & v5) + (v13 & v7) + (v2 & v14) + (v2 & v5) + (v2 & v6) + (v14 & v6) + (v14 & v8) + (v3 & v15) + (v3 & v10) + (v4 & v16) + (v4 & v11) + (v5 & v15) + (v5 & v9) + (v6 & v9) + (v6 & v16) + (v7 & v11) + (v7 & v17) + (v8 & v10) + (v8 & v17) + (v15 & v9) + (v15 & v10) + (v9 & v16) + (v16 & v11) + (v10 & v17) + (v11 & v17);
+  const unsigned lo = ((unsigned)v0 << 0) | ((unsigned)v1 << 1) | ((unsigned)v2 << 2) | ((unsigned)v3 << 3) | ((unsigned)v4 << 4) | ((unsigned)v5 << 5) | ((unsigned)v6 << 6) | ((unsigned)v7 << 7) | ((unsigned)v8 << 8) | ((unsigned)v9 << 9) | ((unsigned)v10 << 10) | ((unsigned)v11 << 11) | ((unsigned)v12 << 12) | ((unsigned)v13 << 13) | ((unsigned)v14 << 14) | ((unsigned)v15 << 15) | ((unsigned)v16 << 16) | ((unsigned)v17 << 17) | ((unsigned)v18 << 18) | ((unsigned)v19 << 19) | ((unsigned)v20 << 20) | ((unsigned)v21 << 21) | ((unsigned)v22 << 22) | ((unsigned)v23 << 23) | ((unsigned)v24 << 24) | ((unsigned)v25 << 25) | ((unsigned)v26 << 26) | ((unsigned)v27 << 27) | ((unsigned)v28 << 28) | ((unsigned)v29 << 29) | ((unsigned)v30 << 30) | ((unsigned)v31 << 31);
+  const unsigned hi = ((unsigned)v32 << 0) | ((unsigned)v33 << 1) | ((unsigned)v34 << 2) | ((unsigned)v35 << 3) | ((unsigned)v36 << 4) | ((unsigned)v37 << 5) | ((unsigned)v38 << 6) | ((unsigned)v39 << 7) | ((unsigned)v40 << 8) | ((unsigned)v41 << 9);
+  env = ((unsigned long long)hi << 32) | lo;
+}
+
 // owned[g] = number of clusters of orbit g anchored at this site (its
 // lexicographically smallest point) whose other sites are all 1
 template <int P>

@@ -291,14 +291,18 @@ int cem_set_option(cem_replicas *r, const char *key, int64_t value);
 int cem_get_option(cem_replicas *r, const char *key, int64_t *value);
 
 /* ---- Learned proposal (canonical swaps, binary FCC of the generated topology).
- * A network scores each site's environment (its 42 neighbours in the first three
- * shells, then its own occupant: 43 inputs) -> 64 -> 64 -> 1 logit z, with bf16
- * parameters and fp32 accumulation. Site weight w = max(1, round(4096 exp(z)))
- * with z clamped to [-12, 8]. A swap draws one A site and one B site with
- * probability proportional to w from per-species int64 sum trees; acceptance
- * min(1, exp(-beta dE) q_rev / q_fwd) with the exact proposal probabilities,
- * so the canonical distribution is sampled whatever the network predicts.
- * Parameter vector (fp32 masters): W1[43][64] (input-major), b1[64],
+ * A network scores each site's environment (its 42 neighbours in the first
+ * three shells, 0/1 occupants) -> 64 -> 64 -> 1 logit z, with bf16 parameters
+ * and fp32 accumulation, trained toward -beta dE_AB / 2 (dE_AB: energy change
+ * of putting B on the site in that environment). A site holding A has weight
+ * w = max(1, round(4096 exp(z))), a site holding B the same of -z, z clamped
+ * to [-10, 10]. cem_learned_run: a swap draws one A site and one B site with
+ * probability proportional to w from per-species int64 sum trees over the
+ * whole replica; acceptance min(1, exp(-beta dE) q_rev / q_fwd) with the exact
+ * proposal probabilities, so the canonical distribution is sampled whatever
+ * the network predicts. cem_learned_group_run: the same proposal inside
+ * groups of non-interacting sites, many swaps in flight per replica.
+ * Parameter vector (fp32 masters): W1[42][64] (input-major), b1[64],
  * W2[64][64] (input-major), b2[64], w3[64], b3. No counterpart in the
  * reference (its canonical proposal is uniform, CanonicalCalculator.cc:78-83). */
 typedef struct cem_mlp cem_mlp;
@@ -307,8 +311,12 @@ int cem_mlp_create(uint64_t seed, cem_mlp **out);
 int cem_mlp_destroy(cem_mlp *m);
 int cem_mlp_get_params(cem_mlp *m, float *master);
 int cem_mlp_set_params(cem_mlp *m, const float *master);
-/* logits of n environments (n x 43 int8 occupants) */
+/* logits of n environments (n x 42 int8 occupants) */
 int cem_mlp_forward(cem_mlp *m, int64_t n, const int8_t *features, float *logits);
+/* the same logits on the tensor cores (mma.sync, bf16 operands, fp32
+ * accumulation; layer-1 activations rounded to bf16 as layer 2's operand):
+ * the inference path of cem_learned_group_run */
+int cem_mlp_forward_tc(cem_mlp *m, int64_t n, const int8_t *features, float *logits);
 /* gradient of the mean-squared error 1/(2n) sum (z - t)^2 at the current
  * (bf16) parameters, and the loss */
 int cem_mlp_gradient(cem_mlp *m, int64_t n, const int8_t *features, const float *targets,
@@ -316,9 +324,9 @@ int cem_mlp_gradient(cem_mlp *m, int64_t n, const int8_t *features, const float 
 /* Adam (Kingma & Ba 2015) on the same loss, minibatches in a seeded order */
 int cem_mlp_train(cem_mlp *m, int64_t n, const int8_t *features, const float *targets,
                   int epochs, int batch, float lr, uint64_t seed, double *loss_per_epoch);
-/* Environments of every site of a replica and the training target
- * t = clamp(-beta dE_flip / 2, -12, 8) (half the log Metropolis weight of
- * flipping the site), from the device occupation. */
+/* Environments of every site of a replica (n_sites x 42) and the training
+ * target t = clamp(-beta dE_AB / 2, -10, 10) (half the log Metropolis weight
+ * of putting B on the site), from the device occupation. */
 int cem_learned_features(cem_replicas *r, int replica, int8_t *features, float *targets);
 /* n_passes x n_sites proposals per replica with the learned proposal
  * (m == NULL: every weight 1, i.e. the uniform global swap proposal).
@@ -326,6 +334,32 @@ int cem_learned_features(cem_replicas *r, int replica, int8_t *features, float *
  * sqrt(sum_k (x_k - x)^2) over the four simple-cubic sublattices. */
 int cem_learned_run(cem_replicas *r, const cem_mlp *m, int64_t n_passes, int64_t n_equil,
                     int record_samples);
+/* Learned group sweep: n_passes passes per replica of a parallel canonical
+ * sampler in which the proposal weights choose the swaps. A pass visits the 27
+ * colour classes of period 3 (sites whose cell coordinates agree modulo 3: no
+ * two share a cluster) in a random order; each class is split into groups of
+ * 32 sites by a random permutation drawn per sub-step, and each group runs
+ * `rounds` Metropolis-Hastings swaps: one A site drawn with probability
+ * w_A / W_A and one B site with w_B / W_B among the group's members, accepted
+ * with min(1, exp(-beta dE) q_rev / q_fwd) from the exact integer weights and
+ * totals (the members do not interact, so dE is the sum of the two sites'
+ * exact flip energies and only the two swapped sites change weight). Then
+ * `local_substeps` sub-steps of nearest-neighbour swaps (plain Metropolis)
+ * move atoms between classes, which keeps the chain ergodic.
+ * weights: 0 every weight 1 (uniform swaps inside groups); 1 the network m
+ * (w_A = round(2^12 exp(z)), w_B = round(2^12 exp(-z)) of the site's
+ * environment logit z, evaluated once per site and sub-step on the tensor
+ * cores); 2 the exact locally balanced weights, z = -beta dE_AB / 2, the
+ * quantity the network is trained to predict. rounds 1..CEM_LGROUP_MAX_ROUNDS,
+ * local_substeps 1..CEM_LGROUP_MAX_LOCAL. Equal cubic supercells of 12, 24,
+ * 36 or 48 cells. Samples per pass as cem_learned_run (cem_learned_samples);
+ * statistics as cem_run (cem_get_stats). No counterpart in the reference (its
+ * canonical proposal is uniform, CanonicalCalculator.cc:78-83). */
+#define CEM_LGROUP_MAX_ROUNDS 32
+#define CEM_LGROUP_MAX_LOCAL 64
+int cem_learned_group_run(cem_replicas *r, const cem_mlp *m, int weights, int rounds,
+                          int local_substeps, int64_t n_passes, int64_t n_equil,
+                          int record_samples);
 int cem_learned_samples(cem_replicas *r, int replica, double *energy, double *order,
                         int64_t capacity, int64_t *n_samples);
 

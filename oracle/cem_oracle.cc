@@ -1272,6 +1272,39 @@ double ora_run_threads(void *h, signed char *occ, int n_rep, int ensemble, const
   return std::chrono::duration<double>(t1 - t0).count();
 }
 
+// Independent sequential chains with their per-pass samples: chain r runs on
+// occupation block r with engine seed + r (the loop of ora_run, i.e.
+// occupation_metropolis.hh:92-120 restated); chains are spread over n_threads
+// host threads. samp_potential [n_rep][n_passes] and samp_comp
+// [n_rep][n_passes][n_occ - 1] receive potential energy and param
+// composition per unit cell after each pass. Returns wall seconds, or -1 on
+// error (ora_last_error).
+double ora_run_chains(void *h, signed char *occ, int n_rep, int ensemble, const double *temps,
+                      const double *mus, u64 seed, i64 n_passes, int n_threads,
+                      double *samp_potential, double *samp_comp) {
+  System &s = *(System *)h;
+  auto t0 = std::chrono::steady_clock::now();
+  std::vector<std::thread> th;
+  std::vector<int> rc(n_rep, 0);
+  const int nc = s.n_occ - 1;
+  int nt = std::max(1, std::min(n_threads, n_rep));
+  for (int w = 0; w < nt; ++w)
+    th.emplace_back([&, w]() {
+      for (int r = w; r < n_rep; r += nt) {
+        rc[r] = ora_run(h, occ + (size_t)r * s.n_sites, ensemble, temps[r], mus + r * nc,
+                        seed + r, n_passes, 0, nullptr, nullptr, nullptr, nullptr, nullptr,
+                        samp_potential ? samp_potential + (size_t)r * n_passes : nullptr,
+                        samp_comp ? samp_comp + (size_t)r * n_passes * nc : nullptr, nullptr,
+                        nullptr);
+      }
+    });
+  for (auto &t : th) t.join();
+  for (int r = 0; r < n_rep; ++r)
+    if (rc[r]) return -1.0;
+  auto t1 = std::chrono::steady_clock::now();
+  return std::chrono::duration<double>(t1 - t0).count();
+}
+
 // ---- random-stream probes used to pin the transforms the GPU restates.
 void ora_mt19937_64(u64 seed, i64 n, u64 *out) {
   std::mt19937_64 e(seed);

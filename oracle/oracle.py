@@ -81,6 +81,11 @@ def lib():
             P, i8p, C.c_int, C.c_int, f64p, f64p, C.c_uint64, C.c_int64, C.c_int,
             C.POINTER(C.c_int64),
         ]
+        L.ora_run_chains.restype = C.c_double
+        L.ora_run_chains.argtypes = [
+            P, i8p, C.c_int, C.c_int, f64p, f64p, C.c_uint64, C.c_int64, C.c_int,
+            C.c_void_p, C.c_void_p,
+        ]
         L.ora_enforce_composition.restype = C.c_int64
         L.ora_enforce_composition.argtypes = [P, i8p, f64p, C.c_uint64, u64p]
         L.ora_exp_neg.restype = C.c_double
@@ -262,6 +267,24 @@ class OracleSystem:
             raise RuntimeError(lib().ora_last_error().decode())
         return dict(n=int(n), site=rec_site[:record], occ=rec_occ[:record], dt=rec_dt[:record],
                     stats=st)
+
+    def run_chains(self, occ, ensemble, temps, mus, seed, n_passes, n_threads):
+        """Independent sequential chains (chain r: block r of ``occ``, updated
+        in place, engine seed + r), spread over ``n_threads`` host threads.
+        Returns (potential [n_rep, n_passes], comp [n_rep, n_passes, n_occ-1],
+        wall seconds) with the per-unit-cell samples after every pass."""
+        nrep = len(temps)
+        nc = self.ce.prim.n_occ - 1
+        assert occ.dtype == np.int8 and occ.flags.c_contiguous and occ.size == nrep * self.n_sites
+        pot = np.zeros((nrep, n_passes))
+        comp = np.zeros((nrep, n_passes, nc))
+        secs = lib().ora_run_chains(
+            self.h, occ, nrep, int(ensemble), np.ascontiguousarray(temps, dtype=np.float64),
+            np.ascontiguousarray(mus, dtype=np.float64).reshape(-1), int(seed), int(n_passes),
+            int(n_threads), _ptr(pot), _ptr(comp))
+        if secs < 0:
+            raise RuntimeError(lib().ora_last_error().decode())
+        return pot, comp, secs
 
     def run_threads(self, occ, ensemble, temps, mus, seed, n_passes, n_threads):
         nrep = len(temps)

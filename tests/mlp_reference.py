@@ -1,10 +1,10 @@
-"""FP64 reference of the proposal network (43 -> 64 -> 64 -> 1, ReLU) used
+"""FP64 reference of the proposal network (42 -> 64 -> 64 -> 1, ReLU) used
 to check the GPU inference and gradient kernels. The GPU computes with bf16
 parameters, so the reference rounds the fp32 parameters to bf16 first."""
 
 import numpy as np
 
-N_IN, H = 43, 64
+N_IN, H = 42, 64
 
 
 def bf16_round(p):
@@ -51,3 +51,12 @@ def gradient(p, X, t):
     db1 = d1.sum(0)
     g = np.concatenate([dW1.ravel(), db1, dW2.ravel(), db2, dw3, [db3]])
     return g, 0.5 * float(np.mean(r * r))
+
+
+def forward_bf16_hidden(p, X):
+    """The tensor-core inference path: layer-1 activations rounded to bf16
+    before layer 2 (parameters already bf16-rounded by the caller)."""
+    W1, b1, W2, b2, w3, b3 = unpack(p)
+    h1 = bf16_round(np.maximum(b1 + X @ W1, 0).astype(np.float32))
+    h2 = np.maximum(b2 + h1 @ W2, 0)
+    return b3 + h2 @ w3
