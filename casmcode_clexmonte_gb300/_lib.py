@@ -15,6 +15,7 @@ import numpy as np
 from .build import LIB
 
 CEM_OK = 0
+CEM_STOPPED = 5  # cem_synchronize: the run was stopped early (not an error)
 CEM_SEMIGRAND_CANONICAL = 0
 CEM_CANONICAL = 1
 
@@ -53,7 +54,7 @@ EXPORTS = [
     "cem_set_seed", "cem_set_occupation", "cem_get_occupation", "cem_set_occupation_all",
     "cem_get_occupation_all", "cem_host_alloc", "cem_host_free", "cem_energy",
     "cem_delta_energy", "cem_replay", "cem_enforce_composition", "cem_nfold_run", "cem_run", "cem_get_stats", "cem_get_samples",
-    "cem_reset_stats", "cem_synchronize", "cem_last_kernel_ms", "cem_smem_bandwidth",
+    "cem_reset_stats", "cem_synchronize", "cem_request_stop", "cem_last_kernel_ms", "cem_smem_bandwidth",
     "cem_set_option", "cem_get_option", "cem_autotune", "cem_step_async", "cem_delta_energy_noalloc",
     "cem_mlp_info", "cem_mlp_create", "cem_mlp_destroy", "cem_mlp_get_params",
     "cem_mlp_set_params", "cem_mlp_forward", "cem_mlp_forward_tc", "cem_mlp_gradient", "cem_mlp_train",

@@ -54,7 +54,31 @@ def build(force: bool = False, verbose: bool = False) -> str:
         if verbose:
             print(" ".join(cmd))
         subprocess.run(cmd, check=True)
+    build_plugin(force, verbose)
     return LIB
+
+
+PLUGIN_DIR = os.path.join(HERE, "plugin")
+PLUGIN = os.path.join(BUILD, "libcem_plugin.so")
+PLUGIN_SOURCES = ["GpuMonteCalculator.cc", "plugin_capi.cc"]
+
+
+def build_plugin(force: bool = False, verbose: bool = False) -> str:
+    """The C++ calculator plugin (BaseMonteCalculator adaptors and their C
+    entry points) over the C ABI of ``libcem_gb300.so``, with g++."""
+    srcs = [os.path.join(PLUGIN_DIR, f) for f in PLUGIN_SOURCES]
+    deps = srcs + [os.path.join(ROOT, "include", "cem.h"), LIB]
+    for d, _, files in os.walk(os.path.join(PLUGIN_DIR, "shim")):
+        deps += [os.path.join(d, f) for f in files]
+    if force or _stale(PLUGIN, deps):
+        cxx = os.environ.get("CXX", "g++")
+        cmd = [cxx, "-std=c++17", "-O2", "-fPIC", "-shared", "-I", os.path.join(ROOT, "include"),
+               "-I", os.path.join(PLUGIN_DIR, "shim"), *srcs, "-o", PLUGIN, "-L", BUILD,
+               "-lcem_gb300", "-Wl,-rpath,$ORIGIN"]
+        if verbose:
+            print(" ".join(cmd))
+        subprocess.run(cmd, check=True)
+    return PLUGIN
 
 
 if __name__ == "__main__":

@@ -209,8 +209,19 @@ class ReplicaBatch:
         check(self.lib.cem_get_option(self.handle, key.encode(), C.byref(v)))
         return v.value
 
-    def synchronize(self):
-        check(self.lib.cem_synchronize(self.handle))
+    def synchronize(self) -> bool:
+        """Wait for the batch's work; True when the last run was stopped early
+        by ``request_stop``."""
+        rc = self.lib.cem_synchronize(self.handle)
+        if rc == _lib.CEM_STOPPED:
+            return True
+        check(rc)
+        return False
+
+    def request_stop(self):
+        """Ask the run in flight to stop at its next pass boundary (may be
+        called from another thread while ``synchronize`` waits)."""
+        check(self.lib.cem_request_stop(self.handle))
 
     def get_state(self, i: int):
         """(occupation, state bytes) checkpoint of replica i."""
@@ -405,13 +416,40 @@ class MonteCarloState:
 
 @dataclass
 class SamplingFixtureParams:
-    """Fixed-length sampling: ``n_passes`` passes, statistics over the
-    passes after the first ``n_equil`` (one sample per pass, like a
-    sampling period of one pass in the reference's fixtures)."""
+    """Sampling fixture: one sample per pass (a sampling period of one pass
+    in the reference's fixtures) after ``n_equil`` unsampled passes.
+
+    Without ``requested_precision`` the run has a fixed length of
+    ``n_passes`` passes. With it (absolute precisions, e.g.
+    ``{"potential_energy": 0.001}`` as the reference's default canonical
+    fixture, CanonicalCalculator.cc:261-270, or also "param_composition"),
+    the run stops at the first completion check, every ``check_period``
+    sampled passes, at which every requested quantity is equilibrated (the
+    two-partition test of ``casm_io.equilibration_index``) and its calculated
+    precision over the equilibrated tail, z(confidence) x the standard error
+    corrected by the integrated autocorrelation time, is within the request;
+    ``n_passes`` is then the cutoff (maximum passes) and ``min_samples`` the
+    fewest samples checked."""
 
     n_passes: int = 1000
     n_equil: int = 200
     record_samples: bool = True
+    requested_precision: dict | None = None
+    check_period: int = 100
+    min_samples: int = 100
+    confidence: float = 0.95
+
+
+def _tail_moments(e, x) -> dict:
+    """The moments ``ReplicaBatch.stats`` reports, over given samples of the
+    potential energy per unit cell and param composition."""
+    e = np.asarray(e, dtype=np.float64)
+    x = np.asarray(x, dtype=np.float64).reshape(e.size, -1)
+    de = e - e.mean()
+    dx = x - x.mean(axis=0)
+    return dict(n_samples=float(e.size), mean_potential=float(e.mean()),
+                var_potential=float(np.mean(de * de)), mean_comp=x.mean(axis=0),
+                cov_comp=(dx.T @ dx) / e.size, cov_e_comp=(dx.T @ de) / e.size)
 
 
 def analyses(stats: dict, temperature: float, n_unitcells: int) -> dict:
@@ -515,17 +553,89 @@ class MonteCalculator:
 
     def run_fixture(self, state: MonteCarloState, sampling_fixture_params: SamplingFixtureParams):
         """Parallel Metropolis run; updates ``state.occupation`` and returns
-        the sampled statistics and analyses."""
+        the sampled statistics and analyses (with requested precisions, also
+        the completion-check results: ``count``, ``is_converged`` per
+        quantity, ``N_samples_for_equilibration``)."""
         p = sampling_fixture_params
         self._bind(state)
         b = self._batch
-        b.run(p.n_passes, p.n_equil, p.record_samples)
-        st = b.stats(0)
-        state.occupation[:] = b.get_occupation(0)
         L = state.L
         n_uc = int(L[0] * L[1] * L[2])
+        T = state.conditions["temperature"]
+        if not p.requested_precision:
+            b.run(p.n_passes, p.n_equil, p.record_samples)
+            st = b.stats(0)
+            state.occupation[:] = b.get_occupation(0)
+            res = dict(st)
+            res.update(analyses(st, T, n_uc))
+            if p.record_samples:
+                res["samples_potential"], res["samples_comp"] = b.samples(0, p.n_passes)
+            return res
+        return self._run_to_precision(state, p, n_uc, T)
+
+    def _run_to_precision(self, state, p, n_uc, T):
+        """Completion-checked run (CanonicalCalculator.cc:261-270): chunks of
+        ``check_period`` sampled passes until every requested quantity is
+        equilibrated and within its requested absolute precision, or the
+        cutoff of ``n_passes`` passes."""
+        from . import casm_io
+        from .stats import mean_error
+
+        b = self._batch
+        z = casm_io._z(p.confidence)
+        req = dict(p.requested_precision)
+        unknown = set(req) - {"potential_energy", "param_composition"}
+        if unknown:
+            raise ValueError(f"requested precision for unknown quantities: {sorted(unknown)}")
+        if p.n_equil > 0:
+            b.run(p.n_equil, p.n_equil)  # unsampled passes
+        b.reset_stats()
+        pots, comps = [], []
+        count = p.n_equil
+        max_count = max(p.n_passes, p.n_equil + 1)
+        done = False
+        conv = {}
+        eq_at = None
+        while not done and count < max_count:
+            chunk = min(p.check_period, max_count - count)
+            b.run(chunk, 0, record_samples=True)
+            pot, comp = b.samples(0, chunk)
+            pots.append(pot)
+            comps.append(comp)
+            count += chunk
+            e = np.concatenate(pots)
+            x = np.concatenate(comps).reshape(e.size, -1)
+            if e.size < p.min_samples:
+                continue
+            series = []
+            if "potential_energy" in req:
+                series.append(("potential_energy", e, req["potential_energy"]))
+            if "param_composition" in req:
+                series += [("param_composition", x[:, k], req["param_composition"])
+                           for k in range(x.shape[1])]
+            starts = [casm_io.equilibration_index(v, r) for _, v, r in series]
+            if any(s0 is None for s0 in starts):
+                continue
+            eq_at = max(starts)
+            conv = {}
+            for (name, v, r) in series:
+                prec = z * mean_error(v[eq_at:])[1]
+                conv[name] = conv.get(name, True) and bool(prec <= r)
+            done = all(conv.values())
+        state.occupation[:] = b.get_occupation(0)
+        e = np.concatenate(pots)
+        x = np.concatenate(comps).reshape(e.size, -1)
+        s0 = eq_at if eq_at is not None else 0
+        st = dict(b.stats(0))
+        st.update(_tail_moments(e[s0:], x[s0:]))
+        st["mean_formation"] = st["mean_potential"]
+        if self.method == "semigrand_canonical":  # E_f = E_pot + mu . x per unit cell
+            mu = np.atleast_1d(np.asarray(state.conditions["param_chem_pot"], dtype=float))
+            st["mean_formation"] = st["mean_potential"] + float(mu @ st["mean_comp"])
         res = dict(st)
-        res.update(analyses(st, state.conditions["temperature"], n_uc))
-        if p.record_samples:
-            res["samples_potential"], res["samples_comp"] = b.samples(0, p.n_passes)
+        res.update(analyses(st, T, n_uc))
+        res.update(count=count, is_converged=conv, all_converged=bool(done),
+                   N_samples_for_equilibration=None if eq_at is None else int(eq_at),
+                   requested_precision=req)
+        res["samples_potential"], res["samples_comp"] = e[s0:], x[s0:]
         return res

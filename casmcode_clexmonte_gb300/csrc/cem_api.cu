@@ -2,7 +2,10 @@
 // transfers and launches. See include/cem.h for the contract.
 #include <cuda_runtime.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -36,6 +39,15 @@ struct Err : std::runtime_error {
     if (e_ != cudaSuccess)                                                            \
       throw Err(CEM_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));      \
   } while (0)
+
+// NVTX range over a host call (shows the library's runs on a profiler's
+// timeline; costs nothing when no tool is attached)
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 template <class F>
 int guard(F &&f) {
@@ -105,6 +117,10 @@ struct cem_replicas {
   const cem_system *sys = nullptr;
   int n = 0, ensemble = 0;
   int device = 0;  // the device current when the batch was created
+  // stop flag of the running sweep: page-locked host memory mapped into the
+  // device's address space; the persistent kernels read it once per pass
+  volatile int *h_stop = nullptr;
+  int *d_stop = nullptr;
   std::vector<Replica> reps;
   std::vector<ReplicaStats> stats_host;
   Replica *d_reps = nullptr;
@@ -123,6 +139,8 @@ struct cem_replicas {
   int threads = SWEEP_THREADS;
   // replica -> CTA schedule: 0 = CTA i runs replica i, 1 = largest replicas first
   int cta_order = 0;
+  // CTAs per replica of the learned group sweep (0 automatic) and the last used
+  int group_cluster = 0, last_group_cluster = 0;
   int *d_cta_rep = nullptr;
   bool reps_dirty = true, stats_valid = false;
   cudaStream_t stream = nullptr;
@@ -169,6 +187,7 @@ struct cem_replicas {
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (stream) cudaStreamDestroy(stream);
+    if (h_stop) cudaFreeHost(const_cast<int *>(h_stop));
   }
   void upload_reps() {
     if (!reps_dirty) return;
@@ -631,6 +650,13 @@ int cem_replicas_create(const cem_system *sys, int n, const int *L, int ensemble
     CUDA_OK(cudaMalloc(&r->d_counts, sizeof(unsigned long long) * (MAX_FUNCS + 8)));
     CUDA_OK(cudaMalloc(&r->d_result, sizeof(long long) * 4));
     r->sample_width = sys->T.n_occ + 1;  // potential, (n_occ-1) compositions, order parameter
+    {
+      int *h = nullptr;
+      CUDA_OK(cudaHostAlloc(&h, sizeof(int), cudaHostAllocMapped));
+      *h = 0;
+      r->h_stop = h;
+      CUDA_OK(cudaHostGetDevicePointer(reinterpret_cast<void **>(&r->d_stop), h, 0));
+    }
     *out = r.release();
   });
 }
@@ -1142,6 +1168,8 @@ int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_sampl
                 " bytes needed) and has no HBM-streamed kernel",
             CEM_ERR_UNSUPPORTED);
     r->upload_reps();
+    *r->h_stop = 0;  // a stop request applies to the run in flight
+    NvtxRange nvtx("cem_run");
     if (r->streamed) {
       const int L = r->reps[0].L[0];
       const long long hb = stream_halo_bytes(L, r->stream_pitch);
@@ -1190,13 +1218,14 @@ int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_sampl
       }
       double RT[16] = {0};
       for (size_t k = 0; k < r->sys->RT.size() && k < 16; ++k) RT[k] = r->sys->RT[k];
+      long long launched = 0;
       CUDA_OK(stream_run(r->sys->T, r->sstate, r->d_reps, r->d_stats, r->d_occ, r->n, L,
                          r->stream_pitch, r->max_classes,
                          r->ensemble == CEM_CANONICAL ? r->n_pair_sweeps : 0,
                          r->ensemble == CEM_CANONICAL ? r->n_local_sweeps : 1, RT, n_passes, n_equil,
                          r->stream_pass, samples, cap, r->sample_width, fresh ? 1 : 0, r->stream,
-                         r->ev0, r->ev1));
-      r->stream_pass += n_passes;
+                         r->ev0, r->ev1, r->h_stop, &launched));
+      r->stream_pass += launched;
       return;
     }
     // binary systems compute the exact initial stats inside the sweep kernel
@@ -1217,6 +1246,7 @@ int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_sampl
     P.n_pair_sweeps = r->n_pair_sweeps;
     P.n_local_sweeps = r->n_local_sweeps;
     P.cta_rep = r->d_cta_rep;
+    P.stop = r->d_stop;
     const CeTables &T = r->sys->T;
     for (size_t k = 0; k < r->sys->RT.size() && k < 16; ++k) P.RT[k] = r->sys->RT[k];
     if (record_samples) {
@@ -1400,6 +1430,12 @@ int cem_set_option(cem_replicas *r, const char *key, int64_t value) {
       r->threads = (int)value;
     } else if (k == "cta_order") {
       set_cta_order(r, (int)value);
+    } else if (k == "group_cluster") {
+      // CTAs per replica of the learned group sweep (0: as many of 4, 2, 1
+      // as keep every replica's cluster on its own SMs)
+      require(value == 0 || value == 1 || value == 2 || value == 4,
+              "group_cluster must be 0 (automatic), 1, 2 or 4");
+      r->group_cluster = (int)value;
     } else if (k == "orbit_walk") {
       // the kernels of large cluster expansions, also for small ones:
       // 1 = one thread per site walking the tables one orbit at a time,
@@ -1441,6 +1477,7 @@ int cem_get_option(cem_replicas *r, const char *key, int64_t *value) {
     else if (k == "streamed") *value = r->streamed ? 1 : 0;
     else if (k == "threads") *value = r->threads;
     else if (k == "cta_order") *value = r->cta_order;
+    else if (k == "group_cluster") *value = r->last_group_cluster;
     else throw Err(CEM_ERR_INVALID, "unknown option '" + k + "'");
   });
 }
@@ -1512,10 +1549,20 @@ int cem_get_order_samples(cem_replicas *r, int i, double *order, int64_t capacit
 }
 
 int cem_synchronize(cem_replicas *r) {
-  return guard([&] {
+  int stopped = 0;
+  const int rc = guard([&] {
     require(r != nullptr, "null handle");
     CUDA_OK(cudaStreamSynchronize(r->stream));
+    stopped = *r->h_stop;
   });
+  return rc == CEM_OK && stopped ? CEM_STOPPED : rc;
+}
+
+int cem_request_stop(cem_replicas *r) {
+  if (!r) return CEM_ERR_INVALID;
+  *r->h_stop = 1;
+  std::atomic_thread_fence(std::memory_order_seq_cst);
+  return CEM_OK;
 }
 
 int cem_last_kernel_ms(cem_replicas *r, double *ms) {
@@ -1861,7 +1908,11 @@ int cem_learned_features(cem_replicas *r, int i, int8_t *features, float *target
   return guard([&] {
     check_rep(r, i);
     require(features && targets, "null argument");
-    require_learned(r);
+    require(r->sys->fcc_generated && r->ensemble == CEM_CANONICAL,
+            "the learned proposal supports canonical binary FCC systems of the generated topology",
+            CEM_ERR_UNSUPPORTED);
+    require(r->reps[i].L[0] == r->reps[i].L[1] && r->reps[i].L[1] == r->reps[i].L[2],
+            "features need a cubic supercell", CEM_ERR_UNSUPPORTED);
     const Replica &R = r->reps[i];
     const int n = R.n_sites;
     int8_t *dx = nullptr;
@@ -1979,10 +2030,19 @@ int cem_learned_group_run(cem_replicas *r, const cem_mlp *m, int weights, int ro
       cap = r->lsample_capacity;
       r->lsamples_recorded = std::max<long long>(0, n_passes - n_equil);
     }
+    int cl = r->group_cluster;
+    if (cl == 0) {
+      int sms = 0;
+      CUDA_OK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+      cl = (4 * r->n <= sms) ? 4 : ((2 * r->n <= sms) ? 2 : 1);
+    }
+    r->last_group_cluster = cl;
+    *r->h_stop = 0;
+    NvtxRange nvtx("cem_learned_group_run");
     CUDA_OK(cudaEventRecord(r->ev0, r->stream));
     CUDA_OK(lgroup_run(r->sys->T, r->d_reps, r->d_stats, r->d_occ,
                        weights == 1 ? m->d_params : nullptr, weights, rounds, local_substeps, r->n,
-                       L, n_passes, n_equil, samples, cap, r->stream));
+                       L, n_passes, n_equil, samples, cap, r->d_stop, cl, r->stream));
     CUDA_OK(cudaEventRecord(r->ev1, r->stream));
     r->stats_valid = false;  // the sweep recomputes its own state next time
   });

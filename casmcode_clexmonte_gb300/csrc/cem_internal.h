@@ -43,6 +43,7 @@ struct SweepParams {
   int init;                    // binary systems: compute the exact initial stats in-kernel
   int pack16;                  // cooperative sweep: 16-bit partner offsets and weights
   const int *cta_rep;          // replica of each CTA (null: CTA i runs replica i)
+  const volatile int *stop;    // host-mapped stop flag (null: none)
   double RT[16];               // (n_occ-1) x n_occ
 };
 
@@ -92,7 +93,8 @@ cudaError_t stream_run(const CeTables &T, StreamState &st, const Replica *reps, 
                        int8_t *occ_all, int n_rep, int L2, int pitch, int n_classes, int n_pair_sw,
                        int n_local_sw, const double *RT, long long n_passes, long long n_equil,
                        long long start_pass, double *samples, long long capacity, int width,
-                       int count_sub, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1);
+                       int count_sub, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1,
+                       const volatile int *stop_host, long long *launched);
 
 // learned proposal (cem_learned.cu)
 struct TreeGeo;
@@ -122,7 +124,8 @@ int lgroup_smem_bytes(int L);
 cudaError_t lgroup_run(const CeTables &T, const Replica *reps, ReplicaStats *stats, int8_t *occ,
                        const __nv_bfloat16 *params, int mode, int rounds, int n_local,
                        int n_replicas, int L, long long n_passes, long long n_equil,
-                       double *samples, long long capacity, cudaStream_t st);
+                       double *samples, long long capacity, const volatile int *stop,
+                       int cluster, cudaStream_t st);
 
 // n-fold way (cem_nfold.cu)
 // 32-ary sum tree over n leaves: level 0 = leaves, level k + 1 has

@@ -1467,8 +1467,15 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
   const int n_sub = n_sweeps * n_classes;
   uint32_t *skey = sched, *spar = sched + n_sub;
 
+  // stop requests of the host (a flag in host-mapped memory): thread 0 reads
+  // it at the start of a pass and publishes it at the end of that pass, so
+  // the read's latency is hidden by the pass; the block leaves at the next
+  // pass boundary with a consistent state
+  __shared__ int s_stop;
+  if (tid == 0) s_stop = 0;
   for (long long ip = 0; ip < P.n_passes; ++ip, ++pass_global) {
     const uint32_t plo = (uint32_t)pass_global, phi = (uint32_t)(pass_global >> 32) & 0xFFFFu;
+    const int stop_seen = (tid == 0 && P.stop) ? *P.stop : 0;
     // schedule: per sweep a random order of the classes, plus parameters
     for (int e = tid; e < n_sub; e += nth) {
       const int c = e % n_classes;
@@ -1484,6 +1491,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
       spar[e] = par;
     }
     __syncthreads();
+    if (s_stop) break;  // the host asked the run to stop
     // rank each class inside its sweep and decode its sub-step into that slot
     for (int e = tid; e < n_sub; e += nth) {
       const int sw = e / n_classes, c = e - sw * n_classes;
@@ -1856,6 +1864,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
         for (int k = 0; k < 16; ++k) tot[k] = __shfl_sync(0xffffffffu, v, k);
         double dtot = __shfl_sync(0xffffffffu, dv, 16);
         if (lane == 0) {
+          s_stop = stop_seen;
           if constexpr (EXACT) {
             dtot = 0.0;
             for (int g = 0; g < T.n_orbits; ++g)

@@ -30,11 +30,20 @@
 // mode 2 the exact locally balanced weights z = -beta dE_AB / 2 that the
 // network is trained to predict.
 //
+// One replica runs on a thread-block cluster of 1, 2 or 4 CTAs (one per SM):
+// every CTA holds a full copy of the replica in its shared memory, takes a
+// share of the groups (and of the nearest-neighbour anchors) of each
+// sub-step, and writes every accepted change into all copies through
+// distributed shared memory; a cluster barrier ends each sub-step. A group's
+// draws depend only on (pass, sub-step, group, round), so the chain is the
+// same for every cluster size.
+//
 // Network evaluation: the two dense layers of 32 environments at a time on
 // the tensor cores (mma.sync m16n8k16, bf16 operands, fp32 accumulation):
 // inputs (0/1, exact in bf16) x W1[42->48 padded][64], ReLU, x W2[64][64],
 // ReLU, dot w3; the accumulator fragments of layer 1 are the A fragments of
 // layer 2.
+#include <cooperative_groups.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -62,6 +71,8 @@ struct LGroupParams {
   long long n_passes, n_equil;
   double *samples;  // [rep][capacity][3]: energy per unit cell, x_B, order parameter
   long long sample_capacity;
+  const volatile int *stop;  // host-mapped stop flag (null: none)
+  int cluster;               // CTAs per replica (thread-block cluster size)
 };
 
 __device__ __forceinline__ void mma_bf16_16816(float (&c)[4], uint32_t a0, uint32_t a1,
@@ -255,7 +266,11 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
   static_assert(L % 6 == 0, "the learned group sweep needs L a multiple of 6");
   constexpr int N_SITES = L * L * L, N_C = M * M * M, N_GROUPS = (N_C + 31) / 32;
   constexpr int V = PITCH * PITCH * (L + 2 * RH);
-  const int rep = blockIdx.x;
+  namespace cg = cooperative_groups;
+  const cg::cluster_group cluster = cg::this_cluster();
+  const int CL = LP.cluster;
+  const int crank = (int)cluster.block_rank();
+  const int rep = blockIdx.x / CL;
   const Replica &R = LP.reps[rep];
   ReplicaStats &S = LP.stats[rep];
   Geo G;
@@ -271,8 +286,10 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
   __shared__ uint32_t s_key[LG_CLASSES], s_ainv[LG_CLASSES], s_boff[LG_CLASSES];
   __shared__ int s_local[64];  // class | parity << 5 | neighbour << 8
   __shared__ int s_red[LG_NW][12];
+  __shared__ int s_part[4][12];  // per-CTA pass totals, gathered in rank 0
   __shared__ long long s_cnt[gen_fcc::N_ORBITS], s_sub[4], s_n1;
   __shared__ double s_energy;
+  __shared__ int s_stop;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int mode = LP.mode;
   const int rounds = LP.rounds, n_local = LP.n_local;
@@ -295,10 +312,14 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
   }
   if (tid < gen_fcc::N_ORBITS) s_cnt[tid] = 0;
   if (tid < 4) s_sub[tid] = 0;
-  if (tid == 0) s_n1 = 0;
+  if (tid == 0) {
+    s_n1 = 0;
+    s_stop = 0;
+  }
   __syncthreads();
   // ---- exact initial energy (owned clusters) and species / sublattice counts
-  {
+  // (rank 0 keeps the replica's running statistics)
+  if (crank == 0) {
     long long cnt[gen_fcc::N_ORBITS] = {0, 0, 0, 0, 0, 0};
     long long sub[4] = {0, 0, 0, 0}, n1 = 0;
     for (int l = tid; l < N_SITES; l += LG_THREADS) {
@@ -317,7 +338,7 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
     atomicAdd((unsigned long long *)&s_n1, (unsigned long long)n1);
   }
   __syncthreads();
-  if (tid == 0) {
+  if (tid == 0 && crank == 0) {
     double e = T.w[0] * (double)N_SITES;
     for (int g = 0; g < T.n_orbits; ++g) e += T.w[T.orb_func_base[g]] * (double)s_cnt[g];
     s_energy = e;
@@ -334,12 +355,20 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
   __syncthreads();
 
   const LgNet net{fw1, fw2, fb, fb + 64, fb + 128, mode == 1 ? fb[192] : 0.f};
+  // every copy of the replica (own and peers' shared memory) receives each
+  // accepted change
+  auto put_all = [&](int x, int y, int z, int8_t v) {
+    for (int r = 0; r < CL; ++r) put_site(cluster.map_shared_rank(occ, r), G, 0, x, y, z, v);
+  };
+  cluster.sync();  // every copy is staged before any peer writes into it
   long long pass_global = S.pass;
   long long nsub[4];
   for (int k = 0; k < 4; ++k) nsub[k] = s_sub[k];
   const long long n_b = s_n1;
   for (long long ip = 0; ip < LP.n_passes; ++ip, ++pass_global) {
     const uint32_t plo = (uint32_t)pass_global, phi = (uint32_t)(pass_global >> 32) & 0xFFFFu;
+    // the host's stop flag, read here and published at the end of the pass
+    const int stop_seen = (tid == 0 && crank == 0 && LP.stop) ? *LP.stop : 0;
     // ---- schedule: class order, group permutations, local sub-steps
     if (tid < LG_CLASSES) {
       const U4 r = philox4x32_10(U4{(uint32_t)tid, 0u, plo, phi | (TAG_LG_SCHED << 16)}, k0, k1);
@@ -370,6 +399,7 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
       s_order[rank] = tid;
     }
     __syncthreads();
+    if (s_stop) break;  // the host asked the run to stop
 
     int n_prop = 0, n_acc = 0;
     int dcn[gen_fcc::N_ORBITS] = {0, 0, 0, 0, 0, 0};
@@ -379,7 +409,7 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
       const int c = s_order[sub];
       const int cx = c % 3, cy = (c / 3) % 3, cz = c / 9;
       const uint32_t ainv = s_ainv[c], boff = s_boff[c];
-      for (int grp = warp; grp < N_GROUPS; grp += LG_NW) {
+      for (int grp = crank * LG_NW + warp; grp < N_GROUPS; grp += CL * LG_NW) {
         const int r = grp * 32 + lane;
         const bool act = r < N_C;
         int x = 0, y = 0, z = 0, ad = 0, o = 0;
@@ -420,18 +450,27 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
           ub_own = ((unsigned long long)p.z << 32) | p.w;
           uu_own = p2.x;
         }
+        // inclusive prefix sums of the A and B weights over the lanes; they
+        // change only when a swap is accepted
+        uint32_t sa = 0u, sb = 0u, WA = 0u, WB = 0u;
+        bool dirty = true;
         for (int t = 0; t < rounds; ++t) {
-          uint32_t sa = (act && o == 0) ? wc : 0u, sb = (act && o == 1) ? wc : 0u;
+          if (dirty) {
+            sa = (act && o == 0) ? wc : 0u;
+            sb = (act && o == 1) ? wc : 0u;
 #pragma unroll
-          for (int off = 1; off < 32; off <<= 1) {
-            const uint32_t va = __shfl_up_sync(0xffffffffu, sa, off);
-            const uint32_t vb = __shfl_up_sync(0xffffffffu, sb, off);
-            if (lane >= off) {
-              sa += va;
-              sb += vb;
+            for (int off = 1; off < 32; off <<= 1) {
+              const uint32_t va = __shfl_up_sync(0xffffffffu, sa, off);
+              const uint32_t vb = __shfl_up_sync(0xffffffffu, sb, off);
+              if (lane >= off) {
+                sa += va;
+                sb += vb;
+              }
             }
+            WA = __shfl_sync(0xffffffffu, sa, 31);
+            WB = __shfl_sync(0xffffffffu, sb, 31);
+            dirty = false;
           }
-          const uint32_t WA = __shfl_sync(0xffffffffu, sa, 31), WB = __shfl_sync(0xffffffffu, sb, 31);
           if (WA == 0u || WB == 0u) break;  // one species absent from the group
           const unsigned long long ua = shfl64(ua_own, t), ub = shfl64(ub_own, t);
           const uint32_t uu = __shfl_sync(0xffffffffu, uu_own, t);
@@ -448,9 +487,11 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
           if (mode == 0) {
             accept = accept_de(dE, beta_f, u24(uu));
           } else {
-            // q_rev / q_fwd = (W_A W_B / (W_A' W_B')) (w'_a w'_b / (w_a w_b))
-            const float ratio = FMUL(FMUL(__fdiv_rn((float)WA, (float)WA2), __fdiv_rn((float)WB, (float)WB2)),
-                                     FMUL(__fdiv_rn((float)waa, (float)wca), __fdiv_rn((float)wab, (float)wcb)));
+            // q_rev / q_fwd = (W_A W_B / (W_A' W_B')) (w'_a w'_b / (w_a w_b)); each
+            // product stays below 2^32 x 2^32 x 2^27 x 2^27 < 2^128
+            const float num = FMUL(FMUL((float)WA, (float)WB), FMUL((float)waa, (float)wab));
+            const float den = FMUL(FMUL((float)WA2, (float)WB2), FMUL((float)wca, (float)wcb));
+            const float ratio = __fdiv_rn(num, den);
             const float lr = FFMA(-beta_f, dE, logf(ratio));
             accept = (lr >= 0.f) || (u24(uu) < cem_expf_neg(lr));
           }
@@ -458,23 +499,26 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
             ++n_prop;
             n_acc += accept ? 1 : 0;
           }
-          if (accept && (lane == la || lane == lb)) {
-            o ^= 1;
-            eme = -eme;
-            const uint32_t tmp = wc;
-            wc = wa;
-            wa = tmp;
+          if (accept) {
+            dirty = true;
+            if (lane == la || lane == lb) {
+              o ^= 1;
+              eme = -eme;
+              const uint32_t tmp = wc;
+              wc = wa;
+              wa = tmp;
+            }
           }
         }
         if (act && o != o0) {
-          put_site(occ, G, 0, x, y, z, (int8_t)o);
+          put_all(x, y, z, (int8_t)o);
           const int d = o - o0;
 #pragma unroll
           for (int g = 0; g < gen_fcc::N_ORBITS; ++g) dcn[g] += d * n[g];
           dsub.add(sc_sublattice(x, y, z), d);
         }
       }
-      __syncthreads();
+      cluster.sync();  // the class's changes are in every copy
     }
     // ---- nearest-neighbour swaps (plain Metropolis) between classes
     constexpr int H = M / 2, N_ANCHOR = H * H * H;
@@ -483,7 +527,7 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
       const int c = code & 31, par = (code >> 5) & 7, dl = code >> 8;
       const int cx = c % 3, cy = (c / 3) % 3, cz = c / 9;
       const int dx = gen_fcc::NB_D[dl][0], dy = gen_fcc::NB_D[dl][1], dz = gen_fcc::NB_D[dl][2];
-      for (int q = tid; q < N_ANCHOR; q += LG_THREADS) {
+      for (int q = crank * LG_THREADS + tid; q < N_ANCHOR; q += CL * LG_THREADS) {
         const int i = q % H, j = (q / H) % H, k = q / (H * H);
         const int xa = cx + 3 * (2 * i + (par & 1)), ya = cy + 3 * (2 * j + ((par >> 1) & 1)),
                   za = cz + 3 * (2 * k + ((par >> 2) & 1));
@@ -495,9 +539,10 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
         const U4 rr = philox4x32_10(U4{(uint32_t)la, (uint32_t)(LG_CLASSES + ls), plo,
                                        phi | (TAG_LG_LOCAL << 16)},
                                     k0, k1);
-        // the first change is applied before either flower is read (a site's
-        // flower never contains the site): a sees the original state, b sees
-        // a changed, as for a sequence of two changes
+        // the first change is applied (in this CTA's copy) before either
+        // flower is read (a site's flower never contains the site): a sees
+        // the original state, b sees a changed, as for a sequence of two
+        // changes
         put_site(occ, G, 0, xa, ya, za, (int8_t)ob);
         int na[gen_fcc::N_ORBITS], nb[gen_fcc::N_ORBITS];
         gen_fcc::counts<PITCH>(occ + ada, na);
@@ -516,7 +561,8 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
         ++n_prop;
         if (accept_de(de, beta_f, u24(rr.x))) {
           ++n_acc;
-          put_site(occ, G, 0, xb, yb, zb, (int8_t)oa);
+          put_all(xa, ya, za, (int8_t)ob);
+          put_all(xb, yb, zb, (int8_t)oa);
 #pragma unroll
           for (int g = 0; g < gen_fcc::N_ORBITS; ++g) dcn[g] += dc[g];
           dsub.add(sc_sublattice(xa, ya, za), d);
@@ -525,7 +571,7 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
           put_site(occ, G, 0, xa, ya, za, (int8_t)oa);
         }
       }
-      __syncthreads();
+      cluster.sync();
     }
     // ---- end of pass: reduce, update the exact running energy, sample
     {
@@ -542,11 +588,21 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
       if (lane == 0)
         for (int k = 0; k < 12; ++k) s_red[warp][k] = vals[k];
       __syncthreads();
-      if (tid == 0) {
+      if (tid == 0) {  // this CTA's totals -> rank 0
+        int *part = cluster.map_shared_rank(&s_part[0][0], 0) + 12 * crank;
+        for (int k = 0; k < 12; ++k) {
+          int t = 0;
+          for (int w = 0; w < LG_NW; ++w) t += s_red[w][k];
+          part[k] = t;
+        }
+      }
+      cluster.sync();
+      if (tid == 0 && crank == 0) {
+        for (int r = 0; r < CL; ++r) *cluster.map_shared_rank(&s_stop, r) = stop_seen;
         long long tot[12];
         for (int k = 0; k < 12; ++k) {
           tot[k] = 0;
-          for (int w = 0; w < LG_NW; ++w) tot[k] += s_red[w][k];
+          for (int r = 0; r < CL; ++r) tot[k] += s_part[r][k];
         }
         double de = 0.0;
         for (int g = 0; g < T.n_orbits; ++g) de += T.w[T.orb_func_base[g]] * (double)tot[2 + g];
@@ -581,19 +637,22 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
           }
         }
       }
-      __syncthreads();
+      cluster.sync();  // the stop decision is in every CTA
     }
   }
-  // ---- write back
-  for (int l = tid; l < N_SITES; l += LG_THREADS) {
-    const int x = l % L, y = (l / L) % L, z = l / (L * L);
-    LP.occ[R.occ_offset + l] = occ[G.addr(0, x, y, z)];
+  // ---- write back (rank 0; every copy is identical)
+  if (crank == 0) {
+    for (int l = tid; l < N_SITES; l += LG_THREADS) {
+      const int x = l % L, y = (l / L) % L, z = l / (L * L);
+      LP.occ[R.occ_offset + l] = occ[G.addr(0, x, y, z)];
+    }
+    if (tid == 0) {
+      S.energy = s_energy;
+      S.pass = pass_global;
+      for (int k = 0; k < 4; ++k) S.n_sub[k] = nsub[k];
+    }
   }
-  if (tid == 0) {
-    S.energy = s_energy;
-    S.pass = pass_global;
-    for (int k = 0; k < 4; ++k) S.n_sub[k] = nsub[k];
-  }
+  cluster.sync();  // no CTA leaves while a peer may still write to it
 }
 
 cudaError_t mlp_forward_tc(const __nv_bfloat16 *params, const int8_t *X, long long n, float *z,
@@ -615,8 +674,10 @@ bool lgroup_supported(int L) { return L == 12 || L == 24 || L == 36 || L == 48; 
 cudaError_t lgroup_run(const CeTables &T, const Replica *reps, ReplicaStats *stats, int8_t *occ,
                        const __nv_bfloat16 *params, int mode, int rounds, int n_local,
                        int n_replicas, int L, long long n_passes, long long n_equil,
-                       double *samples, long long capacity, cudaStream_t st) {
+                       double *samples, long long capacity, const volatile int *stop,
+                       int cluster, cudaStream_t st) {
   LGroupParams LP{};
+  LP.stop = stop;
   LP.reps = reps;
   LP.stats = stats;
   LP.occ = occ;
@@ -628,14 +689,28 @@ cudaError_t lgroup_run(const CeTables &T, const Replica *reps, ReplicaStats *sta
   LP.n_equil = n_equil;
   LP.samples = samples;
   LP.sample_capacity = capacity;
+  LP.cluster = cluster;
   const int smem = lgroup_smem_bytes(L);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(n_replicas * cluster));
+  cfg.blockDim = dim3(LG_THREADS);
+  cfg.dynamicSmemBytes = (size_t)smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
   cudaError_t e = cudaSuccess;
   switch (L) {
 #define CEM_LGROUP_CASE(LL)                                                                      \
   case LL:                                                                                       \
     e = cudaFuncSetAttribute(k_lgroup<LL + 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem); \
     if (e != cudaSuccess) return e;                                                              \
-    k_lgroup<LL + 4><<<n_replicas, LG_THREADS, smem, st>>>(T, LP);                               \
+    e = cudaLaunchKernelEx(&cfg, k_lgroup<LL + 4>, T, LP);                                       \
+    if (e != cudaSuccess) return e;                                                              \
     break;
     CEM_LGROUP_CASE(12)
     CEM_LGROUP_CASE(24)

@@ -363,7 +363,8 @@ static cudaError_t stream_run_t(const CeTables &T, StreamState &st, const Replic
                                 int n_classes, int n_pair_sw, int n_local_sw, const double *RT,
                                 long long n_passes, long long n_equil, long long start_pass,
                                 double *samples, long long capacity, int width, int count_sub,
-                                cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1) {
+                                cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1,
+                                const volatile int *stop_host, long long *launched) {
   cudaError_t e;
   const long long stride = stream_halo_bytes(L2, PITCH);
   // run parameters (device)
@@ -422,8 +423,15 @@ static cudaError_t stream_run_t(const CeTables &T, StreamState &st, const Replic
     st.key = key;
   }
   if ((e = cudaEventRecord(ev0, s)) != cudaSuccess) return e;
-  for (long long p = 0; p < n_passes; ++p)
+  // one graph per pass; a stop request of the host ends the queueing (the
+  // launch queue fills up on long runs, so the check sees it within the
+  // passes already queued)
+  long long p = 0;
+  for (; p < n_passes; ++p) {
+    if (stop_host && *stop_host) break;
     if ((e = cudaGraphLaunch(st.exec, s)) != cudaSuccess) return e;
+  }
+  if (launched) *launched = p;
   if ((e = cudaEventRecord(ev1, s)) != cudaSuccess) return e;
   k_halo_store<PITCH><<<g2, 256, 0, s>>>(reps, occ_all, st.halo, stride);
   return cudaGetLastError();
@@ -433,16 +441,17 @@ cudaError_t stream_run(const CeTables &T, StreamState &st, const Replica *reps, 
                        int8_t *occ_all, int n_rep, int L2, int pitch, int n_classes, int n_pair_sw,
                        int n_local_sw, const double *RT, long long n_passes, long long n_equil,
                        long long start_pass, double *samples, long long capacity, int width,
-                       int count_sub, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1) {
+                       int count_sub, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1,
+                       const volatile int *stop_host, long long *launched) {
   switch (pitch) {
     case 100:
       return stream_run_t<100>(T, st, reps, stats, occ_all, n_rep, L2, n_classes, n_pair_sw,
                                n_local_sw, RT, n_passes, n_equil, start_pass, samples, capacity,
-                               width, count_sub, s, ev0, ev1);
+                               width, count_sub, s, ev0, ev1, stop_host, launched);
     case 28:
       return stream_run_t<28>(T, st, reps, stats, occ_all, n_rep, L2, n_classes, n_pair_sw,
                               n_local_sw, RT, n_passes, n_equil, start_pass, samples, capacity,
-                              width, count_sub, s, ev0, ev1);
+                              width, count_sub, s, ev0, ev1, stop_host, launched);
     default:
       return cudaErrorInvalidValue;
   }

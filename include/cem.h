@@ -34,6 +34,9 @@ extern "C" {
 #define CEM_ERR_CUDA 2        /* CUDA runtime error (message says which) */
 #define CEM_ERR_UNSUPPORTED 3 /* valid input outside this build's limits */
 #define CEM_ERR_DEVICE 4      /* a kernel reported an error status */
+#define CEM_STOPPED 5         /* cem_synchronize: the run was stopped early by
+                                 cem_request_stop (not an error: the state is
+                                 consistent at a pass boundary) */
 
 #define CEM_SEMIGRAND_CANONICAL 0
 #define CEM_CANONICAL 1
@@ -283,7 +286,12 @@ int cem_step_async(cem_replicas *r, const int8_t *host_in, int8_t *host_out, int
  *                  fit in shared memory (binary FCC, equal even supercells);
  *   "threads" (512 or 256): threads per replica of the shared-memory sweep
  *                  (256: two replicas per SM);
- *   "cta_order" (0 or 1): replica -> CTA schedule (1: largest first).
+ *   "cta_order" (0 or 1): replica -> CTA schedule (1: largest first);
+ *   "group_cluster" (0, 1, 2, 4): CTAs per replica of cem_learned_group_run,
+ *                  a thread-block cluster whose CTAs share the replica's
+ *                  sub-steps through distributed shared memory (0, the
+ *                  default: 4, 2 or 1, the largest that keeps every cluster
+ *                  on its own SMs; the chain does not depend on it).
  * cem_get_option also reads "pitch" (> 0 generated evaluator, 0 run-time
  * tables, -1 one orbit at a time), "smem_bytes", "colour_classes" and
  * "streamed". */
@@ -390,8 +398,22 @@ int cem_state_bytes(const cem_replicas *r, int64_t *bytes);
 int cem_get_state(cem_replicas *r, int replica, int8_t *occ, void *state);
 int cem_set_state(cem_replicas *r, int replica, const int8_t *occ, const void *state);
 
-/* Wait for all work of this batch. */
+/* Wait for all work of this batch. Returns CEM_STOPPED when a stop was
+ * requested (cem_request_stop) during the last run. */
 int cem_synchronize(cem_replicas *r);
+
+/* Ask the run in flight (cem_run, cem_learned_group_run) to stop early. The
+ * only entry point that may be called from another host thread while a run is
+ * in flight: it writes a flag in page-locked host memory mapped into the
+ * device. The persistent shared-memory kernels read it once per pass and
+ * leave at the next pass boundary, writing back occupations and statistics
+ * as a completed run does (cem_get_stats reports the passes actually run);
+ * an HBM-streamed run stops queueing its per-pass graphs, so it ends after
+ * the passes already queued. Each run clears the flag when it starts. The
+ * reference stops long runs from the host through its run manager's
+ * completion checks (BaseMonteCalculator.hh:223-225, RunManager); this is
+ * the batch form of that control for one long launch. */
+int cem_request_stop(cem_replicas *r);
 
 /* Device time of the last cem_run's main kernel, in milliseconds (CUDA
  * events on the batch's stream). */

@@ -106,3 +106,48 @@ def test_zero_temperature_accepts_only_downhill(cm, oracle_mod):
     got = b.replay(0, 5, 3 * 512)
     np.testing.assert_array_equal(got["accept"], ref["accept"])
     assert np.all(got["dE"][got["accept"] == 1] < 0)
+
+
+@pytest.mark.parametrize("kernel", ["sweep", "group"])
+def test_host_stop_request_ends_a_long_run_at_a_pass_boundary(kernel, cm):
+    """A run of a million passes, stopped from the host after a fraction of a
+    second: cem_synchronize reports CEM_STOPPED, the replicas hold a
+    consistent state (running energy equals a fresh recompute, composition
+    conserved), and the next run starts normally."""
+    import time
+
+    ce = workloads.fcc_binary_ce(0)
+    L = (12, 12, 12)
+    n = 4
+    sysd = cm.System(ce)
+    b = cm.ReplicaBatch(sysd, "canonical", [L] * n)
+    rng = np.random.default_rng(8)
+    occ0 = [workloads.fixed_composition(rng, 12 ** 3, 0.4) for _ in range(n)]
+    for i in range(n):
+        b.set_conditions(i, 700.0)
+        b.set_seed(i, 31 + i)
+        b.set_occupation(i, occ0[i])
+    big = 1_000_000
+    t0 = time.perf_counter()
+    if kernel == "sweep":
+        b.run(big, 0)
+    else:
+        b.learned_group_run(None, big, 0, weights="uniform", rounds=8, local_substeps=2)
+    time.sleep(0.3)
+    b.request_stop()
+    assert b.synchronize() is True
+    assert time.perf_counter() - t0 < 10.0
+    for i in range(n):
+        st = b.stats(i)
+        assert 0 < st["passes"] < big
+        e, _ = b.energy(i)
+        assert abs(st["energy"] - e) <= 1e-9 * max(1.0, abs(e))
+        assert b.get_occupation(i).sum() == occ0[i].sum()
+    # the flag is cleared by the next run
+    p0 = b.stats(0)["passes"]
+    if kernel == "sweep":
+        b.run(5, 0)
+    else:
+        b.learned_group_run(None, 5, 0, weights="uniform", rounds=8, local_substeps=2)
+    assert b.synchronize() is False
+    assert b.stats(0)["passes"] == p0 + 5

@@ -259,3 +259,37 @@ def test_learned_group_sweep_equilibrium_matches_oracle(T, cm, oracle_mod):
     msg = "\n".join(rows) + f"\n{n2} of {len(zs)} beyond 2 sigma (allowed {k}); bound {bound:.2f}"
     print(msg)
     assert ok, msg
+
+
+def test_learned_group_chain_does_not_depend_on_cluster_size(cm):
+    """A group's draws depend only on (pass, sub-step, group, round) and every
+    accepted change reaches every CTA's copy of the replica, so 1, 2 and 4
+    CTAs per replica run the same chain: identical occupations, running
+    energies and acceptance counts."""
+    L, T, nrep = 24, 150.0, 3
+    ce = workloads.fcc_binary_ce(3, nn1=0.08)
+    sysd = cm.System(ce)
+    rng = np.random.default_rng(4)
+    occ0 = [workloads.fixed_composition(rng, L ** 3, 0.25) for _ in range(nrep)]
+    _, _, _, X, t = _snapshot_features(cm, T=T)
+    net = cm.LearnedProposal(seed=2)
+    net.train(X, t, epochs=2, batch=512, lr=3e-3, seed=1)
+    results = []
+    for cl in (1, 2, 4):
+        b = cm.ReplicaBatch(sysd, "canonical", [(L, L, L)] * nrep)
+        b.set_option("group_cluster", cl)
+        for i in range(nrep):
+            b.set_conditions(i, T)
+            b.set_seed(i, 60 + i)
+            b.set_occupation(i, occ0[i])
+        b.learned_group_run(net, 40, 10, record_samples=True, rounds=8, local_substeps=4)
+        assert b.get_option("group_cluster") == cl
+        results.append(([b.get_occupation(i) for i in range(nrep)],
+                        [(b.stats(i)["energy"], b.stats(i)["n_accepted"], b.stats(i)["n_proposed"])
+                         for i in range(nrep)],
+                        [b.learned_samples(i, 30)[0] for i in range(nrep)]))
+    for occ, st, smp in results[1:]:
+        for i in range(nrep):
+            assert np.array_equal(occ[i], results[0][0][i])
+            assert st[i] == results[0][1][i]
+            assert np.array_equal(smp[i], results[0][2][i])
