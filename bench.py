@@ -12,6 +12,12 @@ host buffers: copy occupations in, one pass, copy occupations out; two
 replica batches on two streams alternate so that one batch's copies overlap
 the other's pass.
 
+The line also carries `learned_vs_plain`, the headline half of the metric:
+effective independent samples per second of the learned group sweep against
+the plain sweep on configuration 3 (32 x 48^3 FCC, L1_2 cluster expansion,
+x_B = 0.25, T = 0.9 T_c), both continued from one equilibrated state, with
+their <E> compared within 2 standard errors (`--no-learned` leaves it out).
+
 --impl reference runs the CPU restatement of the reference loop (one
 sequential std::mt19937_64 chain per host thread) on a bounded sample of the
 same workload.
@@ -283,21 +289,25 @@ def run_gb300(args):
     t_dev = reduce_max(dist, kernel_ms / 1e3)
     props_all = reduce_sum(dist, props)
     value = props_all / t_dev
-    # effective independent samples of the potential energy per pass
+    # effective independent samples of the potential energy: the first tenth
+    # of the timed passes is left out as equilibration, and the estimate is
+    # reported only where every replica's series holds >= 50 tau_int
     n_eff = n_eff_op = 0.0
     taus = []
+    min_ratio = float("inf")
     for i in range(w.n_replicas):
         pot, _ = batch.samples(i, args.steps)
         op = batch.order_samples(i, args.steps)
-        t = tau_int(pot) if pot.size > 16 else float("nan")
-        t_op = tau_int(op) if op.size > 16 else float("nan")
+        pot, op = pot[pot.size // 10:], op[op.size // 10:]
+        t = tau_int(pot) if pot.size >= 8 else float("inf")
+        t_op = tau_int(op) if op.size >= 8 else float("inf")
         taus.append(t)
-        if np.isfinite(t):
-            n_eff += pot.size / (2.0 * t)
-        if np.isfinite(t_op):
-            n_eff_op += op.size / (2.0 * t_op)
+        min_ratio = min(min_ratio, pot.size / t, op.size / t_op)
+        n_eff += pot.size / (2.0 * t)
+        n_eff_op += op.size / (2.0 * t_op)
     n_eff = reduce_sum(dist, n_eff)
     n_eff_op = reduce_sum(dist, n_eff_op)
+    eff_ok = min_ratio >= 50.0
 
     # end-to-end through the C ABI with pinned host buffers: two replica
     # batches (each with its own stream) alternate, so one batch's host <->
@@ -363,8 +373,10 @@ def run_gb300(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
         "config": workload_config(w, {
-            "arithmetic": "int8 occupations, integer delta correlations, float-float "
-                          "(2 x f32) ECI dot, f32 acceptance, f64 running energy",
+            "arithmetic": "int8 occupations; integer cluster-count changes; energy change = "
+                          "exact int32 sum of integer multiples of a power-of-two quantum plus "
+                          "one f32 FMA chain of the weight remainders; f32 acceptance; f64 "
+                          "running energy from integer counts",
             "parallelism": f"replicas only, {w.n_replicas} per GPU",
             "schedule": {"threads_per_replica": tuned["threads"],
                          "cta_order": "largest first" if tuned["cta_order"] else "replica order",
@@ -372,10 +384,14 @@ def run_gb300(args):
         }),
         "proposals": int(props_all), "acceptance": p_acc,
         "proposals_per_s_per_replica": value / (w.n_replicas * ws),
-        "effective_samples_per_s": n_eff / t_dev,
-        "effective_samples_per_s_order_parameter": n_eff_op / t_dev,
+        "effective_samples_per_s": n_eff / t_dev if eff_ok else None,
+        "effective_samples_per_s_order_parameter": n_eff_op / t_dev if eff_ok else None,
+        "effective_samples_note": ("timed passes after the first tenth; every replica's series "
+                                   f"holds >= {min_ratio:.0f} tau_int") if eff_ok else
+                                  (f"not reported: the timed run holds only {min_ratio:.1f} "
+                                   "tau_int per replica (< 50)"),
         "running_energy_rel_drift_vs_recompute": drift,
-        "tau_int_potential_median": float(np.nanmedian(taus)),
+        "tau_int_potential_median": float(np.median(taus)) if eff_ok else None,
         "host_wall_s": t1 - t0,
         "e2e": {"value": e2e_props / e2e_time, "unit": "proposals/s",
                 "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
@@ -384,6 +400,9 @@ def run_gb300(args):
                             "CUDA graph: upload occupations, one pass, read occupations back"},
         "roofline": {"bound": "smem", "achieved": achieved, "peak": smem_gbs, "unit": "GB/s",
                      "frac": achieved / smem_gbs, "traffic": traffic,
+                     "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                       "k_sweep launch of this workload, ncu capture "
+                                       "summarised in profiles/k_sweep_fcc24_canonical_ncu.md",
                      "peak_source": "measured in this run by cem_smem_bandwidth "
                                     "(16-byte shared loads, all SMs)",
                      "bytes_per_proposal": bytes_per_prop,
@@ -391,6 +410,10 @@ def run_gb300(args):
         "gpu_launches": 1,
         "clocks": clocks,
     }
+    if rank == 0 and not args.no_learned:
+        # the headline half of the metric: learned vs plain GPU Metropolis in
+        # effective independent samples per second (configuration 3)
+        line["learned_vs_plain"] = learned_vs_plain(cm, 0.9 * T_C_CONFIG3_K)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w, os.cpu_count() or 1)
     if rank == 0:
@@ -479,21 +502,23 @@ def run_other_workload(args):
     return 0
 
 
-def run_learned_comparison(args):
-    """Configuration 3: T_c from a temperature scan of the plain sampler, then
-    plain vs learned-proposal effective independent samples per second of the
-    energy and the L1_2 order parameter at T = 0.9 T_c (48^3, x_B = 0.25)."""
-    from casmcode_clexmonte_gb300 import build as B
+T_C_CONFIG3_K = 100.0  # heat-capacity maximum of a plain-sweep temperature scan (--tc-scan)
 
-    B.build()
-    from casmcode_clexmonte_gb300 import calculator as cm
+
+def _l12_state(L: int, k: int) -> np.ndarray:
+    """Perfect L1_2 order on an L^3 FCC supercell: B on simple-cubic
+    sublattice k (site index x + L (y + L z), primitive-cell coordinates)."""
+    x, y, z = np.meshgrid(np.arange(L), np.arange(L), np.arange(L), indexing="ij")
+    x, y, z = (a.transpose(2, 1, 0).ravel() for a in (x, y, z))
+    return ((((y + z) & 1) | (((x + z) & 1) << 1)) == k).astype(np.int8)
+
+
+def tc_scan(cm, ce):
+    """T_c of an L1_2 cluster expansion: heat-capacity maximum of the plain
+    sweep over 20..320 K (24^3, x_B = 0.25, 3000 + 3000 passes)."""
     from casmcode_clexmonte_gb300 import workloads
-    from casmcode_clexmonte_gb300.stats import tau_int
 
-    w = workloads.config(3)
-    ce = w.ce
     sysd = cm.System(ce)
-    # 1. temperature scan (24^3, plain sampler): heat capacity peak
     temps = np.linspace(20.0, 320.0, 31)
     scan = cm.ReplicaBatch(sysd, "canonical", [(24, 24, 24)] * len(temps))
     rng = np.random.default_rng(3)
@@ -505,36 +530,79 @@ def run_learned_comparison(args):
     cv = np.array([scan.stats(i)["var_potential"] * 24 ** 3 / (8.617333262e-5 * t * t)
                    for i, t in enumerate(temps)])
     inner = slice(1, len(temps) - 1)  # a maximum at the scan's edge is no transition
-    tc = float(temps[inner][int(np.argmax(cv[inner]))])
-    T = 0.9 * tc
-    # 2. plain sampler, 32 x 48^3
+    return float(temps[inner][int(np.argmax(cv[inner]))]), temps, cv
+
+
+def learned_vs_plain(cm, T: float, plain_passes: int = 12000, learned_passes: int = 1200,
+                     equil_passes: int = 5000, rounds: int = 8, local_substeps: int = 8,
+                     weights=("network",)) -> dict:
+    """Configuration 3 (32 x 48^3 FCC, L1_2 cluster expansion, canonical
+    x_B = 0.25) at temperature T: plain GPU Metropolis (the colour-class
+    sweep) against the learned group sweep, both continued from one common
+    state equilibrated by the plain sweep from perfect L1_2 order.
+
+    Per sampler: integrated autocorrelation times of E and of the L1_2 order
+    parameter per replica (Sokal window; the run must hold >= 50 tau_int),
+    effective independent samples per second = sum over replicas of
+    n / (2 tau_int) / device seconds, and <E> with the standard error of the
+    replica means (32 independent chains). The network is trained on the GPU
+    on 10^6 environments of the equilibrated plain states."""
+    from casmcode_clexmonte_gb300 import workloads
+    from casmcode_clexmonte_gb300.stats import tau_int
+
+    w = workloads.config(3)
+    sysd = cm.System(w.ce)
+    L = w.L[0][0]
     n_rep = w.n_replicas
-    plain = cm.ReplicaBatch(sysd, "canonical", w.L)
+
+    def batch():
+        b = cm.ReplicaBatch(sysd, "canonical", w.L)
+        for i in range(n_rep):
+            b.set_conditions(i, T)
+            b.set_seed(i, 1000 + i)
+        return b
+
+    def summary(e_series, op_series, seconds, props, accs, passes):
+        te = np.array([tau_int(e) for e in e_series])
+        to = np.array([tau_int(o) for o in op_series])
+        means = np.array([e.mean() for e in e_series])
+        n = len(e_series[0])
+        return {
+            "passes": passes, "device_s": seconds, "ms_per_pass": 1e3 * seconds / passes,
+            "proposals_per_s": props / seconds, "acceptance": accs / max(1, props),
+            "tau_int_E_median": float(np.median(te)), "tau_int_E_max": float(te.max()),
+            "tau_int_order_median": float(np.median(to)),
+            "samples_over_tau_min": float(n / max(te.max(), to.max())),
+            "eff_samples_per_s_E": float(np.sum(n / (2.0 * te)) / seconds),
+            "eff_samples_per_s_order": float(np.sum(n / (2.0 * to)) / seconds),
+            "mean_E": float(means.mean()), "mean_E_sigma": float(means.std(ddof=1) / np.sqrt(n_rep)),
+        }
+
+    plain = batch()
     for i in range(n_rep):
-        plain.set_conditions(i, T)
-        plain.set_seed(i, 1000 + i)
-        plain.set_occupation(i, w.occupation[i])
-    plain.run(args.warmup * 50, 0)
-    plain.run(args.steps, 0, record_samples=True)
+        plain.set_occupation(i, _l12_state(L, i % 4))
+    plain.run(equil_passes, 0)
+    plain.synchronize()
+    common = plain.get_occupation_all()
+    st0 = [plain.stats(i) for i in range(n_rep)]
+    plain.run(plain_passes, 0, record_samples=True)
     plain.synchronize()
     t_plain = plain.kernel_ms() / 1e3
-    prop_plain = sum(plain.stats(i)["n_proposed"] for i in range(n_rep))
-    neff_e = neff_op = 0.0
-    taus_p = []
-    for i in range(n_rep):
-        e, _ = plain.samples(i, args.steps)
-        op = plain.order_samples(i, args.steps)
-        te, to = tau_int(e), tau_int(op)
-        taus_p.append((te, to))
-        neff_e += e.size / (2 * te)
-        neff_op += op.size / (2 * to)
-    e_rep_plain = np.array([plain.stats(i)["mean_potential"] for i in range(n_rep)])
-    mean_e_plain = float(e_rep_plain.mean())
-    sig_plain = float(e_rep_plain.std(ddof=1) / np.sqrt(n_rep))
-    # 3. train the proposal network on plain-sampler snapshots (1e6 environments)
+    st1 = [plain.stats(i) for i in range(n_rep)]
+    e_p = [plain.samples(i, plain_passes)[0] for i in range(n_rep)]
+    o_p = [plain.order_samples(i, plain_passes) for i in range(n_rep)]
+    out = {"workload": w.name, "temperature_K": T, "T_c_K": T_C_CONFIG3_K,
+           "start": f"one state: perfect L1_2 order + {equil_passes} plain passes",
+           "plain": summary(e_p, o_p, t_plain,
+                            sum(b["n_proposed"] - a["n_proposed"] for a, b in zip(st0, st1)),
+                            sum(b["n_accepted"] - a["n_accepted"] for a, b in zip(st0, st1)),
+                            plain_passes)}
+    # network trained on the equilibrated plain states (10^6 environments)
+    eq = batch()
+    eq.set_occupation_all(common)
     X, t = [], []
     for i in range(n_rep):
-        x_i, t_i = plain.learned_features(i)
+        x_i, t_i = eq.learned_features(i)
         X.append(x_i)
         t.append(t_i)
     X = np.concatenate(X)[:1_000_000]
@@ -542,62 +610,60 @@ def run_learned_comparison(args):
     net = cm.LearnedProposal(seed=11)
     t0 = time.perf_counter()
     losses = net.train(X, t, epochs=4, batch=4096, lr=2e-3, seed=5)
-    train_s = time.perf_counter() - t0
-    # 4. learned-proposal sampler from the equilibrated plain states
-    lp = args.learned_passes
-    plain.learned_run(net, lp, lp // 5, record_samples=True)
-    plain.synchronize()
-    t_learned = plain.kernel_ms() / 1e3
-    neff_e_l = neff_op_l = 0.0
-    taus_l = []
-    acc_l = []
-    for i in range(n_rep):
-        e, op = plain.learned_samples(i, lp)
-        te, to = tau_int(e), tau_int(op)
-        taus_l.append((te, to))
-        neff_e_l += e.size / (2 * te)
-        neff_op_l += op.size / (2 * to)
-    e_rep_learned = np.array([plain.learned_samples(i, lp)[0].mean() for i in range(n_rep)])
-    mean_e_learned = float(e_rep_learned.mean())
-    sig_learned = float(e_rep_learned.std(ddof=1) / np.sqrt(n_rep))
-    sig_diff = float(np.hypot(sig_plain, sig_learned))
-    # 5. the plain sampler again, from the learned chain's final states (its global
-    # swaps have removed the antiphase boundaries the plain chain was still
-    # coarsening): both chains then sample the same equilibrium state
-    plain.run(args.steps, 0, record_samples=True)
-    plain.synchronize()
-    e_rep_plain2 = np.array([plain.stats(i)["mean_potential"] for i in range(n_rep)])
-    mean_e_plain2 = float(e_rep_plain2.mean())
-    sig_plain2 = float(e_rep_plain2.std(ddof=1) / np.sqrt(n_rep))
-    sig_diff2 = float(np.hypot(sig_plain2, sig_learned))
-    line = {
-        "metric": "effective samples/s (learned vs plain GPU Metropolis, same <E>)",
-        "workload": w.name, "T_c_scan_K": tc, "temperature_K": T,
-        "heat_capacity_scan": {"T_K": [float(x) for x in temps], "C_per_uc": [float(x) for x in cv]},
-        "plain": {"passes": args.steps, "seconds": t_plain, "proposals_per_s": prop_plain / t_plain,
-                  "tau_int_E_median": float(np.median([a for a, _ in taus_p])),
-                  "tau_int_order_median": float(np.median([b for _, b in taus_p])),
-                  "eff_samples_per_s_E": neff_e / t_plain,
-                  "eff_samples_per_s_order": neff_op / t_plain, "mean_E": mean_e_plain,
-                  "mean_E_sigma": sig_plain},
-        "learned": {"passes": lp, "seconds": t_learned,
-                    "proposals_per_s": n_rep * lp * int(w.n_sites[0]) / t_learned,
-                    "tau_int_E_median": float(np.median([a for a, _ in taus_l])),
-                    "tau_int_order_median": float(np.median([b for _, b in taus_l])),
-                    "eff_samples_per_s_E": neff_e_l / t_learned,
-                    "eff_samples_per_s_order": neff_op_l / t_learned, "mean_E": mean_e_learned,
-                    "mean_E_sigma": sig_learned,
-                    "train_seconds": train_s, "train_loss": [float(x) for x in losses]},
-        "ratio_learned_over_plain_E": (neff_e_l / t_learned) / (neff_e / t_plain),
-        "ratio_learned_over_plain_order": (neff_op_l / t_learned) / (neff_op / t_plain),
-        "same_E_within_2sigma": bool(abs(mean_e_learned - mean_e_plain) <= 2 * sig_diff),
-        "E_difference_over_sigma": abs(mean_e_learned - mean_e_plain) / sig_diff if sig_diff > 0 else None,
-        "plain_from_learned_states": {
-            "passes": args.steps, "mean_E": mean_e_plain2, "mean_E_sigma": sig_plain2,
-            "same_E_within_2sigma": bool(abs(mean_e_learned - mean_e_plain2) <= 2 * sig_diff2),
-            "E_difference_over_sigma": abs(mean_e_learned - mean_e_plain2) / sig_diff2
-            if sig_diff2 > 0 else None},
-    }
+    out["network"] = {"train_s": time.perf_counter() - t0, "environments": int(len(X)),
+                      "loss_per_epoch": [float(v) for v in losses]}
+    for wname in weights:
+        b = batch()
+        b.set_occupation_all(common)
+        prop = net if wname == "network" else None
+        b.learned_group_run(prop, learned_passes, 0, record_samples=True, weights=wname,
+                            rounds=rounds, local_substeps=local_substeps)
+        b.synchronize()
+        t_l = b.kernel_ms() / 1e3
+        st1 = [b.stats(i) for i in range(n_rep)]
+        e_l = [b.learned_samples(i, learned_passes)[0] for i in range(n_rep)]
+        o_l = [b.learned_samples(i, learned_passes)[1] for i in range(n_rep)]
+        r = summary(e_l, o_l, t_l, sum(y["n_proposed"] for y in st1),
+                    sum(y["n_accepted"] for y in st1), learned_passes)
+        r.update(weights=wname, rounds=rounds, local_substeps=local_substeps,
+                 cluster_ctas_per_replica=b.get_option("group_cluster"))
+        key = "learned" if wname == "network" else f"informed_{wname}"
+        out[key] = r
+        sig = float(np.hypot(out["plain"]["mean_E_sigma"], r["mean_E_sigma"]))
+        z = abs(r["mean_E"] - out["plain"]["mean_E"]) / sig if sig > 0 else float("inf")
+        sfx = "" if wname == "network" else f"_{wname}"
+        out[f"ratio_learned_over_plain_E{sfx}"] = r["eff_samples_per_s_E"] / out["plain"]["eff_samples_per_s_E"]
+        out[f"ratio_learned_over_plain_order{sfx}"] = (r["eff_samples_per_s_order"] /
+                                                       out["plain"]["eff_samples_per_s_order"])
+        out[f"E_difference_over_sigma{sfx}"] = z
+        out[f"same_E_within_2sigma{sfx}"] = bool(z <= 2.0)
+    out["runs_hold_50_tau"] = bool(min(v["samples_over_tau_min"] for k, v in out.items()
+                                       if isinstance(v, dict) and "samples_over_tau_min" in v) >= 50)
+    return out
+
+
+def run_learned_comparison(args):
+    """Configuration 3: plain vs learned-proposal effective independent
+    samples per second of the energy and the L1_2 order parameter at
+    T = 0.9 T_c (48^3, x_B = 0.25), from one common equilibrated state."""
+    from casmcode_clexmonte_gb300 import build as B
+
+    B.build()
+    from casmcode_clexmonte_gb300 import calculator as cm
+    from casmcode_clexmonte_gb300 import workloads
+
+    tc = T_C_CONFIG3_K
+    scan = None
+    if args.tc_scan:
+        tc, temps, cv = tc_scan(cm, workloads.config(3).ce)
+        scan = {"T_K": [float(x) for x in temps], "C_per_uc": [float(x) for x in cv]}
+    res = learned_vs_plain(cm, 0.9 * tc, plain_passes=args.plain_passes,
+                           learned_passes=args.learned_passes,
+                           weights=("network", "exact", "uniform"))
+    res["T_c_K"] = tc
+    if scan:
+        res["heat_capacity_scan"] = scan
+    line = {"metric": "effective samples/s (learned vs plain GPU Metropolis, same <E>)", **res}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -748,7 +814,12 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", type=int, default=WORKLOAD_INDEX, choices=[0, 1, 2, 3, 4])
-    ap.add_argument("--learned-passes", type=int, default=40)
+    ap.add_argument("--learned-passes", type=int, default=1200)
+    ap.add_argument("--plain-passes", type=int, default=12000)
+    ap.add_argument("--tc-scan", action="store_true",
+                    help="workload 3: locate T_c by a heat-capacity scan first")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="leave the learned-vs-plain comparison out of the default line")
     ap.add_argument("--nfold", action="store_true",
                     help="n-fold way vs Metropolis sweep (semi-grand canonical, low T)")
     ap.add_argument("--nfold-temperature", type=float, default=150.0)

@@ -158,7 +158,7 @@ def test_canonical_bench_conditions_match_oracle(cm, oracle_mod):
     mus = [None] * len(grid)
     labels = [(f"T={T:.0f} x_B={x}", T) for T, x in grid]
     g, _ = _gpu_chains(cm, ce, "canonical", L, temps, mus, xs, 32, 3000, 500, 71)
-    o = _oracle_chains(oracle_mod, ce, "canonical", L, temps, mus, xs, 16, 260, 60, 73)
+    o = _oracle_chains(oracle_mod, ce, "canonical", L, temps, mus, xs, 16, 560, 60, 73)
     print(_compare(labels, g, o, int(np.prod(L)), sgc=False))
 
 
