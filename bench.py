@@ -533,8 +533,8 @@ def tc_scan(cm, ce):
     return float(temps[inner][int(np.argmax(cv[inner]))]), temps, cv
 
 
-def learned_vs_plain(cm, T: float, plain_passes: int = 12000, learned_passes: int = 1200,
-                     equil_passes: int = 5000, rounds: int = 8, local_substeps: int = 8,
+def learned_vs_plain(cm, T: float, plain_passes: int = 30000, learned_passes: int = 2000,
+                     equil_passes: int = 5000, rounds: int = 4, local_substeps: int = 8,
                      weights=("network",)) -> dict:
     """Configuration 3 (32 x 48^3 FCC, L1_2 cluster expansion, canonical
     x_B = 0.25) at temperature T: plain GPU Metropolis (the colour-class
@@ -814,8 +814,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", type=int, default=WORKLOAD_INDEX, choices=[0, 1, 2, 3, 4])
-    ap.add_argument("--learned-passes", type=int, default=1200)
-    ap.add_argument("--plain-passes", type=int, default=12000)
+    ap.add_argument("--learned-passes", type=int, default=2000)
+    ap.add_argument("--plain-passes", type=int, default=30000)
     ap.add_argument("--tc-scan", action="store_true",
                     help="workload 3: locate T_c by a heat-capacity scan first")
     ap.add_argument("--no-learned", action="store_true",
