@@ -658,8 +658,8 @@ def run_learned_comparison(args):
         tc, temps, cv = tc_scan(cm, workloads.config(3).ce)
         scan = {"T_K": [float(x) for x in temps], "C_per_uc": [float(x) for x in cv]}
     res = learned_vs_plain(cm, 0.9 * tc, plain_passes=args.plain_passes,
-                           learned_passes=args.learned_passes,
-                           weights=("network", "exact", "uniform"))
+                           learned_passes=args.learned_passes, equil_passes=args.equil_passes,
+                           rounds=args.rounds, weights=("network", "exact", "uniform"))
     res["T_c_K"] = tc
     if scan:
         res["heat_capacity_scan"] = scan
@@ -816,6 +816,10 @@ def main():
     ap.add_argument("--workload", type=int, default=WORKLOAD_INDEX, choices=[0, 1, 2, 3, 4])
     ap.add_argument("--learned-passes", type=int, default=2000)
     ap.add_argument("--plain-passes", type=int, default=30000)
+    ap.add_argument("--equil-passes", type=int, default=5000,
+                    help="workload 3: plain passes that equilibrate the common state")
+    ap.add_argument("--rounds", type=int, default=4,
+                    help="workload 3: swap rounds per group of the learned group sweep")
     ap.add_argument("--tc-scan", action="store_true",
                     help="workload 3: locate T_c by a heat-capacity scan first")
     ap.add_argument("--no-learned", action="store_true",
