@@ -4,6 +4,7 @@
 # Needs the reference sources (present only where they are mounted).
 #   build_ref.sh        FCC_binary_vacancy bset.default (one sublattice)
 #   build_ref.sh zro    Clex_ZrO_Occ bset.formation_energy (hcp Zr + O/Va)
+#   build_ref.sh fcc-time  timing probe of the FCC Clexulator's delta evaluation
 # Prints the path of the built probe on its last line.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
@@ -22,6 +23,12 @@ case "${1:-fcc}" in
     [ -f "$SRC" ] || { echo "reference sources not found: $SRC" >&2; exit 2; }
     g++ -O1 -std=c++17 -I "$HERE/ref_shim" "$SRC" "$HERE/ref_probe_fcc.cc" -o "$HERE/_ref/fcc_clexulator_probe"
     echo "$HERE/_ref/fcc_clexulator_probe"
+    ;;
+  fcc-time)
+    SRC="$DATA/FCC_binary_vacancy/basis_sets/bset.default/FCC_binary_vacancy_Clexulator_default.cc"
+    [ -f "$SRC" ] || { echo "reference sources not found: $SRC" >&2; exit 2; }
+    g++ -O3 -std=c++17 -I "$HERE/ref_shim" "$SRC" "$HERE/ref_time_fcc.cc" -o "$HERE/_ref/fcc_clexulator_time"
+    echo "$HERE/_ref/fcc_clexulator_time"
     ;;
   zro)
     SRC="$DATA/Clex_ZrO_Occ/basis_sets/bset.formation_energy/ZrO_Clexulator_formation_energy.cc"

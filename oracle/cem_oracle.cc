@@ -871,6 +871,22 @@ double ora_delta(void *h, const signed char *occ, int n, const i64 *sites, const
   return event_delta(s, o, n, sites, new_occ, dcount);
 }
 
+// Single-thread timing of n independent one-site energy changes on one
+// occupation (each evaluated as ora_delta does, the state left unchanged):
+// the oracle's counterpart of a Clexulator's per-site delta evaluation.
+// Returns seconds; *checksum receives the sum of the energy changes.
+double ora_time_delta(void *h, const signed char *occ, i64 n, const i64 *sites, const int *new_occ,
+                      double *checksum) {
+  System &s = *(System *)h;
+  std::vector<signed char> o(occ, occ + s.n_sites);
+  double sum = 0.0;
+  const auto t0 = std::chrono::steady_clock::now();
+  for (i64 e = 0; e < n; ++e) sum += event_delta(s, o, 1, sites + e, new_occ + e, nullptr);
+  const auto t1 = std::chrono::steady_clock::now();
+  if (checksum) *checksum = sum;
+  return std::chrono::duration<double>(t1 - t0).count();
+}
+
 // occ_delta_per_supercell of the semi-grand canonical potential.
 double ora_delta_sgc(void *h, const signed char *occ, int n, const i64 *sites,
                      const int *new_occ, const double *mu, i64 *dcount) {

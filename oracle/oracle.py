@@ -81,6 +81,9 @@ def lib():
             P, i8p, C.c_int, C.c_int, f64p, f64p, C.c_uint64, C.c_int64, C.c_int,
             C.POINTER(C.c_int64),
         ]
+        L.ora_time_delta.restype = C.c_double
+        L.ora_time_delta.argtypes = [P, i8p, C.c_int64, C.c_void_p, C.c_void_p,
+                                     C.POINTER(C.c_double)]
         L.ora_run_chains.restype = C.c_double
         L.ora_run_chains.argtypes = [
             P, i8p, C.c_int, C.c_int, f64p, f64p, C.c_uint64, C.c_int64, C.c_int,
@@ -267,6 +270,17 @@ class OracleSystem:
             raise RuntimeError(lib().ora_last_error().decode())
         return dict(n=int(n), site=rec_site[:record], occ=rec_occ[:record], dt=rec_dt[:record],
                     stats=st)
+
+    def time_delta(self, occ, sites, new_occ):
+        """(seconds, checksum) of independent one-site energy changes on one
+        thread (the state is left unchanged)."""
+        sites = np.ascontiguousarray(sites, dtype=np.int64)
+        new_occ = np.ascontiguousarray(new_occ, dtype=np.int32)
+        o = np.ascontiguousarray(occ, dtype=np.int8)
+        cs = C.c_double()
+        secs = lib().ora_time_delta(self.h, o, len(sites), sites.ctypes.data, new_occ.ctypes.data,
+                                    C.byref(cs))
+        return secs, cs.value
 
     def run_chains(self, occ, ensemble, temps, mus, seed, n_passes, n_threads):
         """Independent sequential chains (chain r: block r of ``occ``, updated
