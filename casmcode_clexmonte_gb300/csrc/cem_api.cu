@@ -1816,6 +1816,38 @@ int cem_mlp_forward_tc(cem_mlp *m, int64_t n, const int8_t *features, float *log
   });
 }
 
+int cem_mlp_forward_umma(cem_mlp *m, int64_t n, const int8_t *features, float *logits) {
+  return guard([&] {
+    require(m && features && logits && n >= 0, "bad argument");
+    if (n == 0) return;
+    int8_t *dx = nullptr;
+    float *dz = nullptr;
+    int *dst = nullptr;
+    auto cleanup = [&] {
+      cudaFree(dx);
+      cudaFree(dz);
+      cudaFree(dst);
+    };
+    try {
+      CUDA_OK(cudaMalloc(&dx, (size_t)n * MLP_IN));
+      CUDA_OK(cudaMalloc(&dz, (size_t)n * 4));
+      CUDA_OK(cudaMalloc(&dst, 4));
+      CUDA_OK(cudaMemsetAsync(dst, 0, 4, m->stream));
+      CUDA_OK(cudaMemcpyAsync(dx, features, (size_t)n * MLP_IN, cudaMemcpyHostToDevice, m->stream));
+      CUDA_OK(mlp_forward_umma(m->d_params, dx, n, dz, dst, m->stream));
+      int status = 0;
+      CUDA_OK(cudaMemcpyAsync(logits, dz, (size_t)n * 4, cudaMemcpyDeviceToHost, m->stream));
+      CUDA_OK(cudaMemcpyAsync(&status, dst, 4, cudaMemcpyDeviceToHost, m->stream));
+      CUDA_OK(cudaStreamSynchronize(m->stream));
+      if (status) throw Err(CEM_ERR_DEVICE, "a tensor-core MMA did not complete within the wait limit");
+    } catch (...) {
+      cleanup();
+      throw;
+    }
+    cleanup();
+  });
+}
+
 int cem_mlp_gradient(cem_mlp *m, int64_t n, const int8_t *features, const float *targets,
                      float *grad, double *loss) {
   return guard([&] {

@@ -51,6 +51,7 @@
 
 #include "cem_kernels.cuh"
 #include "cem_learned.cuh"
+#include "cem_umma.cuh"
 
 namespace cem {
 
@@ -653,6 +654,62 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
     }
   }
   cluster.sync();  // no CTA leaves while a peer may still write to it
+}
+
+// Inference of n environments on tcgen05 (the network of umma_network): 4
+// warpgroups per CTA, 128 environments per warpgroup and batch; status[0]
+// is set when an MMA wait ran out.
+constexpr int UMMA_FWD_THREADS = 512;
+constexpr int UMMA_FWD_SMEM = UMMA_B1_BYTES + UMMA_B2_BYTES + 4 * UMMA_A_BYTES + 1024;
+__global__ void __launch_bounds__(UMMA_FWD_THREADS)
+    k_mlp_forward_umma(const __nv_bfloat16 *__restrict__ params, const int8_t *__restrict__ X,
+                       long long n, float *__restrict__ z, int *status) {
+  extern __shared__ __align__(128) unsigned char usm[];
+  unsigned char *b1 = usm, *b2 = usm + UMMA_B1_BYTES;
+  unsigned char *abufs = b2 + UMMA_B2_BYTES;
+  float *fb = reinterpret_cast<float *>(abufs + 4 * UMMA_A_BYTES);  // 193 floats
+  uint64_t *bars = reinterpret_cast<uint64_t *>(fb + 196);             // 4 mbarriers
+  uint32_t *slot = reinterpret_cast<uint32_t *>(bars + 4);
+  const int tid = threadIdx.x, warp = tid >> 5, wg = warp >> 2;
+  umma_load_net(params, b1, b2, fb, tid, UMMA_FWD_THREADS);
+  if (tid < 4) mbar_init(&bars[tid], 1);
+  if (warp == 0) tmem_alloc(slot, 4 * UMMA_COLS);
+  mbar_init_fence();
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tm = *slot + (uint32_t)(wg * UMMA_COLS);
+  const UmmaNet net{b1, b2, fb, fb + 64, fb + 128, fb[192]};
+  unsigned char *abuf = abufs + wg * UMMA_A_BYTES;
+  uint32_t phase = 0;
+  bool timeout = false;
+  const int row = tid & 127;
+  for (long long t = (long long)blockIdx.x * 4 + wg; t * 128 < n; t += (long long)gridDim.x * 4) {
+    const long long e = t * 128 + row;
+    unsigned long long env = 0ull;
+    if (e < n)
+      for (int k = 0; k < MLP_IN; ++k) env |= (unsigned long long)(X[e * MLP_IN + k] != 0) << k;
+    const float zz = umma_network(net, abuf, tm, &bars[wg], phase, wg, env, timeout);
+    if (e < n) z[e] = zz;
+  }
+  if (timeout) atomicExch(status, 1);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(*slot, 4 * UMMA_COLS);
+}
+
+cudaError_t mlp_forward_umma(const __nv_bfloat16 *params, const int8_t *X, long long n, float *z,
+                             int *status, cudaStream_t st) {
+  cudaError_t e =
+      cudaFuncSetAttribute(k_mlp_forward_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, UMMA_FWD_SMEM);
+  if (e != cudaSuccess) return e;
+  long long grid = (n + 511) / 512;
+  if (grid > 304) grid = 304;  // two CTAs per SM: 2 x 256 tensor-memory columns
+  if (grid < 1) grid = 1;
+  k_mlp_forward_umma<<<(int)grid, UMMA_FWD_THREADS, UMMA_FWD_SMEM, st>>>(params, X, n, z, status);
+  return cudaGetLastError();
 }
 
 cudaError_t mlp_forward_tc(const __nv_bfloat16 *params, const int8_t *X, long long n, float *z,

@@ -325,6 +325,10 @@ int cem_mlp_forward(cem_mlp *m, int64_t n, const int8_t *features, float *logits
  * accumulation; layer-1 activations rounded to bf16 as layer 2's operand):
  * the inference path of cem_learned_group_run */
 int cem_mlp_forward_tc(cem_mlp *m, int64_t n, const int8_t *features, float *logits);
+/* the same logits on the 5th-generation tensor cores (tcgen05.mma, operands
+ * bf16 in shared memory, fp32 accumulators in tensor memory, 128
+ * environments per warpgroup); CEM_ERR_DEVICE if an MMA wait ran out */
+int cem_mlp_forward_umma(cem_mlp *m, int64_t n, const int8_t *features, float *logits);
 /* gradient of the mean-squared error 1/(2n) sum (z - t)^2 at the current
  * (bf16) parameters, and the loss */
 int cem_mlp_gradient(cem_mlp *m, int64_t n, const int8_t *features, const float *targets,
