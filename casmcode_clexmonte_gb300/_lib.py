@@ -57,7 +57,7 @@ EXPORTS = [
     "cem_reset_stats", "cem_synchronize", "cem_request_stop", "cem_last_kernel_ms", "cem_smem_bandwidth",
     "cem_set_option", "cem_get_option", "cem_autotune", "cem_step_async", "cem_delta_energy_noalloc",
     "cem_mlp_info", "cem_mlp_create", "cem_mlp_destroy", "cem_mlp_get_params",
-    "cem_mlp_set_params", "cem_mlp_forward", "cem_mlp_forward_tc", "cem_mlp_forward_umma",
+    "cem_mlp_set_params", "cem_mlp_forward", "cem_mlp_forward_tc",
     "cem_mlp_gradient", "cem_mlp_train",
     "cem_learned_features", "cem_learned_run", "cem_learned_group_run", "cem_learned_samples",
     "cem_get_order_samples",
@@ -121,7 +121,6 @@ def load(path: str = LIB):
     L.cem_mlp_set_params.argtypes = [P, vp]
     L.cem_mlp_forward.argtypes = [P, C.c_int64, vp, vp]
     L.cem_mlp_forward_tc.argtypes = [P, C.c_int64, vp, vp]
-    L.cem_mlp_forward_umma.argtypes = [P, C.c_int64, vp, vp]
     L.cem_mlp_gradient.argtypes = [P, C.c_int64, vp, vp, vp, C.POINTER(C.c_double)]
     L.cem_mlp_train.argtypes = [P, C.c_int64, vp, vp, C.c_int, C.c_int, C.c_float, C.c_uint64, vp]
     L.cem_learned_features.argtypes = [P, C.c_int, vp, vp]

@@ -382,17 +382,10 @@ class LearnedProposal:
         return z
 
     def forward_tc(self, X) -> np.ndarray:
-        """Logits on the tensor-core path of the group sweep."""
+        """Logits on the tensor-core (tcgen05) path of the group sweep."""
         X = np.ascontiguousarray(X, dtype=np.int8)
         z = np.zeros(len(X), dtype=np.float32)
         check(self.lib.cem_mlp_forward_tc(self.handle, len(X), ptr(X), ptr(z)))
-        return z
-
-    def forward_umma(self, X) -> np.ndarray:
-        """Logits on the tcgen05 path (tensor-memory accumulators)."""
-        X = np.ascontiguousarray(X, dtype=np.int8)
-        z = np.zeros(len(X), dtype=np.float32)
-        check(self.lib.cem_mlp_forward_umma(self.handle, len(X), ptr(X), ptr(z)))
         return z
 
     def gradient(self, X, t):

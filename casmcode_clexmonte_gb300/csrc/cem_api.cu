@@ -1291,6 +1291,10 @@ int cem_get_stats(cem_replicas *r, int i, cem_stats *out) {
     if (S.status == 5)
       throw Err(CEM_ERR_DEVICE,
                 "a shared-memory staging copy did not complete; the replica was left unchanged");
+    if (S.status == 8)
+      throw Err(CEM_ERR_DEVICE,
+                "a tensor-core MMA of the learned group sweep did not complete within the wait "
+                "limit; the run's results are invalid");
     if (S.status == 6)
       throw Err(CEM_ERR_DEVICE,
                 "a shared-memory staging copy did not complete and was still in flight when the "
@@ -1799,29 +1803,6 @@ int cem_mlp_forward_tc(cem_mlp *m, int64_t n, const int8_t *features, float *log
     if (n == 0) return;
     int8_t *dx = nullptr;
     float *dz = nullptr;
-    try {
-      CUDA_OK(cudaMalloc(&dx, (size_t)n * MLP_IN));
-      CUDA_OK(cudaMalloc(&dz, (size_t)n * 4));
-      CUDA_OK(cudaMemcpyAsync(dx, features, (size_t)n * MLP_IN, cudaMemcpyHostToDevice, m->stream));
-      CUDA_OK(mlp_forward_tc(m->d_params, dx, n, dz, m->stream));
-      CUDA_OK(cudaMemcpyAsync(logits, dz, (size_t)n * 4, cudaMemcpyDeviceToHost, m->stream));
-      CUDA_OK(cudaStreamSynchronize(m->stream));
-    } catch (...) {
-      cudaFree(dx);
-      cudaFree(dz);
-      throw;
-    }
-    cudaFree(dx);
-    cudaFree(dz);
-  });
-}
-
-int cem_mlp_forward_umma(cem_mlp *m, int64_t n, const int8_t *features, float *logits) {
-  return guard([&] {
-    require(m && features && logits && n >= 0, "bad argument");
-    if (n == 0) return;
-    int8_t *dx = nullptr;
-    float *dz = nullptr;
     int *dst = nullptr;
     auto cleanup = [&] {
       cudaFree(dx);
@@ -1834,7 +1815,7 @@ int cem_mlp_forward_umma(cem_mlp *m, int64_t n, const int8_t *features, float *l
       CUDA_OK(cudaMalloc(&dst, 4));
       CUDA_OK(cudaMemsetAsync(dst, 0, 4, m->stream));
       CUDA_OK(cudaMemcpyAsync(dx, features, (size_t)n * MLP_IN, cudaMemcpyHostToDevice, m->stream));
-      CUDA_OK(mlp_forward_umma(m->d_params, dx, n, dz, dst, m->stream));
+      CUDA_OK(mlp_forward_tc(m->d_params, dx, n, dz, dst, m->stream));
       int status = 0;
       CUDA_OK(cudaMemcpyAsync(logits, dz, (size_t)n * 4, cudaMemcpyDeviceToHost, m->stream));
       CUDA_OK(cudaMemcpyAsync(&status, dst, 4, cudaMemcpyDeviceToHost, m->stream));

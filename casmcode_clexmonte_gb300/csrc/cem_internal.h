@@ -118,9 +118,7 @@ cudaError_t learned_run(const CeTables &T, const Replica *reps, ReplicaStats *st
 
 // learned group sweep (cem_lgroup.cu)
 cudaError_t mlp_forward_tc(const __nv_bfloat16 *params, const int8_t *X, long long n, float *z,
-                           cudaStream_t st);
-cudaError_t mlp_forward_umma(const __nv_bfloat16 *params, const int8_t *X, long long n, float *z,
-                             int *status, cudaStream_t st);
+                           int *status, cudaStream_t st);
 bool lgroup_supported(int L);
 int lgroup_smem_bytes(int L);
 cudaError_t lgroup_run(const CeTables &T, const Replica *reps, ReplicaStats *stats, int8_t *occ,

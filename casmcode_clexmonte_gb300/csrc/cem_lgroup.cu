@@ -38,11 +38,11 @@
 // draws depend only on (pass, sub-step, group, round), so the chain is the
 // same for every cluster size.
 //
-// Network evaluation: the two dense layers of 32 environments at a time on
-// the tensor cores (mma.sync m16n8k16, bf16 operands, fp32 accumulation):
-// inputs (0/1, exact in bf16) x W1[42->48 padded][64], ReLU, x W2[64][64],
-// ReLU, dot w3; the accumulator fragments of layer 1 are the A fragments of
-// layer 2.
+// Network evaluation on the 5th-generation tensor cores (cem_umma.cuh): the
+// four warps of a warpgroup evaluate their 4 groups (128 sites) together,
+// one tcgen05.mma issuer per warpgroup, bf16 operands in shared memory, fp32
+// accumulators in tensor memory (64 columns per warpgroup), one site per
+// thread in the epilogue.
 #include <cooperative_groups.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -59,8 +59,9 @@ constexpr int LG_THREADS = 512;
 constexpr int LG_NW = LG_THREADS / 32;
 constexpr int LG_CLASSES = 27;
 constexpr uint32_t TAG_LG_SCHED = 0x5u, TAG_LG_GROUP = 0x6u, TAG_LG_LOCAL = 0x7u;
-// fragment tables of the network: [k-step][n-tile][lane] (b0, b1)
-constexpr int LG_W1_FRAGS = 3 * 8 * 32, LG_W2_FRAGS = 4 * 8 * 32;
+// network tables of the tcgen05 path: W1^T, W2^T, one operand buffer per
+// warpgroup, biases (193 floats), per-warpgroup mbarriers, tensor-memory slot
+constexpr int LG_NET_BYTES = UMMA_B1_BYTES + UMMA_B2_BYTES + 4 * UMMA_A_BYTES + 1024;
 
 struct LGroupParams {
   const Replica *reps;
@@ -76,149 +77,10 @@ struct LGroupParams {
   int cluster;               // CTAs per replica (thread-block cluster size)
 };
 
-__device__ __forceinline__ void mma_bf16_16816(float (&c)[4], uint32_t a0, uint32_t a1,
-                                               uint32_t a2, uint32_t a3, uint32_t b0,
-                                               uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-      "{%8,%9}, {%0,%1,%2,%3};"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
-// bf16 pair (lower half: element k) of bits k and k + 1 of a 0/1 mask.
-__device__ __forceinline__ uint32_t lg_bits2(unsigned long long e, int k) {
-  const uint32_t x = (uint32_t)(e >> k) & 3u;
-  return ((x & 1u) * 0x3F80u) | ((x >> 1) * 0x3F800000u);
-}
-
-__device__ __forceinline__ uint32_t lg_pack(float lo, float hi) {
-  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-  return *reinterpret_cast<const uint32_t *>(&v);
-}
-
 __device__ __forceinline__ unsigned long long shfl64(unsigned long long v, int src) {
   const uint32_t lo = __shfl_sync(0xffffffffu, (uint32_t)v, src);
   const uint32_t hi = __shfl_sync(0xffffffffu, (uint32_t)(v >> 32), src);
   return ((unsigned long long)hi << 32) | lo;
-}
-
-// Network tables in shared memory: B fragments of W1 (rows 42..47 zero) and
-// W2, and the fp32 biases and output weights.
-struct LgNet {
-  const uint2 *w1, *w2;
-  const float *b1, *b2, *w3;
-  float b3;
-};
-
-// Logit of the environment of each lane's site (all 32 lanes take part).
-__device__ __forceinline__ float lg_network(const LgNet &N, unsigned long long env, int lane) {
-  const int g = lane >> 2, tig = lane & 3;
-  float zout = 0.f;
-#pragma unroll
-  for (int mt = 0; mt < 2; ++mt) {
-    const unsigned long long e0 = shfl64(env, 16 * mt + g), e1 = shfl64(env, 16 * mt + g + 8);
-    float acc[8][4];
-#pragma unroll
-    for (int t = 0; t < 8; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
-#pragma unroll
-    for (int s = 0; s < 3; ++s) {
-      const int k0 = 16 * s + 2 * tig;
-      const uint32_t a0 = lg_bits2(e0, k0), a1 = lg_bits2(e1, k0);
-      const uint32_t a2 = lg_bits2(e0, k0 + 8), a3 = lg_bits2(e1, k0 + 8);
-#pragma unroll
-      for (int t = 0; t < 8; ++t) {
-        const uint2 b = N.w1[(s * 8 + t) * 32 + lane];
-        mma_bf16_16816(acc[t], a0, a1, a2, a3, b.x, b.y);
-      }
-    }
-    uint32_t A2[4][4];
-#pragma unroll
-    for (int t = 0; t < 8; ++t) {
-      const int c0 = 8 * t + 2 * tig;
-      const float v0 = fmaxf(acc[t][0] + N.b1[c0], 0.f), v1 = fmaxf(acc[t][1] + N.b1[c0 + 1], 0.f);
-      const float v2 = fmaxf(acc[t][2] + N.b1[c0], 0.f), v3 = fmaxf(acc[t][3] + N.b1[c0 + 1], 0.f);
-      A2[t >> 1][(t & 1) * 2 + 0] = lg_pack(v0, v1);
-      A2[t >> 1][(t & 1) * 2 + 1] = lg_pack(v2, v3);
-    }
-    float p0 = 0.f, p1 = 0.f;
-#pragma unroll
-    for (int t = 0; t < 8; ++t) {
-      float c[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const uint2 b = N.w2[(j * 8 + t) * 32 + lane];
-        mma_bf16_16816(c, A2[j][0], A2[j][1], A2[j][2], A2[j][3], b.x, b.y);
-      }
-      const int c0 = 8 * t + 2 * tig;
-      p0 = fmaf(fmaxf(c[0] + N.b2[c0], 0.f), N.w3[c0], p0);
-      p0 = fmaf(fmaxf(c[1] + N.b2[c0 + 1], 0.f), N.w3[c0 + 1], p0);
-      p1 = fmaf(fmaxf(c[2] + N.b2[c0], 0.f), N.w3[c0], p1);
-      p1 = fmaf(fmaxf(c[3] + N.b2[c0 + 1], 0.f), N.w3[c0 + 1], p1);
-    }
-    p0 += __shfl_xor_sync(0xffffffffu, p0, 1);
-    p0 += __shfl_xor_sync(0xffffffffu, p0, 2);
-    p1 += __shfl_xor_sync(0xffffffffu, p1, 1);
-    p1 += __shfl_xor_sync(0xffffffffu, p1, 2);
-    const int r = lane - 16 * mt;  // this lane's row in the m-tile
-    const float q0 = __shfl_sync(0xffffffffu, p0, 4 * (r & 7));
-    const float q1 = __shfl_sync(0xffffffffu, p1, 4 * (r & 7));
-    if (r >= 0 && r < 16) zout = (r < 8 ? q0 : q1) + N.b3;
-  }
-  return zout;
-}
-
-// Network tables in shared memory from the bf16 parameter block: B
-// fragments of W1 (rows >= 42 zero) and W2, biases and output weights.
-__device__ __forceinline__ void lg_load_net(const __nv_bfloat16 *__restrict__ P, uint2 *fw1,
-                                            uint2 *fw2, float *fb, int tid, int nth) {
-  auto w1 = [&](int k, int j) -> __nv_bfloat16 {
-    return k < MLP_IN ? P[MLP_W1 + k * MLP_H + j] : __float2bfloat16_rn(0.f);
-  };
-  auto pair = [](__nv_bfloat16 lo, __nv_bfloat16 hi) -> uint32_t {
-    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
-  };
-  for (int i = tid; i < LG_W1_FRAGS; i += nth) {
-    const int ln = i & 31, st = i >> 5, t = st & 7, s = st >> 3;
-    const int g = ln >> 2, tg = ln & 3, n = 8 * t + g, k = 16 * s + 2 * tg;
-    fw1[i] = make_uint2(pair(w1(k, n), w1(k + 1, n)), pair(w1(k + 8, n), w1(k + 9, n)));
-  }
-  const __nv_bfloat16 *W2 = P + MLP_W2;
-  for (int i = tid; i < LG_W2_FRAGS; i += nth) {
-    const int ln = i & 31, st = i >> 5, t = st & 7, s = st >> 3;
-    const int g = ln >> 2, tg = ln & 3, n = 8 * t + g, k = 16 * s + 2 * tg;
-    fw2[i] = make_uint2(pair(W2[k * MLP_H + n], W2[(k + 1) * MLP_H + n]),
-                        pair(W2[(k + 8) * MLP_H + n], W2[(k + 9) * MLP_H + n]));
-  }
-  for (int i = tid; i < MLP_H; i += nth) {
-    fb[i] = __bfloat162float(P[MLP_B1 + i]);
-    fb[64 + i] = __bfloat162float(P[MLP_B2 + i]);
-    fb[128 + i] = __bfloat162float(P[MLP_W3 + i]);
-  }
-  if (tid == 0) fb[192] = __bfloat162float(P[MLP_B3]);
-}
-
-// Inference of n environments (n x 42 occupants) on the tensor cores, the
-// path the group sweep uses: 32 environments per warp, layer-1 activations
-// rounded to bf16 as layer 2's operand.
-__global__ void k_mlp_forward_tc(const __nv_bfloat16 *__restrict__ params,
-                                 const int8_t *__restrict__ X, long long n, float *__restrict__ z) {
-  __shared__ uint2 fw1[LG_W1_FRAGS], fw2[LG_W2_FRAGS];
-  __shared__ float fb[200];
-  lg_load_net(params, fw1, fw2, fb, threadIdx.x, blockDim.x);
-  __syncthreads();
-  const LgNet net{fw1, fw2, fb, fb + 64, fb + 128, fb[192]};
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (long long tile = (long long)blockIdx.x * nw + warp; tile * 32 < n;
-       tile += (long long)gridDim.x * nw) {
-    const long long e = tile * 32 + lane;
-    unsigned long long env = 0ull;
-    if (e < n)
-      for (int k = 0; k < MLP_IN; ++k)
-        env |= (unsigned long long)(X[e * MLP_IN + k] != 0) << k;
-    const float zz = lg_network(net, env, lane);
-    if (e < n) z[e] = zz;
-  }
 }
 
 // a^-1 mod n for gcd(a, n) = 1 (extended Euclid)
@@ -280,9 +142,12 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
   G.W = G.H = PITCH;
   G.V = V;
   int8_t *occ = reinterpret_cast<int8_t *>(smem);
-  uint2 *fw1 = reinterpret_cast<uint2 *>(smem + align16(V));
-  uint2 *fw2 = fw1 + LG_W1_FRAGS;
-  float *fb = reinterpret_cast<float *>(fw2 + LG_W2_FRAGS);  // b1[64], b2[64], w3[64], b3
+  unsigned char *nb1 = smem + ((align16(V) + 127) & ~127);  // 128-byte aligned operands
+  unsigned char *nb2 = nb1 + UMMA_B1_BYTES;
+  unsigned char *abufs = nb2 + UMMA_B2_BYTES;  // [4 warpgroups][UMMA_A_BYTES]
+  float *fb = reinterpret_cast<float *>(abufs + 4 * UMMA_A_BYTES);  // b1, b2, w3, b3
+  uint64_t *nbar = reinterpret_cast<uint64_t *>(fb + 196);          // [4]
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(nbar + 4);
   __shared__ int s_order[LG_CLASSES];
   __shared__ uint32_t s_key[LG_CLASSES], s_ainv[LG_CLASSES], s_boff[LG_CLASSES];
   __shared__ int s_local[64];  // class | parity << 5 | neighbour << 8
@@ -297,7 +162,14 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
   const float beta_f = R.beta_f;
   const uint32_t k0 = (uint32_t)R.seed, k1 = (uint32_t)(R.seed >> 32);
 
-  if (mode == 1) lg_load_net(LP.params, fw1, fw2, fb, tid, LG_THREADS);
+  if (mode == 1) {
+    umma_load_net(LP.params, nb1, nb2, fb, tid, LG_THREADS);
+    if (tid < 4) mbar_init(&nbar[tid], 1);
+    if (warp == 0) tmem_alloc(tslot, 4 * UMMA_COLS);
+    mbar_init_fence();
+    fence_proxy_async_smem();
+    tc_fence_before();
+  }
   // ---- stage the replica with its periodic halo
   const int8_t *gocc = LP.occ + R.occ_offset;
   for (int l = tid; l < N_SITES; l += LG_THREADS) {
@@ -355,7 +227,12 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
   }
   __syncthreads();
 
-  const LgNet net{fw1, fw2, fb, fb + 64, fb + 128, mode == 1 ? fb[192] : 0.f};
+  if (mode == 1) tc_fence_after();  // the barriers above ordered the allocation
+  const UmmaNet net{nb1, nb2, fb, fb + 64, fb + 128, mode == 1 ? fb[192] : 0.f};
+  const int wg = warp >> 2;
+  const uint32_t tm = mode == 1 ? *tslot + (uint32_t)(wg * UMMA_COLS) : 0u;
+  uint32_t nphase = 0;
+  bool ntimeout = false;
   // every copy of the replica (own and peers' shared memory) receives each
   // accepted change
   auto put_all = [&](int x, int y, int z, int8_t v) {
@@ -410,9 +287,16 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
       const int c = s_order[sub];
       const int cx = c % 3, cy = (c / 3) % 3, cz = c / 9;
       const uint32_t ainv = s_ainv[c], boff = s_boff[c];
-      for (int grp = crank * LG_NW + warp; grp < N_GROUPS; grp += CL * LG_NW) {
+      // warps iterate in step so that the four warps of a warpgroup evaluate
+      // the network together; a warpgroup stops when its first warp has no
+      // group left (the later warps then have none either)
+      const int n_iter = (N_GROUPS + CL * LG_NW - 1) / (CL * LG_NW);
+      for (int it = 0; it < n_iter; ++it) {
+        const int grp0 = it * CL * LG_NW + crank * LG_NW;
+        if (grp0 + 4 * wg >= N_GROUPS) break;
+        const int grp = grp0 + warp;
         const int r = grp * 32 + lane;
-        const bool act = r < N_C;
+        const bool act = grp < N_GROUPS && r < N_C;
         int x = 0, y = 0, z = 0, ad = 0, o = 0;
         int n[gen_fcc::N_ORBITS] = {0, 0, 0, 0, 0, 0};
         unsigned long long env = 0ull;
@@ -431,7 +315,7 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
         }
         const float eab = lg_eab(T, n);
         float zl = 0.f;
-        if (mode == 1) zl = lg_network(net, env, lane);
+        if (mode == 1) zl = umma_network(net, abufs + wg * UMMA_A_BYTES, tm, &nbar[wg], nphase, wg, env, ntimeout);
         else if (mode == 2) zl = FMUL(-0.5f * beta_f, eab);
         const uint32_t wA = mode ? (uint32_t)logit_weight(zl) : 1u;
         const uint32_t wB = mode ? (uint32_t)logit_weight(-zl) : 1u;
@@ -653,6 +537,13 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
       for (int k = 0; k < 4; ++k) S.n_sub[k] = nsub[k];
     }
   }
+  if (mode == 1) {
+    if (ntimeout) atomicExch(&S.status, 8);  // an MMA wait ran out: results are invalid
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(*tslot, 4 * UMMA_COLS);
+  }
   cluster.sync();  // no CTA leaves while a peer may still write to it
 }
 
@@ -662,7 +553,7 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
 constexpr int UMMA_FWD_THREADS = 512;
 constexpr int UMMA_FWD_SMEM = UMMA_B1_BYTES + UMMA_B2_BYTES + 4 * UMMA_A_BYTES + 1024;
 __global__ void __launch_bounds__(UMMA_FWD_THREADS)
-    k_mlp_forward_umma(const __nv_bfloat16 *__restrict__ params, const int8_t *__restrict__ X,
+    k_mlp_forward_tc(const __nv_bfloat16 *__restrict__ params, const int8_t *__restrict__ X,
                        long long n, float *__restrict__ z, int *status) {
   extern __shared__ __align__(128) unsigned char usm[];
   unsigned char *b1 = usm, *b2 = usm + UMMA_B1_BYTES;
@@ -700,30 +591,21 @@ __global__ void __launch_bounds__(UMMA_FWD_THREADS)
   if (warp == 0) tmem_dealloc(*slot, 4 * UMMA_COLS);
 }
 
-cudaError_t mlp_forward_umma(const __nv_bfloat16 *params, const int8_t *X, long long n, float *z,
+cudaError_t mlp_forward_tc(const __nv_bfloat16 *params, const int8_t *X, long long n, float *z,
                              int *status, cudaStream_t st) {
   cudaError_t e =
-      cudaFuncSetAttribute(k_mlp_forward_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, UMMA_FWD_SMEM);
+      cudaFuncSetAttribute(k_mlp_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, UMMA_FWD_SMEM);
   if (e != cudaSuccess) return e;
   long long grid = (n + 511) / 512;
   if (grid > 304) grid = 304;  // two CTAs per SM: 2 x 256 tensor-memory columns
   if (grid < 1) grid = 1;
-  k_mlp_forward_umma<<<(int)grid, UMMA_FWD_THREADS, UMMA_FWD_SMEM, st>>>(params, X, n, z, status);
-  return cudaGetLastError();
-}
-
-cudaError_t mlp_forward_tc(const __nv_bfloat16 *params, const int8_t *X, long long n, float *z,
-                           cudaStream_t st) {
-  long long grid = (n + 255) / 256;
-  if (grid > 4096) grid = 4096;
-  if (grid < 1) grid = 1;
-  k_mlp_forward_tc<<<(int)grid, 256, 0, st>>>(params, X, n, z);
+  k_mlp_forward_tc<<<(int)grid, UMMA_FWD_THREADS, UMMA_FWD_SMEM, st>>>(params, X, n, z, status);
   return cudaGetLastError();
 }
 
 int lgroup_smem_bytes(int L) {
   const int pitch = L + 4;
-  return align16(pitch * pitch * pitch) + (LG_W1_FRAGS + LG_W2_FRAGS) * 8 + 200 * 4;
+  return ((align16(pitch * pitch * pitch) + 127) & ~127) + LG_NET_BYTES;
 }
 
 bool lgroup_supported(int L) { return L == 12 || L == 24 || L == 36 || L == 48; }

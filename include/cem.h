@@ -321,14 +321,12 @@ int cem_mlp_get_params(cem_mlp *m, float *master);
 int cem_mlp_set_params(cem_mlp *m, const float *master);
 /* logits of n environments (n x 42 int8 occupants) */
 int cem_mlp_forward(cem_mlp *m, int64_t n, const int8_t *features, float *logits);
-/* the same logits on the tensor cores (mma.sync, bf16 operands, fp32
- * accumulation; layer-1 activations rounded to bf16 as layer 2's operand):
- * the inference path of cem_learned_group_run */
+/* the same logits on the 5th-generation tensor cores, the inference path of
+ * cem_learned_group_run: tcgen05.mma with bf16 operands in shared memory and
+ * fp32 accumulators in tensor memory, 128 environments per warpgroup,
+ * layer-1 activations rounded to bf16 as layer 2's operand; CEM_ERR_DEVICE if
+ * an MMA wait ran out */
 int cem_mlp_forward_tc(cem_mlp *m, int64_t n, const int8_t *features, float *logits);
-/* the same logits on the 5th-generation tensor cores (tcgen05.mma, operands
- * bf16 in shared memory, fp32 accumulators in tensor memory, 128
- * environments per warpgroup); CEM_ERR_DEVICE if an MMA wait ran out */
-int cem_mlp_forward_umma(cem_mlp *m, int64_t n, const int8_t *features, float *logits);
 /* gradient of the mean-squared error 1/(2n) sum (z - t)^2 at the current
  * (bf16) parameters, and the loss */
 int cem_mlp_gradient(cem_mlp *m, int64_t n, const int8_t *features, const float *targets,
@@ -361,7 +359,7 @@ int cem_learned_run(cem_replicas *r, const cem_mlp *m, int64_t n_passes, int64_t
  * weights: 0 every weight 1 (uniform swaps inside groups); 1 the network m
  * (w_A = round(2^12 exp(z)), w_B = round(2^12 exp(-z)) of the site's
  * environment logit z, evaluated once per site and sub-step on the tensor
- * cores); 2 the exact locally balanced weights, z = -beta dE_AB / 2, the
+ * cores, tcgen05); 2 the exact locally balanced weights, z = -beta dE_AB / 2, the
  * quantity the network is trained to predict. rounds 1..CEM_LGROUP_MAX_ROUNDS,
  * local_substeps 1..CEM_LGROUP_MAX_LOCAL. Equal cubic supercells of 12, 24,
  * 36 or 48 cells. Samples per pass as cem_learned_run (cem_learned_samples);
