@@ -30,6 +30,29 @@ struct StreamParams {
   double RT[16];
 };
 
+// A CTA's share of a sub-step's candidate grid (g0 x g1 x g2, x fastest):
+// full x rows over a (y, z) tile of a grid of ny x nz tiles, ny nz <= the
+// CTAs per replica. A box of rows keeps the neighbour reads of a CTA local
+// (a slab of contiguous candidates would span whole planes and read each
+// plane's halo rows again in the next CTA). Candidate ql of the tile, ql <
+// count, is cell (ql mod g0, y0 + (ql / g0) mod cy, z0 + ql / (g0 cy)).
+struct StreamTile {
+  int y0, z0, cy, cz, count;
+  __device__ StreamTile(int g0, int g1, int g2) {
+    const int nb = gridDim.x;
+    int nz = 1;
+    while ((nz + 1) * (nz + 1) <= nb) ++nz;
+    const int ny = nb / nz;
+    const int ty = (g1 + ny - 1) / ny, tz = (g2 + nz - 1) / nz;
+    const int b = blockIdx.x, by = b % ny, bz = b / ny;
+    y0 = by * ty;
+    z0 = bz * tz;
+    cy = (b < ny * nz) ? max(0, min(g1, y0 + ty) - y0) : 0;
+    cz = (b < ny * nz) ? max(0, min(g2, z0 + tz) - z0) : 0;
+    count = g0 * cy * cz;
+  }
+};
+
 // Schedule of a pass (the shared-memory sweep's: class order by key rank
 // within each sweep, parameters per class): one CTA per replica, one thread
 // per (sweep, class).
@@ -96,13 +119,12 @@ __global__ void __launch_bounds__(256) k_stream_sub(const __grid_constant__ CeTa
   auto wrap_lt2 = [](int v, int L) { return v >= L ? v - L : v; };  // v < 2L
   if (ensemble == 0) {
     // ---------------- flips: every class site is a proposal
-    const int n = d0 * d1 * d2;
-    const int per = (n + gridDim.x - 1) / gridDim.x;
-    const int q0 = blockIdx.x * per, q1 = min(n, q0 + per);
-    const FastDiv f0(d0), f1(d1);
-    for (int q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
-      const int t = f0.div(q), iz = f1.div(t);
-      const int x = 2 * (q - t * d0) + cc0, y = 2 * (t - iz * d1) + cc1, z = 2 * iz + cc2;
+    const StreamTile tile(d0, d1, d2);
+    const FastDiv f0(d0), fy(max(1, tile.cy));
+    for (int q = threadIdx.x; q < tile.count; q += blockDim.x) {
+      const int t = f0.div(q), tz = fy.div(t);
+      const int x = 2 * (q - t * d0) + cc0, y = 2 * (tile.y0 + t - tz * tile.cy) + cc1,
+                z = 2 * (tile.z0 + tz) + cc2;
       const int ad = G.addr(0, x, y, z);
       const int o_i = occ[ad];
       const int l = x + G.L0 * (y + G.L1 * z);
@@ -152,10 +174,12 @@ __global__ void __launch_bounds__(256) k_stream_sub(const __grid_constant__ CeTa
       g1 = d1 / 2;
       n = g0 * g1 * (d2 / 2);
     }
-    const FastDiv fe0(g0), fe1(g1), fpm(pm);
+    const int g2 = g1 > 0 && g0 > 0 ? n / (g0 * g1) : 0;
+    const StreamTile tile(g0, g1, g2);
+    const FastDiv fe0(g0), fey(max(1, tile.cy)), fpm(pm);
     auto sites_of = [&](int q, int &xa, int &ya, int &za, int &xb, int &yb, int &zb) {
-      const int t = fe0.div(q), i2 = fe1.div(t);
-      const int i0 = q - t * g0, i1 = t - i2 * g1;
+      const int t = fe0.div(q), tz = fey.div(t);
+      const int i0 = q - t * g0, i1 = tile.y0 + t - tz * tile.cy, i2 = tile.z0 + tz;
       if (!local) {
         const int jj = pa == 0 ? i0 : (pa == 1 ? i1 : i2);
         const int jq = fpm.div(jj);
@@ -176,12 +200,11 @@ __global__ void __launch_bounds__(256) k_stream_sub(const __grid_constant__ CeTa
         zb = wrapc(za + du2, G.L2);
       }
     };
-    // phase A: this CTA's chunk, split between its warps, compacted in order
-    const int per = (n + gridDim.x - 1) / gridDim.x;
-    const int q0 = blockIdx.x * per, q1 = min(n, q0 + per);
+    // phase A: this CTA's tile, split between its warps, compacted in order
+    const int per = tile.count;
     const int nw = blockDim.x >> 5;
     const int wper = (per + nw - 1) / nw;
-    const int wq0 = q0 + warp * wper, wq1 = min(q1, wq0 + wper);
+    const int wq0 = warp * wper, wq1 = min(per, wq0 + wper);
     int kept = 0;
     for (int qb = wq0; qb < wq1; qb += 32) {
       const int q = qb + lane;
@@ -409,7 +432,13 @@ static cudaError_t stream_run_t(const CeTables &T, StreamState &st, const Replic
     const long long half = L2 / 2, n_max = half * half * half;
     int bx = blocks / n_rep > 0 ? blocks / n_rep : 1;
     if (bx < (n_max + 8191) / 8192) bx = (int)((n_max + 8191) / 8192);
-    const int smem = (int)(4 * ((n_max + bx - 1) / bx + 8));
+    // list capacity: the largest tile (full x rows of the candidate grid over
+    // a y, z tile; the grid is at most (L/2)^3), split over 8 warps
+    int nz = 1;
+    while ((nz + 1) * (nz + 1) <= bx) ++nz;
+    const int ny = bx / nz;
+    const long long tile_max = half * ((half + ny - 1) / ny) * ((half + nz - 1) / nz);
+    const int smem = (int)(4 * (8 * ((tile_max + 7) / 8) + 8));
     k_stream_sched<<<n_rep, 64, 0, s>>>(T, SP);
     for (int sub = 0; sub < n_sub; ++sub) {
       SP.sub = sub;
