@@ -534,7 +534,7 @@ def tc_scan(cm, ce):
 
 
 def learned_vs_plain(cm, T: float, plain_passes: int = 30000, learned_passes: int = 2000,
-                     equil_passes: int = 5000, rounds: int = 4, local_substeps: int = 8,
+                     equil_passes: int = 5000, rounds: int = 2, local_substeps: int = 4,
                      weights=("network",)) -> dict:
     """Configuration 3 (32 x 48^3 FCC, L1_2 cluster expansion, canonical
     x_B = 0.25) at temperature T: plain GPU Metropolis (the colour-class
@@ -820,7 +820,7 @@ def main():
     ap.add_argument("--plain-passes", type=int, default=30000)
     ap.add_argument("--equil-passes", type=int, default=5000,
                     help="workload 3: plain passes that equilibrate the common state")
-    ap.add_argument("--rounds", type=int, default=4,
+    ap.add_argument("--rounds", type=int, default=2,
                     help="workload 3: swap rounds per group of the learned group sweep")
     ap.add_argument("--tc-scan", action="store_true",
                     help="workload 3: locate T_c by a heat-capacity scan first")
