@@ -236,8 +236,9 @@ def test_learned_group_sweep_equilibrium_matches_oracle(T, cm, oracle_mod):
     # the ordered phase (tau_int ~ 200 passes at 90 K); they are checked in the
     # disordered phase, where runs of 2500 samples hold >= 50 tau_int
     modes = ("network", "exact") if ordered else ("uniform", "network", "exact")
-    # on 12^3 in the ordered phase single chains reach tau_int ~ 100 passes
-    n_pass, n_eq = (9000, 1000) if ordered else (3000, 500)
+    # on 12^3 in the ordered phase single chains reach tau_int ~ 200 passes
+    # (two groups per class, few neighbour swaps per pass on so small a box)
+    n_pass, n_eq = (22000, 2000) if ordered else (3000, 500)
     for weights in modes:
         b = cm.ReplicaBatch(sysd, "canonical", [(L, L, L)] * nrep)
         for i in range(nrep):
