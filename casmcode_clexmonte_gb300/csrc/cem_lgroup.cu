@@ -61,7 +61,8 @@ constexpr int LG_CLASSES = 27;
 constexpr uint32_t TAG_LG_SCHED = 0x5u, TAG_LG_GROUP = 0x6u, TAG_LG_LOCAL = 0x7u;
 // network tables of the tcgen05 path: W1^T, W2^T, one operand buffer per
 // warpgroup, biases (193 floats), per-warpgroup mbarriers, tensor-memory slot
-constexpr int LG_NET_BYTES = UMMA_B1_BYTES + UMMA_B2_BYTES + 4 * UMMA_A_BYTES + 1024;
+constexpr int LG_NET_BYTES =
+    UMMA_B1_BYTES + UMMA_B2_BYTES + 4 * UMMA_A_BYTES + UMMA_BITS_BYTES + 1024;
 
 struct LGroupParams {
   const Replica *reps;
@@ -145,8 +146,9 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
   unsigned char *nb1 = smem + ((align16(V) + 127) & ~127);  // 128-byte aligned operands
   unsigned char *nb2 = nb1 + UMMA_B1_BYTES;
   unsigned char *abufs = nb2 + UMMA_B2_BYTES;  // [4 warpgroups][UMMA_A_BYTES]
-  float *fb = reinterpret_cast<float *>(abufs + 4 * UMMA_A_BYTES);  // b1, b2, w3, b3
-  uint64_t *nbar = reinterpret_cast<uint64_t *>(fb + 196);          // [4]
+  uint4 *nbits = reinterpret_cast<uint4 *>(abufs + 4 * UMMA_A_BYTES);  // byte -> 8 bf16 0/1
+  float *fb = reinterpret_cast<float *>(abufs + 4 * UMMA_A_BYTES + UMMA_BITS_BYTES);  // b2, w3, b3
+  uint64_t *nbar = reinterpret_cast<uint64_t *>(fb + 132);  // [4]
   uint32_t *tslot = reinterpret_cast<uint32_t *>(nbar + 4);
   __shared__ int s_order[LG_CLASSES];
   __shared__ uint32_t s_key[LG_CLASSES], s_ainv[LG_CLASSES], s_boff[LG_CLASSES];
@@ -163,7 +165,7 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
   const uint32_t k0 = (uint32_t)R.seed, k1 = (uint32_t)(R.seed >> 32);
 
   if (mode == 1) {
-    umma_load_net(LP.params, nb1, nb2, fb, tid, LG_THREADS);
+    umma_load_net(LP.params, nb1, nb2, nbits, fb, tid, LG_THREADS);
     if (tid < 4) mbar_init(&nbar[tid], 1);
     if (warp == 0) tmem_alloc(tslot, 4 * UMMA_COLS);
     mbar_init_fence();
@@ -228,7 +230,7 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
   __syncthreads();
 
   if (mode == 1) tc_fence_after();  // the barriers above ordered the allocation
-  const UmmaNet net{nb1, nb2, fb, fb + 64, fb + 128, mode == 1 ? fb[192] : 0.f};
+  const UmmaNet net{nb1, nb2, nbits, fb, fb + 64, mode == 1 ? fb[128] : 0.f};
   const int wg = warp >> 2;
   const uint32_t tm = mode == 1 ? *tslot + (uint32_t)(wg * UMMA_COLS) : 0u;
   uint32_t nphase = 0;
@@ -551,18 +553,20 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
 // warpgroups per CTA, 128 environments per warpgroup and batch; status[0]
 // is set when an MMA wait ran out.
 constexpr int UMMA_FWD_THREADS = 512;
-constexpr int UMMA_FWD_SMEM = UMMA_B1_BYTES + UMMA_B2_BYTES + 4 * UMMA_A_BYTES + 1024;
+constexpr int UMMA_FWD_SMEM =
+    UMMA_B1_BYTES + UMMA_B2_BYTES + 4 * UMMA_A_BYTES + UMMA_BITS_BYTES + 1024;
 __global__ void __launch_bounds__(UMMA_FWD_THREADS)
     k_mlp_forward_tc(const __nv_bfloat16 *__restrict__ params, const int8_t *__restrict__ X,
                        long long n, float *__restrict__ z, int *status) {
   extern __shared__ __align__(128) unsigned char usm[];
   unsigned char *b1 = usm, *b2 = usm + UMMA_B1_BYTES;
   unsigned char *abufs = b2 + UMMA_B2_BYTES;
-  float *fb = reinterpret_cast<float *>(abufs + 4 * UMMA_A_BYTES);  // 193 floats
-  uint64_t *bars = reinterpret_cast<uint64_t *>(fb + 196);             // 4 mbarriers
+  uint4 *bits = reinterpret_cast<uint4 *>(abufs + 4 * UMMA_A_BYTES);
+  float *fb = reinterpret_cast<float *>(abufs + 4 * UMMA_A_BYTES + UMMA_BITS_BYTES);  // 129 floats
+  uint64_t *bars = reinterpret_cast<uint64_t *>(fb + 132);  // 4 mbarriers
   uint32_t *slot = reinterpret_cast<uint32_t *>(bars + 4);
   const int tid = threadIdx.x, warp = tid >> 5, wg = warp >> 2;
-  umma_load_net(params, b1, b2, fb, tid, UMMA_FWD_THREADS);
+  umma_load_net(params, b1, b2, bits, fb, tid, UMMA_FWD_THREADS);
   if (tid < 4) mbar_init(&bars[tid], 1);
   if (warp == 0) tmem_alloc(slot, 4 * UMMA_COLS);
   mbar_init_fence();
@@ -571,7 +575,7 @@ __global__ void __launch_bounds__(UMMA_FWD_THREADS)
   __syncthreads();
   tc_fence_after();
   const uint32_t tm = *slot + (uint32_t)(wg * UMMA_COLS);
-  const UmmaNet net{b1, b2, fb, fb + 64, fb + 128, fb[192]};
+  const UmmaNet net{b1, b2, bits, fb, fb + 64, fb[128]};
   unsigned char *abuf = abufs + wg * UMMA_A_BYTES;
   uint32_t phase = 0;
   bool timeout = false;

@@ -3,9 +3,11 @@
 // the MMAs for the warpgroup's 128 environments (one per thread: warp q of
 // the warpgroup owns rows 32q..32q+31, the tensor-memory lanes it may read).
 //
-//   layer 1: D[128 x 64] = X[128 x 48] * W1[48 x 64]   (3 MMAs, K = 16 each;
-//            X holds the 0/1 neighbour occupants exactly in bf16, rows 42..47 0)
-//   layer 2: D[128 x 64] = H1[128 x 64] * W2[64 x 64]  (4 MMAs), H1 = bf16(ReLU(D + b1))
+//   layer 1: D[128 x 64] = X[128 x 48] * W1'[48 x 64]  (3 MMAs, K = 16 each;
+//            X holds the 0/1 neighbour occupants exactly in bf16 in columns
+//            0..41 and 1 in column 42; W1' is W1 with the bias b1 as row 42,
+//            so D = X W1 + b1 exactly in the bf16 parameters; columns 43..47 0)
+//   layer 2: D[128 x 64] = H1[128 x 64] * W2[64 x 64]  (4 MMAs), H1 = bf16(ReLU(D))
 //   logit  : z = b3 + sum_j ReLU(D_j + b2_j) w3_j, fp32, one row per thread
 //
 // Operands are bf16 in shared memory in the no-swizzle K-major layout of
@@ -33,6 +35,8 @@ constexpr int UMMA_B1_BYTES = 64 * 48 * 2, UMMA_B2_BYTES = 64 * 64 * 2;
 constexpr int UMMA_A_BYTES = 128 * 64 * 2;  // one warpgroup's operand rows (layer 2 size)
 constexpr int UMMA_COLS = 64;               // tensor-memory columns per warpgroup
 constexpr int UMMA_WAIT_ITERS = 1 << 22;
+// bf16 0/1 expansion of a byte: entry x = 8 bf16 (bit k of x -> element k)
+constexpr int UMMA_BITS_BYTES = 256 * 16;
 
 // instruction descriptor of kind::f16: D f32 (bits 4-5 = 1), A and B bf16
 // (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bit 17,
@@ -111,20 +115,33 @@ __device__ __forceinline__ void wg_bar(int id) {
 
 // Network tables in shared memory for the tensor-core path.
 struct UmmaNet {
-  unsigned char *b1, *b2;  // W1^T [64 x 48], W2^T [64 x 64], bf16 core-matrix layout
-  const float *bias1, *bias2, *w3;
+  unsigned char *b1, *b2;  // W1'^T [64 x 48], W2^T [64 x 64], bf16 core-matrix layout
+  const uint4 *bits;       // byte -> 8 bf16 0/1 (UMMA_BITS_BYTES)
+  const float *bias2, *w3;
   float b3;
 };
 
-// W1^T and W2^T into the core-matrix layout (row n = hidden unit, K = inputs),
-// fp32 biases and output weights. fb: b1[64], b2[64], w3[64], b3.
+// W1'^T (W1 with b1 as input row MLP_IN) and W2^T into the core-matrix layout
+// (row n = hidden unit, K = inputs), the byte expansion table, fp32 layer-2
+// biases and output weights. fb: b2[64], w3[64], b3 (64-float aligned).
 __device__ __forceinline__ void umma_load_net(const __nv_bfloat16 *__restrict__ P,
-                                              unsigned char *b1, unsigned char *b2, float *fb,
-                                              int tid, int nth) {
+                                              unsigned char *b1, unsigned char *b2, uint4 *bits,
+                                              float *fb, int tid, int nth) {
+  static_assert(MLP_IN < 48, "layer 1 keeps a spare input column for its bias");
   for (int i = tid; i < 64 * 48; i += nth) {
     const int n = i / 48, k = i - 48 * (i / 48);
-    const __nv_bfloat16 v = k < MLP_IN ? P[MLP_W1 + k * MLP_H + n] : __float2bfloat16_rn(0.f);
+    const __nv_bfloat16 v = k < MLP_IN    ? P[MLP_W1 + k * MLP_H + n]
+                            : k == MLP_IN ? P[MLP_B1 + n]
+                                          : __float2bfloat16_rn(0.f);
     *reinterpret_cast<__nv_bfloat16 *>(b1 + umma_off(n, k >> 3, UMMA_NK1) + (k & 7) * 2) = v;
+  }
+  for (int x = tid; x < 256; x += nth) {
+    uint32_t w[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      w[j] = (((uint32_t)x >> (2 * j)) & 1u) * 0x3F80u +
+             (((uint32_t)x >> (2 * j + 1)) & 1u) * 0x3F800000u;  // bf16 1.0 = 0x3F80
+    bits[x] = make_uint4(w[0], w[1], w[2], w[3]);
   }
   for (int i = tid; i < 64 * 64; i += nth) {
     const int n = i >> 6, k = i & 63;
@@ -132,22 +149,33 @@ __device__ __forceinline__ void umma_load_net(const __nv_bfloat16 *__restrict__ 
         P[MLP_W2 + k * MLP_H + n];
   }
   for (int i = tid; i < MLP_H; i += nth) {
-    fb[i] = __bfloat162float(P[MLP_B1 + i]);
-    fb[64 + i] = __bfloat162float(P[MLP_B2 + i]);
-    fb[128 + i] = __bfloat162float(P[MLP_W3 + i]);
+    fb[i] = __bfloat162float(P[MLP_B2 + i]);
+    fb[64 + i] = __bfloat162float(P[MLP_W3 + i]);
   }
-  if (tid == 0) fb[192] = __bfloat162float(P[MLP_B3]);
+  if (tid == 0) fb[128] = __bfloat162float(P[MLP_B3]);
 }
 
-// bf16 pair of bits k and k + 1 of a 0/1 mask (lower half: element k)
-__device__ __forceinline__ uint32_t umma_bits2(unsigned long long e, int k) {
-  const uint32_t x = (uint32_t)(e >> k) & 3u;
-  return ((x & 1u) * 0x3F80u) | ((x >> 1) * 0x3F800000u);
+// bf16x2 of ReLU(lo), ReLU(hi), round to nearest even (lower half: lo)
+__device__ __forceinline__ uint32_t umma_relu_pack(float lo, float hi) {
+  uint32_t r;
+  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+  return r;
 }
 
-__device__ __forceinline__ uint32_t umma_pack(float lo, float hi) {
-  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-  return *reinterpret_cast<const uint32_t *>(&v);
+// packed fp32 pairs (Blackwell f32x2 arithmetic)
+__device__ __forceinline__ unsigned long long f2_pack(float lo, float hi) {
+  return ((unsigned long long)__float_as_uint(hi) << 32) | __float_as_uint(lo);
+}
+__device__ __forceinline__ unsigned long long f2_add(unsigned long long a, unsigned long long b) {
+  unsigned long long d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b,
+                                                     unsigned long long c) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
 }
 
 // Logit of the environment `env` (bit k = neighbour k) of this thread's row.
@@ -162,16 +190,11 @@ __device__ __forceinline__ float umma_network(const UmmaNet &N, unsigned char *a
   const int lane = threadIdx.x & 31, wq = (threadIdx.x >> 5) & 3;
   const int row = 32 * wq + lane;
   const uint32_t tlane = tm + ((uint32_t)(32 * wq) << 16);
-  // ---- layer 1 operand: the row's 48 inputs as bf16 0/1
+  // ---- layer 1 operand: the row's 42 inputs and the bias input as bf16 0/1
+  const unsigned long long e = env | (1ull << MLP_IN);
 #pragma unroll
-  for (int c = 0; c < UMMA_NK1; ++c) {
-    uint4 v;
-    v.x = umma_bits2(env, 8 * c);
-    v.y = umma_bits2(env, 8 * c + 2);
-    v.z = umma_bits2(env, 8 * c + 4);
-    v.w = umma_bits2(env, 8 * c + 6);
-    *reinterpret_cast<uint4 *>(abuf + umma_off(row, c, UMMA_NK1)) = v;
-  }
+  for (int c = 0; c < UMMA_NK1; ++c)
+    *reinterpret_cast<uint4 *>(abuf + umma_off(row, c, UMMA_NK1)) = N.bits[(e >> (8 * c)) & 255u];
   fence_proxy_async_smem();
   tc_fence_before();
   wg_bar(1 + wg);
@@ -187,21 +210,18 @@ __device__ __forceinline__ float umma_network(const UmmaNet &N, unsigned char *a
   if (!mbar_wait(bar, phase, UMMA_WAIT_ITERS)) timeout = true;
   phase ^= 1u;
   tc_fence_after();
-  // ---- layer 2 operand: bf16(ReLU(D + b1)), 32 columns at a time
+  // ---- layer 2 operand: bf16(ReLU(D)), 32 columns at a time
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     float v[32];
     tmem_ld32(tlane + 32 * h, v);
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-      float a[8];
-#pragma unroll
-      for (int i = 0; i < 8; ++i) a[i] = fmaxf(v[8 * c + i] + N.bias1[32 * h + 8 * c + i], 0.f);
       uint4 u;
-      u.x = umma_pack(a[0], a[1]);
-      u.y = umma_pack(a[2], a[3]);
-      u.z = umma_pack(a[4], a[5]);
-      u.w = umma_pack(a[6], a[7]);
+      u.x = umma_relu_pack(v[8 * c], v[8 * c + 1]);
+      u.y = umma_relu_pack(v[8 * c + 2], v[8 * c + 3]);
+      u.z = umma_relu_pack(v[8 * c + 4], v[8 * c + 5]);
+      u.w = umma_relu_pack(v[8 * c + 6], v[8 * c + 7]);
       *reinterpret_cast<uint4 *>(abuf + umma_off(row, 4 * h + c, UMMA_NK2)) = u;
     }
   }
@@ -220,17 +240,29 @@ __device__ __forceinline__ float umma_network(const UmmaNet &N, unsigned char *a
   if (!mbar_wait(bar, phase, UMMA_WAIT_ITERS)) timeout = true;
   phase ^= 1u;
   tc_fence_after();
-  float z = N.b3;
+  // logit: two interleaved fp32 chains (even and odd hidden units) in f32x2
+  unsigned long long z2 = 0ull;
+  const float4 *b2v = reinterpret_cast<const float4 *>(N.bias2);
+  const float4 *w3v = reinterpret_cast<const float4 *>(N.w3);
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     float v[32];
     tmem_ld32(tlane + 32 * h, v);
 #pragma unroll
-    for (int i = 0; i < 32; ++i)
-      z = fmaf(fmaxf(v[i] + N.bias2[32 * h + i], 0.f), N.w3[32 * h + i], z);
+    for (int i = 0; i < 8; ++i) {
+      const float4 b = b2v[8 * h + i], w = w3v[8 * h + i];
+      const unsigned long long t0 = f2_add(f2_pack(v[4 * i], v[4 * i + 1]), f2_pack(b.x, b.y));
+      const unsigned long long t1 = f2_add(f2_pack(v[4 * i + 2], v[4 * i + 3]), f2_pack(b.z, b.w));
+      const unsigned long long r0 =
+          f2_pack(fmaxf(__uint_as_float((uint32_t)t0), 0.f), fmaxf(__uint_as_float((uint32_t)(t0 >> 32)), 0.f));
+      const unsigned long long r1 =
+          f2_pack(fmaxf(__uint_as_float((uint32_t)t1), 0.f), fmaxf(__uint_as_float((uint32_t)(t1 >> 32)), 0.f));
+      z2 = f2_fma(r0, f2_pack(w.x, w.y), z2);
+      z2 = f2_fma(r1, f2_pack(w.z, w.w), z2);
+    }
   }
   tc_fence_before();  // the next call's MMAs come after these reads
-  return z;
+  return N.b3 + (__uint_as_float((uint32_t)z2) + __uint_as_float((uint32_t)(z2 >> 32)));
 }
 
 }  // namespace cem
