@@ -1,7 +1,9 @@
 """Build the in-tree CUDA library ``_build/libcem_gb300.so`` for sm_103a.
 
-Two translation units compiled in parallel with nvcc, linked with
-``nvcc -shared``; no cmake. Run as ``python -m casmcode_clexmonte_gb300.build``.
+The translation units of ``csrc/`` (SOURCES) are compiled in parallel with
+nvcc and linked with ``nvcc -shared``; then the C++ calculator plugin is
+compiled with g++ against it. No cmake. Run as
+``python -m casmcode_clexmonte_gb300.build``.
 """
 
 from __future__ import annotations
