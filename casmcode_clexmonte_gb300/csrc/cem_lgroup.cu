@@ -316,27 +316,33 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
           gen_fcc::counts_env<PITCH>(occ + ad, n, env);
         }
         const float eab = lg_eab(T, n);
+        // this lane's round: two Philox blocks (64-bit uniforms for both
+        // draws, 24 bits for the acceptance). Even warpgroups draw them before
+        // the network and odd ones after it, so that the warpgroups of a CTA
+        // do not all wait on their MMAs at the same time.
+        unsigned long long ua_own = 0ull, ub_own = 0ull;
+        uint32_t uu_own = 0u;
+        auto draw = [&]() {
+          if (lane < rounds) {
+            const uint32_t ctr = (uint32_t)grp | ((uint32_t)sub << 16);
+            const U4 p = philox4x32_10(U4{ctr, (uint32_t)lane, plo, phi | (TAG_LG_GROUP << 16)}, k0, k1);
+            const U4 p2 = philox4x32_10(U4{ctr, (uint32_t)lane | 0x100u, plo, phi | (TAG_LG_GROUP << 16)},
+                                        k0, k1);
+            ua_own = ((unsigned long long)p.x << 32) | p.y;
+            ub_own = ((unsigned long long)p.z << 32) | p.w;
+            uu_own = p2.x;
+          }
+        };
+        if ((wg & 1) == 0) draw();
         float zl = 0.f;
         if (mode == 1) zl = umma_network(net, abufs + wg * UMMA_A_BYTES, tm, &nbar[wg], nphase, wg, env, ntimeout);
         else if (mode == 2) zl = FMUL(-0.5f * beta_f, eab);
+        if (wg & 1) draw();
         const uint32_t wA = mode ? (uint32_t)logit_weight(zl) : 1u;
         const uint32_t wB = mode ? (uint32_t)logit_weight(-zl) : 1u;
         const int o0 = o;
         uint32_t wc = o ? wB : wA, wa = o ? wA : wB;
         float eme = o ? -eab : eab;  // this member's flip energy in its current state
-        // this lane's round: two Philox blocks (64-bit uniforms for both
-        // draws, 24 bits for the acceptance)
-        unsigned long long ua_own = 0ull, ub_own = 0ull;
-        uint32_t uu_own = 0u;
-        if (lane < rounds) {
-          const uint32_t ctr = (uint32_t)grp | ((uint32_t)sub << 16);
-          const U4 p = philox4x32_10(U4{ctr, (uint32_t)lane, plo, phi | (TAG_LG_GROUP << 16)}, k0, k1);
-          const U4 p2 = philox4x32_10(U4{ctr, (uint32_t)lane | 0x100u, plo, phi | (TAG_LG_GROUP << 16)},
-                                      k0, k1);
-          ua_own = ((unsigned long long)p.x << 32) | p.y;
-          ub_own = ((unsigned long long)p.z << 32) | p.w;
-          uu_own = p2.x;
-        }
         // inclusive prefix sums of the A and B weights over the lanes; they
         // change only when a swap is accepted
         uint32_t sa = 0u, sb = 0u, WA = 0u, WB = 0u;
