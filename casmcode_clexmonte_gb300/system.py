@@ -199,6 +199,58 @@ class FlowerCluster:
     lut: np.ndarray  # int16 [(n_sf)**size] -> global function index
 
 
+def _lattice_index(vecs) -> int:
+    """Index in Z^3 of the lattice spanned by integer 3-vectors (0 if they
+    span less than three dimensions): integer row echelon form by Euclid's
+    algorithm, index = |product of the pivots|."""
+    rows = [list(v) for v in vecs if any(v)]
+    det = 1
+    for col in range(3):
+        piv, rest = None, []
+        for r in rows:
+            if r[col] == 0:
+                rest.append(r)
+            elif piv is None:
+                piv = r
+            else:
+                a, b = piv, r
+                while b[col] != 0:
+                    q = a[col] // b[col]
+                    a = [x - q * y for x, y in zip(a, b)]
+                    a, b = b, a
+                piv = a
+                if any(b):
+                    rest.append(b)
+        if piv is None:
+            return 0
+        det *= piv[col]
+        rows = [r for r in rest if any(r)]
+    return abs(det)
+
+
+def _swaps_connect(subl, edges) -> bool:
+    """Whether swaps of site (b, x) with (pb, x + du), for the given edges
+    (b, pb, du), connect every site of the sublattices ``subl`` on the
+    infinite lattice: the graph over the sublattices is connected and the
+    translations of its cycles generate Z^3."""
+    adj = {b: [] for b in subl}
+    for b, pb, du in edges:
+        adj[b].append((pb, du))
+        adj[pb].append((b, tuple(-x for x in du)))
+    pot = {subl[0]: (0, 0, 0)}
+    stack = [subl[0]]
+    while stack:
+        b = stack.pop()
+        for pb, du in adj[b]:
+            if pb not in pot:
+                pot[pb] = tuple(p + d for p, d in zip(pot[b], du))
+                stack.append(pb)
+    if len(pot) != len(subl):
+        return False
+    cycles = [tuple(p + d - q for p, d, q in zip(pot[b], du, pot[pb])) for b, pb, du in edges]
+    return _lattice_index(cycles) == 1
+
+
 class ClusterExpansion:
     """Orbits, occupation-basis functions and ECI for a ``Prim``.
 
@@ -390,13 +442,43 @@ class ClusterExpansion:
         return r
 
     def neighbour_partners(self, b: int) -> list:
-        """Nearest-neighbour sites of sublattice b (partners of the shortest
-        pair orbit), used as canonical local-swap displacements."""
-        pair_orbits = [o for o in self.orbits if o.size == 2]
-        if not pair_orbits:
-            return []
-        o0 = pair_orbits[0].index
-        return [c.partners[0] for c in self.flowers[b] if c.orbit == o0]
+        """Displacements (partner sublattice, cell offset) of the canonical
+        local swaps of sublattice b: the partners of the shortest pair
+        orbits. Orbits are taken in order of length until the swaps connect
+        every site of every sublattice with a degree of freedom, i.e. the
+        displacement graph over those sublattices is connected and its cycle
+        translations generate the whole lattice Z^3. Swaps inside a colour
+        class only permute that class, so this connectivity is what makes the
+        canonical chain ergodic (the reference's canonical proposal swaps any
+        two sites, CanonicalCalculator.cc:78-83). FCC and BCC: the nearest
+        neighbours already do; hcp Zr-O: the O-O pairs along c do not (they
+        only link the octahedral sites of one column), the in-plane pairs are
+        added."""
+        return [c.partners[0] for c in self.flowers[b] if c.orbit in self.local_swap_orbits()]
+
+    def local_swap_orbits(self) -> frozenset:
+        """Indices of the pair orbits whose partners are the local-swap
+        displacements (see neighbour_partners)."""
+        cached = getattr(self, "_local_swap_orbits", None)
+        if cached is not None:
+            return cached
+        pairs = sorted((o for o in self.orbits if o.size == 2), key=lambda o: (o.max_length, o.index))
+        subl = sorted(self.flowers)
+        chosen = set()
+        result = frozenset()
+        for o in pairs:
+            chosen.add(o.index)
+            edges = [(b, c.partners[0][0], tuple(int(x) for x in c.partners[0][1]))
+                     for b in subl for c in self.flowers[b] if c.orbit in chosen]
+            if _swaps_connect(subl, edges):
+                result = frozenset(chosen)
+                break
+        else:
+            if pairs:
+                raise ValueError("no set of pair orbits connects the sites with a degree of freedom: "
+                                 "canonical local swaps would not be ergodic")
+        self._local_swap_orbits = result
+        return result
 
     def function_signatures(self) -> list:
         """For each function f >= 1: decorated-cluster invariant of its

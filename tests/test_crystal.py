@@ -180,3 +180,34 @@ def test_summary_writer_follows_zro_composition_axes(tmp_path):
     mc = data["statistics"]["mol_composition"]
     assert mc["component_names"] == ["Zr", "Va", "O"]
     assert [mc[c]["mean"][0] for c in ("Zr", "Va", "O")] == pytest.approx([2.0, 1.5, 0.5])
+
+
+def test_local_swaps_connect_every_site(ce):
+    """Canonical local-swap displacements are the partners of the shortest
+    pair orbits, taken until the swaps connect every site with a degree of
+    freedom (graph over the sublattices connected, cycle translations
+    generating Z^3). FCC: the nearest neighbours. ZrO: the O-O pairs along c
+    only link the octahedral sites of one column (a conserved O count per
+    column colour would make the canonical chain non-ergodic), so the
+    in-plane O-O pairs are added."""
+    from casmcode_clexmonte_gb300.system import _lattice_index, _swaps_connect
+
+    assert _lattice_index([(1, 0, 0), (0, 1, 0), (0, 0, 1)]) == 1
+    assert _lattice_index([(1, 1, 0), (0, 1, 1), (1, 0, 1)]) == 2
+    assert _lattice_index([(1, 1, 0), (0, 1, 1), (1, 0, 1), (1, 0, 0)]) == 1
+    assert _lattice_index([(0, 0, 1), (0, 0, 2)]) == 0
+    fcc = workloads.fcc_binary_ce(0)
+    shortest = min((o for o in fcc.orbits if o.size == 2), key=lambda o: o.max_length).index
+    assert fcc.local_swap_orbits() == {shortest}
+    assert len(fcc.neighbour_partners(0)) == 12
+    pairs = sorted((o for o in ce.orbits if o.size == 2), key=lambda o: o.max_length)
+    subl = sorted(ce.flowers)
+    only_c = [(b, c.partners[0][0], tuple(c.partners[0][1])) for b in subl for c in ce.flowers[b]
+              if c.orbit == pairs[0].index]
+    assert all(du[0] == 0 and du[1] == 0 for _, _, du in only_c)
+    assert not _swaps_connect(subl, only_c)
+    sel = ce.local_swap_orbits()
+    assert pairs[0].index in sel and len(sel) == 2
+    edges = [(b, pb, tuple(du)) for b in subl for pb, du in ce.neighbour_partners(b)]
+    assert _swaps_connect(subl, edges)
+    assert all(len(ce.neighbour_partners(b)) <= 16 for b in subl)

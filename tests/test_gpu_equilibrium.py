@@ -30,12 +30,10 @@ import numpy as np
 import pytest
 
 from casmcode_clexmonte_gb300 import workloads
-from casmcode_clexmonte_gb300.stats import family_2sigma, jackknife_chains
-from tests.stat_checks import check_chain_lengths as _check_chain_lengths
+from tests.stat_checks import compare as _compare
 
 pytestmark = pytest.mark.gpu
 
-KB = 8.617333262e-5
 THREADS = os.cpu_count() or 1
 
 
@@ -55,41 +53,6 @@ def oracle_mod():
 
     oracle.build_oracle()
     return oracle
-
-
-def _observables(E, X, T, n_uc, sgc):
-    """[(name, estimator over pooled [n, 1 + nc] samples)]"""
-    out = [("<E>", lambda a: a[:, 0].mean()),
-           ("C", lambda a: a[:, 0].var() * n_uc / (KB * T * T))]
-    if sgc:
-        nc = X.shape[-1]
-        for k in range(nc):
-            out.append((f"<x{k}>", lambda a, k=k: a[:, 1 + k].mean()))
-            out.append((f"chi_E{k}", lambda a, k=k: np.cov(a[:, 0], a[:, 1 + k], bias=True)[0, 1]
-                        * n_uc / (KB * T)))
-            for k2 in range(k, nc):
-                out.append((f"chi_{k}{k2}",
-                            lambda a, k=k, k2=k2: np.cov(a[:, 1 + k], a[:, 1 + k2], bias=True)[0, 1]
-                            * n_uc / (KB * T)))
-    return out
-
-
-def _compare(conditions, gpu_chains, ora_chains, n_uc, sgc):
-    rows, zs = [], []
-    for (label, T), g, o in zip(conditions, gpu_chains, ora_chains):
-        _check_chain_lengths(g, sgc, f"GPU {label}")
-        _check_chain_lengths(o, sgc, f"oracle {label}")
-        for name, f in _observables(g[0][:, 0], g[0][:, 1:], T, n_uc, sgc):
-            eg, sg = jackknife_chains(f, g)
-            eo, so = jackknife_chains(f, o)
-            z = (eg - eo) / np.hypot(sg, so)
-            zs.append(z)
-            rows.append(f"{label:>24s} {name:>8s} gpu {eg:+.6e} +- {sg:.1e}  oracle {eo:+.6e} "
-                        f"+- {so:.1e}  z {z:+.2f}")
-    ok, k, bound, n2 = family_2sigma(zs)
-    msg = "\n".join(rows) + f"\n{n2} of {len(zs)} beyond 2 sigma (allowed {k}); bound {bound:.2f}"
-    assert ok, msg
-    return msg
 
 
 def _gpu_chains(cm, ce, ens, L, conds, mus, xs, n_rep, n_passes, n_equil, seed):

@@ -7,7 +7,6 @@ import numpy as np
 import pytest
 
 from casmcode_clexmonte_gb300 import workloads
-from casmcode_clexmonte_gb300.stats import batch_means
 
 pytestmark = pytest.mark.gpu
 
@@ -75,65 +74,60 @@ def test_training_reduces_loss(cm):
     assert after < 0.2 * before, (before, after, losses)
 
 
-@pytest.mark.parametrize("trained", [False, True])
-def test_learned_sampler_equilibrium_matches_oracle(trained, cm, oracle_mod):
-    """<E> of the learned-proposal chain (exact MH correction) against the
-    sequential oracle chain with uniform swaps, within 4 standard errors."""
-    L, T, nrep = 10, 900.0, 16
-    ce = workloads.fcc_binary_ce(3, nn1=0.08)
-    rng = np.random.default_rng(12)
-    occ0 = workloads.fixed_composition(rng, L ** 3, 0.25)
-    o = oracle_mod.OracleSystem(ce, (L, L, L))
-    ref = o.run(occ0.copy(), 1, T, np.zeros(1), 77, 4000)
-    e_o, se_o = batch_means(ref["energy"][500:])
-    sysd = cm.System(ce)
-    net = None
-    if trained:
-        _, _, _, X, t = _snapshot_features(cm, T=T)
-        net = cm.LearnedProposal(seed=4)
-        net.train(X, t, epochs=8, batch=512, lr=3e-3, seed=1)
-    b = cm.ReplicaBatch(sysd, "canonical", [(L, L, L)] * nrep)
-    for i in range(nrep):
-        b.set_conditions(i, T)
-        b.set_seed(i, 900 + i)
-        b.set_occupation(i, occ0)
-    b.learned_run(net, 400, 100, record_samples=True)
-    means = np.array([b.learned_samples(i, 300)[0].mean() for i in range(nrep)])
-    e_g, se_g = means.mean(), means.std(ddof=1) / np.sqrt(nrep)
-    assert abs(e_g - e_o) < 4.0 * np.hypot(se_g, se_o), (e_g, se_g, e_o, se_o)
-    st = b.stats(0)
-    assert st["n_proposed"] == 400 * L ** 3
-    e_now, _ = b.energy(0)
-    assert abs(st["energy"] - e_now) <= 1e-9 * max(1.0, abs(e_now))
-    occ = b.get_occupation(0)
-    assert occ.sum() == occ0.sum()
+@pytest.mark.parametrize("T", [900.0, 90.0])
+def test_learned_sampler_equilibrium_matches_oracle(T, cm, oracle_mod):
+    """The global learned sampler (per-species sum trees over the replica,
+    exact Metropolis-Hastings correction) against the oracle's sequential
+    chains with uniform swaps, 10^3 cells, x_B = 0.25: with uniform weights
+    and with the trained network at 900 K (disordered; random initial
+    states), with the network at 90 K (0.9 T_c of this expansion,
+    L1_2-ordered initial states, where the trained weights are far from
+    uniform). <E> and C of pooled independent chains (GPU 16, oracle 16),
+    jackknife errors, >= 50 tau_int per chain, 2 sigma per comparison at a
+    1 % family-wise level (tests/test_gpu_equilibrium.py)."""
+    from tests.stat_checks import compare
 
-
-def test_learned_sampler_ordered_phase_matches_oracle(cm, oracle_mod):
-    """The same check in the L1_2-ordered phase (90 K, 0.9 T_c of this
-    expansion), where the trained weights are far from uniform: <E> of the
-    learned chain against the oracle's uniform-swap chain within 4 standard
-    errors."""
-    L, T, nrep = 10, 90.0, 16
+    L, nrep = 10, 16
+    n = L ** 3
     ce = workloads.fcc_binary_ce(3, nn1=0.08)
-    rng = np.random.default_rng(19)
-    occ0 = workloads.fixed_composition(rng, L ** 3, 0.25)
+    ordered = T < 100.0
+    rng = np.random.default_rng(int(T) + 12)
+
+    def initial(i):
+        return _l12(L, i % 4) if ordered else workloads.fixed_composition(rng, n, 0.25)
+
     o = oracle_mod.OracleSystem(ce, (L, L, L))
-    ref = o.run(occ0.copy(), 1, T, np.zeros(1), 91, 6000)
-    e_o, se_o = batch_means(ref["energy"][1500:])
+    # the oracle's uniform swaps decorrelate slowly in the ordered phase
+    # (tau_int ~ 130 passes at 90 K on 10^3)
+    n_o, eq_o = (12000, 1000) if ordered else (1500, 300)
+    occ = np.ascontiguousarray(np.concatenate([initial(i) for i in range(16)]), dtype=np.int8)
+    pot, _, _ = o.run_chains(occ, 1, np.full(16, T), np.zeros((16, 1)), 77, n_o, os.cpu_count() or 1)
+    ora = [pot[i, eq_o:, None] for i in range(16)]
     sysd = cm.System(ce)
-    _, _, _, X, t = _snapshot_features(cm, T=T, passes=300)
-    net = cm.LearnedProposal(seed=6)
-    net.train(X, t, epochs=8, batch=512, lr=3e-3, seed=2)
-    b = cm.ReplicaBatch(sysd, "canonical", [(L, L, L)] * nrep)
-    for i in range(nrep):
-        b.set_conditions(i, T)
-        b.set_seed(i, 1900 + i)
-        b.set_occupation(i, occ0)
-    b.learned_run(net, 500, 150, record_samples=True)
-    means = np.array([b.learned_samples(i, 350)[0].mean() for i in range(nrep)])
-    e_g, se_g = means.mean(), means.std(ddof=1) / np.sqrt(nrep)
-    assert abs(e_g - e_o) < 4.0 * np.hypot(se_g, se_o), (e_g, se_g, e_o, se_o)
+    _, _, _, X, t = _snapshot_features(cm, T=T, passes=300 if ordered else 50)
+    net = cm.LearnedProposal(seed=4)
+    net.train(X, t, epochs=8, batch=512, lr=3e-3, seed=1)
+    modes = (("network", net),) if ordered else (("uniform", None), ("network", net))
+    n_pass, n_eq = (600, 100) if ordered else (400, 100)
+    conds, gpus, oras = [], [], []
+    for name, prop in modes:
+        b = cm.ReplicaBatch(sysd, "canonical", [(L, L, L)] * nrep)
+        for i in range(nrep):
+            b.set_conditions(i, T)
+            b.set_seed(i, 900 + i)
+            b.set_occupation(i, initial(i))
+        b.learned_run(prop, n_pass, n_eq, record_samples=True)
+        gpus.append([b.learned_samples(i, n_pass - n_eq)[0][:, None] for i in range(nrep)])
+        oras.append(ora)
+        conds.append((f"global {name} T={T:.0f}", T))
+        # bookkeeping: one proposal per site and pass, exact running energy,
+        # conserved composition
+        st = b.stats(0)
+        assert st["n_proposed"] == n_pass * n
+        e_now, _ = b.energy(0)
+        assert abs(st["energy"] - e_now) <= 1e-9 * max(1.0, abs(e_now))
+        assert b.get_occupation(0).sum() == initial(0).sum()
+    print(compare(conds, gpus, oras, n, sgc=False))
 
 
 def test_trained_network_raises_acceptance(cm):
