@@ -5,6 +5,7 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -102,6 +103,7 @@ struct cem_system {
   // host copies used for colouring checks
   std::vector<int> fl_sub, fl_pb, fl_du;
   int nb_reach = 0;
+  bool swaps_connect = false;  // local-swap displacements connect every site (canonical ergodicity)
   bool fcc_generated = false;  // flower matches the generated binary FCC evaluator
   bool big = false;            // more orbits than the register accumulators hold
   bool coop = false;           // big binary system for the warp-cooperative sweep
@@ -198,6 +200,79 @@ struct cem_replicas {
 };
 
 namespace {
+
+// Index in Z^3 of the lattice spanned by integer 3-vectors (0 below rank 3):
+// integer row echelon form by Euclid's algorithm, |product of the pivots|.
+long long lattice_index(std::vector<std::array<long long, 3>> rows) {
+  long long det = 1;
+  for (int col = 0; col < 3; ++col) {
+    std::vector<std::array<long long, 3>> rest;
+    bool have = false;
+    std::array<long long, 3> piv{};
+    for (auto r : rows) {
+      if (r[0] == 0 && r[1] == 0 && r[2] == 0) continue;
+      if (r[col] == 0) {
+        rest.push_back(r);
+      } else if (!have) {
+        piv = r;
+        have = true;
+      } else {
+        auto a = piv, b = r;
+        while (b[col] != 0) {
+          const long long q = a[col] / b[col];  // any quotient reduces |remainder| below |b[col]|
+          for (int k = 0; k < 3; ++k) a[k] -= q * b[k];
+          std::swap(a, b);
+        }
+        piv = a;
+        rest.push_back(b);
+      }
+    }
+    if (!have) return 0;
+    det *= piv[col];
+    rows.swap(rest);
+  }
+  return det < 0 ? -det : det;
+}
+
+// Whether swaps of site (b, x) with (nb_b, x + nb_du) connect every site of
+// every sublattice on the infinite lattice: the graph over the sublattices is
+// connected and the translations of its cycles generate Z^3. Swaps inside a
+// colour class only permute the class, so this is what makes the canonical
+// chain ergodic.
+bool swaps_connect(const CeTables &T) {
+  const int ns = T.n_sublat;
+  std::vector<std::array<long long, 3>> pot(ns);
+  std::vector<int> seen(ns, 0), stack{0};
+  seen[0] = 1;
+  pot[0] = {0, 0, 0};
+  while (!stack.empty()) {
+    const int b = stack.back();
+    stack.pop_back();
+    for (int b2 = 0; b2 < ns; ++b2)
+      for (int k = 0; k < T.n_nb[b2]; ++k) {
+        const int pb = T.nb_b[b2][k];
+        const int *du = T.nb_du[b2][k];
+        int from = -1, to = -1, sgn = 1;
+        if (b2 == b && !seen[pb]) from = b, to = pb, sgn = 1;
+        else if (pb == b && !seen[b2]) from = b, to = b2, sgn = -1;
+        if (from < 0) continue;
+        for (int a = 0; a < 3; ++a) pot[to][a] = pot[from][a] + sgn * du[a];
+        seen[to] = 1;
+        stack.push_back(to);
+      }
+  }
+  for (int b = 0; b < ns; ++b)
+    if (!seen[b]) return false;
+  std::vector<std::array<long long, 3>> cycles;
+  for (int b = 0; b < ns; ++b)
+    for (int k = 0; k < T.n_nb[b]; ++k) {
+      const int pb = T.nb_b[b][k];
+      std::array<long long, 3> v;
+      for (int a = 0; a < 3; ++a) v[a] = pot[b][a] + T.nb_du[b][k][a] - pot[pb][a];
+      cycles.push_back(v);
+    }
+  return lattice_index(cycles) == 1;
+}
 
 // HBM-streamed mode: binary FCC of the generated topology, equal even cubic
 // supercells whose pitch L + 4 has a compiled kernel
@@ -444,6 +519,7 @@ int cem_system_create(const cem_system_desc *d, cem_system **out) {
       }
     }
     s->nb_reach = nbr;
+    s->swaps_connect = swaps_connect(T);
     s->w.assign(d->weights, d->weights + d->n_funcs);
     std::vector<float> whi(d->n_funcs), wlo(d->n_funcs);
     for (int f = 0; f < d->n_funcs; ++f) {
@@ -568,6 +644,10 @@ int cem_replicas_create(const cem_system *sys, int n, const int *L, int ensemble
     *out = nullptr;
     require(n >= 1, "need at least one replica");
     require(ensemble == CEM_CANONICAL || ensemble == CEM_SEMIGRAND_CANONICAL, "bad ensemble");
+    require(ensemble != CEM_CANONICAL || sys->swaps_connect,
+            "the local-swap displacements do not connect every site (their graph over the "
+            "sublattices must be connected and its cycle translations generate the lattice): "
+            "the canonical chain would not be ergodic");
     auto r = std::make_unique<cem_replicas>();
     r->sys = sys;
     r->n = n;

@@ -85,7 +85,12 @@ typedef struct cem_system_desc {
   const int *owned_partner_sublat;
   const int *owned_partner_du;
   const int16_t *owned_lut;
-  /* canonical local-swap displacements (nearest neighbours), per sublattice */
+  /* canonical local-swap displacements, per sublattice: site (b, x) swaps
+     with (neighbour_sublat, x + neighbour_du). They must connect every site
+     (graph over the sublattices connected, cycle translations generating
+     Z^3), else canonical batches are refused: swaps inside a colour class
+     only permute that class. The Python builder takes the partners of the
+     shortest pair orbits until this holds. */
   const int *n_neighbour;       /* [n_sublat], each <= 16 */
   const int *neighbour_sublat;  /* [n_sublat*16] */
   const int *neighbour_du;      /* [n_sublat*16*3] */

@@ -151,3 +151,22 @@ def test_host_stop_request_ends_a_long_run_at_a_pass_boundary(kernel, cm):
         b.learned_group_run(None, 5, 0, weights="uniform", rounds=8, local_substeps=2)
     assert b.synchronize() is False
     assert b.stats(0)["passes"] == p0 + 5
+
+
+def test_canonical_batch_needs_connecting_local_swaps(cm):
+    """The C ABI refuses canonical batches whose local-swap displacements do
+    not connect every site (the chain would conserve the occupant count of a
+    set of colour classes): here the hcp Zr-O system with only its O-O pairs
+    along c. Semi-grand canonical batches need no swaps and are accepted."""
+    from tests.zro_fixture import zro_ce
+
+    ce = zro_ce()
+    shortest = min((o for o in ce.orbits if o.size == 2), key=lambda o: o.max_length).index
+    ce._local_swap_orbits = frozenset({shortest})  # the pre-fix choice: one column per swap set
+    sysd = cm.System(ce)
+    with pytest.raises(RuntimeError, match="do not connect every site"):
+        cm.ReplicaBatch(sysd, "canonical", [(8, 8, 8)])
+    b = cm.ReplicaBatch(sysd, "semigrand_canonical", [(8, 8, 8)])
+    assert b.n == 1
+    ce2 = zro_ce()
+    cm.ReplicaBatch(cm.System(ce2), "canonical", [(8, 8, 8)])
