@@ -154,3 +154,47 @@ def test_semigrand_bcc_ternary_matches_oracle(cm, oracle_mod):
     o = _oracle_chains(oracle_mod, ce, "semigrand_canonical", L, temps, mus, [None] * 2, 16, 1200,
                        200, 93)
     print(_compare(labels, g, o, int(np.prod(L)), sgc=True))
+
+
+def test_canonical_bcc_ternary_matches_oracle(cm, oracle_mod):
+    """Canonical ternary BCC A/B/C (configuration 2's cluster expansion, two
+    sublattices, two site functions), 8^3 conventional cells at fixed
+    composition (A 0.5, B 0.3, C 0.2): <E> and C at 1200 and 700 K. The GPU
+    swaps pairs of different species inside colour classes and with
+    neighbours; the oracle draws the reference's swap types."""
+    w = workloads.config(2, scale=1.0 / 128)
+    ce, L = w.ce, (8, 8, 8)
+    n_sites = int(np.prod(L)) * ce.prim.n_basis
+    counts = (n_sites // 2, (3 * n_sites) // 10)
+    temps = [1200.0, 700.0]
+
+    def initial(rng):
+        occ = np.zeros(n_sites, dtype=np.int8)
+        perm = rng.permutation(n_sites)
+        occ[perm[:counts[1]]] = 1
+        occ[perm[counts[1]:n_sites - counts[0]]] = 2
+        return occ
+
+    rng = np.random.default_rng(95)
+    n_rep, n_o_rep = 32, 16
+    sysd = cm.System(ce)
+    b = cm.ReplicaBatch(sysd, "canonical", [L] * (len(temps) * n_rep))
+    for c, T in enumerate(temps):
+        for r in range(n_rep):
+            i = c * n_rep + r
+            b.set_conditions(i, T)
+            b.set_seed(i, 9500 + i)
+            b.set_occupation(i, initial(rng))
+    n_pass, n_eq = 3000, 500
+    b.run(n_pass, n_eq, record_samples=True)
+    g = [[b.samples(c * n_rep + r, n_pass - n_eq)[0][:, None] for r in range(n_rep)]
+         for c in range(len(temps))]
+    o = oracle_mod.OracleSystem(ce, L)
+    occ = np.ascontiguousarray(np.concatenate([initial(rng) for _ in range(len(temps) * n_o_rep)]),
+                               dtype=np.int8)
+    n_o, eq_o = 1200, 200
+    pot, _, _ = o.run_chains(occ, 1, np.repeat(temps, n_o_rep), np.zeros((len(temps) * n_o_rep, 2)),
+                             97, n_o, THREADS)
+    ora = [[pot[c * n_o_rep + r, eq_o:, None] for r in range(n_o_rep)] for c in range(len(temps))]
+    labels = [(f"BCC ternary canonical T={T:.0f}", T) for T in temps]
+    print(_compare(labels, g, ora, int(np.prod(L)), sgc=False))
