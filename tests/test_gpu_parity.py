@@ -170,19 +170,21 @@ def test_parallel_deterministic_for_fixed_seed(cm):
     np.testing.assert_array_equal(outs[0], outs[1])
 
 
-@pytest.mark.parametrize("ens", ["semigrand_canonical", "canonical"])
-def test_parallel_equilibrium_matches_oracle(ens, cm, oracle_mod):
+@pytest.mark.parametrize("ens,edge", [("semigrand_canonical", 8), ("canonical", 8),
+                                      ("semigrand_canonical", 9), ("canonical", 9)])
+def test_parallel_equilibrium_matches_oracle(ens, edge, cm, oracle_mod):
     """Equilibrium averages of the parallel GPU sampler against the oracle's
-    sequential chains, 8^3 FCC (configuration 0's expansion) at 900 K: <E>
-    and C, and semi-grand canonical also <x>, chi and the thermo-chemical
-    chi. Independent chains on each side (GPU 16, oracle 16), pooled,
-    jackknife errors, >= 50 tau_int per chain, 2 sigma per comparison at a
-    1 % family-wise level (tests/test_gpu_equilibrium.py)."""
+    sequential chains, 8^3 and 9^3 FCC (configuration 0's expansion; an odd
+    edge takes colour blocks of unequal sizes) at 900 K: <E> and C, and
+    semi-grand canonical also <x>, chi and the thermo-chemical chi.
+    Independent chains on each side (GPU 16, oracle 16), pooled, jackknife
+    errors, >= 50 tau_int per chain, 2 sigma per comparison at a 1 %
+    family-wise level (tests/test_gpu_equilibrium.py)."""
     from tests.stat_checks import compare
 
     ce = workloads.fcc_binary_ce(0)
-    L = (8, 8, 8)
-    n, nrep = 512, 16
+    L = (edge, edge, edge)
+    n, nrep = edge ** 3, 16
     T = 900.0
     mu = np.array([0.05])
     sgc = ens == "semigrand_canonical"
@@ -206,7 +208,7 @@ def test_parallel_equilibrium_matches_oracle(ens, cm, oracle_mod):
     for i in range(nrep):
         p_i, c_i = b.samples(i, n_pass - n_eq)
         gpu.append(np.column_stack([p_i, c_i.reshape(n_pass - n_eq, -1)]))
-    print(compare([(f"8^3 {ens} T={T:.0f}", T)], [gpu], [ora], n, sgc=sgc))
+    print(compare([(f"{edge}^3 {ens} T={T:.0f}", T)], [gpu], [ora], n, sgc=sgc))
 
 
 @pytest.mark.parametrize("ens,L", [("canonical", (24, 24, 24)), ("semigrand_canonical", (10, 10, 10)),
