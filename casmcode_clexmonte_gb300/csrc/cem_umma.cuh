@@ -178,19 +178,21 @@ __device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsig
   return d;
 }
 
-// Logit of the environment `env` (bit k = neighbour k) of this thread's row.
-// Collective over the warpgroup wg (all 128 threads call it together);
-// abuf = the warpgroup's operand rows, tm = its 64 tensor-memory columns, bar
-// = its mbarrier with phase bit `phase` (toggled twice per call). Sets
-// *timeout when an MMA did not complete within the wait limit (the logit is
-// then meaningless).
-__device__ __forceinline__ float umma_network(const UmmaNet &N, unsigned char *abuf, uint32_t tm,
-                                              uint64_t *bar, uint32_t &phase, int wg,
-                                              unsigned long long env, bool &timeout) {
+// The network in three stages, so that a caller can do other work while an
+// MMA runs. Each stage is collective over the warpgroup wg (all 128 threads
+// call it together); abuf = the warpgroup's operand rows, tm = its 64
+// tensor-memory columns, bar = its mbarrier with phase bit `phase` (toggled
+// by each wait). A wait that runs out sets `timeout` (the logit is then
+// meaningless).
+//
+// Stage 1: write this thread's row of the layer-1 operand (env: bit k =
+// neighbour k) and issue layer 1.
+__device__ __forceinline__ void umma_layer1_issue(const UmmaNet &N, unsigned char *abuf,
+                                                  uint32_t tm, uint64_t *bar, int wg,
+                                                  unsigned long long env) {
   const int lane = threadIdx.x & 31, wq = (threadIdx.x >> 5) & 3;
   const int row = 32 * wq + lane;
-  const uint32_t tlane = tm + ((uint32_t)(32 * wq) << 16);
-  // ---- layer 1 operand: the row's 42 inputs and the bias input as bf16 0/1
+  // the row's 42 inputs and the bias input as bf16 0/1
   const unsigned long long e = env | (1ull << MLP_IN);
 #pragma unroll
   for (int c = 0; c < UMMA_NK1; ++c)
@@ -207,10 +209,20 @@ __device__ __forceinline__ float umma_network(const UmmaNet &N, unsigned char *a
                umma_desc(b0 + 256 * s, 128, UMMA_NK1 * 128), UMMA_IDESC_BF16_M128_N64, s > 0);
     umma_commit(bar);
   }
+}
+
+// Stage 2: wait for layer 1, write the layer-2 operand bf16(ReLU(D)) and
+// issue layer 2.
+__device__ __forceinline__ void umma_layer2_issue(const UmmaNet &N, unsigned char *abuf,
+                                                  uint32_t tm, uint64_t *bar, uint32_t &phase,
+                                                  int wg, bool &timeout) {
+  const int lane = threadIdx.x & 31, wq = (threadIdx.x >> 5) & 3;
+  const int row = 32 * wq + lane;
+  const uint32_t tlane = tm + ((uint32_t)(32 * wq) << 16);
   if (!mbar_wait(bar, phase, UMMA_WAIT_ITERS)) timeout = true;
   phase ^= 1u;
   tc_fence_after();
-  // ---- layer 2 operand: bf16(ReLU(D)), 32 columns at a time
+  // 32 columns at a time
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     float v[32];
@@ -237,10 +249,18 @@ __device__ __forceinline__ float umma_network(const UmmaNet &N, unsigned char *a
                umma_desc(b0 + 256 * s, 128, UMMA_NK2 * 128), UMMA_IDESC_BF16_M128_N64, s > 0);
     umma_commit(bar);
   }
+}
+
+// Stage 3: wait for layer 2 and form this row's logit
+// z = b3 + sum_j ReLU(D_j + b2_j) w3_j (two interleaved fp32 chains, even and
+// odd hidden units, in f32x2).
+__device__ __forceinline__ float umma_logit(const UmmaNet &N, uint32_t tm, uint64_t *bar,
+                                            uint32_t &phase, bool &timeout) {
+  const int wq = (threadIdx.x >> 5) & 3;
+  const uint32_t tlane = tm + ((uint32_t)(32 * wq) << 16);
   if (!mbar_wait(bar, phase, UMMA_WAIT_ITERS)) timeout = true;
   phase ^= 1u;
   tc_fence_after();
-  // logit: two interleaved fp32 chains (even and odd hidden units) in f32x2
   unsigned long long z2 = 0ull;
   const float4 *b2v = reinterpret_cast<const float4 *>(N.bias2);
   const float4 *w3v = reinterpret_cast<const float4 *>(N.w3);
@@ -263,6 +283,16 @@ __device__ __forceinline__ float umma_network(const UmmaNet &N, unsigned char *a
   }
   tc_fence_before();  // the next call's MMAs come after these reads
   return N.b3 + (__uint_as_float((uint32_t)z2) + __uint_as_float((uint32_t)(z2 >> 32)));
+}
+
+// Logit of the environment `env` of this thread's row: the three stages back
+// to back.
+__device__ __forceinline__ float umma_network(const UmmaNet &N, unsigned char *abuf, uint32_t tm,
+                                              uint64_t *bar, uint32_t &phase, int wg,
+                                              unsigned long long env, bool &timeout) {
+  umma_layer1_issue(N, abuf, tm, bar, wg, env);
+  umma_layer2_issue(N, abuf, tm, bar, phase, wg, timeout);
+  return umma_logit(N, tm, bar, phase, timeout);
 }
 
 }  // namespace cem
