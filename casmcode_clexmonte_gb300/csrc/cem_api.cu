@@ -1044,11 +1044,17 @@ int cem_nfold_run(cem_replicas *r, int64_t n_events, int64_t n_equil, int64_t re
         same = same && R.L[0] + 4 == p0 && R.L[1] + 4 == p0;
       if (same) pitch = p0;
     }
-    int smem = 0;
-    for (const Replica &R : r->reps)
-      smem = std::max(smem, nfold_smem_bytes(T, R.L[0], R.L[1], R.L[2], pitch));
+    // rate trees in shared memory when every replica's fits beside its
+    // occupation, else in global memory
+    int smem = 0, smem_tree = 0;
+    for (const Replica &R : r->reps) {
+      smem = std::max(smem, nfold_smem_bytes(T, R.L[0], R.L[1], R.L[2], pitch, 0));
+      smem_tree = std::max(smem_tree, nfold_smem_bytes(T, R.L[0], R.L[1], R.L[2], pitch, 1));
+    }
     require(smem <= maxsm, "supercell does not fit in shared memory for the n-fold kernel",
             CEM_ERR_UNSUPPORTED);
+    const int tree_smem = smem_tree <= maxsm ? 1 : 0;
+    if (tree_smem) smem = smem_tree;
     if (!r->d_nftree) {
       std::vector<long long> off(r->n);
       long long total = 0;
@@ -1070,6 +1076,7 @@ int cem_nfold_run(cem_replicas *r, int64_t n_events, int64_t n_equil, int64_t re
     P.occ = r->d_occ;
     P.tree = r->d_nftree;
     P.tree_off = r->d_nftree_off;
+    P.tree_smem = tree_smem;
     P.n_events = n_events;
     P.n_equil = n_equil;
     P.rec_cap = record_capacity;

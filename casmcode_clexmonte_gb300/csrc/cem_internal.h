@@ -154,8 +154,9 @@ struct NfoldParams {
   const Replica *reps;
   ReplicaStats *stats;
   int8_t *occ;
-  double *tree;               // per replica trees, back to back
+  double *tree;               // per replica trees, back to back (tree_smem == 0)
   const long long *tree_off;  // [n_rep] offset of each replica's tree
+  int tree_smem;              // 1: each CTA keeps its replica's tree in shared memory
   long long n_events, n_equil;
   long long rec_cap;          // recorded events per replica (0: none)
   long long *rec_site;
@@ -163,7 +164,7 @@ struct NfoldParams {
   double *rec_dt;
   double RT[16];
 };
-int nfold_smem_bytes(const CeTables &T, int L0, int L1, int L2, int pitch);
+int nfold_smem_bytes(const CeTables &T, int L0, int L1, int L2, int pitch, int tree_smem);
 cudaError_t launch_nfold(const CeTables &T, const NfoldParams &P, int n_replicas, int smem,
                          int pitch, cudaStream_t st);
 

@@ -7,7 +7,9 @@
 // exp(-beta dE), with dE the semi-grand canonical potential change
 // (CompleteEventCalculator::calculate_rate, src/casm/clexmonte/nfold/nfold_events.cc:24-60).
 // Each step draws one event with probability rate / total from a 32-ary
-// FP64 sum tree over all events of the replica, applies it and recomputes the
+// FP64 sum tree over all events of the replica (a node is the pairwise sum of
+// its 32 children, zero-padded: (c0 + c1) + (c2 + c3), ...; a descent walks
+// down the same binary tree inside each node), applies it and recomputes the
 // rates of the events whose site shares a cluster with the changed site. The
 // state before the step is weighted by its expected residence time in
 // Metropolis trials, n_possible / total, with n_possible = sites x n_occ x
@@ -15,7 +17,11 @@
 // per unit cell x unit cells).
 //
 // One CTA per replica; the replica's occupation stays in shared memory (the
-// sweep kernel's halo'd layout), the tree in global memory (L2 resident).
+// sweep kernel's halo'd layout), and so does the tree when it fits beside it
+// (24^3 binary: 14 271 doubles, 114 KB), else it lives in global memory (L2
+// resident). Pairwise sums keep the dependent chain of a node short (depth 5
+// instead of 31 sequential additions on the narrow FP64 pipe); warp 0
+// descends with one child per lane.
 // Every floating-point operation that decides the trajectory (energy change,
 // rate, tree sums, descent) is explicitly rounded, so the oracle's sequential
 // restatement reproduces the event sequence bit for bit.
@@ -67,11 +73,11 @@ __device__ __forceinline__ double orbit_fold_fp64(const CeTables &T, int g, cons
 }
 
 struct NfoldLayout {
-  int occ, cl_off, lutoff, lut, stats, imp, misc, total;
+  int occ, cl_off, lutoff, lut, stats, imp, misc, tree, total;
 };
 
 inline __host__ __device__ void nfold_layout(const CeTables &T, int L0, int L1, int L2, int pitch,
-                                             NfoldLayout &s) {
+                                             int tree_smem, NfoldLayout &s) {
   const int R = T.reach;
   const int W = pitch ? pitch : L0 + 2 * R, H = pitch ? pitch : L1 + 2 * R;
   const int V = W * H * (L2 + 2 * R);
@@ -91,6 +97,9 @@ inline __host__ __device__ void nfold_layout(const CeTables &T, int L0, int L1, 
   o += align16((MAX_FP + 1) * 4);
   s.misc = o;  // selected event
   o += 16;
+  s.tree = o;  // the rate tree (tree_smem)
+  if (tree_smem)
+    o += align16((int)(8 * rate_tree_size((long long)L0 * L1 * L2 * T.n_sublat * (T.n_occ - 1))));
   s.total = o;
 }
 
@@ -111,7 +120,7 @@ __global__ void __launch_bounds__(NF_THREADS)
   G.V = G.W * G.H * (G.L2 + 2 * G.R);
   const int n_uc = G.L0 * G.L1 * G.L2, nsl = T.n_sublat, n_sites = n_uc * nsl;
   NfoldLayout lay;
-  nfold_layout(T, G.L0, G.L1, G.L2, PITCH, lay);
+  nfold_layout(T, G.L0, G.L1, G.L2, PITCH, P.tree_smem, lay);
   int8_t *occ = reinterpret_cast<int8_t *>(smem + lay.occ);
   int *cl_off = reinterpret_cast<int *>(smem + lay.cl_off);
   int *lutoff = reinterpret_cast<int *>(smem + lay.lutoff);
@@ -185,13 +194,19 @@ __global__ void __launch_bounds__(NF_THREADS)
   const long long n_ev = (long long)n_sites * (NOCC - 1);
   RateTree tg;
   rate_tree_geo(n_ev, tg);
-  double *tr = P.tree + P.tree_off[rep];
+  double *tr = P.tree_smem ? reinterpret_cast<double *>(smem + lay.tree) : P.tree + P.tree_off[rep];
   auto node_sum = [&](int lev, long long node) {
     const double *ch = tr + tg.off[lev - 1];
-    const long long c0 = node * 32, cn = min(c0 + 32, tg.n[lev - 1]);
-    double s = 0.0;
-    for (long long c = c0; c < cn; ++c) s = DADD(s, ch[c]);
-    tr[tg.off[lev] + node] = s;
+    const long long c0 = node * 32;
+    const int cnt = (int)(min(c0 + 32, tg.n[lev - 1]) - c0);
+    double v[32];
+#pragma unroll
+    for (int c = 0; c < 32; ++c) v[c] = c < cnt ? ch[c0 + c] : 0.0;
+#pragma unroll
+    for (int w = 1; w < 32; w *= 2)
+#pragma unroll
+      for (int i = 0; i < 32; i += 2 * w) v[i] = DADD(v[i], v[i + w]);
+    tr[tg.off[lev] + node] = v[0];
   };
   for (long long e = tid; e < n_ev; e += nth) tr[e] = rate_of(e);
   __syncthreads();
@@ -200,23 +215,24 @@ __global__ void __launch_bounds__(NF_THREADS)
     __syncthreads();
   }
 
-  double energy = S.energy;
-  long long nspec[8];
-  for (int a = 0; a < 8; ++a) nspec[a] = S.n_species[a];
+  // the running energy and species counts live in S (shared memory): thread
+  // 0 applies each event to them, warp 1 samples them while warp 0 descends
   long long counter = S.pass;  // events drawn by this replica so far
   const uint32_t k0 = (uint32_t)R.seed, k1 = (uint32_t)(R.seed >> 32);
   const double n_possible = (double)n_sites * (double)(NOCC * (NOCC - 1));
   int status = 0;
   const long long n_total = P.n_equil + P.n_events;
+  const int lane = tid & 31;
   for (long long it = 0; it < n_total; ++it, ++counter) {
-    if (tid == 0) {
+    if (tid == 32 && it >= P.n_equil) {
+      // the state before this step, weighted by its residence time
       const double total = tr[tg.off[tg.n_lev - 1]];
-      long long leaf = -1;
       if (total > 0.0) {
         const double dt = DDIV(n_possible, total);
-        if (it >= P.n_equil) {
+        {
           double x[3] = {0.0, 0.0, 0.0}, ef, ep;
-          sample_values<NOCC>(P.RT, R.mu, nspec, n_sites, n_uc, energy, x, ef, ep);
+          sample_values<NOCC>(P.RT, R.mu, reinterpret_cast<const long long *>(S.n_species), n_sites, n_uc,
+                              S.energy, x, ef, ep);
           S.n_samples = DADD(S.n_samples, dt);
           S.sum_e = DADD(S.sum_e, DMUL(dt, ep));
           S.sum_e2 = DADD(S.sum_e2, DMUL(dt, DMUL(ep, ep)));
@@ -228,50 +244,62 @@ __global__ void __launch_bounds__(NF_THREADS)
               S.sum_xx[k * 3 + k2] = DADD(S.sum_xx[k * 3 + k2], DMUL(dt, DMUL(x[k], x[k2])));
           }
         }
+      }
+    }
+    if (tid < 32) {
+      const double total = tr[tg.off[tg.n_lev - 1]];
+      long long leaf = -1;
+      if (total > 0.0) {
+        const double dt = DDIV(n_possible, total);
         const U4 r = philox4x32_10(
             U4{(uint32_t)counter, (uint32_t)(counter >> 32), 0u, TAG_NFOLD << 16}, k0, k1);
         double tgt = DMUL(u53(r.x, r.y), total);
         long long node = 0;
+        const unsigned full = 0xffffffffu;
         for (int lev = tg.n_lev - 1; lev >= 1; --lev) {
-          const double *ch = tr + tg.off[lev - 1];
-          const long long c0 = node * 32, cn = min(c0 + 32, tg.n[lev - 1]);
-          double cum = 0.0, last_before = 0.0;
-          long long pick = -1, last = -1;
-          for (long long c = c0; c < cn; ++c) {
-            const double v = ch[c];
-            const double nc = DADD(cum, v);
-            if (v > 0.0) {
-              if (tgt < nc) {
-                pick = c;
-                break;
-              }
-              last = c;
-              last_before = cum;
+          const long long c0 = node * 32;
+          const int cnt = (int)(min(c0 + 32, tg.n[lev - 1]) - c0);
+          // one child per lane; p_k on lanes i 2^k holds the sum of children
+          // i 2^k .. (i + 1) 2^k - 1 (the node's binary tree)
+          const double p0 = lane < cnt ? tr[tg.off[lev - 1] + c0 + lane] : 0.0;
+          const double p1 = DADD(p0, __shfl_down_sync(full, p0, 1));
+          const double p2 = DADD(p1, __shfl_down_sync(full, p1, 2));
+          const double p3 = DADD(p2, __shfl_down_sync(full, p2, 4));
+          const double p4 = DADD(p3, __shfl_down_sync(full, p3, 8));
+          // down the binary tree: left when the right half is empty or the
+          // target lies below the left half's sum, else right
+          int base = 0;
+          auto step = [&](double p, int half) {
+            const double left = __shfl_sync(full, p, base), right = __shfl_sync(full, p, base + half);
+            if (!(right == 0.0 || (left > 0.0 && tgt < left))) {
+              tgt = DSUB(tgt, left);
+              base += half;
             }
-            cum = nc;
-          }
-          if (pick < 0) {  // rounding left the target at the end: last non-zero child
-            pick = last;
-            cum = last_before;
-          }
-          tgt = DSUB(tgt, cum);
-          node = pick;
+          };
+          step(p4, 16);
+          step(p3, 8);
+          step(p2, 4);
+          step(p1, 2);
+          step(p0, 1);
+          node = c0 + base;
         }
         leaf = node;
-        if (it < P.rec_cap) {
-          const long long ri = (long long)rep * P.rec_cap + it;
-          const int l = (int)(leaf / (NOCC - 1)), k = (int)(leaf - (long long)l * (NOCC - 1));
-          int b, x, y, z;
-          site_of(l, b, x, y, z);
-          const int o_i = occ[G.addr(b, x, y, z)];
-          P.rec_site[ri] = l;
-          P.rec_occ[ri] = k < o_i ? k : k + 1;
-          P.rec_dt[ri] = dt;
+        if (lane == 0) {
+          if (it < P.rec_cap) {
+            const long long ri = (long long)rep * P.rec_cap + it;
+            const int l = (int)(leaf / (NOCC - 1)), k = (int)(leaf - (long long)l * (NOCC - 1));
+            int b, x, y, z;
+            site_of(l, b, x, y, z);
+            const int o_i = occ[G.addr(b, x, y, z)];
+            P.rec_site[ri] = l;
+            P.rec_occ[ri] = k < o_i ? k : k + 1;
+            P.rec_dt[ri] = dt;
+          }
+          S.n_proposed += 1;
+          S.n_accepted += 1;
         }
-        S.n_proposed += 1;
-        S.n_accepted += 1;
       }
-      sel[0] = leaf;
+      if (lane == 0) sel[0] = leaf;
     }
     __syncthreads();
     const long long leaf = sel[0];
@@ -282,13 +310,13 @@ __global__ void __launch_bounds__(NF_THREADS)
     const int l = (int)(leaf / (NOCC - 1)), kk = (int)(leaf - (long long)l * (NOCC - 1));
     int b, x, y, z;
     site_of(l, b, x, y, z);
+    const int ad_l = G.addr(b, x, y, z);
     if (tid == 0) {
-      const int ad = G.addr(b, x, y, z);
-      const int o_i = occ[ad];
+      const int o_i = occ[ad_l];
       const int o_f = kk < o_i ? kk : kk + 1;
-      energy = DADD(energy, site_de(b, o_i, o_f, ad));
-      nspec[o_i] -= 1;
-      nspec[o_f] += 1;
+      sel[1] = o_i;
+      S.n_species[o_i] -= 1;
+      S.n_species[o_f] += 1;
       put_site(occ, G, b, x, y, z, (int8_t)o_f);
     }
     // impacted sites: the changed site and its flower partners
@@ -302,6 +330,14 @@ __global__ void __launch_bounds__(NF_THREADS)
       imp[t] = s;
     }
     __syncthreads();
+    if (tid == 96) {
+      // the applied change's energy, from the reverse change on the new state:
+      // its delta counts are the exact negatives (the flower excludes the
+      // site), so E - dE_reverse equals E + dE bit for bit; off the critical
+      // path of the rate updates
+      const int o_f = occ[ad_l], o_i = (int)sel[1];
+      S.energy = DSUB(S.energy, site_de(b, o_f, o_i, ad_l));
+    }
     for (int t = tid; t < n_imp * (NOCC - 1); t += nth) {
       const long long e = (long long)imp[t / (NOCC - 1)] * (NOCC - 1) + t % (NOCC - 1);
       tr[e] = rate_of(e);
@@ -321,8 +357,6 @@ __global__ void __launch_bounds__(NF_THREADS)
     P.occ[R.occ_offset + l] = occ[G.addr(b, x, y, z)];
   }
   if (tid == 0) {
-    S.energy = energy;
-    for (int a = 0; a < NOCC; ++a) S.n_species[a] = nspec[a];
     S.pass = counter;
     S.status = status;
   }
@@ -346,9 +380,9 @@ cudaError_t launch_nfold_t(const CeTables &T, const NfoldParams &P, int n_replic
 
 }  // namespace
 
-int nfold_smem_bytes(const CeTables &T, int L0, int L1, int L2, int pitch) {
+int nfold_smem_bytes(const CeTables &T, int L0, int L1, int L2, int pitch, int tree_smem) {
   NfoldLayout s;
-  nfold_layout(T, L0, L1, L2, pitch, s);
+  nfold_layout(T, L0, L1, L2, pitch, tree_smem, s);
   return s.total;
 }
 

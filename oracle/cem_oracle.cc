@@ -1093,10 +1093,13 @@ i64 ora_enforce_composition(void *h, signed char *occ, const double *target, u64
 // src/casm/clexmonte/nfold/nfold_events.cc:24-60). Restated sequentially:
 // events are (site l, k-th other occupant), e = l (n_occ - 1) + k; rate =
 // 1 if dE <= 0 else exp(-beta dE) with dE = sum_f w_f dcount_f - dmu; a
-// 32-ary sum tree whose nodes are sequential sums of their children; each
-// step weights the current state by n_possible / total, draws a uniform
-// u53 from Philox4x32-10 (counter = event index, tag 3), descends the tree,
-// applies the event. All rates are recomputed after every event (the GPU
+// 32-ary sum tree whose nodes are pairwise sums of their children (the 32
+// children, zero-padded, summed as a balanced binary tree: (c0 + c1) +
+// (c2 + c3), ...); each step weights the current state by n_possible /
+// total, draws a uniform u53 from Philox4x32-10 (counter = event index, tag
+// 3), descends the tree (inside a node, down the same binary tree: left when
+// the right half is empty or the target lies below the left half's sum, else
+// right with the left sum subtracted), applies the event. All rates are recomputed after every event (the GPU
 // recomputes only the changed site's flower), so the comparison also checks
 // the GPU's impact lists.
 extern "C" void ora_philox4x32_10(const unsigned *ctr_in, const unsigned *key_in, unsigned *out);
@@ -1123,6 +1126,14 @@ static double exp_neg_restated(double x) {
 }
 
 extern "C" double ora_exp_neg(double x) { return exp_neg_restated(x); }
+
+// The 32 children of a tree node (zero beyond the level's end).
+static void children32(const std::vector<double> &lev, size_t node, double *v) {
+  for (int c = 0; c < 32; ++c) {
+    const size_t i = node * 32 + (size_t)c;
+    v[c] = i < lev.size() ? lev[i] : 0.0;
+  }
+}
 
 // stats_out: [0] total weight, [1] sum w ep, [2] sum w ep^2, [3] sum w ef,
 // [4..6] sum w x_k, [7..15] sum w x_k x_k', [16..18] sum w ep x_k.
@@ -1167,10 +1178,11 @@ extern "C" i64 ora_nfold(void *h, signed char *occ, double temperature, const do
       }
       for (size_t L = 1; L < lev.size(); ++L)
         for (size_t node = 0; node < lev[L].size(); ++node) {
-          double t = 0.0;
-          const size_t c1 = std::min(node * 32 + 32, lev[L - 1].size());
-          for (size_t c = node * 32; c < c1; ++c) t = t + lev[L - 1][c];
-          lev[L][node] = t;
+          double v[32];
+          children32(lev[L - 1], node, v);
+          for (int wdt = 1; wdt < 32; wdt *= 2)
+            for (int i = 0; i < 32; i += 2 * wdt) v[i] = v[i] + v[i + wdt];
+          lev[L][node] = v[0];
         }
     };
     // observables
@@ -1219,29 +1231,23 @@ extern "C" i64 ora_nfold(void *h, signed char *occ, double temperature, const do
       double tgt = u * total;
       i64 node = 0;
       for (int L = (int)lev.size() - 1; L >= 1; --L) {
-        const auto &ch = lev[L - 1];
-        const i64 c0 = node * 32, c1 = std::min<i64>(c0 + 32, (i64)ch.size());
-        double cum = 0.0, last_before = 0.0;
-        i64 pick = -1, last = -1;
-        for (i64 c = c0; c < c1; ++c) {
-          const double v = ch[c];
-          const double nc = cum + v;
-          if (v > 0.0) {
-            if (tgt < nc) {
-              pick = c;
-              break;
-            }
-            last = c;
-            last_before = cum;
+        // the node's binary tree: part[k][i] = sum of children i 2^k ..
+        // (i + 1) 2^k - 1, zero-padded to 32 children
+        double part[6][32];
+        children32(lev[L - 1], (size_t)node, part[0]);
+        for (int k = 1; k <= 5; ++k)
+          for (int i = 0; i < (32 >> k); ++i) part[k][i] = part[k - 1][2 * i] + part[k - 1][2 * i + 1];
+        int j = 0;  // current sub-node at level k
+        for (int k = 4; k >= 0; --k) {
+          const double left = part[k][2 * j], right = part[k][2 * j + 1];
+          if (right == 0.0 || (left > 0.0 && tgt < left)) {
+            j = 2 * j;
+          } else {
+            tgt = tgt - left;
+            j = 2 * j + 1;
           }
-          cum = nc;
         }
-        if (pick < 0) {
-          pick = last;
-          cum = last_before;
-        }
-        tgt = tgt - cum;
-        node = pick;
+        node = node * 32 + j;
       }
       const int l = (int)(node / (no - 1)), k = (int)(node % (no - 1));
       const int oi = occ[l], of = k < oi ? k : k + 1;
