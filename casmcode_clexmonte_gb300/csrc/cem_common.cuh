@@ -221,9 +221,9 @@ CEM_HD float cem_expf_neg(float x) {
 
 // exp(x) for x <= 0 in FP64, for n-fold rates: Cody-Waite reduction
 // x = n ln2 + r with the fdlibm split of ln2 (ln2_hi has 32 significant bits,
-// so n ln2_hi is exact), e^r by its degree-13 Taylor polynomial in Horner
-// form with fused multiply-adds (|r| <= ln2/2: truncation below 2^-56
-// relative), scaled by 2^n. Every operation is explicitly rounded, so host
+// so n ln2_hi is exact), e^r by its degree-13 Taylor polynomial with fused
+// multiply-adds as 1 + (r + r^2 T(r)), T in Estrin's scheme (|r| <= ln2/2:
+// truncation below 2^-56 relative; within 1 ulp of libm), scaled by 2^n. Every operation is explicitly rounded, so host
 // and device give the same bits. x < -745 (or NaN) returns 0.
 #ifdef __CUDA_ARCH__
 #define DADD(a, b) __dadd_rn((a), (b))
@@ -257,8 +257,15 @@ CEM_HD double cem_exp_neg(double x) {
                         0x1.6c16c16c16c17p-10, 0x1.a01a01a01a01ap-13, 0x1.a01a01a01a01ap-16,
                         0x1.71de3a556c734p-19, 0x1.27e4fb7789f5cp-22, 0x1.ae64567f544e4p-26,
                         0x1.1eed8eff8d898p-29, 0x1.6124613a86d09p-33};  // 1/k!
-  double p = c[13];
-  for (int k = 12; k >= 0; --k) p = DFMA(p, r, c[k]);
+  // p = 1 + (r + r^2 T(r)), T = c2 + c3 r + ... + c13 r^11 in Estrin's
+  // scheme: 6 dependent steps instead of 13, the large low-order terms added
+  // last
+  const double r2 = DMUL(r, r), r4 = DMUL(r2, r2);
+  const double a0 = DFMA(c[3], r, c[2]), a1 = DFMA(c[5], r, c[4]), a2 = DFMA(c[7], r, c[6]),
+               a3 = DFMA(c[9], r, c[8]), a4 = DFMA(c[11], r, c[10]), a5 = DFMA(c[13], r, c[12]);
+  const double b0 = DFMA(a1, r2, a0), b1 = DFMA(a3, r2, a2), b2 = DFMA(a5, r2, a4);
+  const double t = DFMA(DFMA(b2, r4, b1), r4, b0);
+  const double p = DADD(DFMA(r2, t, r), c[0]);
 #ifdef __CUDA_ARCH__
   return ldexp(p, (int)n);
 #else

@@ -35,7 +35,7 @@ constexpr int NF_THREADS = 128;
 constexpr uint32_t TAG_NFOLD = 0x3u;
 
 // FP64 energy change of the formation energy from integer delta counts, in
-// function-index order.
+// function-index order, one fused multiply-add per function.
 template <int NOCC>
 __device__ __forceinline__ double de_fp64(const CeTables &T, const Acc<NOCC> &acc) {
   double d = 0.0;
@@ -44,10 +44,10 @@ __device__ __forceinline__ double de_fp64(const CeTables &T, const Acc<NOCC> &ac
     if (g < T.n_orbits) {
       const int base = T.orb_func_base[g];
       if constexpr (NOCC == 2) {
-        d = DADD(d, DMUL(T.w[base], (double)acc.c[g]));
+        d = DFMA(T.w[base], (double)acc.c[g], d);
       } else {
         const int nf = T.orb_n_funcs[g];
-        for (int fl = 0; fl < nf; ++fl) d = DADD(d, DMUL(T.w[base + fl], (double)acc_dc<NOCC>(acc, g, fl)));
+        for (int fl = 0; fl < nf; ++fl) d = DFMA(T.w[base + fl], (double)acc_dc<NOCC>(acc, g, fl), d);
       }
     }
   }
@@ -61,12 +61,12 @@ __device__ __forceinline__ double orbit_fold_fp64(const CeTables &T, int g, cons
                                                   double d) {
   const int base = T.orb_func_base[g];
   if constexpr (NOCC == 2) {
-    return DADD(d, DMUL(T.w[base], (double)a.c));
+    return DFMA(T.w[base], (double)a.c, d);
   } else {
     const int nf = T.orb_n_funcs[g];
     for (int fl = 0; fl < nf; ++fl) {
       const int dc = (int)((a.p >> (8 * fl)) & 255ull) - (int)((a.m >> (8 * fl)) & 255ull);
-      d = DADD(d, DMUL(T.w[base + fl], (double)dc));
+      d = DFMA(T.w[base + fl], (double)dc, d);
     }
     return d;
   }

@@ -1092,7 +1092,8 @@ i64 ora_enforce_composition(void *h, signed char *occ, const double *target, u64
 // nfold_impl.hh:20-108, rates as CompleteEventCalculator::calculate_rate,
 // src/casm/clexmonte/nfold/nfold_events.cc:24-60). Restated sequentially:
 // events are (site l, k-th other occupant), e = l (n_occ - 1) + k; rate =
-// 1 if dE <= 0 else exp(-beta dE) with dE = sum_f w_f dcount_f - dmu; a
+// 1 if dE <= 0 else exp(-beta dE) with dE = sum_f w_f dcount_f - dmu (one
+// fused multiply-add per function, in function order); a
 // 32-ary sum tree whose nodes are pairwise sums of their children (the 32
 // children, zero-padded, summed as a balanced binary tree: (c0 + c1) +
 // (c2 + c3), ...); each step weights the current state by n_possible /
@@ -1105,7 +1106,8 @@ i64 ora_enforce_composition(void *h, signed char *occ, const double *target, u64
 extern "C" void ora_philox4x32_10(const unsigned *ctr_in, const unsigned *key_in, unsigned *out);
 
 // exp(x) for x <= 0: Cody-Waite reduction with the fdlibm split of ln2,
-// degree-13 Taylor polynomial by fused multiply-adds, scaling by 2^n.
+// degree-13 Taylor polynomial by fused multiply-adds in Estrin's scheme,
+// scaling by 2^n.
 static double exp_neg_restated(double x) {
   if (!(x >= -745.0)) return 0.0;
   if (x > 0.0) x = 0.0;
@@ -1120,8 +1122,15 @@ static double exp_neg_restated(double x) {
                                0x1.6c16c16c16c17p-10, 0x1.a01a01a01a01ap-13, 0x1.a01a01a01a01ap-16,
                                0x1.71de3a556c734p-19, 0x1.27e4fb7789f5cp-22, 0x1.ae64567f544e4p-26,
                                0x1.1eed8eff8d898p-29, 0x1.6124613a86d09p-33};
-  double p = c[13];
-  for (int k = 12; k >= 0; --k) p = std::fma(p, r, c[k]);
+  // p = 1 + (r + r^2 T(r)), T = c2 + ... + c13 r^11 in Estrin's scheme, the
+  // same association as the product's
+  const double r2 = r * r, r4 = r2 * r2;
+  const double a0 = std::fma(c[3], r, c[2]), a1 = std::fma(c[5], r, c[4]),
+               a2 = std::fma(c[7], r, c[6]), a3 = std::fma(c[9], r, c[8]),
+               a4 = std::fma(c[11], r, c[10]), a5 = std::fma(c[13], r, c[12]);
+  const double b0 = std::fma(a1, r2, a0), b1 = std::fma(a3, r2, a2), b2 = std::fma(a5, r2, a4);
+  const double t = std::fma(std::fma(b2, r4, b1), r4, b0);
+  const double p = std::fma(r2, t, r) + c[0];
   return std::ldexp(p, (int)n);
 }
 
@@ -1161,7 +1170,7 @@ extern "C" i64 ora_nfold(void *h, signed char *occ, double temperature, const do
       std::fill(dc.begin(), dc.end(), 0);
       site_delta_counts(s, occ, l, of, dc.data());
       double d = 0.0;
-      for (int f = 1; f < s.n_funcs; ++f) d = d + w[f] * (double)dc[f];
+      for (int f = 1; f < s.n_funcs; ++f) d = std::fma(w[f], (double)dc[f], d);
       return d;
     };
     const i64 n_ev = (i64)N * (no - 1);
