@@ -546,7 +546,12 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
     }
   }
   if (mode == 1) {
-    if (ntimeout) atomicExch(&S.status, 8);  // an MMA wait ran out: results are invalid
+    if (ntimeout) {
+      atomicExch(&S.status, 8);  // an MMA wait ran out: results are invalid
+      // let the last committed MMA land before the tensor memory is freed
+      // (bounded; its parity is the one before the last toggle)
+      mbar_wait(&nbar[wg], nphase ^ 1u, UMMA_WAIT_ITERS);
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -594,7 +599,11 @@ __global__ void __launch_bounds__(UMMA_FWD_THREADS)
     const float zz = umma_network(net, abuf, tm, &bars[wg], phase, wg, env, timeout);
     if (e < n) z[e] = zz;
   }
-  if (timeout) atomicExch(status, 1);
+  if (timeout) {
+    atomicExch(status, 1);
+    // let the last committed MMA land before the tensor memory is freed
+    mbar_wait(&bars[wg], phase ^ 1u, UMMA_WAIT_ITERS);
+  }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();

@@ -183,7 +183,9 @@ __device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsig
 // call it together); abuf = the warpgroup's operand rows, tm = its 64
 // tensor-memory columns, bar = its mbarrier with phase bit `phase` (toggled
 // by each wait). A wait that runs out sets `timeout` (the logit is then
-// meaningless).
+// meaningless); once it is set, this thread's later waits try once, so a
+// kernel whose MMAs stopped completing still ends promptly (its control flow,
+// and with it every warpgroup barrier, does not depend on the flag).
 //
 // Stage 1: write this thread's row of the layer-1 operand (env: bit k =
 // neighbour k) and issue layer 1.
@@ -219,7 +221,7 @@ __device__ __forceinline__ void umma_layer2_issue(const UmmaNet &N, unsigned cha
   const int lane = threadIdx.x & 31, wq = (threadIdx.x >> 5) & 3;
   const int row = 32 * wq + lane;
   const uint32_t tlane = tm + ((uint32_t)(32 * wq) << 16);
-  if (!mbar_wait(bar, phase, UMMA_WAIT_ITERS)) timeout = true;
+  if (!mbar_wait(bar, phase, timeout ? 1 : UMMA_WAIT_ITERS)) timeout = true;
   phase ^= 1u;
   tc_fence_after();
   // 32 columns at a time
@@ -258,7 +260,7 @@ __device__ __forceinline__ float umma_logit(const UmmaNet &N, uint32_t tm, uint6
                                             uint32_t &phase, bool &timeout) {
   const int wq = (threadIdx.x >> 5) & 3;
   const uint32_t tlane = tm + ((uint32_t)(32 * wq) << 16);
-  if (!mbar_wait(bar, phase, UMMA_WAIT_ITERS)) timeout = true;
+  if (!mbar_wait(bar, phase, timeout ? 1 : UMMA_WAIT_ITERS)) timeout = true;
   phase ^= 1u;
   tc_fence_after();
   unsigned long long z2 = 0ull;
