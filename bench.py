@@ -533,13 +533,14 @@ def tc_scan(cm, ce):
     return float(temps[inner][int(np.argmax(cv[inner]))]), temps, cv
 
 
-def learned_vs_plain(cm, T: float, plain_passes: int = 30000, learned_passes: int = 2000,
+def learned_vs_plain(cm, T: float, plain_passes: int = 60000, learned_passes: int = 6000,
                      equil_passes: int = 5000, rounds: int = 2, local_substeps: int = 4,
                      weights=("network",)) -> dict:
     """Configuration 3 (32 x 48^3 FCC, L1_2 cluster expansion, canonical
     x_B = 0.25) at temperature T: plain GPU Metropolis (the colour-class
-    sweep) against the learned group sweep, both continued from one common
-    state equilibrated by the plain sweep from perfect L1_2 order.
+    sweep, each replica on a cluster of 4 CTAs) against the learned group
+    sweep (also 4 CTAs per replica), both continued from one common state
+    equilibrated by the plain sweep from perfect L1_2 order.
 
     Per sampler: integrated autocorrelation times of E and of the L1_2 order
     parameter per replica (Sokal window; the run must hold >= 50 tau_int),
@@ -597,6 +598,8 @@ def learned_vs_plain(cm, T: float, plain_passes: int = 30000, learned_passes: in
                             sum(b["n_proposed"] - a["n_proposed"] for a, b in zip(st0, st1)),
                             sum(b["n_accepted"] - a["n_accepted"] for a, b in zip(st0, st1)),
                             plain_passes)}
+    # both samplers spread a replica over a cluster of CTAs when that pays
+    out["plain"]["cluster_ctas_per_replica"] = plain.get_option("sweep_cluster")
     # network trained on the equilibrated plain states (10^6 environments)
     eq = batch()
     eq.set_occupation_all(common)
@@ -816,8 +819,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", type=int, default=WORKLOAD_INDEX, choices=[0, 1, 2, 3, 4])
-    ap.add_argument("--learned-passes", type=int, default=2000)
-    ap.add_argument("--plain-passes", type=int, default=30000)
+    ap.add_argument("--learned-passes", type=int, default=6000)
+    ap.add_argument("--plain-passes", type=int, default=60000)
     ap.add_argument("--equil-passes", type=int, default=5000,
                     help="workload 3: plain passes that equilibrate the common state")
     ap.add_argument("--rounds", type=int, default=2,

@@ -44,6 +44,7 @@ struct SweepParams {
   int pack16;                  // cooperative sweep: 16-bit partner offsets and weights
   const int *cta_rep;          // replica of each CTA (null: CTA i runs replica i)
   const volatile int *stop;    // host-mapped stop flag (null: none)
+  int cluster;                 // CTAs per replica (thread-block cluster; <= 1: one CTA)
   double RT[16];               // (n_occ-1) x n_occ
 };
 

@@ -15,6 +15,7 @@
 // and accumulate +1/-1 in 8-bit fields of a 64-bit word per orbit.
 #pragma once
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -1080,14 +1081,19 @@ struct PairGeom {
   }
 };
 
-// Phase A of a canonical sub-step: warp w scans candidates [w chunk,
-// (w + 1) chunk) and keeps, in order, those whose two occupants differ (the
-// only proposals) in cl[w chunk ...]; wk[w] = number kept.
+// Phase A of a canonical sub-step: warp w scans candidates [v chunk,
+// (v + 1) chunk) of its virtual warp v and keeps, in order, those whose two
+// occupants differ (the only proposals) in cl[w chunk ...]; wk[w] = number
+// kept.
 __device__ __forceinline__ void compact_pairs(const PairGeom &pg, const Geo &G, const int8_t *occ,
-                                              int n, int chunk, int warp, int lane, uint16_t *cl,
-                                              int *wk) {
-  const int q_begin = warp * chunk;
+                                              int n, int chunk, int warp, int vwarp, int lane,
+                                              uint16_t *cl, int *wk) {
+  // scan range of virtual warp vwarp (= warp, or rank x warps + warp when a
+  // cluster of CTAs shares the sub-step); kept candidates stored from
+  // cl[warp chunk]
+  const int q_begin = vwarp * chunk;
   const int q_end = min(n, q_begin + chunk);
+  const int s_begin = warp * chunk;
   int kept = 0;
   for (int q0 = q_begin; q0 < q_end; q0 += 32) {
     const int q = q0 + lane;
@@ -1098,7 +1104,7 @@ __device__ __forceinline__ void compact_pairs(const PairGeom &pg, const Geo &G, 
       act = occ[G.addr(pg.cb, xa, ya, za)] != occ[G.addr(pg.bb, xb, yb, zb)];
     }
     const unsigned m = __ballot_sync(0xffffffffu, act);
-    if (act) cl[q_begin + kept + __popc(m & ((1u << lane) - 1u))] = (uint16_t)q;
+    if (act) cl[s_begin + kept + __popc(m & ((1u << lane) - 1u))] = (uint16_t)q;
     kept += __popc(m);
   }
   if (lane == 0) wk[warp] = kept;
@@ -1291,10 +1297,20 @@ template <int NOCC, int PITCH, int THREADS = SWEEP_THREADS>
 __global__ void __launch_bounds__(THREADS, 512 / THREADS)
     k_sweep(const __grid_constant__ CeTables T, const __grid_constant__ SweepParams P) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int rep = P.cta_rep ? P.cta_rep[blockIdx.x] : blockIdx.x;
+  // a replica per CTA, or per thread-block cluster of CL CTAs (generated
+  // binary evaluator): every CTA keeps a whole copy of the replica, takes
+  // its share of each sub-step's candidates and writes each accepted change
+  // into every copy (distributed shared memory); a cluster barrier ends each
+  // sub-step, and rank 0 keeps the statistics and writes the replica back
+  namespace cg = cooperative_groups;
+  const int CL = (PITCH > 0 && P.cluster > 1) ? P.cluster : 1;
+  const int crank = CL > 1 ? (int)cg::this_cluster().block_rank() : 0;
+  const int cta = (int)blockIdx.x / CL;
+  const int rep = P.cta_rep ? P.cta_rep[cta] : cta;
   const Replica &R = P.reps[rep];
   ReplicaStats &Sg = P.stats[rep];
   constexpr int NW = THREADS / 32;
+  __shared__ long long s_part[8][16];  // per-rank pass totals, gathered in rank 0
   const int tid = threadIdx.x, nth = THREADS;
   Geo G;
   G.L0 = R.L[0];
@@ -1416,7 +1432,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
   const SiteIndex site_of(n_uc, G.L0, G.L1);
   // bulk (TMA) copies when the replica's occupations are 16-byte aligned,
   // byte loads otherwise
-  const bool vec16 = ((R.occ_offset | n_sites) & 15) == 0;
+  const bool vec16 = CL == 1 && ((R.occ_offset | n_sites) & 15) == 0;
   uint8_t *stg = smem + lay.clist;
   const int stg_cap = ((lay.bar - lay.clist) / 16) * 16;
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem + lay.bar);
@@ -1451,6 +1467,19 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
 
   const SiteEval<NOCC, PITCH> ev{&T, cl_off, lutoff, lut};
   const int lane = tid & 31, warp = tid >> 5;
+  // an accepted change reaches every copy of the replica
+  auto put_all = [&](int b, int x, int y, int z, int8_t v) {
+    if (CL == 1) {
+      put_site(occ, G, b, x, y, z, v);
+    } else {
+      cg::cluster_group cluster = cg::this_cluster();
+      for (int r = 0; r < CL; ++r) put_site(cluster.map_shared_rank(occ, r), G, b, x, y, z, v);
+    }
+  };
+  auto sub_barrier = [&]() {
+    if (CL == 1) __syncthreads();
+    else cg::this_cluster().sync();
+  };
   if constexpr (EXACT) {
     if (P.init)
       init_binary_stats<PITCH, NW>(T, occ, G, site_of, ev, n_sites, n_uc,
@@ -1616,8 +1645,8 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
           }
         }
        } else {
-        // ---------------- flips of every site of the class
-        for (int q = tid; q < D.n; q += nth) {
+        // ---------------- flips of every site of the class (this CTA's share)
+        for (int q = crank * nth + tid; q < D.n; q += CL * nth) {
           const int t = fe0.div(q), iz = fe1.div(t);
           const int ix = q - t * d0, iy = t - iz * d1;
           const int x = cx[ix], y = cy[iy], z = cz[iz];
@@ -1653,7 +1682,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
           ++n_prop;
           if (accept_de(de, beta_f, u24(r.x))) {
             ++n_acc;
-            put_site(occ, G, cb, x, y, z, (int8_t)o_f);
+            put_all(cb, x, y, z, (int8_t)o_f);
             eacc.add(acc, d, R.dmu[o_i * NOCC + o_f]);
             dspec.add(o_i, -1);
             dspec.add(o_f, 1);
@@ -1672,11 +1701,11 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
         // the previous phase B: it reads only its own class's sites, which
         // that phase B does not write.
         const PairGeom pg(D, ax_coord);
-        const int buf = sub & 1, chunk = D.chunk;
+        const int buf = sub & 1, chunk = CL == 1 ? D.chunk : (D.n + CL * NW - 1) / (CL * NW);
         uint16_t *cl = clist + buf * clist_cap;
         int *wk = wkept + buf * 32;
         if (a_buf != buf) {
-          compact_pairs(pg, G, occ, D.n, chunk, warp, lane, cl, wk);
+          compact_pairs(pg, G, occ, D.n, chunk, warp, crank * NW + warp, lane, cl, wk);
           __syncthreads();
         }
         const bool local = pg.local;
@@ -1789,8 +1818,10 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
           ++n_prop;
           if (accept_de(de, beta_f, u24(r.x))) {
             ++n_acc;
-            if (!local) put_site(occ, G, cb, xa, ya, za, (int8_t)ob);
-            put_site(occ, G, bb, xb, yb, zb, (int8_t)oa);
+            // (a neighbour swap's first change is already in this copy; the
+            // other copies receive it now)
+            if (!local || CL > 1) put_all(cb, xa, ya, za, (int8_t)ob);
+            put_all(bb, xb, yb, zb, (int8_t)oa);
             eacc.add(acc, d, 0.0);
             if constexpr (PITCH > 0) {
               dsub.add(sc_sublattice(xa, ya, za), ob - oa);
@@ -1806,13 +1837,14 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
           if (Dn.mode == 1 &&
               (Dn.cb != D.cb || Dn.cxo != D.cxo || Dn.cyo != D.cyo || Dn.czo != D.czo)) {
             const PairGeom pn(Dn, ax_coord);
-            compact_pairs(pn, G, occ, Dn.n, Dn.chunk, warp, lane, clist + (buf ^ 1) * clist_cap,
-                          wkept + (buf ^ 1) * 32);
+            const int chunk_n = CL == 1 ? Dn.chunk : (Dn.n + CL * NW - 1) / (CL * NW);
+            compact_pairs(pn, G, occ, Dn.n, chunk_n, warp, crank * NW + warp, lane,
+                          clist + (buf ^ 1) * clist_cap, wkept + (buf ^ 1) * 32);
             a_buf = buf ^ 1;
           }
         }
       }
-      __syncthreads();
+      sub_barrier();  // every copy holds the sub-step's changes
     }
 
     // ---- end of pass: reduce (32-bit per-pass counters), sample
@@ -1850,21 +1882,37 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
         rd_d[warp] = dsum;
       }
       __syncthreads();
+      // lane k < 16 of warp 0 sums slot k over the warps; lane 16 sums the dE
+      // slot in warp order
+      long long v = 0;
+      double dv = 0.0;
       if (warp == 0) {
-        // lane k < 16 sums slot k over the warps; lane 16 sums the dE slot in
-        // warp order
-        long long v = 0;
-        double dv = 0.0;
         if (lane < 16)
           for (int w = 0; w < NW; ++w) v += rd_i[w * 16 + lane];
         if (lane == 16)
           for (int w = 0; w < NW; ++w) dv += rd_d[w];
+      }
+      if (CL > 1) {
+        // a cluster's pass totals (binary: integers only) gather in rank 0
+        cg::cluster_group cluster = cg::this_cluster();
+        if (warp == 0 && lane < 16) *cluster.map_shared_rank(&s_part[crank][lane], 0) = v;
+        cluster.sync();
+        if (warp == 0 && crank == 0 && lane < 16) {
+          v = 0;
+          for (int r = 0; r < CL; ++r) v += s_part[r][lane];
+        }
+      }
+      if (warp == 0 && crank == 0) {
         long long tot[16];
 #pragma unroll
         for (int k = 0; k < 16; ++k) tot[k] = __shfl_sync(0xffffffffu, v, k);
         double dtot = __shfl_sync(0xffffffffu, dv, 16);
         if (lane == 0) {
           s_stop = stop_seen;
+          if (CL > 1) {  // every rank leaves at the same pass boundary
+            cg::cluster_group cluster = cg::this_cluster();
+            for (int r = 1; r < CL; ++r) *cluster.map_shared_rank(&s_stop, r) = stop_seen;
+          }
           if constexpr (EXACT) {
             dtot = 0.0;
             for (int g = 0; g < T.n_orbits; ++g)
@@ -1910,7 +1958,12 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
           }
         }
       }
+      if (CL > 1) cg::this_cluster().sync();  // the stop decision reached every rank
     }
+  }
+  if (CL > 1) {
+    cg::this_cluster().sync();  // no peer writes into this copy any more
+    if (crank != 0) return;     // rank 0 writes the replica and its statistics back
   }
   // ---- write back
   if (vec16) {
@@ -1991,8 +2044,25 @@ cudaError_t launch_sweep_t(const CeTables &T, const SweepParams &P, int n_replic
   cudaError_t e = cudaFuncSetAttribute(k_sweep<NOCC, PITCH, THREADS>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  k_sweep<NOCC, PITCH, THREADS><<<n_replicas, THREADS, smem, st>>>(T, P);
-  return cudaGetLastError();
+  const int cl = (PITCH > 0 && P.cluster > 1) ? P.cluster : 1;
+  if (cl == 1) {
+    k_sweep<NOCC, PITCH, THREADS><<<n_replicas, THREADS, smem, st>>>(T, P);
+    return cudaGetLastError();
+  }
+  // one thread-block cluster of cl CTAs per replica
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)(n_replicas * cl));
+  cfg.blockDim = dim3(THREADS);
+  cfg.dynamicSmemBytes = (size_t)smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)cl;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_sweep<NOCC, PITCH, THREADS>, T, P);
 }
 
 #define CEM_INSTANTIATE(N)                                                                     \
