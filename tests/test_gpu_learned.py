@@ -198,10 +198,11 @@ def test_learned_group_sweep_equilibrium_matches_oracle(T, cm, oracle_mod):
     from casmcode_clexmonte_gb300.stats import family_2sigma, jackknife_chains
     from tests.stat_checks import check_chain_lengths as _check_chain_lengths
 
-    L, nrep, KB = 12, 32, 8.617333262e-5
+    L, KB = 12, 8.617333262e-5
     n = L ** 3
     ce = workloads.fcc_binary_ce(3, nn1=0.08)
     ordered = T < 100.0
+    nrep = 64 if ordered else 32
     rng = np.random.default_rng(int(T))
 
     def initial(i):
@@ -232,9 +233,10 @@ def test_learned_group_sweep_equilibrium_matches_oracle(T, cm, oracle_mod):
     # the ordered phase (tau_int ~ 200 passes at 90 K); they are checked in the
     # disordered phase, where runs of 2500 samples hold >= 50 tau_int
     modes = ("network", "exact") if ordered else ("uniform", "network", "exact")
-    # on 12^3 in the ordered phase single chains reach tau_int ~ 200 passes
-    # (two groups per class, few neighbour swaps per pass on so small a box)
-    n_pass, n_eq = (22000, 2000) if ordered else (3000, 500)
+    # on 12^3 in the ordered phase single chains reach tau_int ~ 130-290
+    # passes (two groups per class, few neighbour swaps per pass on so small a
+    # box): 64 chains of 40 000 passes
+    n_pass, n_eq = (40000, 2000) if ordered else (3000, 500)
     for weights in modes:
         b = cm.ReplicaBatch(sysd, "canonical", [(L, L, L)] * nrep)
         for i in range(nrep):
