@@ -1293,7 +1293,7 @@ __device__ __noinline__ void init_binary_stats(const CeTables &T, const int8_t *
   __syncthreads();
 }
 
-template <int NOCC, int PITCH, int THREADS = SWEEP_THREADS>
+template <int NOCC, int PITCH, int THREADS = SWEEP_THREADS, bool CLUSTERED = false>
 __global__ void __launch_bounds__(THREADS, 512 / THREADS)
     k_sweep(const __grid_constant__ CeTables T, const __grid_constant__ SweepParams P) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -1303,14 +1303,15 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
   // into every copy (distributed shared memory); a cluster barrier ends each
   // sub-step, and rank 0 keeps the statistics and writes the replica back
   namespace cg = cooperative_groups;
-  const int CL = (PITCH > 0 && P.cluster > 1) ? P.cluster : 1;
-  const int crank = CL > 1 ? (int)cg::this_cluster().block_rank() : 0;
+  static_assert(!CLUSTERED || PITCH > 0, "clusters share the generated binary evaluator's sweep");
+  const int CL = CLUSTERED ? P.cluster : 1;  // a compile-time 1 for the one-CTA kernel
+  const int crank = CLUSTERED ? (int)cg::this_cluster().block_rank() : 0;
   const int cta = (int)blockIdx.x / CL;
   const int rep = P.cta_rep ? P.cta_rep[cta] : cta;
   const Replica &R = P.reps[rep];
   ReplicaStats &Sg = P.stats[rep];
   constexpr int NW = THREADS / 32;
-  __shared__ long long s_part[8][16];  // per-rank pass totals, gathered in rank 0
+  __shared__ long long s_part[CLUSTERED ? 8 : 1][16];  // per-rank pass totals, gathered in rank 0
   const int tid = threadIdx.x, nth = THREADS;
   Geo G;
   G.L0 = R.L[0];
@@ -1432,7 +1433,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
   const SiteIndex site_of(n_uc, G.L0, G.L1);
   // bulk (TMA) copies when the replica's occupations are 16-byte aligned,
   // byte loads otherwise
-  const bool vec16 = CL == 1 && ((R.occ_offset | n_sites) & 15) == 0;
+  const bool vec16 = !CLUSTERED && ((R.occ_offset | n_sites) & 15) == 0;
   uint8_t *stg = smem + lay.clist;
   const int stg_cap = ((lay.bar - lay.clist) / 16) * 16;
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem + lay.bar);
@@ -1469,7 +1470,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
   const int lane = tid & 31, warp = tid >> 5;
   // an accepted change reaches every copy of the replica
   auto put_all = [&](int b, int x, int y, int z, int8_t v) {
-    if (CL == 1) {
+    if constexpr (!CLUSTERED) {
       put_site(occ, G, b, x, y, z, v);
     } else {
       cg::cluster_group cluster = cg::this_cluster();
@@ -1477,7 +1478,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
     }
   };
   auto sub_barrier = [&]() {
-    if (CL == 1) __syncthreads();
+    if constexpr (!CLUSTERED) __syncthreads();
     else cg::this_cluster().sync();
   };
   if constexpr (EXACT) {
@@ -1701,7 +1702,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
         // the previous phase B: it reads only its own class's sites, which
         // that phase B does not write.
         const PairGeom pg(D, ax_coord);
-        const int buf = sub & 1, chunk = CL == 1 ? D.chunk : (D.n + CL * NW - 1) / (CL * NW);
+        const int buf = sub & 1, chunk = !CLUSTERED ? D.chunk : (D.n + CL * NW - 1) / (CL * NW);
         uint16_t *cl = clist + buf * clist_cap;
         int *wk = wkept + buf * 32;
         if (a_buf != buf) {
@@ -1820,7 +1821,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
             ++n_acc;
             // (a neighbour swap's first change is already in this copy; the
             // other copies receive it now)
-            if (!local || CL > 1) put_all(cb, xa, ya, za, (int8_t)ob);
+            if (!local || CLUSTERED) put_all(cb, xa, ya, za, (int8_t)ob);
             put_all(bb, xb, yb, zb, (int8_t)oa);
             eacc.add(acc, d, 0.0);
             if constexpr (PITCH > 0) {
@@ -1837,7 +1838,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
           if (Dn.mode == 1 &&
               (Dn.cb != D.cb || Dn.cxo != D.cxo || Dn.cyo != D.cyo || Dn.czo != D.czo)) {
             const PairGeom pn(Dn, ax_coord);
-            const int chunk_n = CL == 1 ? Dn.chunk : (Dn.n + CL * NW - 1) / (CL * NW);
+            const int chunk_n = !CLUSTERED ? Dn.chunk : (Dn.n + CL * NW - 1) / (CL * NW);
             compact_pairs(pn, G, occ, Dn.n, chunk_n, warp, crank * NW + warp, lane,
                           clist + (buf ^ 1) * clist_cap, wkept + (buf ^ 1) * 32);
             a_buf = buf ^ 1;
@@ -1892,7 +1893,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
         if (lane == 16)
           for (int w = 0; w < NW; ++w) dv += rd_d[w];
       }
-      if (CL > 1) {
+      if constexpr (CLUSTERED) {
         // a cluster's pass totals (binary: integers only) gather in rank 0
         cg::cluster_group cluster = cg::this_cluster();
         if (warp == 0 && lane < 16) *cluster.map_shared_rank(&s_part[crank][lane], 0) = v;
@@ -1909,7 +1910,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
         double dtot = __shfl_sync(0xffffffffu, dv, 16);
         if (lane == 0) {
           s_stop = stop_seen;
-          if (CL > 1) {  // every rank leaves at the same pass boundary
+          if constexpr (CLUSTERED) {  // every rank leaves at the same pass boundary
             cg::cluster_group cluster = cg::this_cluster();
             for (int r = 1; r < CL; ++r) *cluster.map_shared_rank(&s_stop, r) = stop_seen;
           }
@@ -1958,10 +1959,10 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
           }
         }
       }
-      if (CL > 1) cg::this_cluster().sync();  // the stop decision reached every rank
+      if constexpr (CLUSTERED) cg::this_cluster().sync();  // the stop decision reached every rank
     }
   }
-  if (CL > 1) {
+  if constexpr (CLUSTERED) {
     cg::this_cluster().sync();  // no peer writes into this copy any more
     if (crank != 0) return;     // rank 0 writes the replica and its statistics back
   }
@@ -2041,28 +2042,32 @@ cudaError_t launch_replay_t(const CeTables &T, const ReplayParams &P, cudaStream
 template <int NOCC, int PITCH, int THREADS = SWEEP_THREADS>
 cudaError_t launch_sweep_t(const CeTables &T, const SweepParams &P, int n_replicas, int smem,
                            cudaStream_t st) {
+  if constexpr (PITCH > 0 && THREADS == SWEEP_THREADS) {
+    if (P.cluster > 1) {
+      // one thread-block cluster of P.cluster CTAs per replica
+      cudaError_t e = cudaFuncSetAttribute(k_sweep<NOCC, PITCH, THREADS, true>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+      if (e != cudaSuccess) return e;
+      cudaLaunchConfig_t cfg{};
+      cfg.gridDim = dim3((unsigned)(n_replicas * P.cluster));
+      cfg.blockDim = dim3(THREADS);
+      cfg.dynamicSmemBytes = (size_t)smem;
+      cfg.stream = st;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = (unsigned)P.cluster;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      return cudaLaunchKernelEx(&cfg, k_sweep<NOCC, PITCH, THREADS, true>, T, P);
+    }
+  }
   cudaError_t e = cudaFuncSetAttribute(k_sweep<NOCC, PITCH, THREADS>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  const int cl = (PITCH > 0 && P.cluster > 1) ? P.cluster : 1;
-  if (cl == 1) {
-    k_sweep<NOCC, PITCH, THREADS><<<n_replicas, THREADS, smem, st>>>(T, P);
-    return cudaGetLastError();
-  }
-  // one thread-block cluster of cl CTAs per replica
-  cudaLaunchConfig_t cfg{};
-  cfg.gridDim = dim3((unsigned)(n_replicas * cl));
-  cfg.blockDim = dim3(THREADS);
-  cfg.dynamicSmemBytes = (size_t)smem;
-  cfg.stream = st;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = (unsigned)cl;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_sweep<NOCC, PITCH, THREADS>, T, P);
+  k_sweep<NOCC, PITCH, THREADS><<<n_replicas, THREADS, smem, st>>>(T, P);
+  return cudaGetLastError();
 }
 
 #define CEM_INSTANTIATE(N)                                                                     \
