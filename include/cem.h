@@ -32,7 +32,7 @@ extern "C" {
 #define CEM_OK 0
 #define CEM_ERR_INVALID 1     /* bad argument or inconsistent input */
 #define CEM_ERR_CUDA 2        /* CUDA runtime error (message says which) */
-#define CEM_ERR_UNSUPPORTED 3 /* valid input outside this build's limits */
+#define CEM_ERR_UNSUPPORTED 3 /* valid input outside the library's limits */
 #define CEM_ERR_DEVICE 4      /* a kernel reported an error status */
 #define CEM_STOPPED 5         /* cem_synchronize: the run was stopped early by
                                  cem_request_stop (not an error: the state is

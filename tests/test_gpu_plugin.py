@@ -146,7 +146,7 @@ def test_plugin_rejects_what_the_reference_rejects(plugin):
     calc.check(calc.set_state(np.diag((8, 8, 8)), occ, 500.0))
     rc, *_ = calc.run(occ.size, -1, 100, 0, 50, 0.0)
     assert rc == -1 and "engine" in lib.cem_plugin_last_error().decode()
-    # non-diagonal supercells are outside this build's limits
+    # non-diagonal supercells are outside the library's limits
     T = np.array([[8, 1, 0], [0, 8, 0], [0, 0, 8]])
     assert calc.set_state(T, occ, 500.0) == -1
     assert "non-diagonal" in lib.cem_plugin_last_error().decode()
