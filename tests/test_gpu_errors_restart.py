@@ -108,28 +108,32 @@ def test_zero_temperature_accepts_only_downhill(cm, oracle_mod):
     assert np.all(got["dE"][got["accept"] == 1] < 0)
 
 
-@pytest.mark.parametrize("kernel", ["sweep", "group"])
+@pytest.mark.parametrize("kernel", ["sweep", "sweep_cluster", "group"])
 def test_host_stop_request_ends_a_long_run_at_a_pass_boundary(kernel, cm):
     """A run of a million passes, stopped from the host after a fraction of a
     second: cem_synchronize reports CEM_STOPPED, the replicas hold a
     consistent state (running energy equals a fresh recompute, composition
-    conserved), and the next run starts normally."""
+    conserved), and the next run starts normally. sweep_cluster: each replica
+    on a cluster of 4 CTAs (rank 0 broadcasts the stop decision)."""
     import time
 
     ce = workloads.fcc_binary_ce(0)
-    L = (12, 12, 12)
+    edge = 24 if kernel == "sweep_cluster" else 12
+    L = (edge, edge, edge)
     n = 4
     sysd = cm.System(ce)
     b = cm.ReplicaBatch(sysd, "canonical", [L] * n)
+    if kernel == "sweep_cluster":
+        b.set_option("sweep_cluster", 4)
     rng = np.random.default_rng(8)
-    occ0 = [workloads.fixed_composition(rng, 12 ** 3, 0.4) for _ in range(n)]
+    occ0 = [workloads.fixed_composition(rng, edge ** 3, 0.4) for _ in range(n)]
     for i in range(n):
         b.set_conditions(i, 700.0)
         b.set_seed(i, 31 + i)
         b.set_occupation(i, occ0[i])
     big = 1_000_000
     t0 = time.perf_counter()
-    if kernel == "sweep":
+    if kernel != "group":
         b.run(big, 0)
     else:
         b.learned_group_run(None, big, 0, weights="uniform", rounds=8, local_substeps=2)
@@ -145,7 +149,7 @@ def test_host_stop_request_ends_a_long_run_at_a_pass_boundary(kernel, cm):
         assert b.get_occupation(i).sum() == occ0[i].sum()
     # the flag is cleared by the next run
     p0 = b.stats(0)["passes"]
-    if kernel == "sweep":
+    if kernel != "group":
         b.run(5, 0)
     else:
         b.learned_group_run(None, 5, 0, weights="uniform", rounds=8, local_substeps=2)
