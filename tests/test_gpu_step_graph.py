@@ -19,10 +19,14 @@ def cm():
     return calculator
 
 
-@pytest.mark.parametrize("kind", ["fcc_canonical", "bcc_sgc"])
+@pytest.mark.parametrize("kind", ["fcc_canonical", "bcc_sgc", "fcc_cluster"])
 def test_step_graph_matches_separate_calls(kind, cm):
+    """fcc_cluster: the step graph launches the sweep on clusters of 4 CTAs
+    per replica, the separate calls on one CTA per replica."""
     if kind == "fcc_canonical":
         ce, ens, Ls, mu = workloads.fcc_binary_ce(3), "canonical", [(8, 8, 8), (12, 12, 12)], None
+    elif kind == "fcc_cluster":
+        ce, ens, Ls, mu = workloads.fcc_binary_ce(3), "canonical", [(48, 48, 48)] * 2, None
     else:
         ce, ens, Ls, mu = workloads.bcc_ternary_ce(3), "semigrand_canonical", [(6, 6, 6), (7, 7, 7)], \
             np.array([0.05, -0.02])
@@ -39,12 +43,16 @@ def test_step_graph_matches_separate_calls(kind, cm):
         return b
 
     a = batch()
+    if kind == "fcc_cluster":
+        a.set_option("sweep_cluster", 4)
     h = a.pinned_buffer()
     h[:] = occ
     for _ in range(3):
         a.step_async(h, h, 2)
     a.synchronize()
     b = batch()
+    if kind == "fcc_cluster":
+        b.set_option("sweep_cluster", 1)
     cur = occ.copy()
     for _ in range(3):
         b.set_occupation_all(cur)
