@@ -61,12 +61,14 @@ def jackknife_chains(estimator, chains) -> tuple:
 
 
 def family_2sigma(z, alpha: float = 0.01) -> tuple:
-    """Two-sigma test of a family of m independent z-scores at family-wise
-    level ``alpha``: each comparison is judged at |z| <= 2; the family passes
-    when at most k of them exceed 2, k the smallest count that exact sampling
-    exceeds with probability below alpha (binomial, p = P(|Z| > 2) = 0.0455),
-    and no |z| exceeds the Bonferroni bound z(1 - alpha / (2 m)).
-    Returns (passed, k, bonferroni_bound, n_beyond_2sigma)."""
+    """Two-sigma test of a family of m independent z-scores: each comparison
+    is judged at |z| <= 2; the family passes when at most k of them exceed 2,
+    k the smallest count that exact sampling exceeds with probability below
+    alpha (binomial, p = P(|Z| > 2) = 0.0455), and no |z| exceeds the
+    Bonferroni bound z(1 - alpha / (2 m)). Each condition alone falsely fails
+    with probability below alpha, so the family's false-alarm level is below
+    2 alpha (for alpha = 0.01 and 2 to 18 comparisons: 1.1-1.8 % by
+    simulation). Returns (passed, k, bonferroni_bound, n_beyond_2sigma)."""
     from scipy import stats as st
 
     z = np.abs(np.asarray(z, dtype=np.float64)).ravel()

@@ -1,6 +1,6 @@
 """Checks shared by the statistical GPU tests: chain-length guard and the
 2-sigma comparison of pooled independent chains (jackknife errors, 1 %
-family-wise level; contract stated in tests/test_gpu_equilibrium.py)."""
+family-wise contract stated in tests/test_gpu_equilibrium.py)."""
 
 import numpy as np
 

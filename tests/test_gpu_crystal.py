@@ -201,7 +201,7 @@ def test_zro_equilibrium_matches_oracle(ens, walk, ce, cm, oracle_mod):
     2500 K: <E> and C, and semi-grand canonical also <x>, chi and the
     thermo-chemical chi. Independent chains on each side (GPU 16, oracle 16),
     pooled, jackknife errors, >= 50 tau_int per chain, 2 sigma per comparison
-    at a 1 % family-wise level (tests/test_gpu_equilibrium.py)."""
+    under the family-wise contract (tests/test_gpu_equilibrium.py)."""
     T, mu = 2500.0, np.array([-0.6])
     sgc = ens == "semigrand_canonical"
     o = oracle_mod.OracleSystem(ce, L)

@@ -21,7 +21,8 @@ Criterion: each comparison |GPU - oracle| is judged at 2 combined standard
 errors. A test of m comparisons passes when at most k exceed 2 sigma, k the
 smallest count that correct sampling exceeds with probability below 1 %
 (binomial, p = 0.0455 per comparison), and none exceeds the Bonferroni bound
-z(1 - 0.01 / (2m)); i.e. the family-wise false-alarm level is 1 %.
+z(1 - 0.01 / (2m)). Each condition alone falsely fails with probability
+below 1 %, together below 2 % (1.1-1.8 % by simulation for 2-18 comparisons).
 """
 
 import os

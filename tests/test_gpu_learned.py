@@ -84,7 +84,7 @@ def test_learned_sampler_equilibrium_matches_oracle(T, cm, oracle_mod):
     L1_2-ordered initial states, where the trained weights are far from
     uniform). <E> and C of pooled independent chains (GPU 16, oracle 16),
     jackknife errors, >= 50 tau_int per chain, 2 sigma per comparison at a
-    1 % family-wise level (tests/test_gpu_equilibrium.py)."""
+    family-wise contract (tests/test_gpu_equilibrium.py)."""
     from tests.stat_checks import compare
 
     L, nrep = 10, 16
@@ -193,8 +193,8 @@ def test_learned_group_sweep_equilibrium_matches_oracle(T, cm, oracle_mod):
     sequential chain (uniform global swaps), 12^3 cells, x_B = 0.25, at 900 K
     (disordered; random initial states) and 90 K (0.9 T_c of this expansion,
     L1_2-ordered; ordered initial states). Pooled chains, jackknife errors,
-    >= 50 tau_int per chain, 2 sigma per comparison at a 1 % family-wise
-    level (tests/test_gpu_equilibrium.py)."""
+    >= 50 tau_int per chain, 2 sigma per comparison under the family-wise
+    contract (tests/test_gpu_equilibrium.py)."""
     from casmcode_clexmonte_gb300.stats import family_2sigma, jackknife_chains
     from tests.stat_checks import check_chain_lengths as _check_chain_lengths
 

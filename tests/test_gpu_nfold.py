@@ -97,7 +97,8 @@ def test_nfold_agrees_with_metropolis_sweep(cm):
     """Residence-weighted n-fold averages reproduce the parallel Metropolis
     sweep's <x> and <E>: 16 independent replicas per sampler (each replica's
     run average one independent sample, standard errors from the replica
-    spread), 2 sigma per comparison at a 1 % family-wise level."""
+    spread), 2 sigma per comparison under the family-wise contract of
+    tests/test_gpu_equilibrium.py."""
     from casmcode_clexmonte_gb300.stats import family_2sigma
 
     ce = workloads.fcc_binary_ce(7)
