@@ -50,7 +50,7 @@ class Stats(C.Structure):
 # every entry point of include/cem.h
 EXPORTS = [
     "cem_last_error", "cem_device_info", "cem_system_create", "cem_system_destroy",
-    "cem_replicas_create", "cem_replicas_destroy", "cem_n_sites", "cem_set_conditions",
+    "cem_replicas_create", "cem_replicas_create_supercells", "cem_supercell_hnf", "cem_replicas_destroy", "cem_n_sites", "cem_set_conditions",
     "cem_set_seed", "cem_set_occupation", "cem_get_occupation", "cem_set_occupation_all",
     "cem_get_occupation_all", "cem_host_alloc", "cem_host_free", "cem_energy",
     "cem_delta_energy", "cem_replay", "cem_enforce_composition", "cem_nfold_run", "cem_run", "cem_get_stats", "cem_get_samples",
@@ -84,6 +84,8 @@ def load(path: str = LIB):
     L.cem_system_create.argtypes = [C.POINTER(SystemDesc), C.POINTER(P)]
     L.cem_system_destroy.argtypes = [P]
     L.cem_replicas_create.argtypes = [P, C.c_int, _ip, C.c_int, C.POINTER(P)]
+    L.cem_replicas_create_supercells.argtypes = [P, C.c_int, vp, C.c_int, C.POINTER(P)]
+    L.cem_supercell_hnf.argtypes = [vp, vp]
     L.cem_replicas_destroy.argtypes = [P]
     L.cem_n_sites.argtypes = [P, C.c_int, C.POINTER(C.c_int64)]
     L.cem_set_conditions.argtypes = [P, C.c_int, C.c_double, _dp]

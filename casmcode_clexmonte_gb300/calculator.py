@@ -64,18 +64,38 @@ class ReplicaBatch:
     """Replicas of one ensemble resident on the GPU (occupations in HBM)."""
 
     def __init__(self, system: System, ensemble: str, L):
+        """``L``: per replica, the three edge lengths of a diagonal supercell
+        or a 3 x 3 ``transformation_matrix_to_super`` (columns = supercell
+        lattice vectors in prim cell coordinates). Non-diagonal supercells
+        number their unit cells on the matrix's lower-triangular Hermite normal
+        form H (cell i + H00 (j + H11 k)) and support the exact paths (energy,
+        delta, replay, enforce_composition, state transfer) only."""
         self.system = system
         self.lib = system.lib
         self.ensemble = ensemble
-        self.L = [tuple(int(x) for x in l) for l in L]
-        Ls = np.ascontiguousarray(np.array(self.L, dtype=np.int32).reshape(-1))
         h = C.c_void_p()
-        check(self.lib.cem_replicas_create(system.handle, len(self.L), _lib.iptr(Ls),
-                                           METHODS[ensemble], C.byref(h)))
+        if any(np.ndim(l) == 2 for l in L):
+            self.L = [tuple(tuple(int(x) for x in row) for row in np.asarray(l))
+                      if np.ndim(l) == 2 else tuple(int(x) for x in l) for l in L]
+            T = np.zeros((len(L), 3, 3), dtype=np.int64)
+            for r, l in enumerate(self.L):
+                T[r] = np.asarray(l) if np.ndim(l) == 2 else np.diag(l)
+            T = np.ascontiguousarray(T.reshape(-1))
+            check(self.lib.cem_replicas_create_supercells(system.handle, len(self.L), ptr(T),
+                                                          METHODS[ensemble], C.byref(h)))
+        else:
+            self.L = [tuple(int(x) for x in l) for l in L]
+            Ls = np.ascontiguousarray(np.array(self.L, dtype=np.int32).reshape(-1))
+            check(self.lib.cem_replicas_create(system.handle, len(self.L), _lib.iptr(Ls),
+                                               METHODS[ensemble], C.byref(h)))
         self.handle = h
         self.n = len(self.L)
-        nb = system.ce.prim.n_basis
-        self.n_sites = np.array([nb * l[0] * l[1] * l[2] for l in self.L], dtype=np.int64)
+        ns = C.c_int64()
+        sizes = []
+        for i in range(self.n):
+            check(self.lib.cem_n_sites(h, i, C.byref(ns)))
+            sizes.append(ns.value)
+        self.n_sites = np.array(sizes, dtype=np.int64)
         self.offsets = np.concatenate([[0], np.cumsum(self.n_sites)])
 
     def __del__(self):

@@ -150,6 +150,8 @@ struct cem_replicas {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;
+  // some replica is a non-diagonal supercell (exact paths only)
+  bool twisted = false;
   // HBM-streamed batches (supercells too large for shared memory)
   bool streamed = false;
   int stream_pitch = 0;
@@ -417,6 +419,200 @@ void set_dmu(const cem_system &s, Replica &R) {
     }
 }
 
+// Lower-triangular Hermite normal form H = T U (U unimodular) of a supercell
+// matrix T whose columns are the supercell lattice vectors in prim cell
+// coordinates (row-major T[3 r + c]): H[r][r] > 0, 0 <= H[r][c] < H[r][r] for
+// c < r, H[r][c] = 0 for c > r. Column operations only (Euclid's algorithm
+// along each row, then reduction below the diagonal), so H generates the same
+// superlattice.
+std::array<long long, 9> hermite_lower(const int64_t *T) {
+  long long h[3][3];
+  for (int a = 0; a < 3; ++a)
+    for (int c = 0; c < 3; ++c) {
+      require(T[3 * a + c] > -(1 << 20) && T[3 * a + c] < (1 << 20),
+              "supercell matrix entry out of range", CEM_ERR_UNSUPPORTED);
+      h[a][c] = T[3 * a + c];
+    }
+  auto col_sub = [&](int dst, int src, long long q) {
+    for (int a = 0; a < 3; ++a) h[a][dst] -= q * h[a][src];
+  };
+  for (int a = 0; a < 3; ++a) {
+    for (int c = a + 1; c < 3; ++c)
+      while (h[a][c] != 0) {
+        col_sub(a, c, h[a][a] / h[a][c]);
+        for (int k = 0; k < 3; ++k) std::swap(h[k][a], h[k][c]);
+      }
+    require(h[a][a] != 0, "singular supercell matrix");
+    if (h[a][a] < 0)
+      for (int k = 0; k < 3; ++k) h[k][a] = -h[k][a];
+  }
+  auto fl = [](long long x, long long m) { return x >= 0 ? x / m : -((m - 1 - x) / m); };
+  col_sub(0, 1, fl(h[1][0], h[1][1]));
+  col_sub(0, 2, fl(h[2][0], h[2][2]));
+  col_sub(1, 2, fl(h[2][1], h[2][2]));
+  std::array<long long, 9> H;
+  for (int a = 0; a < 3; ++a)
+    for (int c = 0; c < 3; ++c) H[3 * a + c] = h[a][c];
+  return H;
+}
+
+// The parallel kernels (sweeps, n-fold way, learned proposals, streamed
+// batches) keep each replica as an axis-aligned periodic box with a halo and
+// colour classes along the three axes; non-diagonal supercells run on the
+// exact paths only.
+void require_box(const cem_replicas *r) {
+  require(!r->twisted,
+          "non-diagonal supercells support energies, energy changes, the sequential replay, "
+          "composition enforcement and state transfer; parallel runs need diagonal supercells",
+          CEM_ERR_UNSUPPORTED);
+}
+
+// L[3 i ..] diagonal of replica i's Hermite normal form, tw[3 i ..] its
+// entries below the diagonal (null: diagonal supercells).
+void create_replicas(const cem_system *sys, int n, const int *L, const int *tw, int ensemble,
+                     cem_replicas **out) {
+  {
+    require(sys && L && out, "null argument");
+    *out = nullptr;
+    require(n >= 1, "need at least one replica");
+    require(ensemble == CEM_CANONICAL || ensemble == CEM_SEMIGRAND_CANONICAL, "bad ensemble");
+    require(ensemble != CEM_CANONICAL || sys->swaps_connect,
+            "the local-swap displacements do not connect every site (their graph over the "
+            "sublattices must be connected and its cycle translations generate the lattice): "
+            "the canonical chain would not be ergodic");
+    auto r = std::make_unique<cem_replicas>();
+    r->sys = sys;
+    r->n = n;
+    r->ensemble = ensemble;
+    CUDA_OK(cudaGetDevice(&r->device));
+    r->reps.resize(n);
+    std::map<std::vector<int>, int> pcache;
+    int64_t off = 0;
+    int max_cls = 1;
+    for (int i = 0; i < n; ++i) {
+      Replica &R = r->reps[i];
+      std::memset(&R, 0, sizeof(R));
+      const bool twist = tw && (tw[3 * i] || tw[3 * i + 1] || tw[3 * i + 2]);
+      for (int a = 0; a < 3; ++a) {
+        R.L[a] = L[3 * i + a];
+        R.tw[a] = twist ? tw[3 * i + a] : 0;
+        if (twist) continue;
+        require(R.L[a] >= 1 && R.L[a] <= MAX_L, "supercell dimension out of range",
+                CEM_ERR_UNSUPPORTED);
+        require(R.L[a] >= 2 * sys->T.reach + 1,
+                "supercell too small for the cluster expansion's reach");
+      }
+      if (twist) {
+        // no lattice vector of the supercell may join two sites of one
+        // cluster: none within 2 reach of the origin along every axis
+        const int64_t n_uc = (int64_t)R.L[0] * R.L[1] * R.L[2];
+        require(R.L[0] >= 1 && R.L[1] >= 1 && R.L[2] >= 1 &&
+                    n_uc * sys->T.n_sublat <= (int64_t)1 << 28,
+                "supercell dimension out of range", CEM_ERR_UNSUPPORTED);
+        require(R.tw[0] >= 0 && R.tw[0] < R.L[1] && R.tw[1] >= 0 && R.tw[1] < R.L[2] &&
+                    R.tw[2] >= 0 && R.tw[2] < R.L[2],
+                "supercell not in Hermite normal form");
+        // no cluster may hold two periodic images of one site: every cluster
+        // is some site's flower cluster, whose sites are the centre (b, 0) and
+        // the partners (pb, du); two of them on one sublattice are images when
+        // their cell offsets differ by a supercell lattice vector
+        const Cells C = R.cells();
+        for (int b = 0; b < sys->T.n_sublat; ++b)
+          for (int c = sys->T.fl_begin[b][0]; c < sys->T.fl_begin[b][sys->T.n_orbits]; ++c) {
+            int sb[4] = {b, -1, -1, -1}, su[4][3] = {{0, 0, 0}};
+            for (int q = 0; q < 3; ++q) {
+              sb[q + 1] = sys->fl_pb[c * 3 + q];
+              for (int a = 0; a < 3; ++a) su[q + 1][a] = sys->fl_du[c * 9 + q * 3 + a];
+            }
+            for (int q1 = 0; q1 < 4; ++q1)
+              for (int q2 = q1 + 1; q2 < 4; ++q2)
+                require(sb[q1] < 0 || sb[q1] != sb[q2] ||
+                            C.index(su[q1][0] - su[q2][0], su[q1][1] - su[q2][1],
+                                    su[q1][2] - su[q2][2]) != 0,
+                        "supercell too small: a cluster contains one site twice");
+          }
+        r->twisted = true;
+      }
+      R.n_sites = R.L[0] * R.L[1] * R.L[2] * sys->T.n_sublat;
+      R.ensemble = ensemble;
+      R.occ_offset = off;
+      off += R.n_sites;
+      int cls = sys->T.n_sublat;
+      if (!twist) {
+        std::vector<int> key{R.L[0], R.L[1], R.L[2]};
+        auto it = pcache.find(key);
+        int p = (it != pcache.end()) ? it->second
+                                     : (pcache[key] = choose_colouring(*sys, R.L, ensemble));
+        R.p = p;
+        for (int a = 0; a < 3; ++a) {
+          auto col = axis_blocks(R.L[a], p);
+          R.n_col[a] = *std::max_element(col.begin(), col.end()) + 1;
+          cls *= R.n_col[a];
+        }
+      } else {
+        for (int a = 0; a < 3; ++a) R.n_col[a] = 1;
+      }
+      max_cls = std::max(max_cls, cls);
+      R.temperature = 1000.0;
+      R.beta = 1.0 / (KB * R.temperature);
+      R.beta_f = (float)R.beta;
+      R.seed = 0x9E3779B97F4A7C15ull * (uint64_t)(i + 1);
+      set_dmu(*sys, R);
+    }
+    r->total_sites = off;
+    r->max_classes = max_cls;
+    int dev = 0, maxsm = 0;
+    CUDA_OK(cudaGetDevice(&dev));
+    CUDA_OK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    int need = 0;
+    for (int i = 0; i < n; ++i)
+      need = std::max({need, r->reps[i].L[0] + 2 * sys->T.reach, r->reps[i].L[1] + 2 * sys->T.reach});
+    int pitch = 0;
+    if (sys->fcc_generated) {
+      // exact fit L + 2 reach when every replica has it, else the smallest that holds all
+      bool same = true;
+      for (int i = 0; i < n; ++i)
+        same = same && r->reps[i].L[0] + 2 * sys->T.reach == need &&
+               r->reps[i].L[1] + 2 * sys->T.reach == need;
+      for (int cand : SWEEP_PITCHES) {
+        if (cand < need) continue;
+        if (same && cand != need && cand != 64) continue;
+        pitch = cand;
+        break;
+      }
+    }
+    if (pitch && batch_smem(r.get(), pitch) > maxsm) pitch = 0;  // generated layout does not fit
+    if (sys->big) pitch = sys->coop ? -2 : -1;  // one warp per site / one orbit at a time
+    if (r->twisted) pitch = 0;
+    r->pitch = pitch;
+    r->sweep_smem = r->twisted ? 0 : batch_smem(r.get(), pitch);
+    if (!r->twisted && r->sweep_smem > maxsm && stream_pitch_for(*sys, r->reps)) {
+      r->streamed = true;
+      r->stream_pitch = stream_pitch_for(*sys, r->reps);
+    }
+    r->stats_host.assign(n, ReplicaStats{});
+    CUDA_OK(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking));
+    CUDA_OK(cudaEventCreate(&r->ev0));
+    CUDA_OK(cudaEventCreate(&r->ev1));
+    CUDA_OK(cudaMalloc(&r->d_reps, sizeof(Replica) * n));
+    CUDA_OK(cudaMalloc(&r->d_stats, sizeof(ReplicaStats) * n));
+    CUDA_OK(cudaMemset(r->d_stats, 0, sizeof(ReplicaStats) * n));
+    CUDA_OK(cudaMalloc(&r->d_occ, (size_t)off + 16));
+    CUDA_OK(cudaMemset(r->d_occ, 0, (size_t)off + 16));
+    CUDA_OK(cudaMalloc(&r->d_counts, sizeof(unsigned long long) * (MAX_FUNCS + 8)));
+    CUDA_OK(cudaMalloc(&r->d_result, sizeof(long long) * 4));
+    r->sample_width = sys->T.n_occ + 1;  // potential, (n_occ-1) compositions, order parameter
+    {
+      int *h = nullptr;
+      CUDA_OK(cudaHostAlloc(&h, sizeof(int), cudaHostAllocMapped));
+      *h = 0;
+      r->h_stop = h;
+      CUDA_OK(cudaHostGetDevicePointer(reinterpret_cast<void **>(&r->d_stop), h, 0));
+    }
+    *out = r.release();
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -663,105 +859,34 @@ int cem_system_destroy(cem_system *sys) {
 
 int cem_replicas_create(const cem_system *sys, int n, const int *L, int ensemble,
                         cem_replicas **out) {
+  return guard([&] { create_replicas(sys, n, L, nullptr, ensemble, out); });
+}
+
+int cem_supercell_hnf(const int64_t *T, int64_t *H) {
   return guard([&] {
-    require(sys && L && out, "null argument");
-    *out = nullptr;
-    require(n >= 1, "need at least one replica");
-    require(ensemble == CEM_CANONICAL || ensemble == CEM_SEMIGRAND_CANONICAL, "bad ensemble");
-    require(ensemble != CEM_CANONICAL || sys->swaps_connect,
-            "the local-swap displacements do not connect every site (their graph over the "
-            "sublattices must be connected and its cycle translations generate the lattice): "
-            "the canonical chain would not be ergodic");
-    auto r = std::make_unique<cem_replicas>();
-    r->sys = sys;
-    r->n = n;
-    r->ensemble = ensemble;
-    CUDA_OK(cudaGetDevice(&r->device));
-    r->reps.resize(n);
-    std::map<std::vector<int>, int> pcache;
-    int64_t off = 0;
-    int max_cls = 1;
+    require(T && H, "null argument");
+    const auto h = hermite_lower(T);
+    for (int a = 0; a < 9; ++a) H[a] = h[a];
+  });
+}
+
+int cem_replicas_create_supercells(const cem_system *sys, int n, const int64_t *T, int ensemble,
+                                   cem_replicas **out) {
+  return guard([&] {
+    require(T != nullptr && n >= 1, "null argument");
+    std::vector<int> L(3 * (size_t)n), tw(3 * (size_t)n);
     for (int i = 0; i < n; ++i) {
-      Replica &R = r->reps[i];
-      std::memset(&R, 0, sizeof(R));
-      for (int a = 0; a < 3; ++a) {
-        R.L[a] = L[3 * i + a];
-        require(R.L[a] >= 1 && R.L[a] <= MAX_L, "supercell dimension out of range",
-                CEM_ERR_UNSUPPORTED);
-        require(R.L[a] >= 2 * sys->T.reach + 1,
-                "supercell too small for the cluster expansion's reach");
-      }
-      R.n_sites = R.L[0] * R.L[1] * R.L[2] * sys->T.n_sublat;
-      R.ensemble = ensemble;
-      R.occ_offset = off;
-      off += R.n_sites;
-      std::vector<int> key{R.L[0], R.L[1], R.L[2]};
-      auto it = pcache.find(key);
-      int p = (it != pcache.end()) ? it->second : (pcache[key] = choose_colouring(*sys, R.L, ensemble));
-      R.p = p;
-      int cls = sys->T.n_sublat;
-      for (int a = 0; a < 3; ++a) {
-        auto col = axis_blocks(R.L[a], p);
-        R.n_col[a] = *std::max_element(col.begin(), col.end()) + 1;
-        cls *= R.n_col[a];
-      }
-      max_cls = std::max(max_cls, cls);
-      R.temperature = 1000.0;
-      R.beta = 1.0 / (KB * R.temperature);
-      R.beta_f = (float)R.beta;
-      R.seed = 0x9E3779B97F4A7C15ull * (uint64_t)(i + 1);
-      set_dmu(*sys, R);
+      const auto H = hermite_lower(T + 9 * (size_t)i);
+      for (int a = 0; a < 3; ++a)
+        require(H[4 * a] < (1 << 20), "supercell dimension out of range", CEM_ERR_UNSUPPORTED);
+      L[3 * i] = (int)H[0];
+      L[3 * i + 1] = (int)H[4];
+      L[3 * i + 2] = (int)H[8];
+      tw[3 * i] = (int)H[3];
+      tw[3 * i + 1] = (int)H[6];
+      tw[3 * i + 2] = (int)H[7];
     }
-    r->total_sites = off;
-    r->max_classes = max_cls;
-    int dev = 0, maxsm = 0;
-    CUDA_OK(cudaGetDevice(&dev));
-    CUDA_OK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    int need = 0;
-    for (int i = 0; i < n; ++i)
-      need = std::max({need, r->reps[i].L[0] + 2 * sys->T.reach, r->reps[i].L[1] + 2 * sys->T.reach});
-    int pitch = 0;
-    if (sys->fcc_generated) {
-      // exact fit L + 2 reach when every replica has it, else the smallest that holds all
-      bool same = true;
-      for (int i = 0; i < n; ++i)
-        same = same && r->reps[i].L[0] + 2 * sys->T.reach == need &&
-               r->reps[i].L[1] + 2 * sys->T.reach == need;
-      for (int cand : SWEEP_PITCHES) {
-        if (cand < need) continue;
-        if (same && cand != need && cand != 64) continue;
-        pitch = cand;
-        break;
-      }
-    }
-    if (pitch && batch_smem(r.get(), pitch) > maxsm) pitch = 0;  // generated layout does not fit
-    if (sys->big) pitch = sys->coop ? -2 : -1;  // one warp per site / one orbit at a time
-    r->pitch = pitch;
-    r->sweep_smem = batch_smem(r.get(), pitch);
-    if (r->sweep_smem > maxsm && stream_pitch_for(*sys, r->reps)) {
-      r->streamed = true;
-      r->stream_pitch = stream_pitch_for(*sys, r->reps);
-    }
-    r->stats_host.assign(n, ReplicaStats{});
-    CUDA_OK(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking));
-    CUDA_OK(cudaEventCreate(&r->ev0));
-    CUDA_OK(cudaEventCreate(&r->ev1));
-    CUDA_OK(cudaMalloc(&r->d_reps, sizeof(Replica) * n));
-    CUDA_OK(cudaMalloc(&r->d_stats, sizeof(ReplicaStats) * n));
-    CUDA_OK(cudaMemset(r->d_stats, 0, sizeof(ReplicaStats) * n));
-    CUDA_OK(cudaMalloc(&r->d_occ, (size_t)off + 16));
-    CUDA_OK(cudaMemset(r->d_occ, 0, (size_t)off + 16));
-    CUDA_OK(cudaMalloc(&r->d_counts, sizeof(unsigned long long) * (MAX_FUNCS + 8)));
-    CUDA_OK(cudaMalloc(&r->d_result, sizeof(long long) * 4));
-    r->sample_width = sys->T.n_occ + 1;  // potential, (n_occ-1) compositions, order parameter
-    {
-      int *h = nullptr;
-      CUDA_OK(cudaHostAlloc(&h, sizeof(int), cudaHostAllocMapped));
-      *h = 0;
-      r->h_stop = h;
-      CUDA_OK(cudaHostGetDevicePointer(reinterpret_cast<void **>(&r->d_stop), h, 0));
-    }
-    *out = r.release();
+    create_replicas(sys, n, L.data(), tw.data(), ensemble, out);
   });
 }
 
@@ -867,8 +992,7 @@ int cem_energy(cem_replicas *r, int i, double *energy, int64_t *counts) {
     check_rep(r, i);
     const Replica &R = r->reps[i];
     const CeTables &T = r->sys->T;
-    CUDA_OK(launch_energy(T, r->d_occ + R.occ_offset, R.L[0], R.L[1], R.L[2], r->d_counts,
-                          r->stream));
+    CUDA_OK(launch_energy(T, r->d_occ + R.occ_offset, R.cells(), r->d_counts, r->stream));
     std::vector<unsigned long long> c(T.n_funcs);
     CUDA_OK(cudaMemcpyAsync(c.data(), r->d_counts, sizeof(unsigned long long) * T.n_funcs,
                             cudaMemcpyDeviceToHost, r->stream));
@@ -922,8 +1046,8 @@ int cem_delta_energy(cem_replicas *r, int i, int n_events, int k, const int64_t 
         CUDA_OK(cudaMemcpyAsync(ddmu, R.dmu, 16 * 8, cudaMemcpyHostToDevice, r->stream));
       }
       if (dcount) CUDA_OK(cudaMalloc(&ddc, (size_t)n_events * T.n_funcs * 8));
-      CUDA_OK(launch_delta(T, r->d_occ + R.occ_offset, R.L[0], R.L[1], R.L[2], n_events, k, ds,
-                           dn, ddmu, dde, ddc, r->stream));
+      CUDA_OK(launch_delta(T, r->d_occ + R.occ_offset, R.cells(), n_events, k, ds, dn, ddmu, dde,
+                           ddc, r->stream));
       CUDA_OK(cudaMemcpyAsync(dE, dde, (size_t)n_events * 8, cudaMemcpyDeviceToHost, r->stream));
       if (dcount)
         CUDA_OK(cudaMemcpyAsync(dcount, ddc, (size_t)n_events * T.n_funcs * 8,
@@ -950,7 +1074,10 @@ int cem_replay(cem_replicas *r, int i, uint64_t mt_seed, int64_t n_steps, uint8_
     require(replay_smem_bytes(R.n_sites, T.n_occ) <= maxsm,
             "supercell too large for the sequential replay kernel", CEM_ERR_UNSUPPORTED);
     ReplayParams P{};
-    for (int a = 0; a < 3; ++a) P.L[a] = R.L[a];
+    for (int a = 0; a < 3; ++a) {
+      P.L[a] = R.L[a];
+      P.tw[a] = R.tw[a];
+    }
     P.n_sites = R.n_sites;
     P.ensemble = R.ensemble;
     P.beta = R.beta;
@@ -1051,6 +1178,7 @@ int cem_nfold_run(cem_replicas *r, int64_t n_events, int64_t n_equil, int64_t re
                   int64_t *rec_site, int32_t *rec_occ, double *rec_dt) {
   return guard([&] {
     require(r != nullptr, "null handle");
+    require_box(r);
     require(r->ensemble == CEM_SEMIGRAND_CANONICAL,
             "the n-fold way runs semi-grand canonical replicas");
     require(n_events >= 0 && n_equil >= 0 && record_capacity >= 0, "counts must be >= 0");
@@ -1197,6 +1325,7 @@ int cem_enforce_composition(cem_replicas *r, const double *target_mol, uint64_t 
 int cem_step_async(cem_replicas *r, const int8_t *host_in, int8_t *host_out, int64_t n_passes) {
   return guard([&] {
     require(r && host_in && host_out, "null argument");
+    require_box(r);
     require(n_passes >= 1, "n_passes must be >= 1");
     require(!r->streamed, "HBM-streamed batches run through cem_run", CEM_ERR_UNSUPPORTED);
     for (const void *p : {(const void *)host_in, (const void *)host_out}) {
@@ -1274,6 +1403,7 @@ int cem_step_async(cem_replicas *r, const int8_t *host_in, int8_t *host_out, int
 int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_samples) {
   return guard([&] {
     require(r != nullptr, "null handle");
+    require_box(r);
     require(n_passes >= 0 && n_equil >= 0, "pass counts must be >= 0");
     int dev = 0, maxsm = 0;
     CUDA_OK(cudaGetDevice(&dev));
@@ -1471,6 +1601,7 @@ int cem_smem_bandwidth(double *gbs) {
 int cem_autotune(cem_replicas *r, int64_t trial_passes, double *best_ms) {
   return guard([&] {
     require(r != nullptr, "null handle");
+    require_box(r);
     require(trial_passes > 0, "trial_passes must be > 0");
     if (best_ms) *best_ms = 0.0;
     if (r->streamed) return;  // one fixed graph per pass
@@ -1800,7 +1931,7 @@ extern "C" int cem_delta_energy_noalloc(cem_replicas *r, int i, int n_events, in
     if (potential)
       CUDA_OK(cudaMemcpyAsync(ddmu, R.dmu, 16 * 8, cudaMemcpyHostToDevice, r->stream));
     // every dE (and dcount) entry of the call is written by the kernel
-    CUDA_OK(launch_delta(T, r->d_occ + R.occ_offset, R.L[0], R.L[1], R.L[2], n_events, k, ds, dn,
+    CUDA_OK(launch_delta(T, r->d_occ + R.occ_offset, R.cells(), n_events, k, ds, dn,
                          potential ? ddmu : nullptr, dde, dcount ? ddc : nullptr, r->stream));
     CUDA_OK(cudaMemcpyAsync(dE, dde, (size_t)n_events * 8, cudaMemcpyDeviceToHost, r->stream));
     if (dcount)
@@ -2044,6 +2175,7 @@ static void require_learned(const cem_replicas *r) {
 int cem_learned_features(cem_replicas *r, int i, int8_t *features, float *targets) {
   return guard([&] {
     check_rep(r, i);
+    require_box(r);
     require(features && targets, "null argument");
     require(r->sys->fcc_generated && r->ensemble == CEM_CANONICAL,
             "the learned proposal supports canonical binary FCC systems of the generated topology",
@@ -2087,6 +2219,7 @@ int cem_learned_run(cem_replicas *r, const cem_mlp *m, int64_t n_passes, int64_t
                     int record_samples) {
   return guard([&] {
     require(r != nullptr, "null handle");
+    require_box(r);
     require(n_passes >= 0 && n_equil >= 0, "pass counts must be >= 0");
     require_learned(r);
     const int L = r->reps[0].L[0], n = r->reps[0].n_sites;
@@ -2130,6 +2263,7 @@ int cem_learned_group_run(cem_replicas *r, const cem_mlp *m, int weights, int ro
                           int record_samples) {
   return guard([&] {
     require(r != nullptr, "null handle");
+    require_box(r);
     require(n_passes >= 0 && n_equil >= 0, "pass counts must be >= 0");
     require(weights >= 0 && weights <= 2, "weights must be 0 (uniform), 1 (network) or 2 (exact)");
     require(weights != 1 || m != nullptr, "network weights need a network");

@@ -76,9 +76,38 @@ struct CeTables {
   // owned clusters use index n_fl + i in the cl_* arrays
 };
 
+// floor(x / n) for n > 0 (one division only for |x| beyond one period).
+CEM_HD int floor_div(int x, int n) {
+  if (x >= 0) return x < n ? 0 : x / n;
+  return x >= -n ? -1 : -((n - 1 - x) / n);
+}
+
+// Unit cells of a supercell in lower-triangular Hermite normal form: the
+// superlattice is generated by the columns (L0, t10, t20), (0, L1, t21) and
+// (0, 0, L2) in prim cell coordinates (0 <= t10 < L1, 0 <= t20, t21 < L2).
+// Cell (i, j, k) with 0 <= i < L0, 0 <= j < L1, 0 <= k < L2 has index
+// i + L0 (j + L1 k); any integer cell reduces along i first (shifting j and k
+// by the first column), then along j (shifting k), then along k. Diagonal
+// supercells have t = 0 and reduce axis by axis.
+struct Cells {
+  int L0, L1, L2, t10, t20, t21;
+  CEM_HD int index(int i, int j, int k) const {
+    int q = floor_div(i, L0);
+    i -= q * L0;
+    j -= q * t10;
+    k -= q * t20;
+    q = floor_div(j, L1);
+    j -= q * L1;
+    k -= q * t21;
+    k -= floor_div(k, L2) * L2;
+    return i + L0 * (j + L1 * k);
+  }
+};
+
 // Per-replica description (device memory array).
 struct Replica {
   int L[3];
+  int tw[3];  // Hermite normal form below the diagonal: t10, t20, t21 (0 if diagonal)
   int n_sites;
   int ensemble;           // 0 = semi-grand canonical flips, 1 = canonical swaps
   int64_t occ_offset;     // into the packed occupation buffer
@@ -92,6 +121,7 @@ struct Replica {
   // colouring: per axis block size >= p, colour of each coordinate
   int n_col[3];
   int p;
+  CEM_HD Cells cells() const { return Cells{L[0], L[1], L[2], tw[0], tw[1], tw[2]}; }
 };
 
 // Per-replica running results (device memory array).

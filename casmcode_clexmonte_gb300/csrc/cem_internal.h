@@ -16,6 +16,7 @@ constexpr int SWEEP_PITCHES[5] = {14, 28, 36, 52, 64};
 
 struct ReplayParams {
   int L[3];
+  int tw[3];                   // Hermite normal form below the diagonal (0: diagonal)
   int n_sites;
   int ensemble;
   double beta;
@@ -48,10 +49,9 @@ struct SweepParams {
   double RT[16];               // (n_occ-1) x n_occ
 };
 
-cudaError_t launch_energy(const CeTables &T, const int8_t *occ, int L0, int L1, int L2,
+cudaError_t launch_energy(const CeTables &T, const int8_t *occ, const Cells &C,
                           unsigned long long *counts, cudaStream_t st);
-cudaError_t launch_delta(const CeTables &T, const int8_t *occ, int L0, int L1, int L2,
-                         int n_events, int k_sites, const long long *sites, const int *new_occ,
+cudaError_t launch_delta(const CeTables &T, const int8_t *occ, const Cells &C, int n_events, int k_sites, const long long *sites, const int *new_occ,
                          const double *dmu, double *dE, long long *dcount, cudaStream_t st);
 int replay_smem_bytes(int n_sites, int n_occ);
 cudaError_t launch_replay(const CeTables &T, const ReplayParams &P, cudaStream_t st);

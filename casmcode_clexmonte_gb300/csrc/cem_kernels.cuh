@@ -180,11 +180,12 @@ __device__ __forceinline__ int wrapc(int x, int L) {
 // ------------------------------------------------------------ full energy
 template <int NOCC>
 __global__ void k_energy(const __grid_constant__ CeTables T, const int8_t *__restrict__ occ,
-                         int L0, int L1, int L2, unsigned long long *__restrict__ counts) {
+                         Cells C, unsigned long long *__restrict__ counts) {
   __shared__ int hist[MAX_FUNCS];
   for (int f = threadIdx.x; f < MAX_FUNCS; f += blockDim.x) hist[f] = 0;
   __syncthreads();
-  const int n_uc = L0 * L1 * L2;
+  const int L0 = C.L0, L1 = C.L1;
+  const int n_uc = L0 * L1 * C.L2;
   const int n = n_uc * T.n_sublat;
   for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < n; l += gridDim.x * blockDim.x) {
     const int b = l / n_uc, uc = l - b * n_uc;
@@ -200,8 +201,7 @@ __global__ void k_energy(const __grid_constant__ CeTables T, const int8_t *__res
         for (int q = 0; q < size - 1; ++q) {
           const int pb = T.cl_pb[cc * 3 + q];
           const int *du = T.cl_du + cc * 9 + q * 3;
-          const int site = pb * n_uc + wrapc(i + du[0], L0) +
-                           L0 * (wrapc(j + du[1], L1) + L1 * wrapc(k + du[2], L2));
+          const int site = pb * n_uc + C.index(i + du[0], j + du[1], k + du[2]);
           const int v = occ[site];
           ok = ok && (v != 0);
           code += (v - 1) * mul;
@@ -230,8 +230,9 @@ __global__ void k_init_stats(const __grid_constant__ CeTables T, const Replica *
   const Replica &R = reps[blockIdx.x];
   for (int f = threadIdx.x; f < MAX_FUNCS; f += blockDim.x) hist[f] = 0ull;
   if (threadIdx.x < 8) spec[threadIdx.x] = 0ull;
-  const int L0 = R.L[0], L1 = R.L[1], L2 = R.L[2];
-  const int n_uc = L0 * L1 * L2, n = n_uc * T.n_sublat;
+  const Cells C = R.cells();
+  const int L0 = C.L0, L1 = C.L1;
+  const int n_uc = L0 * L1 * C.L2, n = n_uc * T.n_sublat;
   const int8_t *gocc = occ_all + R.occ_offset;
   const bool staged = n <= smem_cap;
   if (staged)
@@ -255,8 +256,7 @@ __global__ void k_init_stats(const __grid_constant__ CeTables T, const Replica *
         for (int q = 0; q < size - 1; ++q) {
           const int pb = T.cl_pb[cc * 3 + q];
           const int *du = T.cl_du + cc * 9 + q * 3;
-          const int site = pb * n_uc + wrapc(i + du[0], L0) +
-                           L0 * (wrapc(j + du[1], L1) + L1 * wrapc(k + du[2], L2));
+          const int site = pb * n_uc + C.index(i + du[0], j + du[1], k + du[2]);
           const int v = occ[site];
           ok = ok && (v != 0);
           code += (v - 1) * mul;
@@ -287,13 +287,14 @@ __global__ void k_init_stats(const __grid_constant__ CeTables T, const Replica *
 // ------------------------------------------------------------ batched delta
 template <int NOCC>
 __global__ void k_delta(const __grid_constant__ CeTables T, const int8_t *__restrict__ occ,
-                        int L0, int L1, int L2, int n_events, int k_sites,
+                        Cells C, int n_events, int k_sites,
                         const long long *__restrict__ sites, const int *__restrict__ new_occ,
                         const double *__restrict__ dmu, double *__restrict__ dE,
                         long long *__restrict__ dcount) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n_events) return;
-  const int n_uc = L0 * L1 * L2;
+  const int L0 = C.L0, L1 = C.L1;
+  const int n_uc = L0 * L1 * C.L2;
   double mu_term = 0.0;
   // sequential semantics: site s sees the changes of sites 0 .. s-1
   int ov_site[4], ov_val[4], sb[4], si[4], sj[4], sk[4], soi[4], sof[4];
@@ -323,8 +324,7 @@ __global__ void k_delta(const __grid_constant__ CeTables T, const int8_t *__rest
       auto rd = [&](int c, int jj) -> int {
         const int pb = T.cl_pb[c * 3 + jj];
         const int *du = T.cl_du + c * 9 + jj * 3;
-        const int site = pb * n_uc + wrapc(i + du[0], L0) +
-                         L0 * (wrapc(j + du[1], L1) + L1 * wrapc(k + du[2], L2));
+        const int site = pb * n_uc + C.index(i + du[0], j + du[1], k + du[2]);
         int v = occ[site];
         for (int q = 0; q < s; ++q)
           if (ov_site[q] == site) v = ov_val[q];
@@ -407,8 +407,9 @@ __global__ void k_replay(const __grid_constant__ CeTables T, ReplayParams P) {
   __shared__ long long ev_site[2];
   __shared__ int ev_new[2], ev_n, ev_stop;
   const int lane = threadIdx.x;
-  const int L0 = P.L[0], L1 = P.L[1], L2 = P.L[2];
-  const int n_uc = L0 * L1 * L2;
+  const Cells C{P.L[0], P.L[1], P.L[2], P.tw[0], P.tw[1], P.tw[2]};
+  const int L0 = C.L0, L1 = C.L1;
+  const int n_uc = L0 * L1 * C.L2;
 
   for (int l = lane; l < N; l += 32) occ[l] = P.occ[l];
   __syncwarp();
@@ -516,8 +517,7 @@ __global__ void k_replay(const __grid_constant__ CeTables T, ReplayParams P) {
           for (int q = 0; q < size - 1; ++q) {
             const int pb = T.cl_pb[c * 3 + q];
             const int *du = T.cl_du + c * 9 + q * 3;
-            const int site = pb * n_uc + wrapc(i + du[0], L0) +
-                             L0 * (wrapc(j + du[1], L1) + L1 * wrapc(k + du[2], L2));
+            const int site = pb * n_uc + C.index(i + du[0], j + du[1], k + du[2]);
             const int v = occ[site];
             prod &= v;
             ok = ok && (v != 0);
@@ -1992,25 +1992,25 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
 
 // ------------------------------------------------------------ launchers
 template <int NOCC>
-cudaError_t launch_energy_t(const CeTables &T, const int8_t *occ, int L0, int L1, int L2,
+cudaError_t launch_energy_t(const CeTables &T, const int8_t *occ, const Cells &C,
                             unsigned long long *counts, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(unsigned long long) * T.n_funcs, st);
   if (e != cudaSuccess) return e;
-  const int n = L0 * L1 * L2 * T.n_sublat;
+  const int n = C.L0 * C.L1 * C.L2 * T.n_sublat;
   int grid = (n + 255) / 256;
   if (grid > 4096) grid = 4096;
-  k_energy<NOCC><<<grid, 256, 0, st>>>(T, occ, L0, L1, L2, counts);
+  k_energy<NOCC><<<grid, 256, 0, st>>>(T, occ, C, counts);
   return cudaGetLastError();
 }
 
 template <int NOCC>
-cudaError_t launch_delta_t(const CeTables &T, const int8_t *occ, int L0, int L1, int L2,
+cudaError_t launch_delta_t(const CeTables &T, const int8_t *occ, const Cells &C,
                            int n_events, int k_sites, const long long *sites, const int *new_occ,
                            const double *dmu, double *dE, long long *dcount, cudaStream_t st) {
   const int grid = (n_events + 127) / 128;
   if (grid == 0) return cudaSuccess;
-  k_delta<NOCC><<<grid, 128, 0, st>>>(T, occ, L0, L1, L2, n_events, k_sites, sites, new_occ, dmu,
-                                      dE, dcount);
+  k_delta<NOCC><<<grid, 128, 0, st>>>(T, occ, C, n_events, k_sites, sites, new_occ, dmu, dE,
+                                      dcount);
   return cudaGetLastError();
 }
 
@@ -2071,9 +2071,9 @@ cudaError_t launch_sweep_t(const CeTables &T, const SweepParams &P, int n_replic
 }
 
 #define CEM_INSTANTIATE(N)                                                                     \
-  template cudaError_t launch_energy_t<N>(const CeTables &, const int8_t *, int, int, int,     \
+  template cudaError_t launch_energy_t<N>(const CeTables &, const int8_t *, const Cells &,     \
                                           unsigned long long *, cudaStream_t);                 \
-  template cudaError_t launch_delta_t<N>(const CeTables &, const int8_t *, int, int, int, int, \
+  template cudaError_t launch_delta_t<N>(const CeTables &, const int8_t *, const Cells &, int, \
                                          int, const long long *, const int *, const double *,  \
                                          double *, long long *, cudaStream_t);                 \
   template cudaError_t launch_replay_t<N>(const CeTables &, const ReplayParams &, cudaStream_t); \

@@ -7,12 +7,13 @@ namespace cem {
 // cem_k3.cu, cem_kfcc.cu, cem_kfcc_b.cu); extern declarations keep this file
 // from compiling a second copy of every kernel.
 #define CEM_EXTERN(N)                                                                          \
-  extern template cudaError_t launch_energy_t<N>(const CeTables &, const int8_t *, int, int,   \
-                                                 int, unsigned long long *, cudaStream_t);     \
-  extern template cudaError_t launch_delta_t<N>(const CeTables &, const int8_t *, int, int,    \
-                                                int, int, int, const long long *, const int *, \
-                                                const double *, double *, long long *,         \
-                                                cudaStream_t);                                 \
+  extern template cudaError_t launch_energy_t<N>(const CeTables &, const int8_t *,             \
+                                                 const Cells &, unsigned long long *,          \
+                                                 cudaStream_t);                                \
+  extern template cudaError_t launch_delta_t<N>(const CeTables &, const int8_t *,              \
+                                                const Cells &, int, int, const long long *,    \
+                                                const int *, const double *, double *,         \
+                                                long long *, cudaStream_t);                    \
   extern template cudaError_t launch_replay_t<N>(const CeTables &, const ReplayParams &,       \
                                                  cudaStream_t);                                \
   extern template cudaError_t launch_init_stats_t<N>(const CeTables &, const Replica *,        \
@@ -53,22 +54,20 @@ extern template cudaError_t launch_sweep_t<2, -2, SWEEP_THREADS>(const CeTables 
                                                                  const SweepParams &, int, int,
                                                                  cudaStream_t);
 
-cudaError_t launch_energy(const CeTables &T, const int8_t *occ, int L0, int L1, int L2,
+cudaError_t launch_energy(const CeTables &T, const int8_t *occ, const Cells &C,
                           unsigned long long *counts, cudaStream_t st) {
-  if (T.n_occ == 2) return launch_energy_t<2>(T, occ, L0, L1, L2, counts, st);
-  if (T.n_occ == 3) return launch_energy_t<3>(T, occ, L0, L1, L2, counts, st);
+  if (T.n_occ == 2) return launch_energy_t<2>(T, occ, C, counts, st);
+  if (T.n_occ == 3) return launch_energy_t<3>(T, occ, C, counts, st);
   return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_delta(const CeTables &T, const int8_t *occ, int L0, int L1, int L2,
-                         int n_events, int k_sites, const long long *sites, const int *new_occ,
+cudaError_t launch_delta(const CeTables &T, const int8_t *occ, const Cells &C, int n_events,
+                         int k_sites, const long long *sites, const int *new_occ,
                          const double *dmu, double *dE, long long *dcount, cudaStream_t st) {
   if (T.n_occ == 2)
-    return launch_delta_t<2>(T, occ, L0, L1, L2, n_events, k_sites, sites, new_occ, dmu, dE,
-                             dcount, st);
+    return launch_delta_t<2>(T, occ, C, n_events, k_sites, sites, new_occ, dmu, dE, dcount, st);
   if (T.n_occ == 3)
-    return launch_delta_t<3>(T, occ, L0, L1, L2, n_events, k_sites, sites, new_occ, dmu, dE,
-                             dcount, st);
+    return launch_delta_t<3>(T, occ, C, n_events, k_sites, sites, new_occ, dmu, dE, dcount, st);
   return cudaErrorInvalidValue;
 }
 

@@ -134,6 +134,23 @@ int cem_system_destroy(cem_system *sys);
  * l = b*n_uc + i + L0*(j + L1*k) (canonical_metropolis_test.cpp:34-36). */
 int cem_replicas_create(const cem_system *sys, int n_replicas, const int *L, int ensemble,
                         cem_replicas **out);
+/* The same for general supercells: T[9r..9r+8] is replica r's integer
+ * transformation_matrix_to_super, row-major, columns = the supercell lattice
+ * vectors in prim cell coordinates (Configuration.hh:29-50). Unit cells are
+ * indexed on the matrix's lower-triangular Hermite normal form H (same
+ * superlattice): cell (i, j, k), 0 <= i < H00, 0 <= j < H11, 0 <= k < H22,
+ * has index i + H00*(j + H11*k); for a diagonal matrix with positive entries
+ * this is the order of cem_replicas_create. Non-diagonal supercells support
+ * energies, energy changes, the sequential replay, composition enforcement
+ * and state transfer; the parallel runs return CEM_ERR_UNSUPPORTED for them.
+ * A non-diagonal supercell in which some cluster holds two periodic images
+ * of one site is refused. */
+int cem_replicas_create_supercells(const cem_system *sys, int n_replicas, const int64_t *T,
+                                   int ensemble, cem_replicas **out);
+/* The lower-triangular Hermite normal form H (row-major) that
+ * cem_replicas_create_supercells indexes the supercell T on (no device
+ * needed). */
+int cem_supercell_hnf(const int64_t *T, int64_t *H);
 int cem_replicas_destroy(cem_replicas *r);
 int cem_n_sites(const cem_replicas *r, int replica, int64_t *n_sites);
 

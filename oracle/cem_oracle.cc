@@ -100,6 +100,9 @@ struct System {
   std::vector<Vec3> basis;
   double grid = 1.0;
   int L[3] = {1, 1, 1};
+  // supercell in lower-triangular Hermite normal form: lattice columns
+  // (L0, tw0, tw1), (0, L1, tw2), (0, 0, L2); zeros for a diagonal supercell
+  int tw[3] = {0, 0, 0};
   int n_uc = 1, n_sites = 1;
   int n_funcs = 1;
   std::vector<double> eci, coeff, mult, weight;  // weight = eci*coeff/mult
@@ -133,9 +136,20 @@ Vec3 cart(const System &s, int b, i64 u0, i64 u1, i64 u2) {
   return v;
 }
 
+// Cell (i, j, k) reduced into the Hermite-normal-form box: subtract the
+// first lattice column until 0 <= i < L0, then the second until
+// 0 <= j < L1, then the third; cells are numbered i + L0 (j + L1 k).
 inline int site_index(const System &s, int b, i64 i, i64 j, i64 k) {
-  auto m = [](i64 a, int n) { return (int)(((a % n) + n) % n); };
-  return b * s.n_uc + m(i, s.L[0]) + s.L[0] * (m(j, s.L[1]) + s.L[1] * m(k, s.L[2]));
+  auto fdiv = [](i64 a, i64 n) { return (a - (((a % n) + n) % n)) / n; };
+  i64 q = fdiv(i, s.L[0]);
+  i -= q * s.L[0];
+  j -= q * s.tw[0];
+  k -= q * s.tw[1];
+  q = fdiv(j, s.L[1]);
+  j -= q * s.L[1];
+  k -= q * s.tw[2];
+  k -= fdiv(k, s.L[2]) * s.L[2];
+  return b * s.n_uc + (int)(i + s.L[0] * (j + s.L[1] * k));
 }
 
 void finish_build(System &s, const std::vector<double> &orbit_count);
@@ -671,7 +685,7 @@ double event_delta(const System &s, std::vector<signed char> &occ, int n, const 
                    const int *new_occ, i64 *dcount) {
   thread_local std::vector<i64> d;
   d.assign(s.n_funcs, 0);
-  signed char saved[4];
+  std::vector<signed char> saved(n > 0 ? n : 0);
   for (int i = 0; i < n; ++i) {
     saved[i] = occ[sites[i]];
     site_delta_counts(s, occ.data(), (int)sites[i], new_occ[i], d.data());
@@ -779,9 +793,13 @@ const char *ora_last_error() { return g_err.c_str(); }
 void *ora_system_create(int n_basis, const i64 *lattice, const i64 *basis, double grid, int n_occ,
                         const double *max_length, int n_funcs, const int *func_size,
                         const i64 *func_pts, const int *func_occ, const double *eci,
-                        const double *coeff, const double *RT, int Lx, int Ly, int Lz) {
+                        const double *coeff, const double *RT, int Lx, int Ly, int Lz,
+                        int t10, int t20, int t21) {
   try {
     auto s = std::make_unique<System>();
+    s->tw[0] = t10;
+    s->tw[1] = t20;
+    s->tw[2] = t21;
     s->n_basis = n_basis;
     s->n_occ = n_occ;
     for (int r = 0; r < 3; ++r)
@@ -807,9 +825,13 @@ void *ora_system_create_xtal(int n_basis_all, const double *lattice, const doubl
                              const int *site_kind, const int *site_dof, int n_occ,
                              const double *max_length, int n_funcs, const int *func_size,
                              const i64 *func_sites, const int *func_occ, const double *eci,
-                             const double *coeff, const double *RT, int Lx, int Ly, int Lz) {
+                             const double *coeff, const double *RT, int Lx, int Ly, int Lz,
+                             int t10, int t20, int t21) {
   try {
     auto s = std::make_unique<System>();
+    s->tw[0] = t10;
+    s->tw[1] = t20;
+    s->tw[2] = t21;
     int nd = 0;
     for (int b = 0; b < n_basis_all; ++b) nd += site_dof[b] ? 1 : 0;
     s->n_basis = nd;

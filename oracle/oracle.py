@@ -51,12 +51,12 @@ def lib():
         L.ora_system_create.restype = P
         L.ora_system_create.argtypes = [
             C.c_int, i64p, i64p, C.c_double, C.c_int, f64p, C.c_int, i32p, i64p, i32p,
-            f64p, f64p, f64p, C.c_int, C.c_int, C.c_int,
+            f64p, f64p, f64p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
         ]
         L.ora_system_create_xtal.restype = P
         L.ora_system_create_xtal.argtypes = [
             C.c_int, f64p, f64p, i32p, i32p, C.c_int, f64p, C.c_int, i32p, i64p, i32p,
-            f64p, f64p, f64p, C.c_int, C.c_int, C.c_int,
+            f64p, f64p, f64p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
         ]
         L.ora_system_destroy.argtypes = [P]
         L.ora_n_sites.argtypes = [P]
@@ -119,13 +119,65 @@ def composition_RT(n_basis: int, n_occ: int) -> np.ndarray:
     return np.ascontiguousarray(np.linalg.pinv(Q))
 
 
+def _in_lattice(T, adj, det, v) -> bool:
+    """v in T Z^3: T^-1 v = adj(T) v / det(T) is integral."""
+    w = adj @ np.asarray(v, dtype=np.int64)
+    return bool(np.all(w % det == 0))
+
+
+def hermite_lower(T) -> np.ndarray:
+    """Lower-triangular Hermite normal form of the superlattice T Z^3 (columns
+    of T = supercell lattice vectors in prim cell coordinates), found from its
+    definition rather than by column operations: H22 is the smallest positive
+    z with (0, 0, z) in the lattice; (0, H11, H21) the lattice vector with the
+    smallest positive y among those with x = 0 (0 <= z < H22); (H00, H10, H20)
+    one with the smallest positive x (the gcd of the first row of T, reached by
+    the extended Euclid algorithm) with y and z reduced by the two others."""
+    T = np.asarray(T, dtype=np.int64).reshape(3, 3)
+    det = int(round(np.linalg.det(T)))
+    if det == 0:
+        raise ValueError("singular supercell matrix")
+    adj = np.array([[int(round(x)) for x in row] for row in np.linalg.inv(T) * det], dtype=np.int64)
+    n = abs(det)
+    h22 = next(z for z in range(1, n + 1) if _in_lattice(T, adj, det, (0, 0, z)))
+    h11, h21 = next((y, z) for y in range(1, n + 1) for z in range(h22)
+                    if _in_lattice(T, adj, det, (0, y, z)))
+
+    def egcd(a, b):
+        if b == 0:
+            return (abs(a), (1 if a >= 0 else -1), 0)
+        g, x, y = egcd(b, a % b)
+        return g, y, x - (a // b) * y
+
+    a0, a1, a2 = (int(x) for x in T[0])
+    g01, x0, x1 = egcd(a0, a1)
+    g, y01, y2 = egcd(g01, a2)
+    coef = np.array([y01 * x0, y01 * x1, y2], dtype=np.int64)
+    v = T @ coef  # a lattice vector with first coordinate g
+    assert v[0] == g
+    q = v[1] // h11
+    v = v - q * np.array([0, h11, h21])
+    v[2] %= h22
+    return np.array([[g, 0, 0], [v[1], h11, 0], [v[2], h21, h22]], dtype=np.int64)
+
+
 class OracleSystem:
-    """A cluster expansion on one supercell, evaluated by the oracle."""
+    """A cluster expansion on one supercell, evaluated by the oracle. ``L``:
+    three edge lengths of a diagonal supercell, or a 3 x 3 supercell matrix
+    (columns = supercell lattice vectors in prim cell coordinates), indexed on
+    its lower-triangular Hermite normal form H: cell (i, j, k) with
+    0 <= i < H00, 0 <= j < H11, 0 <= k < H22 is unit cell i + H00 (j + H11 k)."""
 
     def __init__(self, ce, L):
         self.ce = ce
         prim = ce.prim
-        self.L = tuple(int(x) for x in L)
+        if np.ndim(L) == 2:
+            H = hermite_lower(L)
+            self.L = (int(H[0, 0]), int(H[1, 1]), int(H[2, 2]))
+            self.twist = (int(H[1, 0]), int(H[2, 0]), int(H[2, 1]))
+        else:
+            self.L = tuple(int(x) for x in L)
+            self.twist = (0, 0, 0)
         nf = ce.n_funcs
         size = np.zeros(nf, dtype=np.int32)
         occ = np.zeros((nf, 4), dtype=np.int32)
@@ -143,6 +195,7 @@ class OracleSystem:
             np.ascontiguousarray(ce.func_coeff, dtype=np.float64),
             np.ascontiguousarray(self.RT.reshape(-1)),
             *self.L,
+            *self.twist,
         )
         cr = getattr(ce, "crystal", None)
         if cr is not None:
