@@ -172,11 +172,6 @@ class GpuMetropolisCalculator : public BaseMonteCalculator {
     if (!c.scalar_values.count("temperature")) v.error.insert("missing condition 'temperature'");
     if (m_sgc && !c.vector_values.count("param_chem_pot"))
       v.error.insert("missing condition 'param_chem_pot'");
-    const auto &T = state.configuration.transformation_matrix_to_super;
-    for (int a = 0; a < 3; ++a)
-      for (int b = 0; b < 3; ++b)
-        if (a != b && T[a][b] != 0)
-          v.error.insert("non-diagonal supercells are not supported by the GPU calculators");
     return v;
   }
 
@@ -185,15 +180,21 @@ class GpuMetropolisCalculator : public BaseMonteCalculator {
       throw std::runtime_error("Error in " + calculator_name + ": no system (call reset first)");
     const Validator v = validate_state(state);
     if (!v.valid()) throw std::runtime_error("Error in " + calculator_name + ": " + *v.error.begin());
-    const auto &T = state.configuration.transformation_matrix_to_super;
-    const int L[3] = {(int)T[0][0], (int)T[1][1], (int)T[2][2]};
-    if (!m_batch || L[0] != m_L[0] || L[1] != m_L[1] || L[2] != m_L[2]) {
+    // any supercell matrix: non-diagonal ones are indexed on their Hermite
+    // normal form and support the potential (per_supercell,
+    // occ_delta_per_supercell); run() needs a diagonal supercell
+    const auto &Tm = state.configuration.transformation_matrix_to_super;
+    int64_t T[9], H[9];
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) T[3 * a + b] = Tm[a][b];
+    ok(cem_supercell_hnf(T, H), "set_state_and_potential");
+    if (!m_batch || !std::equal(T, T + 9, m_T)) {
       if (m_batch) cem_replicas_destroy(m_batch);
       m_batch = nullptr;
-      ok(cem_replicas_create(system->gpu_system, 1, L, m_sgc ? CEM_SEMIGRAND_CANONICAL : CEM_CANONICAL,
-                             &m_batch),
+      ok(cem_replicas_create_supercells(system->gpu_system, 1, T,
+                                        m_sgc ? CEM_SEMIGRAND_CANONICAL : CEM_CANONICAL, &m_batch),
          "set_state_and_potential");
-      std::copy(L, L + 3, m_L);
+      std::copy(T, T + 9, m_T);
     }
     int64_t n_sites = 0;
     ok(cem_n_sites(m_batch, 0, &n_sites), "set_state_and_potential");
@@ -216,7 +217,7 @@ class GpuMetropolisCalculator : public BaseMonteCalculator {
     state_data = std::make_shared<StateData>();
     state_data->state = &state;
     state_data->occ_location = occ_location;
-    state_data->n_unitcells = (Index)L[0] * L[1] * L[2];
+    state_data->n_unitcells = (Index)(H[0] * H[4] * H[8]);
     potential = std::make_shared<GpuMontePotential>(state_data, m_batch, m_sgc, system);
   }
 
@@ -308,7 +309,7 @@ class GpuMetropolisCalculator : public BaseMonteCalculator {
  protected:
   bool m_sgc;
   cem_replicas *m_batch = nullptr;
-  int m_L[3] = {0, 0, 0};
+  int64_t m_T[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 
  private:
   void _reset() override {

@@ -131,7 +131,8 @@ int cem_system_destroy(cem_system *sys);
  * (CEM_CANONICAL or CEM_SEMIGRAND_CANONICAL). Occupations live in HBM.
  * Replaces state construction + set_state_and_potential
  * (CanonicalCalculator.cc:377-399). Linear site index:
- * l = b*n_uc + i + L0*(j + L1*k) (canonical_metropolis_test.cpp:34-36). */
+ * l = b*n_uc + i + L0*(j + L1*k): sublattice-major as in
+ * canonical_metropolis_test.cpp:34-36, unit cells i fastest. */
 int cem_replicas_create(const cem_system *sys, int n_replicas, const int *L, int ensemble,
                         cem_replicas **out);
 /* The same for general supercells: T[9r..9r+8] is replica r's integer

@@ -136,7 +136,7 @@ def test_plugin_potential_and_run_against_oracle(method, plugin, oracle_mod):
         (mean_e, e_ref, prec_e, se_ref)
 
 
-def test_plugin_rejects_what_the_reference_rejects(plugin):
+def test_plugin_rejects_what_the_reference_rejects(plugin, oracle_mod):
     lib, cm = plugin
     ce = workloads.config(0).ce
     calc = Calc(lib, cm, "canonical", ce)
@@ -146,10 +146,15 @@ def test_plugin_rejects_what_the_reference_rejects(plugin):
     calc.check(calc.set_state(np.diag((8, 8, 8)), occ, 500.0))
     rc, *_ = calc.run(occ.size, -1, 100, 0, 50, 0.0)
     assert rc == -1 and "engine" in lib.cem_plugin_last_error().decode()
-    # non-diagonal supercells are outside the library's limits
+    # non-diagonal supercells: the potential works, run() needs a diagonal one
     T = np.array([[8, 1, 0], [0, 8, 0], [0, 0, 8]])
-    assert calc.set_state(T, occ, 500.0) == -1
-    assert "non-diagonal" in lib.cem_plugin_last_error().decode()
+    calc.check(calc.set_state(T, occ, 500.0))
+    o_t = oracle_mod.OracleSystem(ce, T)
+    for site in (0, 5, 100, 511):
+        de_o, _ = o_t.delta(occ.astype(np.int8), [site], [1 - occ[site]])
+        assert abs(calc.delta([site], [1 - occ[site]]) - de_o) <= 1e-10 * abs(de_o) + 1e-12
+    rc, *_ = calc.run(occ.size, 7, 100, 0, 50, 0.0)
+    assert rc == -1 and "diagonal supercells" in lib.cem_plugin_last_error().decode()
     # missing semi-grand conditions
     sg = Calc(lib, cm, "semigrand_canonical", ce)
     assert sg.set_state(np.diag((8, 8, 8)), occ, 500.0, None) == -1
