@@ -358,7 +358,7 @@ def enforce_composition(state: "MonteCarloState", target_mol_composition, system
         raise ValueError(
             f"Error in enforce_composition: mismatch target_mol_composition={t.tolist()}, "
             f"expected {system.n_occ} components")
-    b = ReplicaBatch(system, "canonical", [tuple(int(x) for x in state.L)])
+    b = ReplicaBatch(system, "canonical", [_supercell_key(state.L)])
     b.set_occupation(0, state.occupation)
     n = int(b.enforce_composition(t, seed)[0])
     state.occupation[:] = b.get_occupation(0)
@@ -428,9 +428,27 @@ class LearnedProposal:
         return losses
 
 
+def _supercell_key(L):
+    """A supercell as given: three edge lengths, or a 3 x 3
+    ``transformation_matrix_to_super`` (tuple of rows)."""
+    if np.ndim(L) == 2:
+        return tuple(tuple(int(x) for x in row) for row in np.asarray(L))
+    return tuple(int(x) for x in L)
+
+
+def _n_unitcells(L) -> int:
+    if np.ndim(L) == 2:
+        return abs(int(round(np.linalg.det(np.asarray(L, dtype=float)))))
+    return int(L[0] * L[1] * L[2])
+
+
 @dataclass
 class MonteCarloState:
-    """Occupation of a diagonal supercell plus thermodynamic conditions."""
+    """Occupation of a supercell plus thermodynamic conditions. ``L``: three
+    edge lengths of a diagonal supercell, or a 3 x 3
+    ``transformation_matrix_to_super`` (non-diagonal supercells support the
+    potential, the replay and composition enforcement; parallel runs need a
+    diagonal supercell)."""
 
     occupation: np.ndarray
     L: tuple
@@ -501,8 +519,7 @@ class MontePotential:
         return self.calculator._batch
 
     def _n_uc(self) -> int:
-        L = self.state.L
-        return int(L[0] * L[1] * L[2])
+        return _n_unitcells(self.state.L)
 
     def per_supercell(self) -> float:
         e, _ = self._batch.energy(0)
@@ -552,7 +569,7 @@ class MonteCalculator:
 
     def _bind(self, state: MonteCarloState):
         self._check_conditions(state)
-        L = tuple(int(x) for x in state.L)
+        L = _supercell_key(state.L)
         if self._batch is None or self._batch.L[0] != L:
             self._batch = ReplicaBatch(self.system, self.method, [L])
         b = self._batch
@@ -582,8 +599,7 @@ class MonteCalculator:
         p = sampling_fixture_params
         self._bind(state)
         b = self._batch
-        L = state.L
-        n_uc = int(L[0] * L[1] * L[2])
+        n_uc = _n_unitcells(state.L)
         T = state.conditions["temperature"]
         if not p.requested_precision:
             b.run(p.n_passes, p.n_equil, p.record_samples)

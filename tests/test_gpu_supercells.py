@@ -187,3 +187,26 @@ def test_cluster_on_two_images_is_refused(cm):
         cm.ReplicaBatch(sysd, "canonical", [FCC_CONV])
     with pytest.raises(RuntimeError, match="singular"):
         cm.ReplicaBatch(sysd, "canonical", [np.array([[1, 2, 3], [2, 4, 6], [0, 0, 1]])])
+
+
+def test_python_calculator_with_a_supercell_matrix(cm, oracle_mod):
+    """The libcasm.clexmonte-style mirror on a non-diagonal state: the
+    potential and the replay work, a parallel run says why it cannot."""
+    ce, T = workloads.fcc_binary_ce(5), SUPERCELLS["sheared"]
+    o = oracle_mod.OracleSystem(ce, T)
+    rng = np.random.default_rng(29)
+    occ = workloads.fixed_composition(rng, o.n_sites, 0.5)
+    state = cm.MonteCarloState(occupation=occ.copy(), L=T, conditions={"temperature": 700.0})
+    calc = cm.MonteCalculator("canonical", cm.System(ce))
+    pot = calc.set_state_and_potential(state)
+    _close(pot.per_supercell(), o.energy(occ))
+    _close(pot.per_unitcell(), o.energy(occ) / 216)
+    for s in rng.integers(0, o.n_sites, 20):
+        _close(pot.occ_delta_per_supercell([s], [1 - occ[s]]), o.delta(occ, [s], [1 - occ[s]])[0])
+    occ_o = occ.copy()
+    ref = o.run(occ_o, 1, 700.0, np.zeros(1), 42, 5, record_steps=5 * o.n_sites)
+    got = calc.replay(state, 42, 5 * o.n_sites)
+    np.testing.assert_array_equal(got["accept"], ref["accept"])
+    np.testing.assert_array_equal(state.occupation, occ_o)
+    with pytest.raises(RuntimeError, match="parallel runs need diagonal supercells"):
+        calc.run_fixture(state, cm.SamplingFixtureParams(n_passes=10, n_equil=0))
