@@ -365,6 +365,111 @@ def enforce_composition(state: "MonteCarloState", target_mol_composition, system
     return n
 
 
+def supercell_hnf(transformation_matrix_to_super) -> np.ndarray:
+    """Lower-triangular Hermite normal form the library numbers a supercell's
+    unit cells on (cell (i, j, k), 0 <= i < H00, 0 <= j < H11, 0 <= k < H22, is
+    unit cell i + H00 (j + H11 k)); no device needed."""
+    t = np.ascontiguousarray(np.asarray(transformation_matrix_to_super, dtype=np.int64).reshape(9))
+    h = np.zeros(9, dtype=np.int64)
+    check(_lib.load().cem_supercell_hnf(ptr(t), ptr(h)))
+    return h.reshape(3, 3)
+
+
+def _cell_index(H, i, j, k):
+    """Unit cells (i, j, k) (arrays) reduced into the Hermite-normal-form box of H."""
+    L0, L1, L2 = int(H[0, 0]), int(H[1, 1]), int(H[2, 2])
+    q = np.floor_divide(i, L0)
+    i, j, k = i - q * L0, j - q * int(H[1, 0]), k - q * int(H[2, 0])
+    q = np.floor_divide(j, L1)
+    j, k = j - q * L1, k - q * int(H[2, 1])
+    return i + L0 * (j + L1 * np.mod(k, L2))
+
+
+def scale_supercell(transformation_matrix_to_super, dirs: str = "abc",
+                    min_volume: int = 1000) -> np.ndarray:
+    """T M with M diagonal: every axis named in ``dirs`` grows by one cell per
+    step until det(T M) >= min_volume (the reference's scale_supercell,
+    python/libcasm/clexmonte/_auto_configuration.py:19-58)."""
+    T = np.asarray(transformation_matrix_to_super, dtype=np.int64).reshape(3, 3)
+    if not any(c in dirs for c in "abc"):
+        raise ValueError("dirs must name at least one of 'a', 'b', 'c'")
+    M = np.eye(3, dtype=np.int64)
+    while int(round(np.linalg.det(T @ M))) < min_volume:
+        for a, c in enumerate("abc"):
+            if c in dirs:
+                M[a, a] += 1
+    return T @ M
+
+
+def tile_motif(motif_occupation, motif_T, T, n_sublat: int) -> np.ndarray:
+    """Occupation of supercell T filled with a motif (its occupation on
+    supercell motif_T, both in this library's site order); T must be a
+    supercell of motif_T."""
+    motif_T = np.asarray(motif_T, dtype=np.int64).reshape(3, 3)
+    T = np.asarray(T, dtype=np.int64).reshape(3, 3)
+    N = np.linalg.solve(motif_T.astype(float), T.astype(float))
+    if not np.allclose(N, np.round(N), atol=1e-9):
+        raise ValueError("Failed to tile motif into supercell")
+    H, Hm = supercell_hnf(T), supercell_hnf(motif_T)
+    k, j, i = np.meshgrid(np.arange(H[2, 2]), np.arange(H[1, 1]), np.arange(H[0, 0]), indexing="ij")
+    cell = _cell_index(Hm, i.ravel(), j.ravel(), k.ravel())  # motif cell of each cell of T
+    m_uc, n_uc = int(np.prod(np.diag(Hm))), int(np.prod(np.diag(H)))
+    occ = np.asarray(motif_occupation, dtype=np.int8).reshape(n_sublat, m_uc)
+    return np.ascontiguousarray(occ[:, cell].reshape(n_sublat * n_uc))
+
+
+def match_composition(state: "MonteCarloState", system: "System") -> None:
+    """Set the state's ``mol_composition`` (species per unit cell) and
+    ``param_composition`` conditions to its occupation's composition (the
+    reference calculators' "match.composition" modifier)."""
+    occ = np.asarray(state.occupation)
+    n_uc = _n_unitcells(state.L)
+    counts = np.bincount(occ, minlength=system.n_occ).astype(np.float64)
+    dn = counts.copy()
+    dn[0] -= occ.size
+    state.conditions["mol_composition"] = counts / n_uc
+    state.conditions["param_composition"] = system.RT @ dn / n_uc
+
+
+def make_canonical_initial_state(calculator: "MonteCalculator", conditions: dict,
+                                 dirs: str = "abc", min_volume: int = 1000,
+                                 transformation_matrix_to_super=None, motif=None,
+                                 seed: int = 0):
+    """Initial state for canonical Monte Carlo (the reference's
+    make_canonical_initial_state, _auto_configuration.py:496-640): the motif
+    (``None``: every site occupant 0 in the prim cell; else a pair
+    (occupation, transformation_matrix_to_super) in this library's site order)
+    is tiled into scale_supercell(transformation_matrix_to_super or the
+    motif's supercell, dirs, min_volume); the composition of ``conditions``
+    (``mol_composition`` or ``param_composition``; neither: the motif's) is
+    enforced by greedy flips drawn from std::mt19937_64(seed); the composition
+    conditions are then matched to the result. The reference also searches the
+    motif's orientations under the prim factor group for the lowest potential;
+    here the motif is tiled as given. Returns (state, motif)."""
+    system = calculator.system
+    nb = system.ce.prim.n_basis
+    if motif is None:
+        motif = (np.zeros(nb, dtype=np.int8), np.eye(3, dtype=np.int64))
+    m_occ, m_T = np.asarray(motif[0], dtype=np.int8), np.asarray(motif[1], dtype=np.int64)
+    conditions = dict(conditions)
+    if "mol_composition" in conditions:
+        target = np.asarray(conditions["mol_composition"], dtype=np.float64)
+    elif "param_composition" in conditions:
+        target = mol_composition(system, conditions["param_composition"])
+    else:
+        counts = np.bincount(m_occ, minlength=system.n_occ).astype(np.float64)
+        target = counts / (m_occ.size // nb)
+    T0 = m_T if transformation_matrix_to_super is None else transformation_matrix_to_super
+    T = scale_supercell(T0, dirs, min_volume)
+    occ = tile_motif(m_occ, m_T, T, nb)
+    L = tuple(int(T[a, a]) for a in range(3)) if np.count_nonzero(T - np.diag(np.diag(T))) == 0 \
+        and np.all(np.diag(T) > 0) else T
+    state = MonteCarloState(occupation=occ, L=L, conditions=conditions)
+    enforce_composition(state, target, system, seed)
+    match_composition(state, system)
+    return state, motif
+
+
 class LearnedProposal:
     """The proposal network (42 neighbour occupants -> 64 -> 64 -> 1 logit,
     bf16 parameters) on the GPU. A site holding A is weighted exp(z), one

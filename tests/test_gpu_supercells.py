@@ -210,3 +210,29 @@ def test_python_calculator_with_a_supercell_matrix(cm, oracle_mod):
     np.testing.assert_array_equal(state.occupation, occ_o)
     with pytest.raises(RuntimeError, match="parallel runs need diagonal supercells"):
         calc.run_fixture(state, cm.SamplingFixtureParams(n_passes=10, n_equil=0))
+
+
+@pytest.mark.parametrize("T", [None, "fcc_conventional"])
+def test_make_canonical_initial_state(T, cm, oracle_mod):
+    """Default motif (pure A) in the scaled supercell, composition enforced to
+    x_B = 0.25 with the oracle's flips, composition conditions matched."""
+    ce = workloads.fcc_binary_ce(2)
+    calc = cm.MonteCalculator("canonical", cm.System(ce))
+    Tm = None if T is None else FCC_CONV
+    state, motif = cm.make_canonical_initial_state(
+        calc, {"temperature": 600.0, "param_composition": [0.25]}, min_volume=1000,
+        transformation_matrix_to_super=Tm, seed=11)
+    n_uc = 1000 if T is None else 1372
+    assert state.occupation.size == n_uc
+    if T is None:
+        assert tuple(state.L) == (10, 10, 10)
+    ref = np.zeros(n_uc, dtype=np.int8)
+    o = oracle_mod.OracleSystem(ce, (10, 10, 10) if T is None else 7 * FCC_CONV)
+    o.enforce_composition(ref, cm.mol_composition(calc.system, [0.25]), 11)
+    np.testing.assert_array_equal(state.occupation, ref)
+    assert abs(state.occupation.sum() - 0.25 * n_uc) <= 1
+    np.testing.assert_allclose(state.conditions["param_composition"], [state.occupation.sum() / n_uc])
+    np.testing.assert_allclose(state.conditions["mol_composition"],
+                               [1 - state.occupation.sum() / n_uc, state.occupation.sum() / n_uc])
+    pot = calc.set_state_and_potential(state)
+    assert pot.per_supercell() == pytest.approx(o.energy(state.occupation), rel=1e-10)

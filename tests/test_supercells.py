@@ -118,3 +118,38 @@ def test_oracle_refuses_a_supercell_with_a_cluster_on_two_images(oracle_mod):
     its own image."""
     with pytest.raises(RuntimeError, match="supercell too small"):
         oracle_mod.OracleSystem(workloads.fcc_binary_ce(3), FCC_CONV)
+
+
+def test_scale_supercell_grows_every_named_axis():
+    from casmcode_clexmonte_gb300 import calculator as c
+
+    np.testing.assert_array_equal(c.scale_supercell(np.eye(3, dtype=int), "abc", 1000), 10 * np.eye(3))
+    np.testing.assert_array_equal(c.scale_supercell(FCC_CONV, "abc", 1000), 7 * FCC_CONV)  # 1372 >= 1000 > 864
+    np.testing.assert_array_equal(c.scale_supercell(np.eye(3, dtype=int), "c", 50), np.diag([1, 1, 50]))
+    np.testing.assert_array_equal(c.scale_supercell(np.diag([2, 3, 4]), "ab", 24), np.diag([2, 3, 4]))
+    np.testing.assert_array_equal(c.scale_supercell(np.diag([2, 3, 4]), "ab", 25), np.diag([4, 6, 4]))
+
+
+def test_tiled_l12_motif(oracle_mod):
+    """The L1_2 motif on the conventional FCC cell (B on one of its four
+    simple-cubic sublattices: prim cells with i = j = k mod 2) tiled into a
+    diagonal supercell holds B exactly there, and tiled into a non-diagonal
+    one it has the same energy per unit cell."""
+    from casmcode_clexmonte_gb300 import build
+    from casmcode_clexmonte_gb300 import calculator as c
+
+    build.build()
+    H = c.supercell_hnf(FCC_CONV)
+    k, j, i = np.meshgrid(np.arange(H[2, 2]), np.arange(H[1, 1]), np.arange(H[0, 0]), indexing="ij")
+    motif = ((i % 2 == j % 2) & (j % 2 == k % 2)).ravel().astype(np.int8)
+    assert motif.sum() == 1 and motif.size == 4
+    diag = c.tile_motif(motif, FCC_CONV, 6 * np.eye(3, dtype=int), 1)
+    k, j, i = np.meshgrid(np.arange(6), np.arange(6), np.arange(6), indexing="ij")
+    np.testing.assert_array_equal(diag, ((i % 2 == j % 2) & (j % 2 == k % 2)).ravel())
+    twisted = c.tile_motif(motif, FCC_CONV, 3 * FCC_CONV, 1)
+    ce = workloads.fcc_binary_ce(3, nn1=0.08)
+    e_d = oracle_mod.OracleSystem(ce, (6, 6, 6)).energy(diag) / 216
+    e_t = oracle_mod.OracleSystem(ce, 3 * FCC_CONV).energy(twisted) / 108
+    assert e_t == pytest.approx(e_d, rel=1e-12, abs=1e-12)
+    with pytest.raises(ValueError, match="Failed to tile"):
+        c.tile_motif(motif, FCC_CONV, np.diag([3, 3, 3]), 1)
