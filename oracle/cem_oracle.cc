@@ -1,7 +1,8 @@
 // CPU FP64 oracle for the cluster-expansion Metropolis hot path.
 //
-// TEST INFRASTRUCTURE ONLY. This file is the checker: it is linked and called
-// by tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg,
+// TEST INFRASTRUCTURE ONLY. The GPU results are compared against this file:
+// it is linked and called by tests/, by __graft_entry__.smoke() and by
+// bench.py's CPU-baseline leg,
 // never by the product library. It restates, independently of the product's
 // table builder, the arithmetic of the reference's hot path:
 //

@@ -1,7 +1,7 @@
 """ctypes wrapper around the CPU FP64 oracle (``oracle/cem_oracle.cc``).
 
 TEST INFRASTRUCTURE ONLY: imported by ``tests/``, ``__graft_entry__.smoke()``
-and the CPU-baseline leg of ``bench.py`` as the checker. The product library
+and the CPU-baseline leg of ``bench.py`` as the comparison. The product library
 never imports this module.
 """
 
