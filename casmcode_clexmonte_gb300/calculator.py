@@ -69,7 +69,7 @@ class ReplicaBatch:
         lattice vectors in prim cell coordinates). Non-diagonal supercells
         number their unit cells on the matrix's lower-triangular Hermite normal
         form H (cell i + H00 (j + H11 k)) and support the exact paths (energy,
-        delta, replay, enforce_composition, state transfer) only."""
+        delta, replay, n-fold way, enforce_composition, state transfer) only."""
         self.system = system
         self.lib = system.lib
         self.ensemble = ensemble

@@ -456,14 +456,15 @@ std::array<long long, 9> hermite_lower(const int64_t *T) {
   return H;
 }
 
-// The parallel kernels (sweeps, n-fold way, learned proposals, streamed
-// batches) keep each replica as an axis-aligned periodic box with a halo and
-// colour classes along the three axes; non-diagonal supercells run on the
-// exact paths only.
+// The parallel kernels (sweeps, learned proposals, streamed batches) keep
+// each replica as an axis-aligned periodic box with a halo and colour classes
+// along the three axes; non-diagonal supercells run on the exact paths and
+// the (sequential) n-fold way only.
 void require_box(const cem_replicas *r) {
   require(!r->twisted,
           "non-diagonal supercells support energies, energy changes, the sequential replay, "
-          "composition enforcement and state transfer; parallel runs need diagonal supercells",
+          "the n-fold way, composition enforcement and state transfer; parallel runs need "
+          "diagonal supercells",
           CEM_ERR_UNSUPPORTED);
 }
 
@@ -1178,7 +1179,6 @@ int cem_nfold_run(cem_replicas *r, int64_t n_events, int64_t n_equil, int64_t re
                   int64_t *rec_site, int32_t *rec_occ, double *rec_dt) {
   return guard([&] {
     require(r != nullptr, "null handle");
-    require_box(r);
     require(r->ensemble == CEM_SEMIGRAND_CANONICAL,
             "the n-fold way runs semi-grand canonical replicas");
     require(n_events >= 0 && n_equil >= 0 && record_capacity >= 0, "counts must be >= 0");

@@ -771,6 +771,26 @@ __device__ __forceinline__ void put_site(int8_t *occ, const Geo &G, int b, int x
   if (ox && oy && oz) occ[base + ox + oy + oz] = v;
 }
 
+// Write occupant v to core site (b,x,y,z) and every periodic image of it in
+// the halo'd box of a supercell in Hermite normal form C (twisted images: a
+// step of L0 along x shifts y and z by t10, t20; a step of L1 along y shifts
+// z by t21). Each box cell [-R, L + R) per axis is an image of exactly one
+// core cell, so the halo holds what the box's gathers read, for boxes thinner
+// than the reach too.
+__device__ __forceinline__ void put_site_cells(int8_t *occ, const Geo &G, const Cells &C, int b,
+                                               int x, int y, int z, int8_t v) {
+  const int R = G.R;
+  for (int xi = x - floor_div(x + R, C.L0) * C.L0; xi < C.L0 + R; xi += C.L0) {
+    const int i = (xi - x) / C.L0;  // exact
+    const int yb = y + i * C.t10, zb = z + i * C.t20;
+    for (int yj = yb - floor_div(yb + R, C.L1) * C.L1; yj < C.L1 + R; yj += C.L1) {
+      const int zc = zb + ((yj - yb) / C.L1) * C.t21;
+      for (int zk = zc - floor_div(zc + R, C.L2) * C.L2; zk < C.L2 + R; zk += C.L2)
+        occ[G.addr(b, xi, yj, zk)] = v;
+    }
+  }
+}
+
 // Energy change of a sweep proposal (f32, minus the chemical potential term
 // mu_hi + mu_lo). Binary systems: exact int32 sum of wq * dC scaled by the
 // power-of-two quantum, plus the f32 remainder terms (one FMA chain); other

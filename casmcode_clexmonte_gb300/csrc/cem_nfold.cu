@@ -151,10 +151,19 @@ __global__ void __launch_bounds__(NF_THREADS)
   }
   const int8_t *gocc = P.occ + R.occ_offset;
   const SiteIndex site_of(n_uc, G.L0, G.L1);
+  // non-diagonal supercells: twisted periodic images
+  const Cells C = R.cells();
+  const bool twisted = (C.t10 | C.t20 | C.t21) != 0;
+  auto put = [&](int b, int x, int y, int z, int8_t v) {
+    if (twisted)
+      put_site_cells(occ, G, C, b, x, y, z, v);
+    else
+      put_site(occ, G, b, x, y, z, v);
+  };
   for (int l = tid; l < n_sites; l += nth) {
     int b, x, y, z;
     site_of(l, b, x, y, z);
-    put_site(occ, G, b, x, y, z, gocc[l]);
+    put(b, x, y, z, gocc[l]);
   }
   __syncthreads();
 
@@ -317,7 +326,7 @@ __global__ void __launch_bounds__(NF_THREADS)
       sel[1] = o_i;
       S.n_species[o_i] -= 1;
       S.n_species[o_f] += 1;
-      put_site(occ, G, b, x, y, z, (int8_t)o_f);
+      put(b, x, y, z, (int8_t)o_f);
     }
     // impacted sites: the changed site and its flower partners
     const int n_imp = 1 + T.n_fp[b];
@@ -325,7 +334,7 @@ __global__ void __launch_bounds__(NF_THREADS)
       int s = l;
       if (t > 0) {
         const int *e = T.fp + ((size_t)b * MAX_FP + (t - 1)) * 4;
-        s = e[0] * n_uc + wrapc(x + e[1], G.L0) + G.L0 * (wrapc(y + e[2], G.L1) + G.L1 * wrapc(z + e[3], G.L2));
+        s = e[0] * n_uc + C.index(x + e[1], y + e[2], z + e[3]);
       }
       imp[t] = s;
     }

@@ -142,8 +142,9 @@ int cem_replicas_create(const cem_system *sys, int n_replicas, const int *L, int
  * superlattice): cell (i, j, k), 0 <= i < H00, 0 <= j < H11, 0 <= k < H22,
  * has index i + H00*(j + H11*k); for a diagonal matrix with positive entries
  * this is the order of cem_replicas_create. Non-diagonal supercells support
- * energies, energy changes, the sequential replay, composition enforcement
- * and state transfer; the parallel runs return CEM_ERR_UNSUPPORTED for them.
+ * energies, energy changes, the sequential replay, the n-fold way,
+ * composition enforcement and state transfer; the parallel runs return
+ * CEM_ERR_UNSUPPORTED for them.
  * A non-diagonal supercell in which some cluster holds two periodic images
  * of one site is refused. */
 int cem_replicas_create_supercells(const cem_system *sys, int n_replicas, const int64_t *T,

@@ -236,3 +236,39 @@ def test_make_canonical_initial_state(T, cm, oracle_mod):
                                [1 - state.occupation.sum() / n_uc, state.occupation.sum() / n_uc])
     pot = calc.set_state_and_potential(state)
     assert pot.per_supercell() == pytest.approx(o.energy(state.occupation), rel=1e-10)
+
+
+@pytest.mark.parametrize("kind", ["fcc_sheared_10", "fcc_conventional_2", "bcc_ternary_general"])
+def test_nfold_matches_oracle_event_for_event(kind, cm, oracle_mod):
+    """The n-fold way on non-diagonal supercells (twisted halo images): the
+    event sequence, residence times and final occupation equal the oracle's.
+    fcc_sheared_10: box 10 x 10 x 10 with one twist, the generated evaluator;
+    fcc_conventional_2: box 2 x 4 x 4, thinner than the cluster reach along x."""
+    rng = np.random.default_rng(41)
+    if kind == "fcc_sheared_10":
+        ce, T, temp, mu = workloads.fcc_binary_ce(3), np.array([[10, 0, 0], [5, 10, 0], [0, 0, 10]]), 600.0, np.array([0.02])
+    elif kind == "fcc_conventional_2":
+        ce, T, temp, mu = workloads.fcc_binary_ce(2), SUPERCELLS["fcc_conventional_2"], 700.0, np.array([0.0])
+    else:
+        ce, T, temp, mu = workloads.bcc_ternary_ce(6), GENERAL, 900.0, np.array([0.05, -0.1])
+    nocc = ce.prim.n_occ
+    o = oracle_mod.OracleSystem(ce, T)
+    occ = rng.integers(0, nocc, o.n_sites).astype(np.int8)
+    sysd = cm.System(ce)
+    b = cm.ReplicaBatch(sysd, "semigrand_canonical", [T])
+    b.set_conditions(0, temp, mu)
+    seed = 0x5EEDF00D
+    b.set_seed(0, seed)
+    b.set_occupation(0, occ)
+    n_events, n_equil = 300, 40
+    rec = b.nfold_run(n_events, n_equil, record=n_events + n_equil)
+    occ_o = occ.copy()
+    ref = o.nfold(occ_o, temp, mu, sysd.arrays["weights"], seed, n_events, n_equil,
+                  record=n_events + n_equil)
+    assert ref["n"] == n_events + n_equil
+    np.testing.assert_array_equal(rec["site"][0], ref["site"])
+    np.testing.assert_array_equal(rec["occ"][0], ref["occ"])
+    np.testing.assert_array_equal(rec["dt"][0], ref["dt"])
+    np.testing.assert_array_equal(b.get_occupation(0), occ_o)
+    e_now, _ = b.energy(0)
+    assert b.stats(0)["energy"] == pytest.approx(e_now, rel=1e-9, abs=1e-9)
