@@ -46,7 +46,7 @@ def _noalloc(lib, batch, sites, new_occ, potential, n_funcs, with_dcount=True):
     return rc, dE, dc
 
 
-@pytest.mark.parametrize("kind", ["fcc_binary_sgc", "bcc_ternary_sgc", "zro_sgc"])
+@pytest.mark.parametrize("kind", ["fcc_binary_sgc", "bcc_ternary_sgc", "zro_sgc", "fcc_twisted_sgc"])
 def test_noalloc_delta_matches_allocating_entry_point(kind, env):
     lib, cm, workloads, _lib = env
     rng = np.random.default_rng(99)
@@ -54,6 +54,10 @@ def test_noalloc_delta_matches_allocating_entry_point(kind, env):
         ce, L, mu = workloads.fcc_binary_ce(1), (10, 10, 10), np.array([0.03])
     elif kind == "bcc_ternary_sgc":
         ce, L, mu = workloads.bcc_ternary_ce(2), (6, 6, 6), np.array([0.1, -0.05])
+    elif kind == "fcc_twisted_sgc":
+        # a non-diagonal supercell (Hermite normal form with all three twists)
+        L = np.array([[6, 0, 0], [3, 6, 0], [3, 3, 6]]) @ np.array([[1, 1, 0], [0, 1, 1], [1, 1, 1]])
+        ce, mu = workloads.fcc_binary_ce(1), np.array([0.03])
     else:
         # the reference's Zr-O basis set: 74 functions, so every event's
         # delta-correlation row in the scratch array is 74 entries wide
