@@ -150,8 +150,10 @@ struct cem_replicas {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;
-  // some replica is a non-diagonal supercell (exact paths only)
-  bool twisted = false;
+  // some replica is a non-diagonal supercell; the parallel sweep then runs
+  // only for semi-grand batches whose twisted replicas all have a colouring,
+  // on the run-time tables, one CTA per replica, shared memory
+  bool twisted = false, twisted_parallel = true;
   // HBM-streamed batches (supercells too large for shared memory)
   bool streamed = false;
   int stream_pitch = 0;
@@ -311,10 +313,14 @@ int sweep_cluster_for(int requested, int pitch, int threads, const std::vector<R
 }
 
 // smallest block size whose colour classes hold no two interacting sites;
-// canonical local pair moves also need 2p - reach(neighbour) > reach(flower)
-int choose_colouring(const cem_system &s, const int L[3], int ensemble) {
+// canonical local pair moves also need 2p - reach(neighbour) > reach(flower).
+// tw: the twists of a supercell in Hermite normal form (null: diagonal); the
+// check follows every flower partner through the supercell's own periodicity,
+// so a colouring it accepts is valid on the twisted box too.
+int choose_colouring(const cem_system &s, const int L[3], int ensemble, const int *tw = nullptr) {
   const CeTables &T = s.T;
   const int n_uc = L[0] * L[1] * L[2];
+  const Cells C{L[0], L[1], L[2], tw ? tw[0] : 0, tw ? tw[1] : 0, tw ? tw[2] : 0};
   for (int p = 2; p <= 8; ++p) {
     std::vector<int> col[3];
     bool ok = true;
@@ -330,7 +336,6 @@ int choose_colouring(const cem_system &s, const int L[3], int ensemble) {
     auto cls = [&](int b, int x, int y, int z) {
       return b * ncol[0] * ncol[1] * ncol[2] + col[0][x] + ncol[0] * (col[1][y] + ncol[1] * col[2][z]);
     };
-    auto wr = [](int x, int Lx) { return ((x % Lx) + Lx) % Lx; };
     for (int b = 0; b < T.n_sublat && ok; ++b)
       for (int z = 0; z < L[2] && ok; ++z)
         for (int y = 0; y < L[1] && ok; ++y)
@@ -342,8 +347,9 @@ int choose_colouring(const cem_system &s, const int L[3], int ensemble) {
                 const int pb = s.fl_pb[c * 3 + q];
                 if (pb < 0) continue;
                 const int *du = &s.fl_du[c * 9 + q * 3];
-                const int px = wr(x + du[0], L[0]), py = wr(y + du[1], L[1]), pz = wr(z + du[2], L[2]);
-                const int l1 = pb * n_uc + px + L[0] * (py + L[1] * pz);
+                const int u1 = C.index(x + du[0], y + du[1], z + du[2]);
+                const int px = u1 % L[0], py = (u1 / L[0]) % L[1], pz = u1 / (L[0] * L[1]);
+                const int l1 = pb * n_uc + u1;
                 if (l1 == l0)
                   throw Err(CEM_ERR_INVALID,
                             "supercell too small: a cluster contains one site twice");
@@ -463,8 +469,21 @@ std::array<long long, 9> hermite_lower(const int64_t *T) {
 void require_box(const cem_replicas *r) {
   require(!r->twisted,
           "non-diagonal supercells support energies, energy changes, the sequential replay, "
-          "the n-fold way, composition enforcement and state transfer; parallel runs need "
-          "diagonal supercells",
+          "the n-fold way, composition enforcement, state transfer and semi-grand parallel "
+          "sweeps; these parallel runs need diagonal supercells",
+          CEM_ERR_UNSUPPORTED);
+}
+
+// The plain sweep on a batch with non-diagonal supercells: semi-grand
+// canonical flips only (the canonical pair geometry assumes an axis-aligned
+// box), with a valid colouring of every twisted replica and the replicas in
+// shared memory.
+void require_sweepable(const cem_replicas *r) {
+  require(!r->twisted || (r->ensemble == CEM_SEMIGRAND_CANONICAL && r->twisted_parallel),
+          "non-diagonal supercells support energies, energy changes, the sequential replay, "
+          "the n-fold way, composition enforcement, state transfer and semi-grand parallel "
+          "sweeps (when an exact colouring exists); canonical parallel runs need diagonal "
+          "supercells",
           CEM_ERR_UNSUPPORTED);
 }
 
@@ -551,7 +570,26 @@ void create_replicas(const cem_system *sys, int n, const int *L, const int *tw, 
           cls *= R.n_col[a];
         }
       } else {
+        // twisted: the semi-grand parallel sweep runs when an exact colouring
+        // exists (checked through the twisted periodicity)
         for (int a = 0; a < 3; ++a) R.n_col[a] = 1;
+        bool coloured = false;
+        if (ensemble == CEM_SEMIGRAND_CANONICAL && !sys->big) {
+          try {
+            R.p = choose_colouring(*sys, R.L, ensemble, R.tw);
+            coloured = true;
+          } catch (const Err &) {
+          }
+        }
+        if (coloured) {
+          for (int a = 0; a < 3; ++a) {
+            auto col = axis_blocks(R.L[a], R.p);
+            R.n_col[a] = *std::max_element(col.begin(), col.end()) + 1;
+            cls *= R.n_col[a];
+          }
+        } else {
+          r->twisted_parallel = false;
+        }
       }
       max_cls = std::max(max_cls, cls);
       R.temperature = 1000.0;
@@ -586,7 +624,8 @@ void create_replicas(const cem_system *sys, int n, const int *L, const int *tw, 
     if (sys->big) pitch = sys->coop ? -2 : -1;  // one warp per site / one orbit at a time
     if (r->twisted) pitch = 0;
     r->pitch = pitch;
-    r->sweep_smem = r->twisted ? 0 : batch_smem(r.get(), pitch);
+    r->sweep_smem = (r->twisted && !r->twisted_parallel) ? 0 : batch_smem(r.get(), pitch);
+    if (r->twisted && r->sweep_smem > maxsm) r->twisted_parallel = false;
     if (!r->twisted && r->sweep_smem > maxsm && stream_pitch_for(*sys, r->reps)) {
       r->streamed = true;
       r->stream_pitch = stream_pitch_for(*sys, r->reps);
@@ -1325,7 +1364,7 @@ int cem_enforce_composition(cem_replicas *r, const double *target_mol, uint64_t 
 int cem_step_async(cem_replicas *r, const int8_t *host_in, int8_t *host_out, int64_t n_passes) {
   return guard([&] {
     require(r && host_in && host_out, "null argument");
-    require_box(r);
+    require_sweepable(r);
     require(n_passes >= 1, "n_passes must be >= 1");
     require(!r->streamed, "HBM-streamed batches run through cem_run", CEM_ERR_UNSUPPORTED);
     for (const void *p : {(const void *)host_in, (const void *)host_out}) {
@@ -1403,7 +1442,7 @@ int cem_step_async(cem_replicas *r, const int8_t *host_in, int8_t *host_out, int
 int cem_run(cem_replicas *r, int64_t n_passes, int64_t n_equil, int record_samples) {
   return guard([&] {
     require(r != nullptr, "null handle");
-    require_box(r);
+    require_sweepable(r);
     require(n_passes >= 0 && n_equil >= 0, "pass counts must be >= 0");
     int dev = 0, maxsm = 0;
     CUDA_OK(cudaGetDevice(&dev));
@@ -1601,7 +1640,7 @@ int cem_smem_bandwidth(double *gbs) {
 int cem_autotune(cem_replicas *r, int64_t trial_passes, double *best_ms) {
   return guard([&] {
     require(r != nullptr, "null handle");
-    require_box(r);
+    require_sweepable(r);
     require(trial_passes > 0, "trial_passes must be > 0");
     if (best_ms) *best_ms = 0.0;
     if (r->streamed) return;  // one fixed graph per pass

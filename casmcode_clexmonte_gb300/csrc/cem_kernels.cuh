@@ -1340,6 +1340,19 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
   G.R = T.reach;
   G.W = PITCH > 0 ? PITCH : G.L0 + 2 * G.R;
   G.H = PITCH > 0 ? PITCH : G.L1 + 2 * G.R;
+  // a non-diagonal supercell (run-time tables only): halo cells are twisted
+  // periodic images of the core
+  const Cells Ctw = R.cells();
+  const bool twisted = PITCH == 0 && (Ctw.t10 | Ctw.t20 | Ctw.t21) != 0;
+  auto put1 = [&](int8_t *o, int b, int x, int y, int z, int8_t v) {
+    if constexpr (PITCH == 0) {
+      if (twisted) {
+        put_site_cells(o, G, Ctw, b, x, y, z, v);
+        return;
+      }
+    }
+    put_site(o, G, b, x, y, z, v);
+  };
   // binary systems with generated or register-accumulated tables keep exact
   // integer delta correlations per orbit for the running energy
   constexpr bool EXACT = (NOCC == 2 && PITCH >= 0);
@@ -1453,7 +1466,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
   const SiteIndex site_of(n_uc, G.L0, G.L1);
   // bulk (TMA) copies when the replica's occupations are 16-byte aligned,
   // byte loads otherwise
-  const bool vec16 = !CLUSTERED && ((R.occ_offset | n_sites) & 15) == 0;
+  const bool vec16 = !CLUSTERED && !twisted && ((R.occ_offset | n_sites) & 15) == 0;
   uint8_t *stg = smem + lay.clist;
   const int stg_cap = ((lay.bar - lay.clist) / 16) * 16;
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem + lay.bar);
@@ -1469,11 +1482,11 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
     for (int l = tid; l < n_sites; l += nth) {
       int b, x, y, z;
       site_of(l, b, x, y, z);
-      put_site(occ, G, b, x, y, z, gocc[l]);
+      put1(occ, b, x, y, z, gocc[l]);
     }
   }
   __syncthreads();  // core and periodic halo images (every halo cell is the
-                    // image of one core site: L >= 2 reach + 1 on every axis)
+                    // image of one core site)
   if constexpr (PITCH == -2) {
     // flower bounds by cluster size (orbits are sorted by size), written after
     // the staging copies, which pass through this area; the schedule's
@@ -1491,7 +1504,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
   // an accepted change reaches every copy of the replica
   auto put_all = [&](int b, int x, int y, int z, int8_t v) {
     if constexpr (!CLUSTERED) {
-      put_site(occ, G, b, x, y, z, v);
+      put1(occ, b, x, y, z, v);
     } else {
       cg::cluster_group cluster = cg::this_cluster();
       for (int r = 0; r < CL; ++r) put_site(cluster.map_shared_rank(occ, r), G, b, x, y, z, v);

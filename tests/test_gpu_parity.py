@@ -178,8 +178,8 @@ def test_parallel_equilibrium_matches_oracle(ens, edge, cm, oracle_mod):
     edge takes colour blocks of unequal sizes) at 900 K: <E> and C, and
     semi-grand canonical also <x>, chi and the thermo-chemical chi.
     Independent chains on each side (GPU 16, oracle 16), pooled, jackknife
-    errors, >= 50 tau_int per chain, 2 sigma per comparison at a 1 %
-    family-wise contract (tests/test_gpu_equilibrium.py)."""
+    errors, >= 50 tau_int per chain, 2 sigma per comparison under the
+    family-wise contract of tests/test_gpu_equilibrium.py."""
     from tests.stat_checks import compare
 
     ce = workloads.fcc_binary_ce(0)
