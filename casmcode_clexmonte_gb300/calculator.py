@@ -69,7 +69,8 @@ class ReplicaBatch:
         lattice vectors in prim cell coordinates). Non-diagonal supercells
         number their unit cells on the matrix's lower-triangular Hermite normal
         form H (cell i + H00 (j + H11 k)) and support the exact paths (energy,
-        delta, replay, n-fold way, enforce_composition, state transfer) only."""
+        delta, replay, n-fold way, enforce_composition, state transfer) and
+        semi-grand canonical runs; canonical runs need a diagonal supercell."""
         self.system = system
         self.lib = system.lib
         self.ensemble = ensemble
@@ -552,8 +553,8 @@ class MonteCarloState:
     """Occupation of a supercell plus thermodynamic conditions. ``L``: three
     edge lengths of a diagonal supercell, or a 3 x 3
     ``transformation_matrix_to_super`` (non-diagonal supercells support the
-    potential, the replay and composition enforcement; parallel runs need a
-    diagonal supercell)."""
+    potential, the replay, composition enforcement and semi-grand canonical
+    runs; canonical runs need a diagonal supercell)."""
 
     occupation: np.ndarray
     L: tuple

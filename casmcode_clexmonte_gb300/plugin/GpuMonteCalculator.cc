@@ -182,7 +182,8 @@ class GpuMetropolisCalculator : public BaseMonteCalculator {
     if (!v.valid()) throw std::runtime_error("Error in " + calculator_name + ": " + *v.error.begin());
     // any supercell matrix: non-diagonal ones are indexed on their Hermite
     // normal form and support the potential (per_supercell,
-    // occ_delta_per_supercell); run() needs a diagonal supercell
+    // occ_delta_per_supercell) and the semi-grand run(); the canonical run()
+    // needs a diagonal supercell
     const auto &Tm = state.configuration.transformation_matrix_to_super;
     int64_t T[9], H[9];
     for (int a = 0; a < 3; ++a)

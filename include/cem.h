@@ -143,7 +143,9 @@ int cem_replicas_create(const cem_system *sys, int n_replicas, const int *L, int
  * has index i + H00*(j + H11*k); for a diagonal matrix with positive entries
  * this is the order of cem_replicas_create. Non-diagonal supercells support
  * energies, energy changes, the sequential replay, the n-fold way,
- * composition enforcement and state transfer; the parallel runs return
+ * composition enforcement, state transfer and semi-grand canonical parallel
+ * sweeps (when a colouring exists; run-time tables, shared memory);
+ * canonical parallel runs, the learned proposals and streamed batches return
  * CEM_ERR_UNSUPPORTED for them.
  * A non-diagonal supercell in which some cluster holds two periodic images
  * of one site is refused. */
