@@ -686,7 +686,15 @@ double event_delta(const System &s, std::vector<signed char> &occ, int n, const 
                    const int *new_occ, i64 *dcount) {
   thread_local std::vector<i64> d;
   d.assign(s.n_funcs, 0);
-  std::vector<signed char> saved(n > 0 ? n : 0);
+  // previous occupants: a stack buffer for the Metropolis events (1-2 sites),
+  // a vector only for longer events
+  signed char small[4];
+  std::vector<signed char> big;
+  signed char *saved = small;
+  if (n > 4) {
+    big.resize(n);
+    saved = big.data();
+  }
   for (int i = 0; i < n; ++i) {
     saved[i] = occ[sites[i]];
     site_delta_counts(s, occ.data(), (int)sites[i], new_occ[i], d.data());
