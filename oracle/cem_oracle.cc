@@ -682,19 +682,12 @@ void all_counts(const System &s, const signed char *occ, i64 *count) {
 
 // ---- event delta with the reference's sequential semantics: each change is
 // applied before the next is evaluated (canonical/canonical.hh:42-45).
-double event_delta(const System &s, std::vector<signed char> &occ, int n, const i64 *sites,
-                   const int *new_occ, i64 *dcount) {
+// Energy change of a series of site changes applied in order (the state is
+// restored); saved holds the n previous occupants.
+double event_delta_into(const System &s, std::vector<signed char> &occ, int n, const i64 *sites,
+                        const int *new_occ, i64 *dcount, signed char *saved) {
   thread_local std::vector<i64> d;
   d.assign(s.n_funcs, 0);
-  // previous occupants: a stack buffer for the Metropolis events (1-2 sites),
-  // a vector only for longer events
-  signed char small[4];
-  std::vector<signed char> big;
-  signed char *saved = small;
-  if (n > 4) {
-    big.resize(n);
-    saved = big.data();
-  }
   for (int i = 0; i < n; ++i) {
     saved[i] = occ[sites[i]];
     site_delta_counts(s, occ.data(), (int)sites[i], new_occ[i], d.data());
@@ -706,6 +699,16 @@ double event_delta(const System &s, std::vector<signed char> &occ, int n, const 
   if (dcount)
     for (int f = 0; f < s.n_funcs; ++f) dcount[f] = d[f];
   return de;
+}
+
+double event_delta(const System &s, std::vector<signed char> &occ, int n, const i64 *sites,
+                   const int *new_occ, i64 *dcount) {
+  if (n > 4) {  // longer events (tests): a heap buffer
+    std::vector<signed char> saved(n);
+    return event_delta_into(s, occ, n, sites, new_occ, dcount, saved.data());
+  }
+  signed char saved[4];
+  return event_delta_into(s, occ, n, sites, new_occ, dcount, saved);
 }
 
 // SGC chemical-potential term: param_chem_pot . (R^T dN), dN per component
