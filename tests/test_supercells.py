@@ -153,3 +153,24 @@ def test_tiled_l12_motif(oracle_mod):
     assert e_t == pytest.approx(e_d, rel=1e-12, abs=1e-12)
     with pytest.raises(ValueError, match="Failed to tile"):
         c.tile_motif(motif, FCC_CONV, np.diag([3, 3, 3]), 1)
+
+
+def test_match_composition_and_unit_cell_count():
+    """The "match.composition" modifier on a ternary system (standard axes:
+    param x_k = N_k / n_uc for one sublattice) and the unit-cell count of a
+    supercell given as a matrix."""
+    from types import SimpleNamespace
+
+    from casmcode_clexmonte_gb300 import calculator as c
+    from casmcode_clexmonte_gb300.system import composition_RT
+
+    system = SimpleNamespace(n_occ=3, RT=composition_RT(1, 3))
+    occ = np.array([0] * 50 + [1] * 30 + [2] * 28, dtype=np.int8)
+    T = np.array([[6, 0, 0], [3, 6, 0], [0, 0, 3]])  # 108 unit cells
+    state = c.MonteCarloState(occupation=occ, L=T, conditions={"temperature": 300.0})
+    assert c._n_unitcells(T) == 108 and c._n_unitcells((4, 5, 6)) == 120
+    c.match_composition(state, system)
+    np.testing.assert_allclose(state.conditions["mol_composition"], [50 / 108, 30 / 108, 28 / 108])
+    np.testing.assert_allclose(state.conditions["param_composition"], [30 / 108, 28 / 108], atol=1e-12)
+    assert c._supercell_key(T) == ((6, 0, 0), (3, 6, 0), (0, 0, 3))
+    assert c._supercell_key(np.array([4, 5, 6])) == (4, 5, 6)
