@@ -462,10 +462,9 @@ std::array<long long, 9> hermite_lower(const int64_t *T) {
   return H;
 }
 
-// The parallel kernels (sweeps, learned proposals, streamed batches) keep
-// each replica as an axis-aligned periodic box with a halo and colour classes
-// along the three axes; non-diagonal supercells run on the exact paths and
-// the (sequential) n-fold way only.
+// The learned proposals and the streamed batches keep each replica as an
+// axis-aligned periodic box (cubic lattices of generated tables, halo tiles
+// in HBM); non-diagonal supercells do not run there.
 void require_box(const cem_replicas *r) {
   require(!r->twisted,
           "non-diagonal supercells support energies, energy changes, the sequential replay, "
@@ -523,8 +522,6 @@ void create_replicas(const cem_system *sys, int n, const int *L, const int *tw, 
                 "supercell too small for the cluster expansion's reach");
       }
       if (twist) {
-        // no lattice vector of the supercell may join two sites of one
-        // cluster: none within 2 reach of the origin along every axis
         const int64_t n_uc = (int64_t)R.L[0] * R.L[1] * R.L[2];
         require(R.L[0] >= 1 && R.L[1] >= 1 && R.L[2] >= 1 &&
                     n_uc * sys->T.n_sublat <= (int64_t)1 << 28,
@@ -575,11 +572,19 @@ void create_replicas(const cem_system *sys, int n, const int *L, const int *tw, 
         for (int a = 0; a < 3; ++a) R.n_col[a] = 1;
         bool coloured = false;
         if (ensemble == CEM_SEMIGRAND_CANONICAL && !sys->big) {
-          try {
-            R.p = choose_colouring(*sys, R.L, ensemble, R.tw);
-            coloured = true;
-          } catch (const Err &) {
+          std::vector<int> key{R.L[0], R.L[1], R.L[2], R.tw[0], R.tw[1], R.tw[2]};
+          auto it = pcache.find(key);
+          if (it != pcache.end()) {
+            R.p = it->second;
+          } else {
+            try {
+              R.p = choose_colouring(*sys, R.L, ensemble, R.tw);
+            } catch (const Err &) {
+              R.p = 0;  // no colouring: the batch does not sweep
+            }
+            pcache[key] = R.p;
           }
+          coloured = R.p > 0;
         }
         if (coloured) {
           for (int a = 0; a < 3; ++a) {
